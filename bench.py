@@ -1,0 +1,276 @@
+#!/usr/bin/env python
+"""Benchmark: particle-updates/s of the explicit MPM step on one GB300.
+
+Workload: the Taylor-bar impact (3-D TLMPM, MUSL, cubic B-spline, Johnson-Cook
+strength + linear EOS, copper bar R = 3.2 mm, L = 32.4 mm at 190 m/s on a rigid
+wall, 2x2x2 particles per cell), at cellsize 0.2 mm: 1,045,872 particles and
+177,507 grid nodes.  As in the reference script, one step runs before the wall
+fix is added; the timed steps follow.  Inputs are synthetic and deterministic
+(the populate lattice).  Particle state (~350 MB touched per step) is larger
+than the 129 MB L2, so no flush is needed between steps.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+N > 1 runs independent replicas (one per GPU, launched by torchrun); the path
+has no data-path collective.  ``--impl reference`` times the CPU
+implementation of the step (the oracle port) on the host cores.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "particle-updates/s on 1 GB300 (Taylor-bar TLMPM MUSL step)"
+UNIT = "particle-updates/s"
+
+# Algorithmic bytes of every phase (FP32 = 4 B): particle fields read or
+# written once per pass, plus 4 B per grid value per touched node per access.
+# (per particle, per node)
+PHASE_BYTES = {
+    "p2g": (64, 24),            # x0, v, m, vol0*PK1 -> nodal p, f
+    "grid_update": (0, 52),     # m, p, f -> v, v_update (+ fixes)
+    "g2p_advance": (60, 24),    # x0, u, v -> u, v ; gathers v, v_update
+    "p2g_velocity": (28, 12),   # x0, m, v -> nodal p
+    "grid_velocity": (0, 52),   # m, p -> v (+ BC), x += dt v
+    "g2p_stress": (200, 12),    # x0, v, F, sigma, eps_p, epsdot, vol0 -> F, sigma, eps_p, epsdot, vol0*PK1
+}
+
+
+def load_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d.get("hbm_gbs", 6800.0)), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index, self.rows, self.proc = index, [], None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm = [float(r[1]) for r in self.rows if len(r) > 2 and r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if len(r) > 2 and r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in self.rows:
+            for k, nm in enumerate(names):
+                if len(r) > 5 + k and r[5 + k].lower() in ("active", "0x1", "1"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(self.rows)}
+
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def run_cpu_sample(cellsize, steps, time_budget, threads):
+    """The oracle (FP64 CPU restatement of the reference step) on the host
+    cores, over a bounded number of steps of the same workload.  Step 1
+    (which builds the frozen TLMPM neighbour lists) is untimed."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as orc
+    from karamelo_gb300 import workloads as W
+    orc.lib().om_set_threads(threads)
+    sim = W.taylor_bar(lambda s: orc.OracleBackend(s, threads=threads), cellsize=cellsize, method="tlmpm")
+    n = sim.s.solids[0].np
+    sim.run(1)
+    W.taylor_bar_wall(sim)
+    done, t0 = 0, time.perf_counter()
+    while done < steps:
+        sim.run(1)
+        done += 1
+        if time.perf_counter() - t0 > time_budget:
+            break
+    dt = time.perf_counter() - t0
+    return n * done / dt, n, done, dt
+
+
+def bench_reference(args):
+    world, rank, _ = dist_env()
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    steps = max(1, min(args.steps, args.ref_steps))
+    v, n, done, dt = run_cpu_sample(args.cellsize, steps, args.ref_budget, threads)
+    sample = f"{done} steps of the {n}-particle bar (cellsize {args.cellsize} mm) after the untimed first step"
+    line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world, "steps": done, "warmup": 1,
+            "ms_per_step": 1000 * dt / done, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic (populate lattice, deterministic)", "impl": "reference",
+            "config": {"workload": f"taylor_bar_tlmpm_musl_cubic_jc h={args.cellsize}mm particles={n}"},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def bench_ours(args):
+    world, rank, local = dist_env()
+    import torch
+    from karamelo_gb300 import workloads as W
+    from karamelo_gb300.gpu import GpuBackend
+
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    sim = W.taylor_bar(None, cellsize=args.cellsize)
+    n = sim.s.solids[0].np
+    nn = sim.s.grids[0].nnodes
+    sim.backend = GpuBackend(sim.s, precision=args.precision, track_strain=False)
+    sim.run(1)
+    W.taylor_bar_wall(sim)
+    be = sim.backend
+    be.run(args.warmup)
+    # per-phase device time (CUDA events on the library's stream, eager launches)
+    phases = be.profile(args.profile_steps)
+    stream = torch.cuda.ExternalStream(be.stream())
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    clocks = ClockSampler(local)
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    clocks.start()
+    time.sleep(0.3)
+    e0.record(stream)
+    be.run(args.steps)
+    e1.record(stream)
+    e1.synchronize()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    clk = clocks.stop()
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * n * args.steps / (ms / 1000.0)
+    launches = be.launches_per_step() * args.steps
+
+    # end to end through the C ABI with host buffers: context creation and the
+    # upload of the particle state, the first step and the wall fix, then the
+    # timed steps with a dump (x, v, rotated sigma downloaded to host) every
+    # 10 steps, as the reference script's set_output(10)
+    sim2 = W.taylor_bar(None, cellsize=args.cellsize)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    sim2.backend = GpuBackend(sim2.s, precision=args.precision, track_strain=False)
+    sim2.run(1)
+    W.taylor_bar_wall(sim2)
+    done, dumps = 0, 0
+    while done < args.steps:
+        k = min(10, args.steps - done)
+        sim2.run(k)
+        done += k
+        for f in ("x", "v", "sigma"):
+            sim2.particles(0, f)
+        dumps += 1
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+    e2e = n * (done + 1) / e2e_s
+    h2d = n * (3 + 3 + 3 + 1 + 1) * 8  # x0, x, v, mass, vol0 as FP64 from the caller
+    d2h = dumps * n * (3 + 3 + 9) * 8
+
+    if rank != 0:
+        return
+    peak, peak_kind = load_peaks()
+    dom = max((k for k in phases if k in PHASE_BYTES), key=lambda k: phases[k])
+    bp, bn = PHASE_BYTES[dom]
+    alg = bp * n + bn * nn
+    achieved = alg / (phases[dom] * 1e-3) / 1e9
+    step_bytes = sum(PHASE_BYTES[k][0] * n + PHASE_BYTES[k][1] * nn for k in phases if k in PHASE_BYTES)
+    traffic = None
+    tp = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tp):
+        with open(tp) as f:
+            traffic = json.load(f).get(dom)
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic (populate lattice, deterministic); inputs larger than L2, no flush",
+        "config": {"workload": f"taylor_bar_tlmpm_musl_cubic_jc h={args.cellsize}mm", "particles": n, "nodes": nn,
+                   "parallelism": f"replicas{world}", "precision": "fp64_islands" if args.precision else "fp32",
+                   "graph": "one CUDA graph per step, replayed"},
+        "gpu_launches": launches,
+        "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d // (done + 1),
+                "d2h_bytes_per_step": d2h // (done + 1),
+                "note": "C ABI from host FP64 arrays: upload + binning + steps + a dump every 10 steps"},
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,
+                     "alg_bytes_per_launch": alg},
+        "step_roofline": {"alg_bytes_per_step": step_bytes, "achieved_gbs": step_bytes / (ms / args.steps * 1e-3) / 1e9,
+                          "frac": step_bytes / (ms / args.steps * 1e-3) / 1e9 / peak},
+        "phases_ms": phases,
+        "clocks": clk,
+    }
+    if world == 1 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        v, npart, done_c, dtc = run_cpu_sample(args.cellsize, args.cpu_steps, args.ref_budget, threads)
+        line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                                "sample": f"{done_c} oracle steps of the same {npart}-particle bar after its untimed first step"}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=500)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cellsize", type=float, default=0.2)
+    ap.add_argument("--precision", type=int, default=0)
+    ap.add_argument("--profile-steps", type=int, default=5)
+    ap.add_argument("--cpu-steps", type=int, default=3)
+    ap.add_argument("--ref-steps", type=int, default=5)
+    ap.add_argument("--ref-budget", type=float, default=60.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        bench_reference(args)
+    else:
+        bench_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,191 @@
+/* kmpm.h -- C ABI of the GB300-native explicit MPM time step (libkmpm.so).
+ *
+ * This is the boundary a Karamelo method style calls.  A maintainer adds the
+ * styles `tlmpm/gpu` and `ulmpm/gpu` (Method, src/method.h:25-54, registered
+ * through src/style_method.h) and `usl/gpu` / `musl/gpu` (Scheme,
+ * src/scheme.h:19-24); their code uploads the state that Karamelo's host
+ * classes built (Domain, Grid::init, Solid::populate, Material, Group, Fix)
+ * and then lets kmpm_run() execute whole time steps on the GPU.  The binding
+ * is shown in INTEGRATION.md.
+ *
+ * Conventions
+ *   - every function returns an int status: KMPM_OK (0) or a negative
+ *     KMPM_ERR_* code; kmpm_last_error() gives the message.  The reference's
+ *     fatal checks (Error::one / Error::all, src/error.cpp:33-68) come back as
+ *     the KMPM_ERR_* codes of the step that raised them;
+ *   - vectors are passed as arrays of n*3 doubles (the memory layout of
+ *     std::vector<Eigen::Vector3d>), tensors as n*9 doubles in row-major
+ *     order; particle arrays are in the order the caller uploaded them;
+ *   - the context owns all device memory and one CUDA stream; host buffers
+ *     stay owned by the caller; no call allocates device memory once
+ *     kmpm_run() has started, except the first kmpm_run() after a solid or
+ *     fix was added;
+ *   - one host thread per context (the reference is single-threaded per rank).
+ */
+#ifndef KMPM_H
+#define KMPM_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define KMPM_OK 0
+#define KMPM_ERR_ARG (-1)          /* bad argument or unsupported combination */
+#define KMPM_ERR_CUDA (-2)         /* CUDA runtime failure / no device */
+#define KMPM_ERR_STATE (-3)        /* call out of order */
+#define KMPM_ERR_J (-10)           /* J <= 0, src/solid.cpp:1208-1215 */
+#define KMPM_ERR_LEFT_DOMAIN (-11) /* particle left the box, src/solid.cpp:617-627 */
+#define KMPM_ERR_NAN (-12)         /* nan wave speed / dtCFL, src/solid.cpp:1387-1397, src/tlmpm.cpp:498-508 */
+#define KMPM_ERR_POLDEC (-13)      /* polar decomposition failed, src/solid.cpp:1229-1236 */
+#define KMPM_ERR_DTCFL (-14)       /* dtCFL == 0, src/tlmpm.cpp:498-502 */
+
+/* method / scheme / basis (Update::create_method, src/update.cpp:108-196) */
+#define KMPM_TLMPM 0
+#define KMPM_ULMPM 1
+#define KMPM_USL 0
+#define KMPM_MUSL 1
+#define KMPM_BASIS_LINEAR 0
+#define KMPM_BASIS_CUBIC 1
+#define KMPM_BASIS_BERNSTEIN 2
+
+/* kmpm_params.precision: arithmetic of the three places that the FP32 bulk
+ * may promote (nodal v = p/m, det/inverse of F, the constitutive return) */
+#define KMPM_PREC_FP32 0
+#define KMPM_PREC_FP64_ISLANDS 1
+
+typedef struct {
+  int method;        /* KMPM_TLMPM / KMPM_ULMPM */
+  int scheme;        /* KMPM_USL / KMPM_MUSL (src/update.cpp:42-45 default MUSL) */
+  int basis;         /* KMPM_BASIS_* */
+  int dim;           /* 1, 2 or 3 (Domain::dimension) */
+  double pic_flip;   /* Update::PIC_FLIP (0 for PIC) */
+  int thermal;       /* method(..., thermo-mechanical) */
+  double dt;         /* Update::dt at the first step (1e-16 unless set_dt) */
+  double dt_factor;  /* Update::dt_factor */
+  int dt_constant;   /* set_dt() was used */
+  double boxlo[3];   /* Domain::boxlo / boxhi */
+  double boxhi[3];
+  int precision;     /* KMPM_PREC_* */
+  int sort_every;    /* ULMPM: particles are re-binned by cell every step; kept for ABI growth */
+  int track_strain;  /* keep Solid::strain_el (needed by the strain-energy output) */
+} kmpm_params;
+
+/* One material: Mat (src/material.h:45-68) with its EOS / Strength / Damage /
+ * Temperature parameters in the argument order of the reference commands:
+ *   eos_p   linear (rho0,K); shock (rho0,K,c0,S,Gamma,cv,Tr,Q1,Q2); fluid (rho0,K,Gamma)
+ *   str_p   linear (G); plastic (G,sigmay); johnson_cook (G,A,B,n,epsdot0,C,m,Tr,Tm);
+ *           swift (G,A,B,C,n); fluid (mu)
+ *   dam_p   damage_johnson_cook (d1,d2,d3,d4,d5,epsdot0,Tr,Tm)
+ *   temp_p  plastic_work (chi,cp,kappa,alpha,T0,Tm) */
+#define KMPM_MAT_LINEAR 0
+#define KMPM_MAT_NEO_HOOKEAN 1
+#define KMPM_MAT_EOS_STRENGTH 2
+typedef struct {
+  int type;
+  double rho0, E, nu, cp, kappa; /* linear / neo-Hookean materials */
+  int eos;                       /* 0 linear, 1 shock, 2 fluid */
+  double eos_p[12];
+  int strength;                  /* 0 linear, 1 plastic, 2 johnson_cook, 3 swift, 4 fluid */
+  double str_p[12];
+  int damage;                    /* -1 none, 0 damage_johnson_cook */
+  double dam_p[8];
+  int temp;                      /* -1 none, 0 plastic_work */
+  double temp_p[6];
+} kmpm_material;
+
+/* fix kinds lowered to the device */
+#define KMPM_FIX_VELOCITY_NODES 0 /* FixVelocityNodes, src/fix_velocity_nodes.cpp:130-271 */
+#define KMPM_FIX_BODY_FORCE 1     /* FixBodyforce, src/fix_body_force.cpp:106-179 */
+
+/* particle fields for kmpm_download_particles / kmpm_upload_particles */
+#define KMPM_P_X 0        /* n*3 */
+#define KMPM_P_X0 1       /* n*3 */
+#define KMPM_P_V 2        /* n*3 */
+#define KMPM_P_SIGMA 3    /* n*9, as stored (unrotated for TLMPM) */
+#define KMPM_P_SIGMA_ROT 4 /* n*9, R sigma R^T for TLMPM dumps (src/dump_particle.cpp:98-102) */
+#define KMPM_P_F 5        /* n*9 */
+#define KMPM_P_EPS_P 6
+#define KMPM_P_EPSDOT_P 7
+#define KMPM_P_DAMAGE 8
+#define KMPM_P_DAMAGE_INIT 9
+#define KMPM_P_T 10
+#define KMPM_P_J 11
+#define KMPM_P_VOL 12
+#define KMPM_P_STRAIN_EL 13 /* n*9 (needs kmpm_params.track_strain) */
+#define KMPM_P_MASS 15
+
+/* grid fields for kmpm_download_grid */
+#define KMPM_G_MASS 0
+#define KMPM_G_V 1
+#define KMPM_G_V_UPDATE 2
+#define KMPM_G_X 3
+#define KMPM_G_T 6
+
+/* Context life cycle.  Replaces what Update::create_method / Method::setup
+ * (src/update.cpp:108-196, src/tlmpm.cpp:51-85) configure. */
+int kmpm_create(const kmpm_params *params, struct kmpm_ctx **out);
+int kmpm_destroy(struct kmpm_ctx *ctx);
+const char *kmpm_last_error(const struct kmpm_ctx *ctx);
+
+/* Material::add_material (src/material.cpp:249-380); returns the id (>= 0). */
+int kmpm_add_material(struct kmpm_ctx *ctx, const kmpm_material *mat);
+
+/* Grid::init (src/grid.cpp:68-413): the caller passes the node lattice it
+ * built (lower bound, cellsize, local node counts n[3] and global counts
+ * nglobal[3] used by the boundary-modified cubic splines).  Returns the id. */
+int kmpm_add_grid(struct kmpm_ctx *ctx, const double lo[3], double cellsize, const int n[3], const int nglobal[3]);
+
+/* Solid state after Solid::populate (src/solid.cpp:1810-2336): n particles
+ * with x0, x, v (n*3), mass, vol0 (n) and the initial temperature.  TLMPM
+ * solids each own one grid; ULMPM solids share grid 0.  Returns the id. */
+int kmpm_add_solid(struct kmpm_ctx *ctx, int grid, int mat, int n, const double *x0, const double *x,
+                   const double *v, const double *mass, const double *vol0, double T0);
+
+/* A fix on the nodes of one grid.  coef[4*d..4*d+3] = (c0,c1,c2,c3) give the
+ * value of axis d as c0 + c1*time + c2*exp(c3*time) (velocity_nodes) or the
+ * constant acceleration c0 (body_force); set[d] != 0 selects the axes. */
+int kmpm_add_fix(struct kmpm_ctx *ctx, int kind, int grid, const unsigned char *node_mask, const int set[3],
+                 const double coef[12]);
+
+/* Scheme::run for nsteps steps (USL::run src/usl.cpp:34-94, MUSL::run
+ * src/musl.cpp:34-95), each step fully on the GPU. */
+int kmpm_run(struct kmpm_ctx *ctx, int nsteps);
+
+/* RunTime::command (src/run_time.cpp:30-60): steps until time >= maxtime. */
+int kmpm_run_time(struct kmpm_ctx *ctx, double maxtime, int *nsteps_done);
+
+/* Update::atime, Update::dt, Update::ntimestep. */
+int kmpm_scalars(struct kmpm_ctx *ctx, double *time, double *dt, long long *ntimestep);
+
+/* Download / upload one particle field of one solid in the caller's
+ * particle order (the download before Output::write, src/output.cpp:128-200). */
+int kmpm_download_particles(struct kmpm_ctx *ctx, int solid, int field, double *out);
+int kmpm_upload_particles(struct kmpm_ctx *ctx, int solid, int field, const double *in);
+
+/* Download one grid field (n*1 or n*3 doubles, reference node order). */
+int kmpm_download_grid(struct kmpm_ctx *ctx, int grid, int field, double *out);
+
+/* out[0] = kinetic energy (FixKineticEnergy, src/fix_kinetic_energy.cpp:78-118),
+ * out[1] = strain energy (ComputeStrainEnergy, src/compute_strain_energy.cpp:64-117),
+ * both over all solids, reduced on the device in a fixed order. */
+int kmpm_energy(struct kmpm_ctx *ctx, double out[2]);
+
+/* The context's CUDA stream (cudaStream_t as void*), for callers that time or
+ * order their own work around kmpm_run. */
+void *kmpm_stream(struct kmpm_ctx *ctx);
+
+/* Number of kernel launches one time step issues (for launch accounting). */
+int kmpm_launches_per_step(struct kmpm_ctx *ctx);
+
+/* Profiling (no counterpart in the reference): runs nsteps steps launched
+ * eagerly with a CUDA event recorded on the context's stream after every
+ * phase, and returns the mean device time of each phase in phase_ms (at most
+ * max_phases); kmpm_profile_phase() names phase i ("p2g", "grid_update",
+ * "g2p_advance", "p2g_velocity", "grid_velocity", "g2p_stress", "dt", ...). */
+int kmpm_profile(struct kmpm_ctx *ctx, int nsteps, double *phase_ms, int max_phases, int *nphases);
+const char *kmpm_profile_phase(struct kmpm_ctx *ctx, int i);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* KMPM_H */

@@ -1,0 +1,1132 @@
+// kmpm_api.cu -- the C ABI of include/kmpm.h: context, device layout, the
+// per-step launch sequence (captured once as a CUDA graph and replayed), and
+// the host<->device conversions between the caller's FP64 arrays and the
+// device's FP32 structure of arrays.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "../../include/kmpm.h"
+#include "kmpm_kernels.cuh"
+
+using namespace kmpm;
+
+namespace kmpm {
+void launch_step_begin(StepScalars *s, int n, cudaStream_t st);
+}
+
+struct kmpm_ctx {
+  kmpm_params prm{};
+  std::string err;
+  cudaStream_t st = nullptr;
+  // ---- host-side definitions
+  std::vector<MatDev> mats;
+  struct HGrid {
+    double lo[3];
+    double cellsize;
+    int n[3], ng[3];
+  };
+  std::vector<HGrid> hgrids;
+  struct HSolid {
+    int grid, mat, n;
+    std::vector<double> x0, x, v, mass, vol0;
+    double T0;
+  };
+  std::vector<HSolid> hsolids;
+  struct HFix {
+    int kind, grid, set[3];
+    std::vector<uint8_t> mask;
+    double c[12];
+  };
+  std::vector<HFix> hfixes;
+  bool built = false, fixes_dirty = true;
+  // ---- device layout
+  size_t ps = 0;
+  int nblk_p = 0;
+  float *buf[2] = {nullptr, nullptr};
+  float **d_pp = nullptr;  // d_pp[0] current buffer, d_pp[1] the other
+  std::vector<RangeDev> ranges;
+  std::vector<int> solid_range, solid_base;
+  RangeDev *d_ranges = nullptr;
+  int *d_blk_range = nullptr;
+  int *d_solid_mat = nullptr;
+  std::vector<GridDev> grids;
+  GridDev *d_grids = nullptr;
+  int *d_blk_grid = nullptr, *d_grid_blk0 = nullptr;
+  int nblk_g = 0, nnodes_pad = 0;
+  MatDev *d_mats = nullptr;
+  float4 *nodeA = nullptr, *nodeB = nullptr, *nodeX = nullptr;
+  float *nodeT = nullptr;
+  int T = 0, NCELL = 0, ntiles_total = 0;
+  int2 *d_tiles = nullptr;
+  int ntiles_launch = 0;
+  int *d_cs = nullptr, *d_ce = nullptr, *d_ts = nullptr, *d_te = nullptr;
+  float *partial = nullptr;
+  size_t pstride_tile = 0;
+  FixDev *d_fixes = nullptr;
+  int *d_fix_start = nullptr, *d_fix_count = nullptr;
+  std::vector<uint8_t *> d_masks;
+  StepScalars *d_scalars = nullptr;
+  int nscalars = 1;
+  double *d_dtcfl = nullptr;
+  ErrState *d_err = nullptr;
+  float *d_blk_c = nullptr, *d_blk_h = nullptr;
+  double *d_eblk = nullptr, *d_eout = nullptr;
+  int *d_keys = nullptr, *d_vals = nullptr;
+  RadixTemp rtmp{};
+  int key_bits = 0;
+  std::vector<int> ul_fields;
+  StepKernels K{};
+  cudaGraphExec_t gexec = nullptr;
+  bool graph_valid = false;
+  int launches_per_step = 0;
+  int smem[4][2] = {{0}};
+  // per-kernel timing (kmpm_profile): events recorded between launches
+  bool profiling = false;
+  std::vector<cudaEvent_t> prof_ev;
+  std::vector<std::string> prof_names;
+  int prof_n = 0;
+  // TLMPM keeps its binning order for the whole run: caller index of every slot
+  std::vector<int> orig_cache, sid_cache;
+  bool TL() const { return prm.method == KMPM_TLMPM; }
+  bool musl() const { return prm.scheme == KMPM_MUSL; }
+};
+
+namespace {
+
+int fail(kmpm_ctx *c, int code, const std::string &msg) {
+  if (c) c->err = msg;
+  return code;
+}
+
+#define CK(call)                                                                                \
+  do {                                                                                          \
+    cudaError_t e_ = (call);                                                                    \
+    if (e_ != cudaSuccess) return fail(c, KMPM_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+template <typename T> int dalloc(kmpm_ctx *c, T **p, size_t n) {
+  CK(cudaMalloc((void **)p, sizeof(T) * std::max<size_t>(n, 1)));
+  CK(cudaMemsetAsync(*p, 0, sizeof(T) * std::max<size_t>(n, 1), c->st));
+  return KMPM_OK;
+}
+#define DALLOC(p, n)                      \
+  do {                                    \
+    int r_ = dalloc(c, &(p), (n));        \
+    if (r_ != KMPM_OK) return r_;         \
+  } while (0)
+
+template <typename T> void dfree(T *&p) {
+  if (p) cudaFree((void *)p);
+  p = nullptr;
+}
+
+MatDev to_dev(const kmpm_material &m) {
+  MatDev d{};
+  d.type = m.type;
+  d.eos = m.eos;
+  d.strength = m.strength;
+  d.damage = m.damage;
+  d.temp = m.temp;
+  for (int i = 0; i < 12; i++) { d.eos_p[i] = m.eos_p[i]; d.str_p[i] = m.str_p[i]; }
+  for (int i = 0; i < 8; i++) d.dam_p[i] = m.dam_p[i];
+  for (int i = 0; i < 6; i++) d.temp_p[i] = m.temp_p[i];
+  // Mat::Mat, src/material.cpp:720-769
+  if (m.type == KMPM_MAT_EOS_STRENGTH) {
+    d.rho0 = m.eos_p[0];
+    d.K = m.eos_p[1];
+    d.G = m.str_p[0];
+    d.lambda = d.K - 2 * d.G / 3;
+    d.signal_velocity = std::sqrt((d.lambda + 2 * d.G) / d.rho0);
+    if (m.temp >= 0) {
+      d.cp = m.temp_p[1];
+      d.invcp = 1.0 / d.cp;
+      d.kappa = m.temp_p[2];
+    }
+  } else {
+    d.rho0 = m.rho0;
+    d.G = m.E / (2 * (1 + m.nu));
+    d.lambda = m.E * m.nu / ((1 + m.nu) * (1 - 2 * m.nu));
+    d.K = m.E / (3 * (1 - 2 * m.nu));
+    d.signal_velocity = std::sqrt(d.K / d.rho0);
+    d.cp = m.cp;
+    d.invcp = m.cp != 0 ? 1.0 / m.cp : 0;
+    d.kappa = m.kappa;
+  }
+  return d;
+}
+
+PartArgs part_args(kmpm_ctx *c) {
+  PartArgs a{};
+  a.Pp = c->d_pp;
+  a.ps = c->ps;
+  a.ranges = c->d_ranges;
+  a.blk_range = c->d_blk_range;
+  a.solid_mat = c->d_solid_mat;
+  a.grids = c->d_grids;
+  a.mats = c->d_mats;
+  a.nodeA = c->nodeA;
+  a.nodeB = c->nodeB;
+  a.nodeT = c->nodeT;
+  a.scalars = c->d_scalars;
+  a.err = c->d_err;
+  a.blk_c = c->d_blk_c;
+  a.blk_h = c->d_blk_h;
+  a.pic_flip = (float)c->prm.pic_flip;
+  for (int d = 0; d < 3; d++) {
+    a.boxlo[d] = (float)c->prm.boxlo[d];
+    a.boxhi[d] = (float)c->prm.boxhi[d];
+  }
+  a.indep = 0;
+  a.use_vu = c->musl() ? 0 : 1;
+  a.thermal = c->prm.thermal;
+  a.track_strain = c->prm.track_strain;
+  a.dim = c->prm.dim;
+  a.tile_T = c->T;
+  return a;
+}
+
+P2GArgs p2g_args(kmpm_ctx *c) {
+  P2GArgs a{};
+  a.Pp = c->d_pp;
+  a.ps = c->ps;
+  a.pos_field = c->TL() ? PF_X0 : PF_X;
+  a.tiles = c->d_tiles;
+  a.grids = c->d_grids;
+  a.cell_start = c->d_cs;
+  a.cell_end = c->d_ce;
+  a.partial = c->partial;
+  a.pstride_tile = c->pstride_tile;
+  a.tile_start = c->d_ts;
+  a.tile_end = c->d_te;
+  return a;
+}
+
+GridArgs grid_args(kmpm_ctx *c, int remap) {
+  GridArgs a{};
+  a.grids = c->d_grids;
+  a.blk_grid = c->d_blk_grid;
+  a.grid_blk0 = c->d_grid_blk0;
+  a.partial = c->partial;
+  a.pstride_tile = c->pstride_tile;
+  a.tile_start = c->d_ts;
+  a.tile_end = c->d_te;
+  a.nodeA = c->nodeA;
+  a.nodeB = c->nodeB;
+  a.nodeX = c->nodeX;
+  a.nodeT = c->nodeT;
+  a.fixes = c->d_fixes;
+  a.fix_start = c->d_fix_start;
+  a.fix_count = c->d_fix_count;
+  a.scalars = c->d_scalars;
+  a.indep = 0;
+  a.remap = remap;
+  return a;
+}
+
+DtArgs dt_args(kmpm_ctx *c) {
+  DtArgs a{};
+  a.ranges = c->d_ranges;
+  a.grids = c->d_grids;
+  a.blk_c = c->d_blk_c;
+  a.blk_h = c->d_blk_h;
+  a.solid_dtcfl = c->d_dtcfl;
+  a.scalars = c->d_scalars;
+  a.err = c->d_err;
+  a.nranges = (int)c->ranges.size();
+  a.indep = 0;
+  a.dt_constant = c->prm.dt_constant;
+  a.dt_factor = c->prm.dt_factor;
+  return a;
+}
+
+int launch(kmpm_ctx *c, void *fn, dim3 grid, dim3 block, size_t smem, void *arg) {
+  void *args[] = {arg};
+  CK(cudaLaunchKernel(fn, grid, block, args, smem, c->st));
+  return KMPM_OK;
+}
+#define LAUNCH(fn, g, b, sm, arg)                               \
+  do {                                                          \
+    int r_ = launch(c, (fn), dim3(g), dim3(b), (sm), (void *)&(arg)); \
+    if (r_ != KMPM_OK) return r_;                               \
+    nl++;                                                       \
+  } while (0)
+
+// records a profiling event after the launches of one phase
+int mark(kmpm_ctx *c, const char *name) {
+  if (!c->profiling) return KMPM_OK;
+  if ((int)c->prof_ev.size() <= c->prof_n) {
+    cudaEvent_t e;
+    CK(cudaEventCreate(&e));
+    c->prof_ev.push_back(e);
+  }
+  if ((int)c->prof_names.size() <= c->prof_n) c->prof_names.push_back(name);
+  else c->prof_names[c->prof_n] = name;
+  CK(cudaEventRecord(c->prof_ev[c->prof_n], c->st));
+  c->prof_n++;
+  return KMPM_OK;
+}
+#define MARK(name)                  \
+  do {                              \
+    int r_ = mark(c, (name));       \
+    if (r_ != KMPM_OK) return r_;   \
+  } while (0)
+
+// particle fields that live in the device buffer for this configuration
+std::vector<int> active_fields(kmpm_ctx *c) {
+  std::vector<int> f;
+  auto add = [&](int base, int n) { for (int i = 0; i < n; i++) f.push_back(base + i); };
+  add(PF_X0, 3); add(PF_X, 3); add(PF_V, 3); add(PF_MASS, 1); add(PF_VOL0, 1); add(PF_H, 9); add(PF_SIG, 6);
+  add(PF_EPSP, 2); add(PF_DMG, 2); add(PF_PK, 9); add(PF_ORIG, 1); add(PF_SID, 1);
+  bool thermal = c->prm.thermal;
+  for (auto &m : c->mats) if (m.cp != 0) thermal = true;
+  if (thermal) { add(PF_T, 2); add(PF_Q, 3); }
+  if (c->prm.track_strain) add(PF_STRAIN, 6);
+  if (!c->TL()) add(PF_XN, 3);
+  return f;
+}
+
+// ---------------------------------------------------------------- build
+int build(kmpm_ctx *c) {
+  const int dim = c->prm.dim, basis = c->prm.basis;
+  if (c->hsolids.empty()) return fail(c, KMPM_ERR_STATE, "no solid was added");
+  get_step_kernels(dim, basis, c->K);
+  c->T = tile_edge(dim, basis);
+  c->NCELL = dim == 3 ? c->T * c->T * c->T : (dim == 2 ? c->T * c->T : c->T);
+  // ---- grids
+  c->grids.clear();
+  int node_off = 0, tile_off = 0;
+  std::vector<int> blk_grid, grid_blk0;
+  for (size_t gi = 0; gi < c->hgrids.size(); gi++) {
+    const auto &h = c->hgrids[gi];
+    GridDev g{};
+    for (int d = 0; d < 3; d++) {
+      g.n[d] = h.n[d];
+      g.ng[d] = h.ng[d];
+      g.lo[d] = (float)h.lo[d];
+      int nc = basis == KMPM_BASIS_BERNSTEIN ? (h.n[d] + 1) / 2 : h.n[d];
+      if (d >= dim) nc = 1;
+      g.ncell[d] = std::max(nc, 1);
+      g.ntile[d] = d < dim ? (g.ncell[d] + c->T - 1) / c->T : 1;
+    }
+    g.cellsize = (float)h.cellsize;
+    g.inv_cellsize = (float)(1.0 / h.cellsize);
+    g.node_off = node_off;
+    g.tile_off = tile_off;
+    g.cell_off = tile_off * c->NCELL;
+    g.solid0 = 0;
+    const int nn = h.n[0] * h.n[1] * h.n[2];
+    const int nb = (nn + 255) / 256;
+    grid_blk0.push_back((int)blk_grid.size());
+    for (int b = 0; b < nb; b++) blk_grid.push_back((int)gi);
+    node_off += nb * 256;
+    tile_off += g.ntile[0] * g.ntile[1] * g.ntile[2];
+    c->grids.push_back(g);
+  }
+  c->nnodes_pad = node_off;
+  c->nblk_g = (int)blk_grid.size();
+  c->ntiles_total = tile_off;
+  if ((long long)c->ntiles_total * c->NCELL > (1LL << 30))
+    return fail(c, KMPM_ERR_ARG, "grid too large for the cell binning");
+  c->key_bits = 1;
+  while ((1LL << c->key_bits) < (long long)c->ntiles_total * c->NCELL) c->key_bits++;
+  // ---- particle ranges
+  c->ranges.clear();
+  c->solid_range.assign(c->hsolids.size(), 0);
+  c->solid_base.assign(c->hsolids.size(), 0);
+  int base = 0;
+  for (size_t s = 0; s < c->hsolids.size(); s++) { c->solid_base[s] = base; base += c->hsolids[s].n; }
+  std::vector<int> blk_range;
+  int pstart = 0;
+  auto add_range = [&](int grid, int mat, int count) {
+    RangeDev r{};
+    r.start = pstart;
+    r.count = count;
+    r.grid = grid;
+    r.mat = mat;
+    r.blk0 = (int)blk_range.size();
+    r.nblk = std::max(1, (count + 255) / 256);
+    for (int b = 0; b < r.nblk; b++) blk_range.push_back((int)c->ranges.size());
+    pstart += r.nblk * 256;
+    c->ranges.push_back(r);
+  };
+  if (c->TL()) {
+    for (size_t s = 0; s < c->hsolids.size(); s++) {
+      c->solid_range[s] = (int)c->ranges.size();
+      add_range(c->hsolids[s].grid, c->hsolids[s].mat, c->hsolids[s].n);
+    }
+  } else {
+    int mat = c->hsolids[0].mat;
+    for (auto &s : c->hsolids) if (s.mat != mat) mat = -1;
+    add_range(0, mat, base);
+  }
+  c->ps = pstart;
+  c->nblk_p = (int)blk_range.size();
+  // ---- device allocations
+  DALLOC(c->buf[0], c->ps * PF_COUNT);
+  DALLOC(c->buf[1], c->ps * PF_COUNT);
+  DALLOC(c->d_pp, 2);
+  {
+    float *pp[2] = {c->buf[0], c->buf[1]};
+    CK(cudaMemcpyAsync(c->d_pp, pp, sizeof(pp), cudaMemcpyHostToDevice, c->st));
+  }
+  DALLOC(c->d_ranges, c->ranges.size());
+  CK(cudaMemcpyAsync(c->d_ranges, c->ranges.data(), sizeof(RangeDev) * c->ranges.size(), cudaMemcpyHostToDevice, c->st));
+  DALLOC(c->d_blk_range, blk_range.size());
+  CK(cudaMemcpyAsync(c->d_blk_range, blk_range.data(), sizeof(int) * blk_range.size(), cudaMemcpyHostToDevice, c->st));
+  std::vector<int> smat(c->hsolids.size());
+  for (size_t s = 0; s < c->hsolids.size(); s++) smat[s] = c->hsolids[s].mat;
+  DALLOC(c->d_solid_mat, smat.size());
+  CK(cudaMemcpyAsync(c->d_solid_mat, smat.data(), sizeof(int) * smat.size(), cudaMemcpyHostToDevice, c->st));
+  DALLOC(c->d_grids, c->grids.size());
+  CK(cudaMemcpyAsync(c->d_grids, c->grids.data(), sizeof(GridDev) * c->grids.size(), cudaMemcpyHostToDevice, c->st));
+  DALLOC(c->d_blk_grid, blk_grid.size());
+  CK(cudaMemcpyAsync(c->d_blk_grid, blk_grid.data(), sizeof(int) * blk_grid.size(), cudaMemcpyHostToDevice, c->st));
+  DALLOC(c->d_grid_blk0, grid_blk0.size());
+  CK(cudaMemcpyAsync(c->d_grid_blk0, grid_blk0.data(), sizeof(int) * grid_blk0.size(), cudaMemcpyHostToDevice, c->st));
+  DALLOC(c->d_mats, c->mats.size());
+  CK(cudaMemcpyAsync(c->d_mats, c->mats.data(), sizeof(MatDev) * c->mats.size(), cudaMemcpyHostToDevice, c->st));
+  DALLOC(c->nodeA, c->nnodes_pad);
+  DALLOC(c->nodeB, c->nnodes_pad);
+  DALLOC(c->nodeX, c->nnodes_pad);
+  DALLOC(c->nodeT, c->nnodes_pad);
+  {
+    std::vector<float4> X(c->nnodes_pad, make_float4(0, 0, 0, 0));
+    for (size_t gi = 0; gi < c->hgrids.size(); gi++) {
+      const auto &h = c->hgrids[gi];
+      const double hh = basis == KMPM_BASIS_BERNSTEIN ? h.cellsize / 2 : h.cellsize;
+      int l = 0;
+      for (int i = 0; i < h.n[0]; i++)
+        for (int j = 0; j < h.n[1]; j++)
+          for (int k = 0; k < h.n[2]; k++, l++)
+            X[c->grids[gi].node_off + l] = make_float4((float)(h.lo[0] + i * hh), dim >= 2 ? (float)(h.lo[1] + j * hh) : 0.f,
+                                                       dim == 3 ? (float)(h.lo[2] + k * hh) : 0.f, 0.f);
+    }
+    CK(cudaMemcpyAsync(c->nodeX, X.data(), sizeof(float4) * X.size(), cudaMemcpyHostToDevice, c->st));
+    CK(cudaStreamSynchronize(c->st));
+  }
+  const int ncells = c->ntiles_total * c->NCELL;
+  DALLOC(c->d_cs, ncells);
+  DALLOC(c->d_ce, ncells);
+  DALLOC(c->d_ts, c->ntiles_total);
+  DALLOC(c->d_te, c->ntiles_total);
+  {
+    int S = stencil_width(basis), SC = stencil_sc(basis);
+    int W = (c->T - 1) * SC + S;
+    int NW = dim == 3 ? W * W * W : (dim == 2 ? W * W : W);
+    c->pstride_tile = (size_t)NW * 10;
+  }
+  DALLOC(c->partial, c->pstride_tile * c->ntiles_total);
+  c->nscalars = 1;
+  DALLOC(c->d_scalars, c->nscalars);
+  {
+    StepScalars s{};
+    s.dt = c->prm.dt;
+    s.time = 0;
+    s.ntimestep = 0;
+    s.dtCFL = 1e22;
+    CK(cudaMemcpyAsync(c->d_scalars, &s, sizeof(s), cudaMemcpyHostToDevice, c->st));
+  }
+  DALLOC(c->d_dtcfl, c->ranges.size());
+  DALLOC(c->d_err, 1);
+  DALLOC(c->d_blk_c, c->nblk_p);
+  DALLOC(c->d_blk_h, c->nblk_p);
+  DALLOC(c->d_eblk, 2 * c->nblk_p);
+  DALLOC(c->d_eout, 2);
+  DALLOC(c->d_keys, c->ps);
+  DALLOC(c->d_vals, c->ps);
+  DALLOC(c->rtmp.k1, c->ps);
+  DALLOC(c->rtmp.v1, c->ps);
+  DALLOC(c->rtmp.hist, 256 * ((c->ps + 2047) / 2048 + 1));
+  DALLOC(c->rtmp.tot, 256);
+  // ---- particle upload (caller order within each solid)
+  {
+    std::vector<float> H((size_t)c->ps * PF_COUNT, 0.f);
+    auto at = [&](int f, int p) -> float & { return H[(size_t)f * c->ps + p]; };
+    for (size_t s = 0; s < c->hsolids.size(); s++) {
+      const auto &S = c->hsolids[s];
+      const RangeDev &r = c->ranges[c->TL() ? c->solid_range[s] : 0];
+      const int off = c->TL() ? r.start : r.start + c->solid_base[s];
+      for (int i = 0; i < S.n; i++) {
+        const int p = off + i;
+        for (int d = 0; d < 3; d++) {
+          at(PF_X0 + d, p) = (float)S.x0[3 * i + d];
+          // positions are stored as the displacement from x0
+          at(PF_X + d, p) = (float)(S.x[3 * i + d] - S.x0[3 * i + d]);
+          if (!c->TL()) at(PF_XN + d, p) = at(PF_X + d, p);
+          at(PF_V + d, p) = (float)S.v[3 * i + d];
+        }
+        at(PF_MASS, p) = (float)S.mass[i];
+        at(PF_VOL0, p) = (float)S.vol0[i];
+        // Solid::populate sets T = T0 only for thermo-mechanical runs; otherwise
+        // the vector is value-initialised (src/solid.cpp:2297-2306, 306-311)
+        at(PF_T, p) = c->prm.thermal ? (float)S.T0 : 0.f;
+        int orig = c->solid_base[s] + i, sid = (int)s;
+        std::memcpy(&at(PF_ORIG, p), &orig, 4);
+        std::memcpy(&at(PF_SID, p), &sid, 4);
+      }
+    }
+    CK(cudaMemcpy(c->buf[0], H.data(), sizeof(float) * H.size(), cudaMemcpyHostToDevice));
+  }
+  // ---- kernel attributes
+  const int modes[4] = {P2G_MASS, P2G_TL, P2G_UL, P2G_VEL};
+  void *fns[4][2] = {{c->K.p2g_mass, c->K.p2g_mass}, {c->K.p2g_tl, c->K.p2g_tl_th}, {c->K.p2g_ul, c->K.p2g_ul_th},
+                     {c->K.p2g_vel, c->K.p2g_vel_th}};
+  for (int m = 0; m < 4; m++)
+    for (int t = 0; t < 2; t++) {
+      c->smem[m][t] = p2g_smem_bytes(dim, basis, modes[m], t == 1);
+      CK(cudaFuncSetAttribute(fns[m][t], cudaFuncAttributeMaxDynamicSharedMemorySize, c->smem[m][t]));
+    }
+  c->ul_fields.clear();
+  for (int f : active_fields(c)) {
+    int src = (f >= PF_X && f < PF_X + 3) ? PF_XN + (f - PF_X) : f;
+    c->ul_fields.push_back((f << 8) | src);
+  }
+  // ---- TLMPM: bin once by x0 (static connectivity, src/tlmpm.cpp:339) and compute the nodal mass
+  if (c->TL()) {
+    PartArgs pa = part_args(c);
+    launch_cell_keys(pa, c->nblk_p, c->d_keys, 1, c->st);
+    std::vector<int> keys(c->ps);
+    CK(cudaMemcpyAsync(keys.data(), c->d_keys, sizeof(int) * c->ps, cudaMemcpyDeviceToHost, c->st));
+    CK(cudaStreamSynchronize(c->st));
+    std::vector<int> perm(c->ps, 0), sorted(c->ps, 0);
+    std::vector<int2> tiles;
+    for (auto &r : c->ranges) {
+      std::vector<int> idx(r.count);
+      std::iota(idx.begin(), idx.end(), 0);
+      const int *kb = keys.data() + r.start;
+      std::stable_sort(idx.begin(), idx.end(), [&](int a, int b) { return kb[a] < kb[b]; });
+      for (int i = 0; i < r.count; i++) {
+        perm[r.start + i] = idx[i];
+        sorted[r.start + i] = kb[idx[i]];
+      }
+      int last = -1;
+      for (int i = 0; i < r.count; i++) {
+        int t = sorted[r.start + i] / c->NCELL;
+        if (t != last) {
+          const GridDev &g = c->grids[r.grid];
+          tiles.push_back(make_int2(r.grid, t - g.tile_off));
+          last = t;
+        }
+      }
+    }
+    CK(cudaMemcpyAsync(c->d_vals, perm.data(), sizeof(int) * c->ps, cudaMemcpyHostToDevice, c->st));
+    CK(cudaMemcpyAsync(c->d_keys, sorted.data(), sizeof(int) * c->ps, cudaMemcpyHostToDevice, c->st));
+    std::vector<int> fl;
+    for (int f : active_fields(c)) fl.push_back((f << 8) | f);
+    for (auto &r : c->ranges)
+      launch_permute(c->d_pp, c->d_pp + 1, c->ps, c->d_vals + r.start, r.start, r.count, fl.data(), (int)fl.size(), c->st);
+    launch_swap_ptrs(c->d_pp, c->st);
+    std::swap(c->buf[0], c->buf[1]);
+    for (auto &r : c->ranges)
+      launch_cell_ranges(c->d_keys + r.start, r.start, r.count, c->NCELL, c->d_cs, c->d_ce, c->d_ts, c->d_te, c->st);
+    c->ntiles_launch = (int)tiles.size();
+    DALLOC(c->d_tiles, tiles.size());
+    CK(cudaMemcpyAsync(c->d_tiles, tiles.data(), sizeof(int2) * tiles.size(), cudaMemcpyHostToDevice, c->st));
+    // nodal mass, once (TLMPM::particles_to_grid, src/tlmpm.cpp:344-351)
+    P2GArgs p = p2g_args(c);
+    int nl = 0;
+    LAUNCH(c->K.p2g_mass, c->ntiles_launch, 256, c->smem[0][0], p);
+    GridArgs ga = grid_args(c, 0);
+    LAUNCH(c->K.grid_mass, c->nblk_g, 256, 0, ga);
+    CK(cudaStreamSynchronize(c->st));
+  } else {
+    // ULMPM: every tile of the box grid is launched; empty ones return at once
+    std::vector<int2> tiles;
+    for (size_t gi = 0; gi < c->grids.size(); gi++) {
+      const GridDev &g = c->grids[gi];
+      for (int t = 0; t < g.ntile[0] * g.ntile[1] * g.ntile[2]; t++) tiles.push_back(make_int2((int)gi, t));
+    }
+    c->ntiles_launch = (int)tiles.size();
+    DALLOC(c->d_tiles, tiles.size());
+    CK(cudaMemcpyAsync(c->d_tiles, tiles.data(), sizeof(int2) * tiles.size(), cudaMemcpyHostToDevice, c->st));
+  }
+  c->built = true;
+  return KMPM_OK;
+}
+
+int upload_fixes(kmpm_ctx *c) {
+  for (auto *m : c->d_masks) cudaFree(m);
+  c->d_masks.clear();
+  dfree(c->d_fixes);
+  dfree(c->d_fix_start);
+  dfree(c->d_fix_count);
+  std::vector<FixDev> fx;
+  std::vector<int> start(c->hgrids.size(), 0), count(c->hgrids.size(), 0);
+  for (size_t gi = 0; gi < c->hgrids.size(); gi++) {
+    start[gi] = (int)fx.size();
+    for (auto &h : c->hfixes) {
+      if (h.grid != (int)gi) continue;
+      FixDev f{};
+      f.kind = h.kind;
+      f.grid = h.grid;
+      for (int d = 0; d < 3; d++) {
+        f.set[d] = h.set[d];
+        for (int k = 0; k < 4; k++) f.c[d][k] = h.c[4 * d + k];
+      }
+      uint8_t *m = nullptr;
+      CK(cudaMalloc(&m, h.mask.size()));
+      CK(cudaMemcpy(m, h.mask.data(), h.mask.size(), cudaMemcpyHostToDevice));
+      c->d_masks.push_back(m);
+      f.mask = m;
+      fx.push_back(f);
+    }
+    count[gi] = (int)fx.size() - start[gi];
+  }
+  DALLOC(c->d_fixes, fx.size());
+  if (!fx.empty()) CK(cudaMemcpy(c->d_fixes, fx.data(), sizeof(FixDev) * fx.size(), cudaMemcpyHostToDevice));
+  DALLOC(c->d_fix_start, start.size());
+  DALLOC(c->d_fix_count, count.size());
+  CK(cudaMemcpy(c->d_fix_start, start.data(), sizeof(int) * start.size(), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(c->d_fix_count, count.data(), sizeof(int) * count.size(), cudaMemcpyHostToDevice));
+  c->fixes_dirty = false;
+  c->graph_valid = false;
+  return KMPM_OK;
+}
+
+// ---------------------------------------------------------------- one step
+// USL::run (src/usl.cpp:43-92) / MUSL::run (src/musl.cpp:43-93)
+int enqueue_step(kmpm_ctx *c) {
+  int nl = 0;
+  const bool TL = c->TL(), th = c->prm.thermal != 0, musl = c->musl();
+  const int prec = c->prm.precision == KMPM_PREC_FP64_ISLANDS ? 1 : 0;
+  PartArgs pa = part_args(c);
+  MARK("begin");
+  launch_step_begin(c->d_scalars, c->nscalars, c->st);
+  nl++;
+  if (!TL) {
+    // compute_grid_weight_functions_and_gradients (src/ulmpm.cpp:88-337):
+    // re-bin all particles by the cell of their current position
+    const RangeDev &r = c->ranges[0];
+    launch_cell_keys(pa, c->nblk_p, c->d_keys, 0, c->st);
+    launch_iota(c->d_vals, r.count, c->st);
+    radix_sort(c->d_keys, c->d_vals, r.count, c->key_bits, c->rtmp, c->st);
+    launch_permute(c->d_pp, c->d_pp + 1, c->ps, c->d_vals, r.start, r.count, c->ul_fields.data(),
+                   (int)c->ul_fields.size(), c->st);
+    launch_swap_ptrs(c->d_pp, c->st);
+    CK(cudaMemsetAsync(c->d_cs, 0, sizeof(int) * (size_t)c->ntiles_total * c->NCELL, c->st));
+    CK(cudaMemsetAsync(c->d_ce, 0, sizeof(int) * (size_t)c->ntiles_total * c->NCELL, c->st));
+    CK(cudaMemsetAsync(c->d_ts, 0, sizeof(int) * c->ntiles_total, c->st));
+    CK(cudaMemsetAsync(c->d_te, 0, sizeof(int) * c->ntiles_total, c->st));
+    launch_cell_ranges(c->d_keys, r.start, r.count, c->NCELL, c->d_cs, c->d_ce, c->d_ts, c->d_te, c->st);
+    nl += 5 + 3 * ((c->key_bits + 7) / 8);
+    MARK("bin_sort");
+  }
+  P2GArgs p = p2g_args(c);
+  GridArgs g1 = grid_args(c, 0);
+  // particles_to_grid
+  if (TL) LAUNCH(th ? c->K.p2g_tl_th : c->K.p2g_tl, c->ntiles_launch, 256, c->smem[1][th], p);
+  else LAUNCH(th ? c->K.p2g_ul_th : c->K.p2g_ul, c->ntiles_launch, 256, c->smem[2][th], p);
+  MARK("p2g");
+  // update_grid_state + fixes
+  LAUNCH(c->K.grid_upd[TL][th], c->nblk_g, 256, 0, g1);
+  MARK("grid_update");
+  // grid_to_points + advance_particles
+  LAUNCH(c->K.g2p1[TL][th], c->nblk_p, 256, 0, pa);
+  MARK("g2p_advance");
+  if (musl) {
+    // velocities_to_grid + post_velocities_to_grid (+ TL grid positions)
+    LAUNCH(th ? c->K.p2g_vel_th : c->K.p2g_vel, c->ntiles_launch, 256, c->smem[3][th], p);
+    MARK("p2g_velocity");
+    GridArgs g2 = grid_args(c, 1);
+    LAUNCH(c->K.grid_vel[TL][th], c->nblk_g, 256, 0, g2);
+    MARK("grid_velocity");
+  } else if (TL) {
+    GridArgs g2 = grid_args(c, 0);
+    LAUNCH(c->K.grid_vel[TL][th], c->nblk_g, 256, 0, g2);
+    MARK("grid_positions");
+  }
+  // compute_rate_deformation_gradient + update_deformation_gradient + update_stress
+  LAUNCH(c->K.g2p2[TL][th][prec], c->nblk_p, 256, 0, pa);
+  MARK("g2p_stress");
+  // update_time + adjust_dt
+  DtArgs da = dt_args(c);
+  launch_dt(da, c->st);
+  nl += 2;
+  MARK("dt");
+  CK(cudaGetLastError());
+  c->launches_per_step = nl;
+  return KMPM_OK;
+}
+
+int ensure_graph(kmpm_ctx *c) {
+  if (c->graph_valid) return KMPM_OK;
+  if (c->gexec) { cudaGraphExecDestroy(c->gexec); c->gexec = nullptr; }
+  cudaGraph_t g;
+  CK(cudaStreamBeginCapture(c->st, cudaStreamCaptureModeThreadLocal));
+  int r = enqueue_step(c);
+  cudaError_t e = cudaStreamEndCapture(c->st, &g);
+  if (r != KMPM_OK) return r;
+  if (e != cudaSuccess) return fail(c, KMPM_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+  CK(cudaGraphInstantiate(&c->gexec, g, 0));
+  cudaGraphDestroy(g);
+  c->graph_valid = true;
+  return KMPM_OK;
+}
+
+int check_error(kmpm_ctx *c) {
+  ErrState e{};
+  CK(cudaMemcpyAsync(&e, c->d_err, sizeof(e), cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  if (e.code == 0) return KMPM_OK;
+  char buf[256];
+  const char *what = e.code == ERR_J ? "J<=0" : e.code == ERR_LEFT ? "particle left the domain"
+                     : e.code == ERR_NAN ? "max_p_wave_speed is nan" : e.code == ERR_POLDEC ? "polar decomposition failed"
+                     : "dtCFL == 0 or nan";
+  std::snprintf(buf, sizeof(buf), "Error: %s (particle slot %d, step %lld)", what, e.particle, e.step);
+  const int code = e.code == ERR_J ? KMPM_ERR_J : e.code == ERR_LEFT ? KMPM_ERR_LEFT_DOMAIN
+                   : e.code == ERR_NAN ? KMPM_ERR_NAN : e.code == ERR_POLDEC ? KMPM_ERR_POLDEC : KMPM_ERR_DTCFL;
+  return fail(c, code, buf);
+}
+
+int prepare(kmpm_ctx *c) {
+  if (!c->built) {
+    int r = build(c);
+    if (r != KMPM_OK) return r;
+  }
+  if (c->fixes_dirty) {
+    int r = upload_fixes(c);
+    if (r != KMPM_OK) return r;
+  }
+  return ensure_graph(c);
+}
+
+int read_scalars(kmpm_ctx *c, StepScalars &s) {
+  CK(cudaMemcpyAsync(&s, c->d_scalars, sizeof(s), cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  return KMPM_OK;
+}
+
+// Newton polar rotation in double (host), for the rotated-stress download
+void polar_host(const double *F, double *R) {
+  double X[9];
+  for (int k = 0; k < 9; k++) X[k] = F[k];
+  for (int it = 0; it < 40; it++) {
+    double C[9];
+    C[0] = X[4] * X[8] - X[5] * X[7]; C[1] = X[5] * X[6] - X[3] * X[8]; C[2] = X[3] * X[7] - X[4] * X[6];
+    C[3] = X[2] * X[7] - X[1] * X[8]; C[4] = X[0] * X[8] - X[2] * X[6]; C[5] = X[1] * X[6] - X[0] * X[7];
+    C[6] = X[1] * X[5] - X[2] * X[4]; C[7] = X[2] * X[3] - X[0] * X[5]; C[8] = X[0] * X[4] - X[1] * X[3];
+    double d = X[0] * C[0] + X[1] * C[1] + X[2] * C[2];
+    double g = std::cbrt(1.0 / std::fabs(d)), gi = 1.0 / (g * d), diff = 0;
+    for (int k = 0; k < 9; k++) {
+      double xn = 0.5 * (g * X[k] + gi * C[k]);
+      diff += (xn - X[k]) * (xn - X[k]);
+      X[k] = xn;
+    }
+    if (diff < 1e-30) break;
+  }
+  for (int k = 0; k < 9; k++) R[k] = X[k];
+}
+
+}  // namespace
+
+// ================================================================ C ABI
+extern "C" {
+
+int kmpm_create(const kmpm_params *params, kmpm_ctx **out) {
+  if (!params || !out) return KMPM_ERR_ARG;
+  *out = nullptr;
+  const kmpm_params &p = *params;
+  if (p.method != KMPM_TLMPM && p.method != KMPM_ULMPM) return KMPM_ERR_ARG;
+  if (p.scheme != KMPM_USL && p.scheme != KMPM_MUSL) return KMPM_ERR_ARG;
+  if (p.basis < 0 || p.basis > 2 || p.dim < 1 || p.dim > 3) return KMPM_ERR_ARG;
+  if (p.method == KMPM_ULMPM && p.basis == KMPM_BASIS_BERNSTEIN) return KMPM_ERR_ARG;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return KMPM_ERR_CUDA;
+  kmpm_ctx *c = new kmpm_ctx();
+  c->prm = p;
+  if (cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking) != cudaSuccess) {
+    delete c;
+    return KMPM_ERR_CUDA;
+  }
+  *out = c;
+  return KMPM_OK;
+}
+
+int kmpm_destroy(kmpm_ctx *c) {
+  if (!c) return KMPM_OK;
+  if (c->st) cudaStreamSynchronize(c->st);
+  if (c->gexec) cudaGraphExecDestroy(c->gexec);
+  for (auto *m : c->d_masks) cudaFree(m);
+  for (auto e : c->prof_ev) cudaEventDestroy(e);
+  dfree(c->buf[0]); dfree(c->buf[1]); dfree(c->d_pp); dfree(c->d_ranges); dfree(c->d_blk_range);
+  dfree(c->d_solid_mat); dfree(c->d_grids); dfree(c->d_blk_grid); dfree(c->d_grid_blk0); dfree(c->d_mats);
+  dfree(c->nodeA); dfree(c->nodeB); dfree(c->nodeX); dfree(c->nodeT); dfree(c->d_tiles);
+  dfree(c->d_cs); dfree(c->d_ce); dfree(c->d_ts); dfree(c->d_te); dfree(c->partial);
+  dfree(c->d_fixes); dfree(c->d_fix_start); dfree(c->d_fix_count); dfree(c->d_scalars); dfree(c->d_dtcfl);
+  dfree(c->d_err); dfree(c->d_blk_c); dfree(c->d_blk_h); dfree(c->d_eblk); dfree(c->d_eout);
+  dfree(c->d_keys); dfree(c->d_vals); dfree(c->rtmp.k1); dfree(c->rtmp.v1); dfree(c->rtmp.hist); dfree(c->rtmp.tot);
+  if (c->st) cudaStreamDestroy(c->st);
+  delete c;
+  return KMPM_OK;
+}
+
+const char *kmpm_last_error(const kmpm_ctx *c) { return c ? c->err.c_str() : "null context"; }
+
+int kmpm_add_material(kmpm_ctx *c, const kmpm_material *m) {
+  if (!c || !m) return KMPM_ERR_ARG;
+  if (c->built) return fail(c, KMPM_ERR_STATE, "materials must be added before the first run");
+  if (m->type < 0 || m->type > 2) return fail(c, KMPM_ERR_ARG, "unsupported material type (rigid has no GPU path)");
+  if (m->type == KMPM_MAT_EOS_STRENGTH) {
+    if (m->eos < 0 || m->eos > 2 || m->strength < 0 || m->strength > 4 || m->damage < -1 || m->damage > 0 ||
+        m->temp < -1 || m->temp > 0)
+      return fail(c, KMPM_ERR_ARG, "unsupported EOS / strength / damage / temperature law");
+    if (m->strength == 2 && m->str_p[7] == m->str_p[8])
+      return fail(c, KMPM_ERR_ARG, "Error: reference temperature Tr equals melting temperature Tm");
+  }
+  c->mats.push_back(to_dev(*m));
+  return (int)c->mats.size() - 1;
+}
+
+int kmpm_add_grid(kmpm_ctx *c, const double lo[3], double cellsize, const int n[3], const int nglobal[3]) {
+  if (!c || !lo || !n || !nglobal || !(cellsize > 0)) return KMPM_ERR_ARG;
+  if (c->built) return fail(c, KMPM_ERR_STATE, "grids must be added before the first run");
+  if (!c->TL() && !c->hgrids.empty()) return fail(c, KMPM_ERR_ARG, "ULMPM uses one grid");
+  kmpm_ctx::HGrid g{};
+  for (int d = 0; d < 3; d++) {
+    g.lo[d] = lo[d];
+    g.n[d] = d < c->prm.dim ? n[d] : 1;
+    g.ng[d] = d < c->prm.dim ? nglobal[d] : 1;
+    if (g.n[d] < 1) return fail(c, KMPM_ERR_ARG, "empty grid");
+  }
+  g.cellsize = cellsize;
+  c->hgrids.push_back(g);
+  return (int)c->hgrids.size() - 1;
+}
+
+int kmpm_add_solid(kmpm_ctx *c, int grid, int mat, int n, const double *x0, const double *x, const double *v,
+                   const double *mass, const double *vol0, double T0) {
+  if (!c || n <= 0 || !x0 || !x || !v || !mass || !vol0) return KMPM_ERR_ARG;
+  if (c->built) return fail(c, KMPM_ERR_STATE, "solids must be added before the first run");
+  if (grid < 0 || grid >= (int)c->hgrids.size() || mat < 0 || mat >= (int)c->mats.size())
+    return fail(c, KMPM_ERR_ARG, "bad grid or material id");
+  if (c->TL())
+    for (auto &s : c->hsolids)
+      if (s.grid == grid) return fail(c, KMPM_ERR_ARG, "each TLMPM solid owns its grid");
+  kmpm_ctx::HSolid s;
+  s.grid = grid; s.mat = mat; s.n = n; s.T0 = T0;
+  s.x0.assign(x0, x0 + 3 * n); s.x.assign(x, x + 3 * n); s.v.assign(v, v + 3 * n);
+  s.mass.assign(mass, mass + n); s.vol0.assign(vol0, vol0 + n);
+  c->hsolids.push_back(std::move(s));
+  return (int)c->hsolids.size() - 1;
+}
+
+int kmpm_add_fix(kmpm_ctx *c, int kind, int grid, const unsigned char *node_mask, const int set[3], const double coef[12]) {
+  if (!c || !node_mask || !set || !coef) return KMPM_ERR_ARG;
+  if (kind != KMPM_FIX_VELOCITY_NODES && kind != KMPM_FIX_BODY_FORCE) return fail(c, KMPM_ERR_ARG, "unsupported fix");
+  if (grid < 0 || grid >= (int)c->hgrids.size()) return fail(c, KMPM_ERR_ARG, "bad grid id");
+  const auto &g = c->hgrids[grid];
+  kmpm_ctx::HFix f{};
+  f.kind = kind;
+  f.grid = grid;
+  for (int d = 0; d < 3; d++) f.set[d] = d < c->prm.dim ? set[d] : 0;
+  for (int k = 0; k < 12; k++) f.c[k] = coef[k];
+  if (kind == KMPM_FIX_BODY_FORCE)
+    for (int d = 0; d < 3; d++)
+      if (f.c[4 * d + 1] != 0 || f.c[4 * d + 2] != 0) return fail(c, KMPM_ERR_ARG, "body_force must be constant");
+  f.mask.assign(node_mask, node_mask + (size_t)g.n[0] * g.n[1] * g.n[2]);
+  c->hfixes.push_back(std::move(f));
+  c->fixes_dirty = true;
+  return (int)c->hfixes.size() - 1;
+}
+
+int kmpm_run(kmpm_ctx *c, int nsteps) {
+  if (!c || nsteps < 0) return KMPM_ERR_ARG;
+  int r = prepare(c);
+  if (r != KMPM_OK) return r;
+  for (int i = 0; i < nsteps; i++) CK(cudaGraphLaunch(c->gexec, c->st));
+  return check_error(c);
+}
+
+int kmpm_run_time(kmpm_ctx *c, double maxtime, int *nsteps_done) {
+  if (!c) return KMPM_ERR_ARG;
+  int r = prepare(c);
+  if (r != KMPM_OK) return r;
+  int done = 0;
+  StepScalars s{};
+  r = read_scalars(c, s);
+  if (r != KMPM_OK) return r;
+  // RunTime::command: loop while time < maxtime (src/run_time.cpp:30-60)
+  while (s.time < maxtime) {
+    double est = (maxtime - s.time) / s.dt;
+    int batch = (int)std::min(256.0, std::max(1.0, std::floor(0.5 * est)));
+    for (int i = 0; i < batch; i++) CK(cudaGraphLaunch(c->gexec, c->st));
+    done += batch;
+    r = check_error(c);
+    if (r != KMPM_OK) return r;
+    r = read_scalars(c, s);
+    if (r != KMPM_OK) return r;
+  }
+  if (nsteps_done) *nsteps_done = done;
+  return KMPM_OK;
+}
+
+int kmpm_scalars(kmpm_ctx *c, double *time, double *dt, long long *ntimestep) {
+  if (!c) return KMPM_ERR_ARG;
+  StepScalars s{};
+  if (c->built) {
+    int r = read_scalars(c, s);
+    if (r != KMPM_OK) return r;
+  } else {
+    s.dt = c->prm.dt;
+  }
+  if (time) *time = s.time;
+  if (dt) *dt = s.dt;
+  if (ntimestep) *ntimestep = s.ntimestep;
+  return KMPM_OK;
+}
+
+// Copies the rows of the listed fields for slots [start, start+n) of the
+// current particle buffer into H (H[f][slot - start]).
+static int fetch_rows(kmpm_ctx *c, const std::vector<int> &fields, int start, int n,
+                      std::vector<std::vector<float>> &H) {
+  CK(cudaStreamSynchronize(c->st));
+  float *cur = nullptr;
+  CK(cudaMemcpy(&cur, c->d_pp, sizeof(float *), cudaMemcpyDeviceToHost));
+  H.assign(PF_COUNT, std::vector<float>());
+  for (int f : fields) {
+    H[f].resize(n);
+    CK(cudaMemcpy(H[f].data(), cur + (size_t)f * c->ps + start, sizeof(float) * n, cudaMemcpyDeviceToHost));
+  }
+  return KMPM_OK;
+}
+
+// caller index and solid of every slot of the range holding `solid`
+static int slot_map(kmpm_ctx *c, const RangeDev &rg, std::vector<int> &orig, std::vector<int> &sid) {
+  if (c->TL() && !c->orig_cache.empty()) {
+    orig.assign(c->orig_cache.begin() + rg.start, c->orig_cache.begin() + rg.start + rg.count);
+    sid.assign(c->sid_cache.begin() + rg.start, c->sid_cache.begin() + rg.start + rg.count);
+    return KMPM_OK;
+  }
+  std::vector<std::vector<float>> H;
+  int r = fetch_rows(c, {PF_ORIG, PF_SID}, rg.start, rg.count, H);
+  if (r != KMPM_OK) return r;
+  orig.resize(rg.count);
+  sid.resize(rg.count);
+  std::memcpy(orig.data(), H[PF_ORIG].data(), sizeof(int) * rg.count);
+  std::memcpy(sid.data(), H[PF_SID].data(), sizeof(int) * rg.count);
+  if (c->TL()) {  // static order: cache it for the whole run
+    if (c->orig_cache.empty()) {
+      c->orig_cache.assign(c->ps, -1);
+      c->sid_cache.assign(c->ps, -1);
+    }
+    std::copy(orig.begin(), orig.end(), c->orig_cache.begin() + rg.start);
+    std::copy(sid.begin(), sid.end(), c->sid_cache.begin() + rg.start);
+    bool all = true;
+    for (auto &q : c->ranges) if (c->orig_cache[q.start] < 0) all = false;
+    if (!all) c->orig_cache.clear(), c->sid_cache.clear();
+  }
+  return KMPM_OK;
+}
+
+static std::vector<int> fields_for(kmpm_ctx *c, int field) {
+  switch (field) {
+    case KMPM_P_X: return c->TL() ? std::vector<int>{PF_X0, PF_X0 + 1, PF_X0 + 2, PF_X, PF_X + 1, PF_X + 2}
+                                  : std::vector<int>{PF_X0, PF_X0 + 1, PF_X0 + 2, PF_XN, PF_XN + 1, PF_XN + 2};
+    case KMPM_P_X0: return {PF_X0, PF_X0 + 1, PF_X0 + 2};
+    case KMPM_P_V: return {PF_V, PF_V + 1, PF_V + 2};
+    case KMPM_P_SIGMA: return {PF_SIG, PF_SIG + 1, PF_SIG + 2, PF_SIG + 3, PF_SIG + 4, PF_SIG + 5};
+    case KMPM_P_SIGMA_ROT: {
+      std::vector<int> f = {PF_SIG, PF_SIG + 1, PF_SIG + 2, PF_SIG + 3, PF_SIG + 4, PF_SIG + 5};
+      if (c->TL()) for (int k = 0; k < 9; k++) f.push_back(PF_H + k);
+      return f;
+    }
+    case KMPM_P_F: case KMPM_P_J: case KMPM_P_VOL: {
+      std::vector<int> f;
+      for (int k = 0; k < 9; k++) f.push_back(PF_H + k);
+      f.push_back(PF_VOL0);
+      return f;
+    }
+    case KMPM_P_EPS_P: return {PF_EPSP};
+    case KMPM_P_EPSDOT_P: return {PF_EPSDOT};
+    case KMPM_P_DAMAGE: return {PF_DMG};
+    case KMPM_P_DAMAGE_INIT: return {PF_DMGI};
+    case KMPM_P_T: return {PF_T};
+    case KMPM_P_STRAIN_EL: return {PF_STRAIN, PF_STRAIN + 1, PF_STRAIN + 2, PF_STRAIN + 3, PF_STRAIN + 4, PF_STRAIN + 5};
+    case KMPM_P_MASS: return {PF_MASS};
+    default: return {};
+  }
+}
+
+int kmpm_download_particles(kmpm_ctx *c, int solid, int field, double *out) {
+  if (!c || !out || solid < 0 || solid >= (int)c->hsolids.size()) return KMPM_ERR_ARG;
+  const auto &S = c->hsolids[solid];
+  if (!c->built) {
+    for (int i = 0; i < S.n; i++) {
+      if (field == KMPM_P_X) for (int d = 0; d < 3; d++) out[3 * i + d] = S.x[3 * i + d];
+      else if (field == KMPM_P_X0) for (int d = 0; d < 3; d++) out[3 * i + d] = S.x0[3 * i + d];
+      else if (field == KMPM_P_V) for (int d = 0; d < 3; d++) out[3 * i + d] = S.v[3 * i + d];
+      else return fail(c, KMPM_ERR_STATE, "field not available before the first run");
+    }
+    return KMPM_OK;
+  }
+  if (field == KMPM_P_STRAIN_EL && !c->prm.track_strain)
+    return fail(c, KMPM_ERR_STATE, "strain_el is tracked only with track_strain");
+  const std::vector<int> fl = fields_for(c, field);
+  if (fl.empty()) return fail(c, KMPM_ERR_ARG, "unknown particle field");
+  const RangeDev &rg = c->ranges[c->TL() ? c->solid_range[solid] : 0];
+  std::vector<int> orig, sid;
+  int r = slot_map(c, rg, orig, sid);
+  if (r != KMPM_OK) return r;
+  std::vector<std::vector<float>> H;
+  r = fetch_rows(c, fl, rg.start, rg.count, H);
+  if (r != KMPM_OK) return r;
+  const int base = c->solid_base[solid];
+  for (int q = 0; q < rg.count; q++) {
+    if (sid[q] != solid) continue;
+    const int i = orig[q] - base;
+    auto f = [&](int fld) { return (double)H[fld][q]; };
+    auto sym = [&](int b, double *m) {
+      const int map[9] = {0, 3, 4, 3, 1, 5, 4, 5, 2};
+      for (int k = 0; k < 9; k++) m[k] = f(b + map[k]);
+    };
+    switch (field) {
+      case KMPM_P_X:
+        for (int d = 0; d < 3; d++) out[3 * i + d] = f(PF_X0 + d) + (c->TL() ? f(PF_X + d) : f(PF_XN + d));
+        break;
+      case KMPM_P_X0:
+        for (int d = 0; d < 3; d++) out[3 * i + d] = f(PF_X0 + d);
+        break;
+      case KMPM_P_V:
+        for (int d = 0; d < 3; d++) out[3 * i + d] = f(PF_V + d);
+        break;
+      case KMPM_P_SIGMA:
+        sym(PF_SIG, out + 9 * i);
+        break;
+      case KMPM_P_SIGMA_ROT: {
+        double sg[9], F[9], R[9], RS[9];
+        sym(PF_SIG, sg);
+        if (!c->TL()) { for (int k = 0; k < 9; k++) out[9 * i + k] = sg[k]; break; }
+        for (int k = 0; k < 9; k++) F[k] = f(PF_H + k) + (k % 4 == 0 ? 1.0 : 0.0);
+        polar_host(F, R);
+        for (int a = 0; a < 3; a++)
+          for (int b = 0; b < 3; b++) RS[3 * a + b] = R[3 * a] * sg[b] + R[3 * a + 1] * sg[3 + b] + R[3 * a + 2] * sg[6 + b];
+        for (int a = 0; a < 3; a++)
+          for (int b = 0; b < 3; b++)
+            out[9 * i + 3 * a + b] = RS[3 * a] * R[3 * b] + RS[3 * a + 1] * R[3 * b + 1] + RS[3 * a + 2] * R[3 * b + 2];
+        break;
+      }
+      case KMPM_P_F:
+        for (int k = 0; k < 9; k++) out[9 * i + k] = f(PF_H + k) + (k % 4 == 0 ? 1.0 : 0.0);
+        break;
+      case KMPM_P_EPS_P: out[i] = f(PF_EPSP); break;
+      case KMPM_P_EPSDOT_P: out[i] = f(PF_EPSDOT); break;
+      case KMPM_P_DAMAGE: out[i] = f(PF_DMG); break;
+      case KMPM_P_DAMAGE_INIT: out[i] = f(PF_DMGI); break;
+      case KMPM_P_T: out[i] = f(PF_T); break;
+      case KMPM_P_J:
+      case KMPM_P_VOL: {
+        double Hd[9];
+        for (int k = 0; k < 9; k++) Hd[k] = f(PF_H + k);
+        double jm1 = (Hd[0] + Hd[4] + Hd[8]) +
+                     (Hd[0] * Hd[4] - Hd[1] * Hd[3] + Hd[0] * Hd[8] - Hd[2] * Hd[6] + Hd[4] * Hd[8] - Hd[5] * Hd[7]) +
+                     (Hd[0] * (Hd[4] * Hd[8] - Hd[5] * Hd[7]) - Hd[1] * (Hd[3] * Hd[8] - Hd[5] * Hd[6]) +
+                      Hd[2] * (Hd[3] * Hd[7] - Hd[4] * Hd[6]));
+        out[i] = field == KMPM_P_J ? 1.0 + jm1 : (1.0 + jm1) * f(PF_VOL0);
+        break;
+      }
+      case KMPM_P_STRAIN_EL: sym(PF_STRAIN, out + 9 * i); break;
+      case KMPM_P_MASS: out[i] = f(PF_MASS); break;
+    }
+  }
+  return KMPM_OK;
+}
+
+int kmpm_upload_particles(kmpm_ctx *c, int solid, int field, const double *in) {
+  if (!c || !in || solid < 0 || solid >= (int)c->hsolids.size()) return KMPM_ERR_ARG;
+  if (field != KMPM_P_V) return fail(c, KMPM_ERR_ARG, "only velocities can be uploaded");
+  auto &S = c->hsolids[solid];
+  if (!c->built) {
+    for (int k = 0; k < 3 * S.n; k++) S.v[k] = in[k];
+    return KMPM_OK;
+  }
+  const RangeDev &rg = c->ranges[c->TL() ? c->solid_range[solid] : 0];
+  std::vector<int> orig, sid;
+  int r = slot_map(c, rg, orig, sid);
+  if (r != KMPM_OK) return r;
+  std::vector<std::vector<float>> H;
+  r = fetch_rows(c, {PF_V, PF_V + 1, PF_V + 2}, rg.start, rg.count, H);
+  if (r != KMPM_OK) return r;
+  for (int q = 0; q < rg.count; q++) {
+    if (sid[q] != solid) continue;
+    const int i = orig[q] - c->solid_base[solid];
+    for (int d = 0; d < 3; d++) H[PF_V + d][q] = (float)in[3 * i + d];
+  }
+  float *cur = nullptr;
+  CK(cudaMemcpy(&cur, c->d_pp, sizeof(float *), cudaMemcpyDeviceToHost));
+  for (int d = 0; d < 3; d++)
+    CK(cudaMemcpy(cur + (size_t)(PF_V + d) * c->ps + rg.start, H[PF_V + d].data(), sizeof(float) * rg.count,
+                  cudaMemcpyHostToDevice));
+  return KMPM_OK;
+}
+
+int kmpm_download_grid(kmpm_ctx *c, int grid, int field, double *out) {
+  if (!c || !out || grid < 0 || grid >= (int)c->hgrids.size()) return KMPM_ERR_ARG;
+  if (!c->built) return fail(c, KMPM_ERR_STATE, "no grid state before the first run");
+  CK(cudaStreamSynchronize(c->st));
+  const GridDev &g = c->grids[grid];
+  const int nn = g.n[0] * g.n[1] * g.n[2];
+  std::vector<float4> A(nn), B(nn);
+  std::vector<float> Tn(nn);
+  if (field == KMPM_G_MASS || field == KMPM_G_V) CK(cudaMemcpy(A.data(), c->nodeA + g.node_off, sizeof(float4) * nn, cudaMemcpyDeviceToHost));
+  else if (field == KMPM_G_V_UPDATE) CK(cudaMemcpy(A.data(), c->nodeB + g.node_off, sizeof(float4) * nn, cudaMemcpyDeviceToHost));
+  else if (field == KMPM_G_X) CK(cudaMemcpy(A.data(), c->nodeX + g.node_off, sizeof(float4) * nn, cudaMemcpyDeviceToHost));
+  else if (field == KMPM_G_T) CK(cudaMemcpy(Tn.data(), c->nodeT + g.node_off, sizeof(float) * nn, cudaMemcpyDeviceToHost));
+  else return fail(c, KMPM_ERR_ARG, "unknown grid field");
+  for (int i = 0; i < nn; i++) {
+    if (field == KMPM_G_MASS) out[i] = A[i].w;
+    else if (field == KMPM_G_T) out[i] = Tn[i];
+    else { out[3 * i] = A[i].x; out[3 * i + 1] = A[i].y; out[3 * i + 2] = A[i].z; }
+  }
+  return KMPM_OK;
+}
+
+int kmpm_energy(kmpm_ctx *c, double out[2]) {
+  if (!c || !out) return KMPM_ERR_ARG;
+  if (!c->built) return fail(c, KMPM_ERR_STATE, "no state before the first run");
+  PartArgs pa = part_args(c);
+  launch_energy(pa, c->nblk_p, c->d_eblk, c->d_eout, c->st);
+  CK(cudaMemcpyAsync(out, c->d_eout, 2 * sizeof(double), cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  return KMPM_OK;
+}
+
+void *kmpm_stream(kmpm_ctx *c) { return c ? (void *)c->st : nullptr; }
+
+int kmpm_profile(kmpm_ctx *c, int nsteps, double *phase_ms, int max_phases, int *nphases) {
+  if (!c || nsteps <= 0 || !phase_ms || !nphases) return KMPM_ERR_ARG;
+  int r = prepare(c);
+  if (r != KMPM_OK) return r;
+  std::vector<double> acc;
+  for (int s = 0; s < nsteps; s++) {
+    c->profiling = true;
+    c->prof_n = 0;
+    r = enqueue_step(c);
+    c->profiling = false;
+    if (r != KMPM_OK) return r;
+    CK(cudaStreamSynchronize(c->st));
+    acc.resize(std::max<size_t>(acc.size(), c->prof_n), 0.0);
+    for (int k = 1; k < c->prof_n; k++) {
+      float ms = 0.f;
+      CK(cudaEventElapsedTime(&ms, c->prof_ev[k - 1], c->prof_ev[k]));
+      acc[k - 1] += ms;
+    }
+  }
+  const int n = std::min(c->prof_n - 1, max_phases);
+  for (int k = 0; k < n; k++) phase_ms[k] = acc[k] / nsteps;
+  *nphases = n;
+  return check_error(c);
+}
+
+const char *kmpm_profile_phase(kmpm_ctx *c, int i) {
+  if (!c || i < 0 || i + 1 >= (int)c->prof_names.size()) return "";
+  return c->prof_names[i + 1].c_str();
+}
+
+int kmpm_launches_per_step(kmpm_ctx *c) { return c ? c->launches_per_step : 0; }
+
+}  // extern "C"

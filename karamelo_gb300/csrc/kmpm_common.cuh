@@ -1,0 +1,486 @@
+// kmpm_common.cuh -- data layout and device helpers shared by the kernels.
+//
+// Layout in HBM (one context):
+//   particles: one FP32 structure of arrays, field f of particle p at
+//              P[f * pstride + p]; each solid's particles are contiguous,
+//              sorted by (tile, cell) of their reference (TL) or current (UL)
+//              position, and padded to a multiple of 256 so that every
+//              256-thread block of a particle kernel belongs to one solid;
+//   nodes:     float4 A = (v, mass) and float4 B = (v_update, T_update) per
+//              node, grids concatenated and padded to multiples of 256;
+//   tiles:     a grid's cells are grouped in tiles of T^dim cells; the
+//              scatter kernel writes each tile's footprint (the nodes its
+//              particles touch) to its own slice of a partial buffer, and the
+//              grid kernel adds the (at most 2^dim) slices covering a node in a
+//              fixed order, so P2G is bit-reproducible without float atomics.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace kmpm {
+
+// ------------------------------------------------------------------ fields
+enum PField : int {
+  PF_X0 = 0,        // 3
+  PF_X = 3,         // 3: displacement x - x0 (weights of ULMPM use x0 + PF_X)
+  PF_V = 6,         // 3
+  PF_MASS = 9,
+  PF_VOL0 = 10,
+  PF_H = 11,        // 9: F - I (row-major)
+  PF_SIG = 20,      // 6: xx yy zz xy xz yz
+  PF_EPSP = 26,
+  PF_EPSDOT = 27,
+  PF_DMG = 28,
+  PF_DMGI = 29,
+  PF_T = 30,
+  PF_GAMMA = 31,
+  PF_Q = 32,        // 3
+  PF_PK = 35,       // 9: TL vol0*PK1 (row-major) ; UL vol*sigma (first 6, sym order)
+  PF_STRAIN = 44,   // 6: strain_el (sym order)
+  PF_XN = 50,       // 3: ULMPM displacement after this step's move (weights use PF_X)
+  PF_ORIG = 53,     // caller index (int bits)
+  PF_SID = 54,      // solid id (int bits), ULMPM only
+  PF_COUNT = 55
+};
+
+// symmetric storage order: xx yy zz xy xz yz
+__host__ __device__ inline int sym_index(int i, int j) {
+  if (i == j) return i;
+  int a = i < j ? i : j, b = i < j ? j : i;
+  return a == 0 ? (b == 1 ? 3 : 4) : 5;
+}
+
+// ------------------------------------------------------------------ tables
+struct GridDev {
+  int n[3];          // local node counts (Grid::nx, ny, nz)
+  int ng[3];         // global node counts (ntype of the boundary-modified cubic)
+  int ncell[3];      // cells per dim
+  int ntile[3];      // tiles per dim
+  int node_off;      // first node in the global node arrays
+  int tile_off;      // first tile in the global tile arrays
+  int cell_off;      // first cell in the global cell arrays
+  int solid0;        // first solid using this grid (for per-solid scalars)
+  float lo[3];       // lower bound of the lattice
+  float inv_cellsize;
+  float cellsize;
+};
+
+// A contiguous particle range that shares one grid: one per solid for TLMPM,
+// one for all solids for ULMPM (whose particles are binned together).
+struct RangeDev {
+  int start, count;  // particle range in the global arrays
+  int grid;
+  int mat;           // material id, or -1: per particle through PF_SID
+  int blk0, nblk;    // 256-particle blocks of this range
+};
+
+// Material in device form (Mat, src/material.h:45-68, and its laws)
+struct MatDev {
+  int type, eos, strength, damage, temp;
+  double rho0, K, G, lambda, signal_velocity, cp, invcp, kappa;
+  double eos_p[12], str_p[12], dam_p[8], temp_p[6];
+};
+
+// Per-solid time-step scalars kept on the device so a captured step replays.
+struct StepScalars {
+  double dt, time;
+  long long ntimestep;
+  double dtCFL;
+};
+
+// A node fix (velocity_nodes / body_force) in device form.
+struct FixDev {
+  int kind, grid, set[3];
+  double c[3][4];
+  const uint8_t *mask;  // node mask of that grid (local node index)
+};
+
+enum ErrCode : int {
+  ERR_NONE = 0,
+  ERR_J = 10,
+  ERR_LEFT = 11,
+  ERR_NAN = 12,
+  ERR_POLDEC = 13,
+  ERR_DTCFL = 14,
+};
+struct ErrState {
+  int code;
+  int particle;
+  long long step;
+};
+
+// ------------------------------------------------------------------ stencils
+// Node stencil of a particle whose base cell index is c along one axis:
+// nodes c*SC - LO + s for s in [0, S).  Linear (src/tlmpm.cpp:141-175): c,c+1.
+// Cubic (src/tlmpm.cpp:209-245): c-1..c+2.  Bernstein (src/tlmpm.cpp:176-208):
+// fine nodes 2c..2c+2 of the h/2 lattice.  Cells of the same colour
+// (index mod C in every axis) have disjoint stencils.
+template <int BASIS> struct Stencil;
+template <> struct Stencil<0> { static constexpr int S = 2, LO = 0, SC = 1, C = 2; };
+template <> struct Stencil<1> { static constexpr int S = 4, LO = 1, SC = 1, C = 4; };
+template <> struct Stencil<2> { static constexpr int S = 3, LO = 0, SC = 2, C = 2; };
+
+template <int DIM, int BASIS> struct TileShape {
+  // cells per tile edge
+  static constexpr int T = DIM == 3 ? (BASIS == 2 ? 4 : 8) : (DIM == 2 ? (BASIS == 2 ? 8 : 16) : 64);
+  static constexpr int S = Stencil<BASIS>::S;
+  static constexpr int W = (T - 1) * Stencil<BASIS>::SC + S;  // footprint nodes per edge
+  static constexpr int NS = DIM == 3 ? S * S * S : (DIM == 2 ? S * S : S);
+  static constexpr int NW = DIM == 3 ? W * W * W : (DIM == 2 ? W * W : W);
+  static constexpr int NCELL = DIM == 3 ? T * T * T : (DIM == 2 ? T * T : T);
+};
+
+__host__ __device__ inline int tile_edge(int dim, int basis) {
+  return dim == 3 ? (basis == 2 ? 4 : 8) : (dim == 2 ? (basis == 2 ? 8 : 16) : 64);
+}
+__host__ __device__ inline int stencil_width(int basis) { return basis == 0 ? 2 : (basis == 1 ? 4 : 3); }
+__host__ __device__ inline int stencil_lo(int basis) { return basis == 1 ? 1 : 0; }
+__host__ __device__ inline int stencil_sc(int basis) { return basis == 2 ? 2 : 1; }
+
+// ntype of a node along one axis (Grid::init, src/grid.cpp:228-240)
+template <int BASIS> __device__ __forceinline__ int node_type(int i, int ng) {
+  if (BASIS == 1) return min(2, i) - min(ng - 1 - i, 2);
+  if (BASIS == 2) return i & 1;
+  return 0;
+}
+
+// ------------------------------------------------------------------ basis
+// BasisFunction::*, src/basis_functions.h:21-138, in FP32.  Value and
+// derivative (already multiplied by 1/cellsize).
+template <int BASIS> __device__ __forceinline__ void basis(float r, int nt, float ih, float &s, float &ds);
+
+template <> __device__ __forceinline__ void basis<0>(float r, int, float ih, float &s, float &ds) {
+  float a = fabsf(r);
+  s = a >= 1.f ? 0.f : 1.f - a;
+  ds = (r >= 1.f || r <= -1.f || r == 0.f) ? 0.f : (r > 0.f ? -ih : ih);
+}
+
+template <> __device__ __forceinline__ void basis<1>(float r, int nt, float ih, float &s, float &ds) {
+  if (r >= 1.f && r < 2.f) {
+    if (nt == 1) { s = 0.f; ds = -ih; }
+    else { s = ((-1.f / 6.f * r + 1.f) * r - 2.f) * r + 4.f / 3.f; ds = ih * ((-0.5f * r + 2.f) * r - 2.f); }
+  } else if (r >= 0.f && r < 1.f) {
+    if (nt == -2) { s = (1.f / 6.f * r * r - 1.f) * r + 1.f; ds = ih * (0.5f * r * r - 1.f); }
+    else if (nt == 2) { s = 1.f; ds = ih; }
+    else if (nt == 1) { s = (1.f / 3.f * r - 1.f) * r * r + 2.f / 3.f; ds = ih * r * (r - 2.f); }
+    else { s = (0.5f * r - 1.f) * r * r + 2.f / 3.f; ds = ih * (1.5f * r - 2.f) * r; }
+  } else if (r >= -1.f && r < 0.f) {
+    if (nt == 2) { s = (-1.f / 6.f * r * r + 1.f) * r + 1.f; ds = ih * (-0.5f * r * r + 1.f); }
+    else if (nt == -1) { s = (-1.f / 3.f * r - 1.f) * r * r + 2.f / 3.f; ds = ih * (-r - 2.f) * r; }
+    else { s = (-0.5f * r - 1.f) * r * r + 2.f / 3.f; ds = ih * (-1.5f * r - 2.f) * r; }
+  } else if (r >= -2.f && r < -1.f) {
+    s = ((1.f / 6.f * r + 1.f) * r + 2.f) * r + 4.f / 3.f;
+    ds = ih * ((0.5f * r + 2.f) * r + 2.f);
+  } else {
+    s = 0.f; ds = 0.f;
+  }
+}
+
+template <> __device__ __forceinline__ void basis<2>(float r, int nt, float ih, float &s, float &ds) {
+  float a = fabsf(r);
+  if (a >= 1.f) { s = 0.f; ds = 0.f; return; }
+  if (nt == 1) {
+    s = a >= 0.5f ? 0.f : 0.5f - 2.f * r * r;
+    ds = a > 0.5f ? 0.f : -4.f * r * ih;
+  } else {
+    s = (1.f - a) * (1.f - a);
+    ds = r > 0.f ? -2.f * (1.f - r) * ih : 2.f * (1.f + r) * ih;
+  }
+}
+
+// Per-axis stencil values of one particle: base node index i0 and, for each
+// stencil slot s, the basis value and derivative (0 where the node is absent).
+template <int BASIS> struct Axis {
+  static constexpr int S = Stencil<BASIS>::S;
+  int i0;
+  float s[S], ds[S];
+  __device__ __forceinline__ void eval(float xp, float lo, float ih, float h, int n, int ng) {
+    // the reference truncates (src/tlmpm.cpp:145); the clamp keeps indices of a
+    // non-finite or far-away position in range (such a particle raises an error)
+    float t = fminf(fmaxf((xp - lo) * ih, -4.f), (float)(n + 4));
+    int c = (int)t;
+    i0 = c * Stencil<BASIS>::SC - Stencil<BASIS>::LO;
+#pragma unroll
+    for (int k = 0; k < S; k++) {
+      int i = i0 + k;
+      if (i < 0 || i >= n) { s[k] = 0.f; ds[k] = 0.f; continue; }
+      float xn = lo + (float)i * h;
+      float r = (xp - xn) * ih;
+      basis<BASIS>(r, node_type<BASIS>(i, ng), ih, s[k], ds[k]);
+    }
+  }
+  // 1-D (unused axis): weight 1, gradient 0, single slot at node 0
+  __device__ __forceinline__ void unit() {
+    i0 = 0;
+#pragma unroll
+    for (int k = 0; k < S; k++) { s[k] = k == 0 ? 1.f : 0.f; ds[k] = 0.f; }
+  }
+};
+
+// ------------------------------------------------------------------ 3x3
+struct f3x3 { float a[9]; };
+__device__ __forceinline__ float det3(const float *m) {
+  return m[0] * (m[4] * m[8] - m[5] * m[7]) - m[1] * (m[3] * m[8] - m[5] * m[6]) + m[2] * (m[3] * m[7] - m[4] * m[6]);
+}
+// cofactor matrix: cof(M) = det(M) M^{-T}
+__device__ __forceinline__ void cof3(const float *m, float *c) {
+  c[0] = m[4] * m[8] - m[5] * m[7];
+  c[1] = m[5] * m[6] - m[3] * m[8];
+  c[2] = m[3] * m[7] - m[4] * m[6];
+  c[3] = m[2] * m[7] - m[1] * m[8];
+  c[4] = m[0] * m[8] - m[2] * m[6];
+  c[5] = m[1] * m[6] - m[0] * m[7];
+  c[6] = m[1] * m[5] - m[2] * m[4];
+  c[7] = m[2] * m[3] - m[0] * m[5];
+  c[8] = m[0] * m[4] - m[1] * m[3];
+}
+__device__ __forceinline__ double det3d(const double *m) {
+  return m[0] * (m[4] * m[8] - m[5] * m[7]) - m[1] * (m[3] * m[8] - m[5] * m[6]) + m[2] * (m[3] * m[7] - m[4] * m[6]);
+}
+__device__ __forceinline__ void cof3d(const double *m, double *c) {
+  c[0] = m[4] * m[8] - m[5] * m[7];
+  c[1] = m[5] * m[6] - m[3] * m[8];
+  c[2] = m[3] * m[7] - m[4] * m[6];
+  c[3] = m[2] * m[7] - m[1] * m[8];
+  c[4] = m[0] * m[8] - m[2] * m[6];
+  c[5] = m[1] * m[6] - m[0] * m[7];
+  c[6] = m[1] * m[5] - m[2] * m[4];
+  c[7] = m[2] * m[3] - m[0] * m[5];
+  c[8] = m[0] * m[4] - m[1] * m[3];
+}
+__device__ __forceinline__ void matmul3(const float *a, const float *b, float *c) {
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int j = 0; j < 3; j++) c[3 * i + j] = a[3 * i] * b[j] + a[3 * i + 1] * b[3 + j] + a[3 * i + 2] * b[6 + j];
+}
+// c = a^T b
+__device__ __forceinline__ void matTmul3(const float *a, const float *b, float *c) {
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int j = 0; j < 3; j++) c[3 * i + j] = a[i] * b[j] + a[3 + i] * b[3 + j] + a[6 + i] * b[6 + j];
+}
+// c = a b^T
+__device__ __forceinline__ void matmulT3(const float *a, const float *b, float *c) {
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int j = 0; j < 3; j++) c[3 * i + j] = a[3 * i] * b[3 * j] + a[3 * i + 1] * b[3 * j + 1] + a[3 * i + 2] * b[3 * j + 2];
+}
+
+// det(I + H) - 1 without cancellation: tr H + (sum of principal 2x2 minors) + det H
+__device__ __forceinline__ float jm1_of_H(const float *H) {
+  float tr = H[0] + H[4] + H[8];
+  float m2 = H[0] * H[4] - H[1] * H[3] + H[0] * H[8] - H[2] * H[6] + H[4] * H[8] - H[5] * H[7];
+  return tr + m2 + det3(H);
+}
+
+// Rotation factor of the polar decomposition F = R U (MPM_Math::PolDec,
+// src/mpm_math.h:104-133) by the scaled Newton iteration of N. J. Higham,
+// "Computing the polar decomposition -- with applications", SIAM J. Sci.
+// Stat. Comput. 7 (1986): X <- (g X + X^-T / g)/2 with g = |det X|^(-1/3).
+// For det F > 0 the limit is the unique proper rotation, which is what the
+// reference's SVD route returns.  Returns false if det F <= 0.
+__device__ inline bool polar_rotation(const float *F, float *R) {
+  float X[9], C[9];
+#pragma unroll
+  for (int k = 0; k < 9; k++) X[k] = F[k];
+  float d = det3(X);
+  if (!(d > 0.f)) return false;
+  for (int it = 0; it < 12; it++) {
+    cof3(X, C);
+    float dx = det3(X);
+    float g = cbrtf(1.f / fabsf(dx));   // scaling (Higham 1986, sec. 3)
+    float gi = 1.f / (g * dx);         // X^-T / g = C / (g det X)
+    float diff = 0.f;
+#pragma unroll
+    for (int k = 0; k < 9; k++) {
+      float xn = 0.5f * (g * X[k] + gi * C[k]);
+      float e = xn - X[k];
+      diff += e * e;
+      X[k] = xn;
+    }
+    if (diff < 1e-14f) break;
+  }
+#pragma unroll
+  for (int k = 0; k < 9; k++) R[k] = X[k];
+  return true;
+}
+
+// Real parts of the eigenvalues of F = I + H (the reference calls
+// Eigen::EigenSolver, src/solid.cpp:1401-1409): the characteristic cubic of H
+// solved in closed form (trigonometric form for three real roots, Cardano
+// otherwise), shifted by 1.  Returns min |Re lambda|.
+__device__ inline float min_abs_eig_real(const float *H) {
+  float a2 = H[0] + H[4] + H[8];
+  float a1 = H[0] * H[4] - H[1] * H[3] + H[0] * H[8] - H[2] * H[6] + H[4] * H[8] - H[5] * H[7];
+  float a0 = det3(H);
+  // mu^3 - a2 mu^2 + a1 mu - a0 = 0 ; mu = t + a2/3
+  float p = a1 - a2 * a2 / 3.f;
+  float q = -2.f * a2 * a2 * a2 / 27.f + a2 * a1 / 3.f - a0;
+  float sh = a2 / 3.f;
+  float disc = q * q / 4.f + p * p * p / 27.f;
+  float m;
+  if (disc <= 0.f) {
+    float r = sqrtf(fmaxf(-p / 3.f, 0.f));
+    float arg = r > 0.f ? (-q / 2.f) / (r * r * r) : 0.f;
+    arg = fminf(1.f, fmaxf(-1.f, arg));
+    float phi = acosf(arg);
+    float e0 = 1.f + sh + 2.f * r * cosf(phi / 3.f);
+    float e1 = 1.f + sh + 2.f * r * cosf((phi + 2.f * 3.14159265358979f) / 3.f);
+    float e2 = 1.f + sh + 2.f * r * cosf((phi + 4.f * 3.14159265358979f) / 3.f);
+    m = fminf(fabsf(e0), fminf(fabsf(e1), fabsf(e2)));
+  } else {
+    float sd = sqrtf(disc);
+    float u = cbrtf(-q / 2.f + sd), v = cbrtf(-q / 2.f - sd);
+    float mu = u + v + sh;
+    float e_real = 1.f + mu;
+    float e_pair = 1.f + (a2 - mu) / 2.f;
+    m = fminf(fabsf(e_real), fabsf(e_pair));
+  }
+  return m;
+}
+
+// ------------------------------------------------------------------ constitutive
+// The reference's truncated constants (src/solid.cpp:39-40, src/strength_jc.cpp:29)
+#define KMPM_SQRT_3_OVER_2 1.224744871
+#define KMPM_FOUR_THIRD 1.333333333333333333333333333333333333333
+
+// Symmetric 3x3 in storage order xx yy zz xy xz yz
+template <typename T> struct Sym {
+  T a[6];
+  __device__ __forceinline__ T tr() const { return a[0] + a[1] + a[2]; }
+  __device__ __forceinline__ T norm() const {  // Frobenius norm of the full matrix
+    return sqrt(a[0] * a[0] + a[1] * a[1] + a[2] * a[2] + T(2) * (a[3] * a[3] + a[4] * a[4] + a[5] * a[5]));
+  }
+  __device__ __forceinline__ void dev() {
+    T t = tr() / T(3);
+    a[0] -= t; a[1] -= t; a[2] -= t;
+  }
+};
+
+struct ConstitutiveIn {
+  float J, Jm1, rho, cellsize;
+};
+
+// EOS::compute_pressure (src/eos_linear.cpp:71-74, src/eos_shock.cpp:99-133,
+// src/eos_fluid.cpp:68-73); T is the particle temperature or 0.
+template <typename R>
+__device__ inline R eos_pressure(const MatDev &m, R J, R Jm1, R rho, R damage, R trD, R cellsize, R T) {
+  if (m.eos == 0) return -R(m.eos_p[1]) * Jm1 * (R(1) - damage);
+  // rho/rho0 = 1/J; the compressions below are written in J - 1 so that FP32
+  // keeps them accurate when J is close to 1 (no 1/J - 1 cancellation)
+  if (m.eos == 2) {  // K ((rho/rho0)^gamma - 1) = K expm1(-gamma log1p(J-1))
+    return R(m.eos_p[1]) * expm1(-R(m.eos_p[2]) * log1p(Jm1));
+  }
+  R rho0 = m.eos_p[0], c0 = m.eos_p[2], S = m.eos_p[3], Gamma = m.eos_p[4], cv = m.eos_p[5], Tr = m.eos_p[6];
+  R Q1 = m.eos_p[7], Q2 = m.eos_p[8];
+  R mu = -Jm1 / J;  // rho/rho0 - 1
+  R dd = R(1) - (S - R(1)) * mu;
+  R pH = rho0 * c0 * c0 * mu * (R(1) + mu) / (dd * dd);
+  R e = T > Tr ? cv * rho0 * (T - Tr) : R(0);
+  R pF = pH + Gamma * e;
+  if (damage > R(0) && pF < R(0)) pF = damage >= R(1) ? R(0) : pF * (R(1) - damage);
+  if ((Q1 != R(0) || Q2 != R(0)) && trD < R(0))
+    pF += rho * cellsize * (Q1 * cellsize * trD * trD - Q2 * c0 * sqrt(J) * trD);
+  return pF;
+}
+
+// Strength::update_deviatoric_stress (src/strength_linear.cpp:59-71,
+// src/strength_plastic.cpp:62-115, src/strength_jc.cpp:100-184,
+// src/strength_swift.cpp:77-147, src/strength_fluid.cpp:46-58).
+// sig: current sigma (full, symmetric storage), D: rate of deformation.
+template <typename R>
+__device__ inline Sym<R> strength_update(const MatDev &m, R dt, const Sym<R> &sig, const Sym<R> &D, R &dep, R epsp,
+                                         R epsdot, R damage, R T) {
+  Sym<R> out;
+  dep = R(0);
+  const double *p = m.str_p;
+  if (m.strength == 0) {  // linear: dev(sigma) + dt 2G(1-D) dev(D)
+    Sym<R> s = sig, d = D;
+    s.dev(); d.dev();
+    R f = dt * R(2) * R(p[0]) * (R(1) - damage);
+#pragma unroll
+    for (int k = 0; k < 6; k++) out.a[k] = s.a[k] + f * d.a[k];
+    return out;
+  }
+  if (m.strength == 4) {  // fluid: 2 mu dev(D)
+    Sym<R> d = D;
+    d.dev();
+#pragma unroll
+    for (int k = 0; k < 6; k++) out.a[k] = R(2) * R(p[0]) * d.a[k];
+    return out;
+  }
+  if (m.strength == 1) {  // perfect plasticity
+    R Gd = R(p[0]) * (R(1) - damage), syD = R(p[1]) * (R(1) - damage);
+    Sym<R> s = sig, d = D;
+    s.dev(); d.dev();
+#pragma unroll
+    for (int k = 0; k < 6; k++) out.a[k] = s.a[k] + dt * R(2) * Gd * d.a[k];
+    R J2 = sqrt(R(1.5)) * out.norm();
+    if (J2 < syD) return out;
+    dep = (J2 - syD) / (R(3) * Gd);
+    R sc = syD / J2;
+#pragma unroll
+    for (int k = 0; k < 6; k++) out.a[k] *= sc;
+    return out;
+  }
+  // Johnson-Cook (2) and Swift (3): closed-form radial return
+  if (damage >= R(1)) {
+#pragma unroll
+    for (int k = 0; k < 6; k++) out.a[k] = R(0);
+    return out;
+  }
+  R G = p[0], ys;
+  if (m.strength == 2) {
+    R A = p[1], B = p[2], n = p[3], epsdot0 = p[4], C = p[5], mm = p[6], Tr = p[7], Tm = p[8];
+    R ratio = epsdot / epsdot0;
+    ratio = ratio > R(1) ? ratio : R(1);
+    ys = epsp < R(1.0e-10) ? A : A + B * pow(epsp, n);
+    if (C != R(0)) ys *= pow(R(1) + ratio, C);
+    if (T < Tm) {
+      if (mm != R(0) && T >= Tr) ys *= R(1) - pow((T - Tr) / (Tm - Tr), mm);
+    } else {
+      ys = R(0);
+    }
+  } else {
+    R A = p[1], B = p[2], C = p[3], n = p[4];
+    ys = (epsp > R(1.0e-10) && epsp > C) ? A + B * pow(epsp - C, n) : A;
+  }
+  R Gd = G;
+  if (damage > R(0)) { Gd *= (R(1) - damage); ys *= (R(1) - damage); }
+  R f = dt * R(2) * Gd;
+#pragma unroll
+  for (int k = 0; k < 6; k++) out.a[k] = sig.a[k] + f * D.a[k];
+  out.dev();
+  R J2 = R(KMPM_SQRT_3_OVER_2) * out.norm();
+  if (J2 < ys) return out;
+  dep = (J2 - ys) / (R(3) * Gd);
+  R sc = ys / J2;
+#pragma unroll
+  for (int k = 0; k < 6; k++) out.a[k] *= sc;
+  return out;
+}
+
+// DamageJohnsonCook::compute_damage, src/damage_jc.cpp:91-143
+template <typename R>
+__device__ inline void damage_update(const MatDev &m, R &dinit, R &damage, R pH, const Sym<R> &sdev, R epsdot, R dep,
+                                     R T) {
+  const double *p = m.dam_p;
+  if (dep == R(0) && damage >= R(1)) return;
+  R vm = R(KMPM_SQRT_3_OVER_2) * sdev.norm();
+  R triax = R(0);
+  if (pH != R(0) && vm != R(0)) triax = -pH / (vm + R(0.001) * fabs(pH));
+  if (triax <= R(-3)) { dinit = R(0); return; }
+  R ef = R(p[0]) + R(p[1]) * exp(R(p[2]) * triax);
+  if (R(p[3]) > R(0) && epsdot > R(p[5])) ef *= (R(1) + R(p[3]) * log(epsdot / R(p[5])));
+  if (R(p[4]) > R(0) && T >= R(p[6])) ef *= R(1) + R(p[4]) * (T - R(p[6])) / (R(p[7]) - R(p[6]));
+  dinit += dep / ef;
+  if (dinit >= R(1)) {
+    R dn = (dinit - R(1)) * R(10);
+    damage = dn < R(1) ? dn : R(1);
+  }
+}
+
+}  // namespace kmpm

@@ -1,0 +1,169 @@
+// kmpm_kernels.cuh -- kernel argument blocks and the per-mode scatter payloads.
+#pragma once
+#include "kmpm_common.cuh"
+
+namespace kmpm {
+
+// scatter modes
+enum P2GMode : int {
+  P2G_MASS = 0,  // m                      (TLMPM: once, Solid::compute_mass_nodes)
+  P2G_TL = 1,    // p, f_int (TL)          (+ mT, Qext, Qint when thermal)
+  P2G_UL = 2,    // m, p, f_int (UL)       (+ mT, Qext, Qint)
+  P2G_VEL = 3,   // p                      (MUSL re-map; + mT)
+};
+enum GridMode : int { GM_MASS = 0, GM_UPDATE = 1, GM_VEL = 2 };
+
+__host__ __device__ constexpr int p2g_nq(int mode, bool th) {
+  return mode == P2G_MASS ? 1 : mode == P2G_TL ? (th ? 9 : 6) : mode == P2G_UL ? (th ? 10 : 7) : (th ? 4 : 3);
+}
+__host__ __device__ constexpr int p2g_nin(int mode, bool th) {
+  return mode == P2G_MASS ? 1 : mode == P2G_TL ? (th ? 17 : 12) : mode == P2G_UL ? (th ? 15 : 10) : (th ? 4 : 3);
+}
+
+struct P2GArgs {
+  float *const *Pp;          // device pointer to the current particle buffer
+  size_t ps;                 // particle field stride
+  int pos_field;             // PF_X0 (TL) or PF_X (UL)
+  const int2 *tiles;         // (grid, tile) of every non-empty tile
+  const GridDev *grids;
+  const int *cell_start, *cell_end;  // particle range of every cell (sorted order)
+  float *partial;            // tile footprint slices
+  size_t pstride_tile;       // floats per tile slice
+  const int *tile_start, *tile_end;  // particle range of every tile (empty tiles are skipped)
+};
+
+struct GridArgs {
+  const GridDev *grids;
+  const int *blk_grid, *grid_blk0;
+  const float *partial;
+  size_t pstride_tile;
+  const int *tile_start, *tile_end;
+  float4 *nodeA, *nodeB, *nodeX;
+  float *nodeT;
+  const FixDev *fixes;
+  const int *fix_start, *fix_count;
+  StepScalars *scalars;
+  int indep;                 // per-solid clocks (independent instances)
+  int remap;                 // GM_VEL: MUSL re-map (else positions only)
+};
+
+struct PartArgs {
+  float *const *Pp;
+  size_t ps;
+  const RangeDev *ranges;
+  const int *blk_range;
+  const int *solid_mat;      // solid id -> material id (ULMPM per-particle lookup)
+  const GridDev *grids;
+  const MatDev *mats;
+  const float4 *nodeA, *nodeB;
+  const float *nodeT;
+  StepScalars *scalars;
+  ErrState *err;
+  float *blk_c, *blk_h;
+  float pic_flip;
+  float boxlo[3], boxhi[3];
+  int indep, use_vu, thermal, track_strain, dim, tile_T;
+};
+
+struct DtArgs {
+  const RangeDev *ranges;
+  const GridDev *grids;
+  const float *blk_c, *blk_h;
+  double *solid_dtcfl;
+  StepScalars *scalars;
+  ErrState *err;
+  int nranges, indep, dt_constant;
+  double dt_factor;
+};
+
+struct LaunchSet {
+  int dummy;
+};
+
+// kernel entry points of one (dim, basis) instantiation
+struct StepKernels {
+  void *p2g_mass, *p2g_tl, *p2g_tl_th, *p2g_ul, *p2g_ul_th, *p2g_vel, *p2g_vel_th;
+  void *grid_mass, *grid_upd[2][2], *grid_vel[2][2];
+  void *g2p1[2][2], *g2p2[2][2][2];
+};
+
+void get_step_kernels(int dim, int basis, StepKernels &k);
+int p2g_smem_bytes(int dim, int basis, int mode, bool thermal);
+
+// kmpm_misc.cu
+void launch_cell_keys(const PartArgs &a, int nblk, int *keys, int use_x0, cudaStream_t st);
+void launch_cell_ranges(const int *sorted_keys, int start, int n, int ncell_per_tile, int *cell_start, int *cell_end,
+                        int *tile_start, int *tile_end, cudaStream_t st);
+void launch_dt(const DtArgs &a, cudaStream_t st);
+void launch_energy(const PartArgs &a, int nblk, double *blk, double *out, cudaStream_t st);
+// stable LSD radix sort of (key, value) pairs by key, 8 bits per pass
+struct RadixTemp {
+  int *k1, *v1, *hist, *tot;
+  int max_blocks;
+};
+void radix_sort(int *keys, int *vals, int n, int key_bits, RadixTemp &tmp, cudaStream_t st);
+void launch_iota(int *v, int n, cudaStream_t st);
+void launch_permute(float *const *src_pp, float *const *dst_pp, size_t ps, const int *perm, int start, int n,
+                    const int *fields, int nfields, cudaStream_t st);
+void launch_swap_ptrs(float **pp, cudaStream_t st);
+
+// ---- payload staged per particle for the scatter
+template <int MODE, bool TH>
+__device__ __forceinline__ void p2g_payload(const P2GArgs &a, const float *P, int p, float *pay) {
+  const size_t ps = a.ps;
+  const float m = P[PF_MASS * ps + p];
+  if (MODE == P2G_MASS) { pay[0] = m; return; }
+  int o = 0;
+  if (MODE == P2G_UL) pay[o++] = m;
+#pragma unroll
+  for (int d = 0; d < 3; d++) pay[o++] = m * P[(PF_V + d) * ps + p];
+  if (MODE == P2G_TL) {
+#pragma unroll
+    for (int k = 0; k < 9; k++) pay[o++] = P[(PF_PK + k) * ps + p];
+  } else if (MODE == P2G_UL) {
+#pragma unroll
+    for (int k = 0; k < 6; k++) pay[o++] = P[(PF_PK + k) * ps + p];
+  }
+  if (TH) {
+    pay[o++] = m * P[PF_T * ps + p];
+    if (MODE != P2G_VEL) {
+      pay[o++] = P[PF_GAMMA * ps + p];
+#pragma unroll
+      for (int d = 0; d < 3; d++) pay[o++] = P[(PF_Q + d) * ps + p];
+    }
+  }
+}
+
+// ---- contribution of one particle to one node
+template <int MODE, bool TH, int Q>
+__device__ __forceinline__ void p2g_accumulate(float *acc, const float *pay, float w, const float *gw) {
+  if (MODE == P2G_MASS) { acc[0] += w * pay[0]; return; }
+  int o = 0, i = 0;
+  if (MODE == P2G_UL) acc[o++] += w * pay[i++];
+#pragma unroll
+  for (int d = 0; d < 3; d++) acc[o++] += w * pay[i++];
+  if (MODE == P2G_TL) {
+    // f -= vol0PK1 * grad w  (src/solid.cpp:468)
+#pragma unroll
+    for (int d = 0; d < 3; d++) acc[o + d] -= pay[i + 3 * d] * gw[0] + pay[i + 3 * d + 1] * gw[1] + pay[i + 3 * d + 2] * gw[2];
+    o += 3;
+    i += 9;
+  } else if (MODE == P2G_UL) {
+    // f -= vol * sigma * grad w  (src/solid.cpp:508); sigma symmetric xx yy zz xy xz yz
+    const float *s = pay + i;
+    acc[o + 0] -= s[0] * gw[0] + s[3] * gw[1] + s[4] * gw[2];
+    acc[o + 1] -= s[3] * gw[0] + s[1] * gw[1] + s[5] * gw[2];
+    acc[o + 2] -= s[4] * gw[0] + s[5] * gw[1] + s[2] * gw[2];
+    o += 3;
+    i += 6;
+  }
+  if (TH) {
+    acc[o++] += w * pay[i++];  // m T
+    if (MODE != P2G_VEL) {
+      acc[o++] += w * pay[i++];  // Qext: w gamma
+      acc[o++] += gw[0] * pay[i] + gw[1] * pay[i + 1] + gw[2] * pay[i + 2];  // Qint: grad w . q
+    }
+  }
+}
+
+}  // namespace kmpm

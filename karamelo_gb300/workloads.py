@@ -1,0 +1,147 @@
+"""The benchmark / parity workloads, written as Karamelo input scripts through
+the :class:`~karamelo_gb300.model.MPM` command mirror.
+
+* ``two_disks``  -- 2-D ULMPM, USL, linear basis, two colliding linear-elastic
+  disks (docs/examples/two-disks.mpm:4-60 with the disks at (0.25,0.25) and
+  (0.75,0.75) in a unit square, h = 0.05, 2x2 particles per cell, +-0.1 m/s
+  per axis, dt = 1e-3).
+* ``taylor_bar`` -- 3-D TLMPM, MUSL, cubic B-spline, copper bar on a rigid wall
+  (examples/Taylor-bar/cylindrical/TLMPM/cylindrical_taylor_bar.mpm:1-89 with
+  R = 3.2 mm, L = 32.4 mm, 2x2x2 particles per cell, Johnson-Cook strength +
+  linear EOS; units GPa, mm, ms).
+* ``dam_break``  -- 3-D ULMPM, MUSL, cubic B-spline, water column in a slip-wall
+  box (examples/Dam-break/water-dam.mpm:1-73 in 3-D; Tait EOS, Newtonian
+  viscosity, gravity).
+* ``tensile_bars`` -- 2-D TLMPM, MUSL, cubic, Johnson-Cook strength + damage,
+  velocity-driven ends (examples/Tensile_with_damage/.../inputfile:1-92 in 2-D).
+
+All inputs are synthetic and deterministic (the populate lattice has no RNG);
+parameter sweeps use seeded generators.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from .model import MPM, TimeFn
+
+
+def two_disks(backend_factory=None, cellsize=0.05, ppc=2, v0=0.1, method="ulmpm/gpu", scheme="usl",
+              basis="linear", pic_flip=0.99):
+    sim = MPM(backend_factory)
+    sim.method(method, "FLIP", basis, pic_flip)
+    sim.scheme(scheme)
+    sim.dimension(2, 0, 1, 0, 1, cellsize)
+    sim.region("rBall1", "cylinder", 0.25, 0.25, 0.2)
+    sim.region("rBall2", "cylinder", 0.75, 0.75, 0.2)
+    sim.material("mat1", "linear", 1000, 1000, 0.3)
+    sim.solid("sBall1", "region", "rBall1", ppc, "mat1", cellsize, 0)
+    sim.solid("sBall2", "region", "rBall2", ppc, "mat1", cellsize, 0)
+    sim.group("gBall1", "particles", "region", "rBall1", "solid", "sBall1")
+    sim.group("gBall2", "particles", "region", "rBall2", "solid", "sBall2")
+    sim.fix("v0Ball1", "initial_velocity_particles", "gBall1", v0, v0, None)
+    sim.fix("v0Ball2", "initial_velocity_particles", "gBall2", -v0, -v0, None)
+    sim.fix("Ek", "kinetic_energy", "all")
+    sim.fix("Es", "strain_energy", "all")
+    sim.set_dt(1e-3)
+    return sim
+
+
+# Copper, units GPa / mm / ms.  E = 115 GPa and nu = 0.31 give the shear
+# modulus the Johnson-Cook law needs (examples/Taylor-bar/.../cylindrical_taylor_bar.mpm:5-8).
+COPPER = dict(E=115.0, nu=0.31, rho=8.94e-6, K=137.0, A=0.09, B=0.292, n=0.31, C=0.025, epsdot0=1e-3,
+              m=0.0, Tr=25.0, Tm=1600.0)
+
+
+def taylor_bar(backend_factory=None, cellsize=0.2, R=3.2, L=32.4, ppc=2, v0=190.0, method="tlmpm/gpu",
+               scheme="musl", basis="cubic-spline", pic_flip=0.99, dt_factor=0.1, params=None):
+    p = dict(COPPER)
+    if params:
+        p.update(params)
+    G = p["E"] / (2 * (1 + p["nu"]))
+    hL = L / 2
+    sim = MPM(backend_factory)
+    sim.method(method, "FLIP", basis, pic_flip)
+    sim.scheme(scheme)
+    x_wall = hL
+    Df = 2.5 * R
+    sim.dimension(3, -hL, x_wall, -Df, Df, -Df, Df, cellsize)
+    sim.eos("eosl", "linear", p["rho"], p["K"])
+    sim.strength("jc", "johnson_cook", G, p["A"], p["B"], p["n"], p["epsdot0"], p["C"], p["m"], p["Tr"], p["Tm"])
+    sim.material("mat", "eos-strength", "eosl", "jc")
+    sim.region("cyl", "cylinder", "x", 0, 0, R, -hL, hL)
+    sim.solid("solid1", "region", "cyl", ppc, "mat", cellsize, p["Tr"])
+    sim.region("region2", "block", x_wall - 0.5 * cellsize, "INF", "INF", "INF", "INF", "INF")
+    sim.group("groupn2", "nodes", "region", "region2", "solid", "solid1")
+    sim.group("gBall1", "particles", "region", "cyl", "solid", "solid1")
+    sim.fix("v0Ball1", "initial_velocity_particles", "gBall1", v0, None, None)
+    sim.dt_factor(dt_factor)
+    return sim
+
+
+def taylor_bar_wall(sim):
+    """The wall fix the Taylor-bar script adds after run(1) (cylindrical_taylor_bar.mpm:86-89)."""
+    sim.fix("BC_Wall", "velocity_nodes", "groupn2", 0, None, None)
+
+
+def dam_break(backend_factory=None, cellsize=0.005, Lx=1.6, Ly=0.4, Lz=0.8, wx=0.4, wy=0.4, wz=0.8, ppc=2,
+              method="ulmpm/gpu", scheme="musl", basis="cubic-spline", pic_flip=0.99, dt_factor=0.1,
+              K=2e6, gamma=7.0, rho0=1000.0, mu=1e-3, g=-9.81):
+    sim = MPM(backend_factory)
+    sim.method(method, "FLIP", basis, pic_flip)
+    sim.scheme(scheme)
+    sim.dimension(3, 0, Lx, 0, Ly, 0, Lz, cellsize)
+    sim.eos("eosf", "fluid", rho0, K, gamma)
+    sim.strength("sf", "fluid", mu)
+    sim.material("water", "eos-strength", "eosf", "sf")
+    sim.region("water", "block", 0, wx, 0, wy, 0, wz)
+    sim.solid("w", "region", "water", ppc, "water", cellsize, 0)
+    q = cellsize / 4
+    # slip walls on the six faces: the normal velocity component is zero
+    sim.region("xlo", "block", "-INF", q, "-INF", "INF", "-INF", "INF")
+    sim.region("xhi", "block", Lx - q, "INF", "-INF", "INF", "-INF", "INF")
+    sim.region("ylo", "block", "-INF", "INF", "-INF", q, "-INF", "INF")
+    sim.region("yhi", "block", "-INF", "INF", Ly - q, "INF", "-INF", "INF")
+    sim.region("zlo", "block", "-INF", "INF", "-INF", "INF", "-INF", q)
+    sim.region("zhi", "block", "-INF", "INF", "-INF", "INF", Lz - q, "INF")
+    for name, axis in (("xlo", 0), ("xhi", 0), ("ylo", 1), ("yhi", 1), ("zlo", 2), ("zhi", 2)):
+        sim.group("g" + name, "nodes", "region", name, "solid", "w")
+        vals = [None, None, None]
+        vals[axis] = 0.0
+        sim.fix("bc" + name, "velocity_nodes", "g" + name, *vals)
+    sim.fix("fbody", "body_force", "all", None, None, g)
+    sim.dt_factor(dt_factor)
+    return sim
+
+
+WELDOX = dict(E=211.0, nu=0.33, rho=7.75e-6, A=0.499, B=0.382, n=0.458, S=1.5, c0=5030.0)
+DAMAGE = dict(d1=0.54, d2=4.89, d3=-3.03, d4=0.014, d5=1.12)
+
+
+def tensile_bar_2d(backend_factory=None, cellsize=0.4, hLx=10.0, hLy=2.0, ppc=2, vend=1.0, damage=None,
+                   method="tlmpm/gpu", scheme="musl", basis="cubic-spline", pic_flip=0.99, dt_factor=0.1):
+    """One 2-D TLMPM tensile bar, aspect ratio hLx/hLy, ends pulled at +-vend."""
+    d = dict(DAMAGE)
+    if damage:
+        d.update(damage)
+    p = WELDOX
+    K = p["E"] / (3 * (1 - 2 * p["nu"]))
+    G = p["E"] / (2 * (1 + p["nu"]))
+    sim = MPM(backend_factory)
+    sim.method(method, "FLIP", basis, pic_flip)
+    sim.scheme(scheme)
+    sim.dimension(2, -2 * hLx, 2 * hLx, -2 * hLy, 2 * hLy, cellsize)
+    sim.eos("eoss", "shock", p["rho"], K, p["c0"], p["S"], 0, 0, 0, 0, 0)
+    sim.strength("sjc", "johnson_cook", G, p["A"], p["B"], p["n"], 1.0, 0.0, 0.0, 0.0, 1000.0)
+    sim.damage("djc", "damage_johnson_cook", d["d1"], d["d2"], d["d3"], d["d4"], d["d5"], 1.0, 0.0, 1000.0)
+    sim.material("mat", "eos-strength", "eoss", "sjc", "djc")
+    sim.region("box", "block", -hLx, hLx, -hLy, hLy)
+    sim.solid("bar", "region", "box", ppc, "mat", cellsize, 0)
+    xbc = hLx - cellsize
+    sim.region("left", "block", "-INF", -xbc, "-INF", "INF")
+    sim.region("right", "block", xbc, "INF", "-INF", "INF")
+    sim.group("gl", "nodes", "region", "left", "solid", "bar")
+    sim.group("gr", "nodes", "region", "right", "solid", "bar")
+    sim.fix("BC_left", "velocity_nodes", "gl", TimeFn(-vend, 0, vend, -1.0), None)
+    sim.fix("BC_right", "velocity_nodes", "gr", TimeFn(vend, 0, -vend, -1.0), None)
+    sim.dt_factor(dt_factor)
+    return sim

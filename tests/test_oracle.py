@@ -1,0 +1,154 @@
+"""The oracle pinned against the reference's own code and closed forms (CPU)."""
+import ctypes
+import os
+
+import numpy as np
+import pytest
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+def _dp(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def test_basis_matches_reference_golden(oracle_mod):
+    """oracle basis functions == src/basis_functions.h compiled unmodified (golden vectors)."""
+    g = np.load(os.path.join(HERE, "golden", "basis_golden.npz"))
+    r, icell = g["r"], float(g["icellsize"])
+    n = 0
+    for key in g.files:
+        if not key.startswith("b"):
+            continue
+        b, nt, k = key[1:].split("_")
+        basis, ntype, kind = int(b), int(nt[1:]), int(k[1:])
+        mine = np.array([oracle_mod.basis(basis, kind, x, ntype, icell) for x in r])
+        np.testing.assert_array_equal(mine, g[key], err_msg=key)
+        n += 1
+    assert n == 16
+
+
+def test_basis_live_reference_if_present(oracle_mod):
+    L = oracle_mod.ref_basis_lib()
+    if L is None:
+        pytest.skip("reference tree not present (golden vectors cover this)")
+    rng = np.random.default_rng(0)
+    for _ in range(2000):
+        basis = int(rng.integers(0, 3))
+        nt = int(rng.choice([-2, -1, 0, 1, 2] if basis == 1 else ([0, 1] if basis == 2 else [0])))
+        x = float(rng.uniform(-2.5, 2.5))
+        for kind in (0, 1):
+            assert oracle_mod.basis(basis, kind, x, nt, 3.0) == L.ref_basis(basis, kind, x, nt, 3.0)
+
+
+def test_partition_of_unity_cubic_interior(oracle_mod):
+    for t in np.linspace(0, 0.999, 37):
+        s = sum(oracle_mod.basis(1, 0, t - k, 0) for k in (-1, 0, 1, 2))
+        ds = sum(oracle_mod.basis(1, 1, t - k, 0) for k in (-1, 0, 1, 2))
+        assert abs(s - 1) < 1e-14 and abs(ds) < 1e-13
+
+
+def test_polar_decomposition(oracle_mod):
+    L = oracle_mod.lib()
+    rng = np.random.default_rng(1)
+    for _ in range(200):
+        Q, _ = np.linalg.qr(rng.standard_normal((3, 3)))
+        if np.linalg.det(Q) < 0:
+            Q[:, 0] *= -1
+        S = rng.standard_normal((3, 3))
+        U = np.eye(3) + 0.3 * (S + S.T)
+        U = U @ U.T + 0.1 * np.eye(3)
+        F = np.ascontiguousarray(Q @ U)
+        R = np.zeros(9)
+        assert L.om_poldec(_dp(F), _dp(R)) == 1
+        np.testing.assert_allclose(R.reshape(3, 3), Q, atol=1e-10)
+
+
+def test_eigen_real_parts(oracle_mod):
+    L = oracle_mod.lib()
+    rng = np.random.default_rng(2)
+    for i in range(3000):
+        scale = [1e-16, 1e-6, 0.3][i % 3]
+        F = np.ascontiguousarray(np.eye(3) + scale * rng.standard_normal((3, 3)))
+        re = np.zeros(3)
+        L.om_eig_real(_dp(F), _dp(re))
+        assert abs(np.abs(re).min() - np.abs(np.linalg.eigvals(F).real).min()) < 1e-9
+
+
+def _material(**kw):
+    from karamelo_gb300.scenario import MaterialParams
+    m = MaterialParams()
+    m.damage = m.temp = -1
+    for k, v in kw.items():
+        if isinstance(v, (list, tuple)):
+            arr = getattr(m, k)
+            for i, x in enumerate(v):
+                arr[i] = x
+        else:
+            setattr(m, k, v)
+    return m
+
+
+def test_johnson_cook_radial_return(oracle_mod):
+    """Closed-form return of src/strength_jc.cpp:100-184: yield surface hit exactly."""
+    from oracle import OracleBackend  # noqa: F401
+    L = oracle_mod.lib()
+    h = L.om_create(0, 1, 1, 3, 0.99, 0, 1e-3, 0.1, 1, _dp(np.zeros(3)), _dp(np.ones(3)))
+    G, A, B, n, ed0, C = 43.9, 0.09, 0.292, 0.31, 1e-3, 0.025
+    m = _material(type=2, eos=0, eos_p=[8.94e-6, 137.0], strength=2, str_p=[G, A, B, n, ed0, C, 0.0, 25.0, 1600.0])
+    mid = L.om_add_material(h, ctypes.byref(m))
+    rng = np.random.default_rng(3)
+    for _ in range(50):
+        S = rng.standard_normal((3, 3)) * 0.05
+        sig = np.ascontiguousarray(S + S.T)
+        D = rng.standard_normal((3, 3)) * 10
+        D = np.ascontiguousarray(D + D.T)
+        epsp, epsdot, dt = 0.1, 5e-3, 1e-3
+        sc = np.array([dt, epsp, epsdot, 0.0, 0.0, 1.0, 8.94e-6, 0.2])
+        out = np.zeros(11)
+        L.om_constitutive(h, mid, _dp(sig), _dp(D), _dp(sc), _dp(out))
+        sdev, dep = out[:9].reshape(3, 3), out[9]
+        ys = (A + B * epsp ** n) * (1 + max(epsdot / ed0, 1.0)) ** C
+        trial = sig + dt * 2 * G * D
+        trial_dev = trial - np.trace(trial) / 3 * np.eye(3)
+        J2 = 1.224744871 * np.linalg.norm(trial_dev)
+        if J2 < ys:
+            np.testing.assert_allclose(sdev, trial_dev, rtol=1e-12, atol=1e-15)
+            assert dep == 0
+        else:
+            np.testing.assert_allclose(1.224744871 * np.linalg.norm(sdev), ys, rtol=1e-12)
+            np.testing.assert_allclose(dep, (J2 - ys) / (3 * G), rtol=1e-12)
+    L.om_destroy(h)
+
+
+def test_linear_eos_and_fluid_eos(oracle_mod):
+    L = oracle_mod.lib()
+    h = L.om_create(1, 1, 1, 3, 0.99, 0, 1e-3, 0.1, 1, _dp(np.zeros(3)), _dp(np.ones(3)))
+    lin = _material(type=2, eos=0, eos_p=[1000.0, 2e6], strength=4, str_p=[1e-3])
+    flu = _material(type=2, eos=2, eos_p=[1000.0, 2e6, 7.0], strength=4, str_p=[1e-3])
+    a, b = L.om_add_material(h, ctypes.byref(lin)), L.om_add_material(h, ctypes.byref(flu))
+    for J in (0.9, 0.99, 1.0, 1.01):
+        out = np.zeros(11)
+        sig, D = np.zeros(9), np.zeros(9)
+        sc = np.array([1e-3, 0, 0, 0, 0, J, 1000.0 / J, 0.01])
+        L.om_constitutive(h, a, _dp(sig), _dp(D), _dp(sc), _dp(out))
+        assert out[10] == pytest.approx(2e6 * (1 - J), rel=1e-14, abs=1e-9)   # src/eos_linear.cpp:73
+        L.om_constitutive(h, b, _dp(sig), _dp(D), _dp(sc), _dp(out))
+        assert out[10] == pytest.approx(2e6 * ((1 / J) ** 7 - 1), rel=1e-12, abs=1e-6)  # src/eos_fluid.cpp:71
+    L.om_destroy(h)
+
+
+def test_oracle_two_disks_energy_exchange(oracle_mod):
+    """C1 (two colliding elastic disks): kinetic energy turns into strain energy and back."""
+    from karamelo_gb300 import workloads as W
+    sim = W.two_disks(oracle_mod.OracleBackend, method="ulmpm")
+    e0 = None
+    ek = []
+    for _ in range(15):
+        sim.run(100)
+        e = sim.energies()
+        if e0 is None:
+            e0 = e[0] + e[1]
+        ek.append(e[0])
+    assert abs(ek[0] - 2.6) < 1e-6  # 416 particles, 1/2 m |v|^2 with |v|^2 = 0.02
+    assert min(ek) < 0.5 * ek[0]    # the disks collide
