@@ -3,6 +3,7 @@
 // the host<->device conversions between the caller's FP64 arrays and the
 // device's FP32 structure of arrays.
 #include <algorithm>
+#include <cstddef>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -203,6 +204,7 @@ P2GArgs p2g_args(kmpm_ctx *c) {
   a.pstride_tile = c->pstride_tile;
   a.tile_start = c->d_ts;
   a.tile_end = c->d_te;
+  a.scalars = c->d_scalars;
   return a;
 }
 
@@ -429,6 +431,7 @@ int build(kmpm_ctx *c) {
     s.time = 0;
     s.ntimestep = 0;
     s.dtCFL = 1e22;
+    s.maxtime = 1e300;
     CK(cudaMemcpyAsync(c->d_scalars, &s, sizeof(s), cudaMemcpyHostToDevice, c->st));
   }
   DALLOC(c->d_dtcfl, c->ranges.size());
@@ -834,9 +837,18 @@ int kmpm_add_fix(kmpm_ctx *c, int kind, int grid, const unsigned char *node_mask
   return (int)c->hfixes.size() - 1;
 }
 
+static int set_maxtime(kmpm_ctx *c, double maxtime) {
+  CK(cudaMemcpyAsync((char *)c->d_scalars + offsetof(StepScalars, maxtime), &maxtime, sizeof(double),
+                     cudaMemcpyHostToDevice, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  return KMPM_OK;
+}
+
 int kmpm_run(kmpm_ctx *c, int nsteps) {
   if (!c || nsteps < 0) return KMPM_ERR_ARG;
   int r = prepare(c);
+  if (r != KMPM_OK) return r;
+  r = set_maxtime(c, 1e300);
   if (r != KMPM_OK) return r;
   for (int i = 0; i < nsteps; i++) CK(cudaGraphLaunch(c->gexec, c->st));
   return check_error(c);
@@ -846,22 +858,25 @@ int kmpm_run_time(kmpm_ctx *c, double maxtime, int *nsteps_done) {
   if (!c) return KMPM_ERR_ARG;
   int r = prepare(c);
   if (r != KMPM_OK) return r;
-  int done = 0;
   StepScalars s{};
   r = read_scalars(c, s);
   if (r != KMPM_OK) return r;
-  // RunTime::command: loop while time < maxtime (src/run_time.cpp:30-60)
+  const long long n0 = s.ntimestep;
+  // RunTime::command (src/run_time.cpp:30-60): steps while time < maxtime.
+  // The steps check the bound on the device, so a batch can be launched
+  // without overshooting; the host only decides when to stop launching.
+  r = set_maxtime(c, maxtime);
+  if (r != KMPM_OK) return r;
   while (s.time < maxtime) {
-    double est = (maxtime - s.time) / s.dt;
-    int batch = (int)std::min(256.0, std::max(1.0, std::floor(0.5 * est)));
-    for (int i = 0; i < batch; i++) CK(cudaGraphLaunch(c->gexec, c->st));
-    done += batch;
+    for (int i = 0; i < 64; i++) CK(cudaGraphLaunch(c->gexec, c->st));
     r = check_error(c);
     if (r != KMPM_OK) return r;
     r = read_scalars(c, s);
     if (r != KMPM_OK) return r;
   }
-  if (nsteps_done) *nsteps_done = done;
+  r = set_maxtime(c, 1e300);
+  if (r != KMPM_OK) return r;
+  if (nsteps_done) *nsteps_done = (int)(s.ntimestep - n0);
   return KMPM_OK;
 }
 

@@ -86,7 +86,12 @@ struct StepScalars {
   double dt, time;
   long long ntimestep;
   double dtCFL;
+  double maxtime;  // RunTime: a step runs only while time < maxtime (+inf for run(n))
 };
+
+// Every kernel of a step returns at once when the run has reached its end
+// time, so a batch of captured steps never overshoots run_time's bound.
+__device__ __forceinline__ bool run_finished(const StepScalars *s) { return !(s->time < s->maxtime); }
 
 // A node fix (velocity_nodes / body_force) in device form.
 struct FixDev {

@@ -30,6 +30,7 @@ struct P2GArgs {
   float *partial;            // tile footprint slices
   size_t pstride_tile;       // floats per tile slice
   const int *tile_start, *tile_end;  // particle range of every tile (empty tiles are skipped)
+  const StepScalars *scalars;
 };
 
 struct GridArgs {

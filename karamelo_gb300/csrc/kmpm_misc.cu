@@ -14,6 +14,7 @@ namespace kmpm {
 // key = global tile * cells_per_tile + cell within tile, from the FP32
 // position the kernels use (TL: x0, UL: x0 + the moved displacement PF_XN)
 __global__ void k_cell_keys(PartArgs a, int *keys, int use_x0) {
+  if (a.scalars != nullptr && run_finished(a.scalars)) return;
   const int ri = a.blk_range[blockIdx.x];
   const RangeDev rd = a.ranges[ri];
   const int p = rd.start + (blockIdx.x - rd.blk0) * 256 + threadIdx.x;
@@ -220,6 +221,7 @@ __device__ __forceinline__ void raise_error_m(ErrState *e, int code, int p, long
 // per range: dtCFL = cellsize * min_h_ratio / max_p_wave_speed (src/solid.cpp:1430)
 __global__ void k_dt_range(DtArgs a) {
   __shared__ float rc[256], rh[256];
+  if (run_finished(a.scalars)) return;
   const RangeDev rd = a.ranges[blockIdx.x];
   float c = 0.f, h = 1.f;
   for (int b = rd.blk0 + threadIdx.x; b < rd.blk0 + rd.nblk; b += blockDim.x) {
@@ -247,6 +249,7 @@ __global__ void k_dt_range(DtArgs a) {
 
 // update_time, then adjust_dt; in independent mode every range keeps its own clock
 __global__ void k_dt_final(DtArgs a) {
+  if (run_finished(a.scalars)) return;
   if (a.indep) {
     for (int r = threadIdx.x; r < a.nranges; r += blockDim.x) {
       StepScalars &s = a.scalars[r];
@@ -268,6 +271,7 @@ __global__ void k_dt_final(DtArgs a) {
 
 // the step counter advances at the start of a step (Update::update_timestep)
 __global__ void k_step_begin(StepScalars *s, int n) {
+  if (run_finished(s)) return;
   for (int r = threadIdx.x; r < n; r += blockDim.x) s[r].ntimestep++;
 }
 

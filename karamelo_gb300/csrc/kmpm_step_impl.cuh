@@ -54,7 +54,7 @@ __global__ void __launch_bounds__(256) k_p2g(P2GArgs a) {
   const int tile_global = g.tile_off + tlin;
   const float h = g.cellsize / SC, ih = g.inv_cellsize;
   const float *P = *a.Pp;
-  if (a.tile_end[tile_global] == a.tile_start[tile_global]) return;
+  if (a.tile_end[tile_global] == a.tile_start[tile_global] || run_finished(a.scalars)) return;
 
   for (int k = threadIdx.x; k < Q * NW; k += blockDim.x) acc[k] = 0.f;
   __syncthreads();
@@ -209,6 +209,7 @@ __device__ __forceinline__ double fix_value(const FixDev &f, int d, double t) {
 // first scatter.  MODE_GRID_VEL: after the MUSL re-map (or USL: positions only).
 template <int DIM, int BASIS, int GMODE, bool TL, bool THERMAL>
 __global__ void __launch_bounds__(256) k_grid(GridArgs a) {
+  if (run_finished(a.scalars)) return;
   const int gi = a.blk_grid[blockIdx.x];
   const GridDev g = a.grids[gi];
   const int li = (blockIdx.x - a.grid_blk0[gi]) * 256 + threadIdx.x;
@@ -330,6 +331,7 @@ __device__ __forceinline__ int range_particle(const PartArgs &a, RangeDev &rd) {
 // grid_to_points + advance_particles (src/solid.cpp:576-635, 786-790)
 template <int DIM, int BASIS, bool TL, bool THERMAL>
 __global__ void __launch_bounds__(256) k_g2p1(PartArgs a) {
+  if (run_finished(a.scalars)) return;
   RangeDev rd;
   const int p = range_particle(a, rd);
   if (p < 0) return;
@@ -398,6 +400,7 @@ __global__ void __launch_bounds__(256) k_g2p1(PartArgs a) {
 template <int DIM, int BASIS, bool TL, bool THERMAL, int PREC>
 __global__ void __launch_bounds__(256) k_g2p2(PartArgs a) {
   __shared__ float red_c[256], red_h[256];
+  if (run_finished(a.scalars)) return;
   RangeDev rd;
   const int p = range_particle(a, rd);
   float my_c = 0.f, my_h = 1.f;

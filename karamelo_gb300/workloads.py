@@ -118,8 +118,9 @@ DAMAGE = dict(d1=0.54, d2=4.89, d3=-3.03, d4=0.014, d5=1.12)
 
 
 def tensile_bar_2d(backend_factory=None, cellsize=0.4, hLx=10.0, hLy=2.0, ppc=2, vend=1.0, damage=None,
-                   method="tlmpm/gpu", scheme="musl", basis="cubic-spline", pic_flip=0.99, dt_factor=0.1):
-    """One 2-D TLMPM tensile bar, aspect ratio hLx/hLy, ends pulled at +-vend."""
+                   method="tlmpm/gpu", scheme="musl", basis="cubic-spline", pic_flip=0.99, dt_factor=0.1, ramp=True):
+    """One 2-D TLMPM tensile bar, aspect ratio hLx/hLy, ends pulled at +-vend
+    (ramped as vend (1 - exp(-time)) like the reference script, or constant)."""
     d = dict(DAMAGE)
     if damage:
         d.update(damage)
@@ -141,7 +142,11 @@ def tensile_bar_2d(backend_factory=None, cellsize=0.4, hLx=10.0, hLy=2.0, ppc=2,
     sim.region("right", "block", xbc, "INF", "-INF", "INF")
     sim.group("gl", "nodes", "region", "left", "solid", "bar")
     sim.group("gr", "nodes", "region", "right", "solid", "bar")
-    sim.fix("BC_left", "velocity_nodes", "gl", TimeFn(-vend, 0, vend, -1.0), None)
-    sim.fix("BC_right", "velocity_nodes", "gr", TimeFn(vend, 0, -vend, -1.0), None)
+    if ramp:
+        sim.fix("BC_left", "velocity_nodes", "gl", TimeFn(-vend, 0, vend, -1.0), None)
+        sim.fix("BC_right", "velocity_nodes", "gr", TimeFn(vend, 0, -vend, -1.0), None)
+    else:
+        sim.fix("BC_left", "velocity_nodes", "gl", -vend, None)
+        sim.fix("BC_right", "velocity_nodes", "gr", vend, None)
     sim.dt_factor(dt_factor)
     return sim
