@@ -62,7 +62,7 @@ struct kmpm_ctx {
   MatDev *d_mats = nullptr;
   float4 *nodeA = nullptr, *nodeB = nullptr, *nodeX = nullptr;
   float *nodeT = nullptr;
-  int T = 0, NCELL = 0, ntiles_total = 0;
+  int tdim[3] = {0, 0, 0}, NCELL = 0, ntiles_total = 0;
   int2 *d_tiles = nullptr;
   int ntiles_launch = 0;
   int *d_cs = nullptr, *d_ce = nullptr, *d_ts = nullptr, *d_te = nullptr;
@@ -93,6 +93,9 @@ struct kmpm_ctx {
   int prof_n = 0;
   // TLMPM keeps its binning order for the whole run: caller index of every slot
   std::vector<int> orig_cache, sid_cache;
+  // temperatures are kept as T - T_ref in FP32 (T_ref: the first solid's
+  // initial temperature in thermo-mechanical runs, 0 otherwise)
+  double T_ref = 0;
   bool TL() const { return prm.method == KMPM_TLMPM; }
   bool musl() const { return prm.scheme == KMPM_MUSL; }
 };
@@ -158,6 +161,13 @@ MatDev to_dev(const kmpm_material &m) {
     d.invcp = m.cp != 0 ? 1.0 / m.cp : 0;
     d.kappa = m.kappa;
   }
+  d.f_rho0 = (float)d.rho0; d.f_K = (float)d.K; d.f_G = (float)d.G; d.f_lambda = (float)d.lambda;
+  d.f_signal_velocity = (float)d.signal_velocity; d.f_cp = (float)d.cp; d.f_invcp = (float)d.invcp;
+  d.f_kappa = (float)d.kappa;
+  d.f_c2 = (float)(d.K + 1.333333333333333333333333333333333333333 * d.G);  // src/solid.cpp:40 FOUR_THIRD
+  for (int i = 0; i < 12; i++) { d.f_eos_p[i] = (float)d.eos_p[i]; d.f_str_p[i] = (float)d.str_p[i]; }
+  for (int i = 0; i < 8; i++) d.f_dam_p[i] = (float)d.dam_p[i];
+  for (int i = 0; i < 6; i++) d.f_temp_p[i] = (float)d.temp_p[i];
   return d;
 }
 
@@ -178,6 +188,7 @@ PartArgs part_args(kmpm_ctx *c) {
   a.blk_c = c->d_blk_c;
   a.blk_h = c->d_blk_h;
   a.pic_flip = (float)c->prm.pic_flip;
+  a.T_ref = (float)c->T_ref;
   for (int d = 0; d < 3; d++) {
     a.boxlo[d] = (float)c->prm.boxlo[d];
     a.boxhi[d] = (float)c->prm.boxhi[d];
@@ -187,7 +198,7 @@ PartArgs part_args(kmpm_ctx *c) {
   a.thermal = c->prm.thermal;
   a.track_strain = c->prm.track_strain;
   a.dim = c->prm.dim;
-  a.tile_T = c->T;
+  for (int d = 0; d < 3; d++) a.tile_t[d] = c->tdim[d];
   return a;
 }
 
@@ -297,8 +308,8 @@ int build(kmpm_ctx *c) {
   const int dim = c->prm.dim, basis = c->prm.basis;
   if (c->hsolids.empty()) return fail(c, KMPM_ERR_STATE, "no solid was added");
   get_step_kernels(dim, basis, c->K);
-  c->T = tile_edge(dim, basis);
-  c->NCELL = dim == 3 ? c->T * c->T * c->T : (dim == 2 ? c->T * c->T : c->T);
+  tile_dims(dim, basis, c->tdim);
+  c->NCELL = c->tdim[0] * c->tdim[1] * c->tdim[2];
   // ---- grids
   c->grids.clear();
   int node_off = 0, tile_off = 0;
@@ -313,7 +324,7 @@ int build(kmpm_ctx *c) {
       int nc = basis == KMPM_BASIS_BERNSTEIN ? (h.n[d] + 1) / 2 : h.n[d];
       if (d >= dim) nc = 1;
       g.ncell[d] = std::max(nc, 1);
-      g.ntile[d] = d < dim ? (g.ncell[d] + c->T - 1) / c->T : 1;
+      g.ntile[d] = d < dim ? (g.ncell[d] + c->tdim[d] - 1) / c->tdim[d] : 1;
     }
     g.cellsize = (float)h.cellsize;
     g.inv_cellsize = (float)(1.0 / h.cellsize);
@@ -418,8 +429,8 @@ int build(kmpm_ctx *c) {
   DALLOC(c->d_te, c->ntiles_total);
   {
     int S = stencil_width(basis), SC = stencil_sc(basis);
-    int W = (c->T - 1) * SC + S;
-    int NW = dim == 3 ? W * W * W : (dim == 2 ? W * W : W);
+    int NW = 1;
+    for (int d = 0; d < dim; d++) NW *= (c->tdim[d] - 1) * SC + S;
     c->pstride_tile = (size_t)NW * 10;
   }
   DALLOC(c->partial, c->pstride_tile * c->ntiles_total);
@@ -447,6 +458,7 @@ int build(kmpm_ctx *c) {
   DALLOC(c->rtmp.hist, 256 * ((c->ps + 2047) / 2048 + 1));
   DALLOC(c->rtmp.tot, 256);
   // ---- particle upload (caller order within each solid)
+  c->T_ref = c->prm.thermal ? c->hsolids[0].T0 : 0.0;
   {
     std::vector<float> H((size_t)c->ps * PF_COUNT, 0.f);
     auto at = [&](int f, int p) -> float & { return H[(size_t)f * c->ps + p]; };
@@ -467,7 +479,7 @@ int build(kmpm_ctx *c) {
         at(PF_VOL0, p) = (float)S.vol0[i];
         // Solid::populate sets T = T0 only for thermo-mechanical runs; otherwise
         // the vector is value-initialised (src/solid.cpp:2297-2306, 306-311)
-        at(PF_T, p) = c->prm.thermal ? (float)S.T0 : 0.f;
+        at(PF_T, p) = c->prm.thermal ? (float)(S.T0 - c->T_ref) : 0.f;
         int orig = c->solid_base[s] + i, sid = (int)s;
         std::memcpy(&at(PF_ORIG, p), &orig, 4);
         std::memcpy(&at(PF_SID, p), &sid, 4);
@@ -535,7 +547,7 @@ int build(kmpm_ctx *c) {
     int nl = 0;
     LAUNCH(c->K.p2g_mass, c->ntiles_launch, 256, c->smem[0][0], p);
     GridArgs ga = grid_args(c, 0);
-    LAUNCH(c->K.grid_mass, c->nblk_g, 256, 0, ga);
+    LAUNCH(c->K.grid_mass[c->prm.precision == KMPM_PREC_FP64_ISLANDS ? 1 : 0], c->nblk_g, 256, 0, ga);
     CK(cudaStreamSynchronize(c->st));
   } else {
     // ULMPM: every tile of the box grid is launched; empty ones return at once
@@ -626,7 +638,7 @@ int enqueue_step(kmpm_ctx *c) {
   else LAUNCH(th ? c->K.p2g_ul_th : c->K.p2g_ul, c->ntiles_launch, 256, c->smem[2][th], p);
   MARK("p2g");
   // update_grid_state + fixes
-  LAUNCH(c->K.grid_upd[TL][th], c->nblk_g, 256, 0, g1);
+  LAUNCH(c->K.grid_upd[TL][th][prec], c->nblk_g, 256, 0, g1);
   MARK("grid_update");
   // grid_to_points + advance_particles
   LAUNCH(c->K.g2p1[TL][th], c->nblk_p, 256, 0, pa);
@@ -636,11 +648,11 @@ int enqueue_step(kmpm_ctx *c) {
     LAUNCH(th ? c->K.p2g_vel_th : c->K.p2g_vel, c->ntiles_launch, 256, c->smem[3][th], p);
     MARK("p2g_velocity");
     GridArgs g2 = grid_args(c, 1);
-    LAUNCH(c->K.grid_vel[TL][th], c->nblk_g, 256, 0, g2);
+    LAUNCH(c->K.grid_vel[TL][th][prec], c->nblk_g, 256, 0, g2);
     MARK("grid_velocity");
   } else if (TL) {
     GridArgs g2 = grid_args(c, 0);
-    LAUNCH(c->K.grid_vel[TL][th], c->nblk_g, 256, 0, g2);
+    LAUNCH(c->K.grid_vel[TL][th][prec], c->nblk_g, 256, 0, g2);
     MARK("grid_positions");
   }
   // compute_rate_deformation_gradient + update_deformation_gradient + update_stress
@@ -1015,7 +1027,12 @@ int kmpm_download_particles(kmpm_ctx *c, int solid, int field, double *out) {
       case KMPM_P_SIGMA_ROT: {
         double sg[9], F[9], R[9], RS[9];
         sym(PF_SIG, sg);
-        if (!c->TL()) { for (int k = 0; k < 9; k++) out[9 * i + k] = sg[k]; break; }
+        // ULMPM stores sigma in the current frame; TLMPM rotates it, except for
+        // neo-Hookean solids, whose R stays the identity (src/solid.cpp:1220)
+        if (!c->TL() || c->mats[S.mat].type == KMPM_MAT_NEO_HOOKEAN) {
+          for (int k = 0; k < 9; k++) out[9 * i + k] = sg[k];
+          break;
+        }
         for (int k = 0; k < 9; k++) F[k] = f(PF_H + k) + (k % 4 == 0 ? 1.0 : 0.0);
         polar_host(F, R);
         for (int a = 0; a < 3; a++)
@@ -1032,7 +1049,7 @@ int kmpm_download_particles(kmpm_ctx *c, int solid, int field, double *out) {
       case KMPM_P_EPSDOT_P: out[i] = f(PF_EPSDOT); break;
       case KMPM_P_DAMAGE: out[i] = f(PF_DMG); break;
       case KMPM_P_DAMAGE_INIT: out[i] = f(PF_DMGI); break;
-      case KMPM_P_T: out[i] = f(PF_T); break;
+      case KMPM_P_T: out[i] = c->T_ref + f(PF_T); break;
       case KMPM_P_J:
       case KMPM_P_VOL: {
         double Hd[9];
@@ -1094,7 +1111,7 @@ int kmpm_download_grid(kmpm_ctx *c, int grid, int field, double *out) {
   else return fail(c, KMPM_ERR_ARG, "unknown grid field");
   for (int i = 0; i < nn; i++) {
     if (field == KMPM_G_MASS) out[i] = A[i].w;
-    else if (field == KMPM_G_T) out[i] = Tn[i];
+    else if (field == KMPM_G_T) out[i] = c->T_ref + Tn[i];
     else { out[3 * i] = A[i].x; out[3 * i + 1] = A[i].y; out[3 * i + 2] = A[i].z; }
   }
   return KMPM_OK;

@@ -79,6 +79,20 @@ struct MatDev {
   int type, eos, strength, damage, temp;
   double rho0, K, G, lambda, signal_velocity, cp, invcp, kappa;
   double eos_p[12], str_p[12], dam_p[8], temp_p[6];
+  // FP32 copies for the FP32 path (no per-particle double conversions)
+  float f_rho0, f_K, f_G, f_lambda, f_signal_velocity, f_cp, f_invcp, f_kappa, f_c2;  // f_c2 = K + 4G/3
+  float f_eos_p[12], f_str_p[12], f_dam_p[8], f_temp_p[6];
+};
+template <typename R> struct MatP;
+template <> struct MatP<float> {
+  __device__ static const float *eos(const MatDev &m) { return m.f_eos_p; }
+  __device__ static const float *str(const MatDev &m) { return m.f_str_p; }
+  __device__ static const float *dam(const MatDev &m) { return m.f_dam_p; }
+};
+template <> struct MatP<double> {
+  __device__ static const double *eos(const MatDev &m) { return m.eos_p; }
+  __device__ static const double *str(const MatDev &m) { return m.str_p; }
+  __device__ static const double *dam(const MatDev &m) { return m.dam_p; }
 };
 
 // Per-solid time-step scalars kept on the device so a captured step replays.
@@ -125,18 +139,33 @@ template <> struct Stencil<0> { static constexpr int S = 2, LO = 0, SC = 1, C = 
 template <> struct Stencil<1> { static constexpr int S = 4, LO = 1, SC = 1, C = 4; };
 template <> struct Stencil<2> { static constexpr int S = 3, LO = 0, SC = 2, C = 2; };
 
+// Tiles of TX x TY x TZ cells.  The scatter kernel gives every warp of the
+// tile an x-slab of L = TX / NWARP cell layers; the warp accumulates its slab
+// into a private footprint (FX x WY x WZ nodes) in shared memory, cell after
+// cell in a fixed order, and the slabs are then summed in warp order.
 template <int DIM, int BASIS> struct TileShape {
-  // cells per tile edge
-  static constexpr int T = DIM == 3 ? (BASIS == 2 ? 4 : 8) : (DIM == 2 ? (BASIS == 2 ? 8 : 16) : 64);
-  static constexpr int S = Stencil<BASIS>::S;
-  static constexpr int W = (T - 1) * Stencil<BASIS>::SC + S;  // footprint nodes per edge
+  static constexpr int S = Stencil<BASIS>::S, SC = Stencil<BASIS>::SC;
+  static constexpr int NWARP = 8;
+  static constexpr int TX = DIM == 3 ? 8 : (DIM == 2 ? 16 : 64);
+  static constexpr int TY = DIM == 3 ? 4 : (DIM == 2 ? 16 : 1);
+  static constexpr int TZ = DIM == 3 ? 4 : 1;
+  static constexpr int L = TX / NWARP;
+  static constexpr int WX = (TX - 1) * SC + S;
+  static constexpr int WY = DIM >= 2 ? (TY - 1) * SC + S : 1;
+  static constexpr int WZ = DIM == 3 ? (TZ - 1) * SC + S : 1;
+  static constexpr int FX = (L - 1) * SC + S;
+  static constexpr int NW = WX * WY * WZ;   // tile footprint nodes
+  static constexpr int NF = FX * WY * WZ;   // slab footprint nodes
   static constexpr int NS = DIM == 3 ? S * S * S : (DIM == 2 ? S * S : S);
-  static constexpr int NW = DIM == 3 ? W * W * W : (DIM == 2 ? W * W : W);
-  static constexpr int NCELL = DIM == 3 ? T * T * T : (DIM == 2 ? T * T : T);
+  static constexpr int NCELL = TX * TY * TZ;
+  static constexpr int CPW = L * TY * TZ;   // cells per warp
 };
 
-__host__ __device__ inline int tile_edge(int dim, int basis) {
-  return dim == 3 ? (basis == 2 ? 4 : 8) : (dim == 2 ? (basis == 2 ? 8 : 16) : 64);
+__host__ __device__ inline void tile_dims(int dim, int basis, int *t) {
+  (void)basis;
+  t[0] = dim == 3 ? 8 : (dim == 2 ? 16 : 64);
+  t[1] = dim == 3 ? 4 : (dim == 2 ? 16 : 1);
+  t[2] = dim == 3 ? 4 : 1;
 }
 __host__ __device__ inline int stencil_width(int basis) { return basis == 0 ? 2 : (basis == 1 ? 4 : 3); }
 __host__ __device__ inline int stencil_lo(int basis) { return basis == 1 ? 1 : 0; }
@@ -193,6 +222,22 @@ template <> __device__ __forceinline__ void basis<2>(float r, int nt, float ih, 
   }
 }
 
+// Cubic B-spline values and slopes of the four nodes c-1..c+2 of a particle at
+// fractional position f in cell c, when all four have ntype 0: the same
+// polynomials as src/basis_functions.h:40-104 evaluated without branches.
+__device__ __forceinline__ bool cubic_interior(int i0, int n, int ng) { return i0 >= 2 && i0 + 3 <= min(n - 1, ng - 3); }
+__device__ __forceinline__ void cubic_weights(float f, float ih, float *s, float *ds) {
+  const float g = 1.f - f, f2 = f * f, g2 = g * g;
+  s[0] = g2 * g * (1.f / 6.f);
+  s[1] = (0.5f * f - 1.f) * f2 + 2.f / 3.f;
+  s[2] = (0.5f * g - 1.f) * g2 + 2.f / 3.f;
+  s[3] = f2 * f * (1.f / 6.f);
+  ds[0] = -0.5f * g2 * ih;
+  ds[1] = (1.5f * f - 2.f) * f * ih;
+  ds[2] = (2.f - 1.5f * g) * g * ih;
+  ds[3] = 0.5f * f2 * ih;
+}
+
 // Per-axis stencil values of one particle: base node index i0 and, for each
 // stencil slot s, the basis value and derivative (0 where the node is absent).
 template <int BASIS> struct Axis {
@@ -205,6 +250,10 @@ template <int BASIS> struct Axis {
     float t = fminf(fmaxf((xp - lo) * ih, -4.f), (float)(n + 4));
     int c = (int)t;
     i0 = c * Stencil<BASIS>::SC - Stencil<BASIS>::LO;
+    if (BASIS == 1 && cubic_interior(i0, n, ng)) {
+      cubic_weights(t - (float)c, ih, s, ds);
+      return;
+    }
 #pragma unroll
     for (int k = 0; k < S; k++) {
       int i = i0 + k;
@@ -293,10 +342,13 @@ __device__ inline bool polar_rotation(const float *F, float *R) {
   for (int k = 0; k < 9; k++) X[k] = F[k];
   float d = det3(X);
   if (!(d > 0.f)) return false;
+  // quadratic convergence: stop once the update is at FP32 rounding level
+  // (|dX|_F < ~3e-7); the determinant scaling is dropped once |det X - 1| is
+  // small, where it no longer accelerates the iteration
   for (int it = 0; it < 12; it++) {
     cof3(X, C);
     float dx = det3(X);
-    float g = cbrtf(1.f / fabsf(dx));   // scaling (Higham 1986, sec. 3)
+    float g = fabsf(dx - 1.f) > 1e-3f ? cbrtf(1.f / fabsf(dx)) : 1.f;  // scaling (Higham 1986, sec. 3)
     float gi = 1.f / (g * dx);         // X^-T / g = C / (g det X)
     float diff = 0.f;
 #pragma unroll
@@ -306,7 +358,7 @@ __device__ inline bool polar_rotation(const float *F, float *R) {
       diff += e * e;
       X[k] = xn;
     }
-    if (diff < 1e-14f) break;
+    if (diff < 1e-13f) break;
   }
 #pragma unroll
   for (int k = 0; k < 9; k++) R[k] = X[k];
@@ -373,14 +425,15 @@ struct ConstitutiveIn {
 // src/eos_fluid.cpp:68-73); T is the particle temperature or 0.
 template <typename R>
 __device__ inline R eos_pressure(const MatDev &m, R J, R Jm1, R rho, R damage, R trD, R cellsize, R T) {
-  if (m.eos == 0) return -R(m.eos_p[1]) * Jm1 * (R(1) - damage);
+  const auto *ep = MatP<R>::eos(m);
+  if (m.eos == 0) return -R(ep[1]) * Jm1 * (R(1) - damage);
   // rho/rho0 = 1/J; the compressions below are written in J - 1 so that FP32
   // keeps them accurate when J is close to 1 (no 1/J - 1 cancellation)
   if (m.eos == 2) {  // K ((rho/rho0)^gamma - 1) = K expm1(-gamma log1p(J-1))
-    return R(m.eos_p[1]) * expm1(-R(m.eos_p[2]) * log1p(Jm1));
+    return R(ep[1]) * expm1(-R(ep[2]) * log1p(Jm1));
   }
-  R rho0 = m.eos_p[0], c0 = m.eos_p[2], S = m.eos_p[3], Gamma = m.eos_p[4], cv = m.eos_p[5], Tr = m.eos_p[6];
-  R Q1 = m.eos_p[7], Q2 = m.eos_p[8];
+  R rho0 = ep[0], c0 = ep[2], S = ep[3], Gamma = ep[4], cv = ep[5], Tr = ep[6];
+  R Q1 = ep[7], Q2 = ep[8];
   R mu = -Jm1 / J;  // rho/rho0 - 1
   R dd = R(1) - (S - R(1)) * mu;
   R pH = rho0 * c0 * c0 * mu * (R(1) + mu) / (dd * dd);
@@ -401,7 +454,7 @@ __device__ inline Sym<R> strength_update(const MatDev &m, R dt, const Sym<R> &si
                                          R epsdot, R damage, R T) {
   Sym<R> out;
   dep = R(0);
-  const double *p = m.str_p;
+  const auto *p = MatP<R>::str(m);
   if (m.strength == 0) {  // linear: dev(sigma) + dt 2G(1-D) dev(D)
     Sym<R> s = sig, d = D;
     s.dev(); d.dev();
@@ -472,7 +525,7 @@ __device__ inline Sym<R> strength_update(const MatDev &m, R dt, const Sym<R> &si
 template <typename R>
 __device__ inline void damage_update(const MatDev &m, R &dinit, R &damage, R pH, const Sym<R> &sdev, R epsdot, R dep,
                                      R T) {
-  const double *p = m.dam_p;
+  const auto *p = MatP<R>::dam(m);
   if (dep == R(0) && damage >= R(1)) return;
   R vm = R(KMPM_SQRT_3_OVER_2) * sdev.norm();
   R triax = R(0);

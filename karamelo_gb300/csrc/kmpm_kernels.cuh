@@ -62,8 +62,10 @@ struct PartArgs {
   ErrState *err;
   float *blk_c, *blk_h;
   float pic_flip;
+  float T_ref;               // particle and nodal temperatures are stored as T - T_ref
   float boxlo[3], boxhi[3];
-  int indep, use_vu, thermal, track_strain, dim, tile_T;
+  int indep, use_vu, thermal, track_strain, dim;
+  int tile_t[3];
 };
 
 struct DtArgs {
@@ -84,7 +86,7 @@ struct LaunchSet {
 // kernel entry points of one (dim, basis) instantiation
 struct StepKernels {
   void *p2g_mass, *p2g_tl, *p2g_tl_th, *p2g_ul, *p2g_ul_th, *p2g_vel, *p2g_vel_th;
-  void *grid_mass, *grid_upd[2][2], *grid_vel[2][2];
+  void *grid_mass[2], *grid_upd[2][2][2], *grid_vel[2][2][2];
   void *g2p1[2][2], *g2p2[2][2][2];
 };
 

@@ -21,18 +21,18 @@ __global__ void k_cell_keys(PartArgs a, int *keys, int use_x0) {
   if (p >= rd.start + rd.count) return;
   const float *P = *a.Pp;
   const GridDev g = a.grids[rd.grid];
-  const int T = a.tile_T;
+  const int *T = a.tile_t;
   int c[3] = {0, 0, 0};
   for (int d = 0; d < a.dim; d++) {
     const float xp = P[(PF_X0 + d) * a.ps + p] + (use_x0 ? 0.f : P[(PF_XN + d) * a.ps + p]);
     int cd = (int)((xp - g.lo[d]) * g.inv_cellsize);
     c[d] = max(0, min(cd, g.ncell[d] - 1));
   }
-  const int t[3] = {c[0] / T, a.dim >= 2 ? c[1] / T : 0, a.dim == 3 ? c[2] / T : 0};
-  const int l[3] = {c[0] % T, a.dim >= 2 ? c[1] % T : 0, a.dim == 3 ? c[2] % T : 0};
-  const int tl = a.dim == 3 ? (t[0] * g.ntile[1] + t[1]) * g.ntile[2] + t[2] : (a.dim == 2 ? t[0] * g.ntile[1] + t[1] : t[0]);
-  const int lc = a.dim == 3 ? (l[0] * T + l[1]) * T + l[2] : (a.dim == 2 ? l[0] * T + l[1] : l[0]);
-  const int ncpt = a.dim == 3 ? T * T * T : (a.dim == 2 ? T * T : T);
+  const int t[3] = {c[0] / T[0], c[1] / T[1], c[2] / T[2]};
+  const int l[3] = {c[0] % T[0], c[1] % T[1], c[2] % T[2]};
+  const int tl = (t[0] * g.ntile[1] + t[1]) * g.ntile[2] + t[2];
+  const int lc = (l[0] * T[1] + l[1]) * T[2] + l[2];
+  const int ncpt = T[0] * T[1] * T[2];
   keys[p] = (g.tile_off + tl) * ncpt + lc;
 }
 
@@ -374,11 +374,15 @@ void get_step_kernels(int dim, int basis, StepKernels &k) {
 }
 
 int p2g_smem_bytes(int dim, int basis, int mode, bool thermal) {
-  const int S = stencil_width(basis), T = tile_edge(dim, basis), SC = stencil_sc(basis);
-  const int W = (T - 1) * SC + S;
-  const int NW = dim == 3 ? W * W * W : (dim == 2 ? W * W : W);
+  const int S = stencil_width(basis), SC = stencil_sc(basis);
+  int t[3];
+  tile_dims(dim, basis, t);
+  const int L = t[0] / 8;
+  const int WY = dim >= 2 ? (t[1] - 1) * SC + S : 1, WZ = dim == 3 ? (t[2] - 1) * SC + S : 1;
+  const int NF = ((L - 1) * SC + S) * WY * WZ;
   const int Q = p2g_nq(mode, thermal), QIN = p2g_nin(mode, thermal);
-  return 4 * (((Q * NW + 3) & ~3) + 8 * (32 * (dim + QIN) + 32 * dim * S * 2));
+  const int slab = (Q * NF + 3) & ~3;
+  return 4 * 8 * (slab + 32 * (dim + QIN) + 32 * dim * S * 2);
 }
 
 }  // namespace kmpm

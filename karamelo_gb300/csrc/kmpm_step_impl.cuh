@@ -16,168 +16,225 @@
 namespace kmpm {
 
 // ============================================================== P2G (scatter)
-// One CTA per non-empty tile of T^DIM cells, 8 warps.  Cells are processed in
-// colour rounds (cell index mod C in every axis); the stencils of the cells of
-// one round are disjoint, so each round adds into the shared footprint
-// accumulator without conflicts, in a fixed order.  Inside a cell, a warp's
-// lanes own the cell's stencil nodes (2 per lane) and loop over the cell's
-// particles in sorted order, accumulating in registers.  The footprint is then
-// written to the tile's slice of the partial buffer.
+// One CTA of 8 warps per non-empty tile.  Warp w owns the x-slab of cells
+// [w L, (w+1) L) of the tile and visits its cells in a fixed order; for every
+// cell the lanes first stage the cell's particles (lane = particle: payload
+// and the per-axis basis values, next cell prefetched into registers), then
+// own the cell's stencil nodes (lane = node) and accumulate over the cell's
+// particles in sorted order, then add the result into the warp's private
+// slab footprint in shared memory.  After one barrier the slab footprints are
+// summed in warp order into the tile's slice of the partial buffer.  No float
+// atomics: the result is bit-reproducible.
 template <int DIM, int BASIS, int MODE, bool THERMAL>
 __global__ void __launch_bounds__(256) k_p2g(P2GArgs a) {
   using TS = TileShape<DIM, BASIS>;
-  constexpr int T = TS::T, S = TS::S, W = TS::W, NS = TS::NS, NW = TS::NW;
-  constexpr int C = Stencil<BASIS>::C, SC = Stencil<BASIS>::SC, LO = Stencil<BASIS>::LO;
+  constexpr int S = TS::S, SC = TS::SC, LO = Stencil<BASIS>::LO;
+  constexpr int TX = TS::TX, TY = TS::TY, TZ = TS::TZ, L = TS::L;
+  constexpr int WX = TS::WX, WY = TS::WY, WZ = TS::WZ, FX = TS::FX, NW = TS::NW, NF = TS::NF, NS = TS::NS;
   constexpr int Q = p2g_nq(MODE, THERMAL);
   constexpr int QIN = p2g_nin(MODE, THERMAL);
-  constexpr int TPC = T / C;  // cells per colour per axis
-  constexpr int NCOL = DIM == 3 ? C * C * C : (DIM == 2 ? C * C : C);
-  constexpr int NCPC = DIM == 3 ? TPC * TPC * TPC : (DIM == 2 ? TPC * TPC : TPC);
   constexpr int NSL = (NS + 31) / 32;  // stencil nodes per lane
+  constexpr bool PAIR = (DIM == 3 && S == 4);  // lane owns (a,b,c) and (a,b,c+2)
+  constexpr int SLAB = (Q * NF + 3) & ~3;
+  constexpr int STAGE = 32 * (DIM + QIN) + 32 * DIM * S * 2;
 
-  constexpr int QNW = (Q * NW + 3) & ~3;  // keeps the float2 staging 16-byte aligned
   extern __shared__ __align__(16) float smem[];
-  float *acc = smem;                              // Q * NW
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  float *wbase = smem + QNW + warp * (32 * (DIM + QIN) + 32 * DIM * S * 2);
-  float *spos = wbase;                            // 32 * DIM
-  float *spay = spos + 32 * DIM;                  // 32 * QIN
-  float2 *sbas = reinterpret_cast<float2 *>(spay + 32 * QIN);  // 32 * DIM * S
+  float *slab = smem + warp * SLAB;                                // Q * NF
+  float *spos = smem + TS::NWARP * SLAB + warp * STAGE;            // 32 * DIM
+  float *spay = spos + 32 * DIM;                                   // 32 * QIN
+  float2 *sbas = reinterpret_cast<float2 *>(spay + 32 * QIN);      // 32 * DIM * S
 
   const int2 td = a.tiles[blockIdx.x];
   const GridDev g = a.grids[td.x];
   const int tlin = td.y;
+  const int tile_global = g.tile_off + tlin;
+  if (a.tile_end[tile_global] == a.tile_start[tile_global] || run_finished(a.scalars)) return;
   int tc[3];
   tc[2] = DIM == 3 ? tlin % g.ntile[2] : 0;
   tc[1] = DIM >= 2 ? (DIM == 3 ? (tlin / g.ntile[2]) % g.ntile[1] : tlin % g.ntile[1]) : 0;
   tc[0] = DIM == 3 ? tlin / (g.ntile[1] * g.ntile[2]) : (DIM == 2 ? tlin / g.ntile[1] : tlin);
-  const int tile_global = g.tile_off + tlin;
   const float h = g.cellsize / SC, ih = g.inv_cellsize;
+  const int gn0 = g.n[0], gn1 = g.n[1], gn2 = g.n[2], gng0 = g.ng[0], gng1 = g.ng[1], gng2 = g.ng[2];
+  const float glo0 = g.lo[0], glo1 = g.lo[1], glo2 = g.lo[2];
   const float *P = *a.Pp;
-  if (a.tile_end[tile_global] == a.tile_start[tile_global] || run_finished(a.scalars)) return;
+  const size_t ps = a.ps;
 
-  for (int k = threadIdx.x; k < Q * NW; k += blockDim.x) acc[k] = 0.f;
-  __syncthreads();
+  for (int k = lane; k < Q * NF; k += 32) slab[k] = 0.f;
 
-  // stencil slots of this lane
+  // stencil slots (a, b, c) of this lane
   int soff[NSL][3];
 #pragma unroll
   for (int u = 0; u < NSL; u++) {
-    int sidx = lane + 32 * u;
-    if (DIM == 3) { soff[u][0] = sidx / (S * S); soff[u][1] = (sidx / S) % S; soff[u][2] = sidx % S; }
-    else if (DIM == 2) { soff[u][0] = sidx / S; soff[u][1] = sidx % S; soff[u][2] = 0; }
-    else { soff[u][0] = sidx; soff[u][1] = 0; soff[u][2] = 0; }
+    if (PAIR) {
+      soff[u][0] = (lane & 15) >> 2; soff[u][1] = lane & 3; soff[u][2] = (lane >> 4) + 2 * u;
+    } else {
+      const int sidx = lane + 32 * u;
+      if (DIM == 3) { soff[u][0] = sidx / (S * S); soff[u][1] = (sidx / S) % S; soff[u][2] = sidx % S; }
+      else if (DIM == 2) { soff[u][0] = sidx / S; soff[u][1] = sidx % S; soff[u][2] = 0; }
+      else { soff[u][0] = sidx; soff[u][1] = 0; soff[u][2] = 0; }
+    }
   }
+  const bool lane_active = PAIR || lane < NS;
 
-  for (int col = 0; col < NCOL; col++) {
-    int cc[3];
-    if (DIM == 3) { cc[0] = col / (C * C); cc[1] = (col / C) % C; cc[2] = col % C; }
-    else if (DIM == 2) { cc[0] = col / C; cc[1] = col % C; cc[2] = 0; }
-    else { cc[0] = col; cc[1] = 0; cc[2] = 0; }
-    for (int kc = warp; kc < NCPC; kc += 8) {
-      int lc[3];
-      if (DIM == 3) { lc[0] = cc[0] + C * (kc / (TPC * TPC)); lc[1] = cc[1] + C * ((kc / TPC) % TPC); lc[2] = cc[2] + C * (kc % TPC); }
-      else if (DIM == 2) { lc[0] = cc[0] + C * (kc / TPC); lc[1] = cc[1] + C * (kc % TPC); lc[2] = 0; }
-      else { lc[0] = cc[0] + C * kc; lc[1] = 0; lc[2] = 0; }
-      const int lcell = DIM == 3 ? (lc[0] * T + lc[1]) * T + lc[2] : (DIM == 2 ? lc[0] * T + lc[1] : lc[0]);
-      const int cell_id = tile_global * TS::NCELL + lcell;
-      const int cstart = a.cell_start[cell_id];
-      const int ccount = a.cell_end[cell_id] - cstart;
-      if (ccount == 0) continue;
-      // base node index of the stencil along each axis
-      int i0[3];
-#pragma unroll
-      for (int d = 0; d < 3; d++) i0[d] = (d < DIM) ? (tc[d] * T + lc[d]) * SC - LO : 0;
+  // the k-th cell of this warp's slab: local cell index (lx*TY + ly)*TZ + lz
+  const int cell_base = tile_global * TS::NCELL + warp * L * TY * TZ;
+  // prefetch registers: one particle per lane
+  float ppos[DIM], ppay[QIN];
+  const bool use_u = a.pos_field == PF_X;
+#define KMPM_LOAD_PARTICLE(p_)                                                                   \
+  do {                                                                                         \
+    const int pp_ = (p_);                                                                      \
+    _Pragma("unroll") for (int d = 0; d < DIM; d++) ppos[d] =                                  \
+        P[(PF_X0 + d) * ps + pp_] + (use_u ? P[(PF_X + d) * ps + pp_] : 0.f);                 \
+    p2g_payload<MODE, THERMAL>(a, P, pp_, ppay);                                               \
+  } while (0)
 
-      float accr[NSL][Q];
+  int nstart = a.cell_start[cell_base];
+  int ncount = a.cell_end[cell_base] - nstart;
+  if (lane < ncount) KMPM_LOAD_PARTICLE(nstart + lane);
+  for (int k = 0; k < TS::CPW; k++) {
+    const int cstart = nstart, ccount = ncount;
+    if (k + 1 < TS::CPW) {
+      nstart = a.cell_start[cell_base + k + 1];
+      ncount = a.cell_end[cell_base + k + 1] - nstart;
+    }
+    if (ccount == 0) {
+      if (k + 1 < TS::CPW && lane < ncount) KMPM_LOAD_PARTICLE(nstart + lane);
+      continue;
+    }
+    const int lc[3] = {warp * L + k / (TY * TZ), (k / TZ) % TY, k % TZ};
+    int i0[3];
+    const int tco[3] = {tc[0] * TX, tc[1] * TY, tc[2] * TZ};
 #pragma unroll
-      for (int u = 0; u < NSL; u++)
-#pragma unroll
-        for (int q = 0; q < Q; q++) accr[u][q] = 0.f;
+    for (int d = 0; d < 3; d++) i0[d] = (d < DIM) ? (tco[d] + lc[d]) * SC - LO : 0;
 
-      for (int c0 = 0; c0 < ccount; c0 += 32) {
-        const int cnt = min(32, ccount - c0);
-        // ---- stage positions and payload (lane = particle)
-        if (lane < cnt) {
-          const int p = cstart + c0 + lane;
+    float accr[NSL][Q];
 #pragma unroll
-          for (int d = 0; d < DIM; d++)
-            spos[lane * DIM + d] = P[(PF_X0 + d) * a.ps + p] + (a.pos_field == PF_X ? P[(PF_X + d) * a.ps + p] : 0.f);
-          float pay[QIN];
-          p2g_payload<MODE, THERMAL>(a, P, p, pay);
+    for (int u = 0; u < NSL; u++)
 #pragma unroll
-          for (int q = 0; q < QIN; q++) spay[lane * QIN + q] = pay[q];
+      for (int q = 0; q < Q; q++) accr[u][q] = 0.f;
+
+    for (int c0 = 0; c0 < ccount; c0 += 32) {
+      const int cnt = min(32, ccount - c0);
+      if (c0 > 0 && lane < cnt) KMPM_LOAD_PARTICLE(cstart + c0 + lane);  // cells with more than 32 particles
+      // ---- stage (lane = particle)
+      if (lane < cnt) {
+#pragma unroll
+        for (int d = 0; d < DIM; d++) spos[lane * DIM + d] = ppos[d];
+#pragma unroll
+        for (int q = 0; q < QIN; q++) spay[lane * QIN + q] = ppay[q];
+      }
+      __syncwarp();
+      // prefetch the next cell while this one is computed
+      if (c0 + 32 >= ccount && k + 1 < TS::CPW && lane < ncount) KMPM_LOAD_PARTICLE(nstart + lane);
+      // ---- per (particle, axis, slot) basis values
+      bool interior = false;
+      if (BASIS == 1) {
+        interior = cubic_interior(i0[0], gn0, gng0);
+        if (DIM >= 2) interior = interior && cubic_interior(i0[1], gn1, gng1);
+        if (DIM == 3) interior = interior && cubic_interior(i0[2], gn2, gng2);
+      }
+      if (interior) {
+        for (int it = lane; it < cnt * DIM; it += 32) {
+          const int j = it / DIM, d = it % DIM;
+          const int i0d = d == 0 ? i0[0] : (d == 1 ? i0[1] : i0[2]);
+          const float lod = d == 0 ? glo0 : (d == 1 ? glo1 : glo2);
+          const float t = (spos[j * DIM + d] - lod) * ih;
+          float sv[4], dsv[4];
+          cubic_weights(t - (float)(i0d + 1), ih, sv, dsv);
+#pragma unroll
+          for (int kk = 0; kk < 4; kk++) sbas[it * S + kk] = make_float2(sv[kk], dsv[kk]);
         }
-        __syncwarp();
-        // ---- per (particle, axis, slot) basis values
-        for (int it = lane; it < cnt * DIM * S; it += 32) {
-          const int j = it / (DIM * S), d = (it / S) % DIM, k = it % S;
-          const int i = i0[d] + k;
-          float s = 0.f, ds = 0.f;
-          if (i >= 0 && i < g.n[d]) {
-            const float xn = g.lo[d] + (float)i * h;
-            const float r = (spos[j * DIM + d] - xn) * ih;
-            basis<BASIS>(r, node_type<BASIS>(i, g.ng[d]), ih, s, ds);
-          }
-          sbas[it] = make_float2(s, ds);
+      } else
+      for (int it = lane; it < cnt * DIM * S; it += 32) {
+        const int j = it / (DIM * S), d = (it / S) % DIM, kk = it % S;
+        // per-axis constants selected without indexing local arrays
+        const int i = (d == 0 ? i0[0] : (d == 1 ? i0[1] : i0[2])) + kk;
+        const int nd = d == 0 ? gn0 : (d == 1 ? gn1 : gn2);
+        const int ngd = d == 0 ? gng0 : (d == 1 ? gng1 : gng2);
+        const float lod = d == 0 ? glo0 : (d == 1 ? glo1 : glo2);
+        float sv = 0.f, dsv = 0.f;
+        if (i >= 0 && i < nd) {
+          const float xn = lod + (float)i * h;
+          const float r = (spos[j * DIM + d] - xn) * ih;
+          basis<BASIS>(r, node_type<BASIS>(i, ngd), ih, sv, dsv);
         }
-        __syncwarp();
-        // ---- accumulate (lane = stencil node)
+        sbas[it] = make_float2(sv, dsv);
+      }
+      __syncwarp();
+      // ---- accumulate (lane = stencil node)
+      if (lane_active) {
         for (int j = 0; j < cnt; j++) {
           const float *pay = spay + j * QIN;
           const float2 *bj = sbas + j * DIM * S;
+          const float2 bx = bj[soff[0][0]];
+          const float2 by = DIM >= 2 ? bj[S + soff[0][1]] : make_float2(1.f, 0.f);
+          const float wxy = bx.x * by.x, gxy0 = bx.y * by.x, gxy1 = bx.x * by.y;
 #pragma unroll
           for (int u = 0; u < NSL; u++) {
-            if (lane + 32 * u >= NS) continue;
-            float2 bx = bj[soff[u][0]];
-            float2 by = DIM >= 2 ? bj[S + soff[u][1]] : make_float2(1.f, 0.f);
-            float2 bz = DIM == 3 ? bj[2 * S + soff[u][2]] : make_float2(1.f, 0.f);
-            float wxy = bx.x * by.x;
-            float w = wxy * bz.x;
+            if (!PAIR && lane + 32 * u >= NS) continue;
+            const float2 bz = DIM == 3 ? bj[2 * S + soff[u][2]] : make_float2(1.f, 0.f);
+            const float w = wxy * bz.x;
             // the reference keeps a particle-node pair only when every 1-D
             // value is non-zero (src/tlmpm.cpp:263, src/ulmpm.cpp:259-272); the
             // cubic spline at ntype 1 has a zero value but a non-zero slope
             if (w == 0.f) continue;
-            float gw[3] = {bx.y * by.x * bz.x, bx.x * by.y * bz.x, wxy * bz.y};
+            const float gw[3] = {gxy0 * bz.x, gxy1 * bz.x, wxy * bz.y};
             p2g_accumulate<MODE, THERMAL, Q>(accr[u], pay, w, gw);
           }
         }
-        __syncwarp();
       }
-      // ---- flush into the footprint (no conflicts within a colour round)
+      __syncwarp();
+    }
+    // ---- add into this warp's slab footprint (only this warp writes it)
+    if (lane_active) {
 #pragma unroll
       for (int u = 0; u < NSL; u++) {
-        if (lane + 32 * u >= NS) continue;
-        int fl[3];
+        if (!PAIR && lane + 32 * u >= NS) continue;
+        const int fx = (lc[0] - warp * L) * SC + soff[u][0];
+        const int fy = DIM >= 2 ? lc[1] * SC + soff[u][1] : 0;
+        const int fz = DIM == 3 ? lc[2] * SC + soff[u][2] : 0;
+        const int fi = (fx * WY + fy) * WZ + fz;
 #pragma unroll
-        for (int d = 0; d < 3; d++) fl[d] = (d < DIM) ? lc[d] * SC + soff[u][d] : 0;
-        const int fi = DIM == 3 ? (fl[0] * W + fl[1]) * W + fl[2] : (DIM == 2 ? fl[0] * W + fl[1] : fl[0]);
-#pragma unroll
-        for (int q = 0; q < Q; q++) acc[q * NW + fi] += accr[u][q];
+        for (int q = 0; q < Q; q++) slab[q * NF + fi] += accr[u][q];
       }
     }
-    __syncthreads();
+    __syncwarp();
   }
-  // ---- write the footprint
+#undef KMPM_LOAD_PARTICLE
+  __syncthreads();
+  // ---- sum the slabs in warp order into the tile footprint
   float *out = a.partial + (size_t)tile_global * a.pstride_tile;
-  for (int k = threadIdx.x; k < Q * NW; k += blockDim.x) out[k] = acc[k];
+  for (int k = threadIdx.x; k < Q * NW; k += blockDim.x) {
+    const int q = k / NW, fi = k % NW;
+    const int fx = fi / (WY * WZ), fyz = fi % (WY * WZ);
+    float sum = 0.f;
+#pragma unroll
+    for (int w = 0; w < TS::NWARP; w++) {
+      const int x = fx - w * L * SC;
+      if (x >= 0 && x < FX) sum += smem[w * SLAB + q * NF + x * WY * WZ + fyz];
+    }
+    out[k] = sum;
+  }
 }
 
 // ============================================================== grid
 // Sum of the tile partials covering one node, in a fixed tile order.
-template <int DIM, int BASIS, int Q>
-__device__ __forceinline__ void gather_partials(const GridArgs &a, const GridDev &g, int li, const int *ix, double *sum) {
+template <int DIM, int BASIS, int Q, typename ACC>
+__device__ __forceinline__ void gather_partials(const GridArgs &a, const GridDev &g, int li, const int *ix, ACC *sum) {
   using TS = TileShape<DIM, BASIS>;
-  constexpr int T = TS::T, W = TS::W, NW = TS::NW, SC = Stencil<BASIS>::SC, LO = Stencil<BASIS>::LO;
-  constexpr int TN = T * SC;  // nodes per tile step
+  constexpr int SC = Stencil<BASIS>::SC, LO = Stencil<BASIS>::LO;
+  const int T[3] = {TS::TX, TS::TY, TS::TZ}, W[3] = {TS::WX, TS::WY, TS::WZ};
   int tlo[3], thi[3];
 #pragma unroll
   for (int d = 0; d < 3; d++) {
     if (d < DIM) {
-      // tile t covers nodes [t*TN - LO, t*TN - LO + W - 1]
-      int hi = (ix[d] + LO) / TN;
-      int lo_num = ix[d] + LO - W + 1;
-      int lo = lo_num <= 0 ? 0 : (lo_num + TN - 1) / TN;
+      // tile t covers nodes [t*T*SC - LO, t*T*SC - LO + W - 1]
+      const int TN = T[d] * SC;
+      const int hi = (ix[d] + LO) / TN;
+      const int lo_num = ix[d] + LO - W[d] + 1;
+      const int lo = lo_num <= 0 ? 0 : (lo_num + TN - 1) / TN;
       tlo[d] = max(lo, 0);
       thi[d] = min(hi, g.ntile[d] - 1);
     } else {
@@ -185,18 +242,19 @@ __device__ __forceinline__ void gather_partials(const GridArgs &a, const GridDev
     }
   }
 #pragma unroll
-  for (int q = 0; q < Q; q++) sum[q] = 0.0;
+  for (int q = 0; q < Q; q++) sum[q] = ACC(0);
   for (int tx = tlo[0]; tx <= thi[0]; tx++)
     for (int ty = tlo[1]; ty <= thi[1]; ty++)
       for (int tz = tlo[2]; tz <= thi[2]; tz++) {
         const int tl = DIM == 3 ? (tx * g.ntile[1] + ty) * g.ntile[2] + tz : (DIM == 2 ? tx * g.ntile[1] + ty : tx);
         const int tg = g.tile_off + tl;
         if (a.tile_end[tg] == a.tile_start[tg]) continue;
-        int fl[3] = {ix[0] - (tx * TN - LO), DIM >= 2 ? ix[1] - (ty * TN - LO) : 0, DIM == 3 ? ix[2] - (tz * TN - LO) : 0};
-        const int fi = DIM == 3 ? (fl[0] * W + fl[1]) * W + fl[2] : (DIM == 2 ? fl[0] * W + fl[1] : fl[0]);
+        const int fl[3] = {ix[0] - (tx * TS::TX * SC - LO), DIM >= 2 ? ix[1] - (ty * TS::TY * SC - LO) : 0,
+                           DIM == 3 ? ix[2] - (tz * TS::TZ * SC - LO) : 0};
+        const int fi = (fl[0] * TS::WY + fl[1]) * TS::WZ + fl[2];
         const float *src = a.partial + (size_t)tg * a.pstride_tile;
 #pragma unroll
-        for (int q = 0; q < Q; q++) sum[q] += (double)src[q * NW + fi];
+        for (int q = 0; q < Q; q++) sum[q] += (ACC)src[q * TS::NW + fi];
       }
   (void)li;
 }
@@ -205,9 +263,10 @@ __device__ __forceinline__ double fix_value(const FixDev &f, int d, double t) {
   return f.c[d][0] + f.c[d][1] * t + f.c[d][2] * exp(f.c[d][3] * t);
 }
 
-// MODE_GRID_MASS: nodal mass only (TL once).  MODE_GRID_UPDATE: after the
-// first scatter.  MODE_GRID_VEL: after the MUSL re-map (or USL: positions only).
-template <int DIM, int BASIS, int GMODE, bool TL, bool THERMAL>
+// GM_MASS: nodal mass only (TL once).  GM_UPDATE: after the first scatter.
+// GM_VEL: after the MUSL re-map (or USL: positions only).  R is the
+// arithmetic of the nodal sums and of v = p/m (double for the FP64 islands).
+template <int DIM, int BASIS, int GMODE, bool TL, bool THERMAL, typename R>
 __global__ void __launch_bounds__(256) k_grid(GridArgs a) {
   if (run_finished(a.scalars)) return;
   const int gi = a.blk_grid[blockIdx.x];
@@ -221,11 +280,12 @@ __global__ void __launch_bounds__(256) k_grid(GridArgs a) {
   ix[0] = li / (g.n[1] * g.n[2]);
   const int node = g.node_off + li;
   const StepScalars &sc = a.scalars[a.indep ? g.solid0 : 0];
-  const double dt = sc.dt, time = sc.time;
+  const R dt = (R)sc.dt;
+  const double time = sc.time;
 
   if (GMODE == GM_MASS) {
-    double s[1];
-    gather_partials<DIM, BASIS, 1>(a, g, li, ix, s);
+    R s[1];
+    gather_partials<DIM, BASIS, 1, R>(a, g, li, ix, s);
     float4 A = a.nodeA[node];
     A.w = (float)s[0];
     a.nodeA[node] = A;
@@ -234,37 +294,40 @@ __global__ void __launch_bounds__(256) k_grid(GridArgs a) {
   if (GMODE == GM_UPDATE) {
     // quantities: TL [p3 f3 (+mT Qext Qint)]; UL [m p3 f3 (+...)]
     constexpr int Q = TL ? (THERMAL ? 9 : 6) : (THERMAL ? 10 : 7);
-    double s[Q];
-    gather_partials<DIM, BASIS, Q>(a, g, li, ix, s);
+    R s[Q];
+    gather_partials<DIM, BASIS, Q, R>(a, g, li, ix, s);
     const int o = TL ? 0 : 1;
     float4 A = a.nodeA[node];
-    double m = TL ? (double)A.w : s[0];
-    double v[3], f[3], mb[3] = {0, 0, 0}, vu[3];
+    const R m = TL ? (R)A.w : s[0];
+    R v[3], f[3], mb[3] = {0, 0, 0}, vu[3];
     // Solid::compute_velocity_nodes: v = p/m only where m > 0 (src/solid.cpp:357)
+    const R im = m > R(0) ? R(1) / m : R(0);
+#pragma unroll
     for (int d = 0; d < 3; d++) {
-      v[d] = m > 0 ? s[o + d] / m : 0.0;
+      v[d] = s[o + d] * im;
       f[d] = s[o + 3 + d];
     }
     // body force on nodes with mass (src/fix_body_force.cpp:122-136)
     for (int k = a.fix_start[gi]; k < a.fix_start[gi] + a.fix_count[gi]; k++) {
       const FixDev &fx = a.fixes[k];
-      if (fx.kind != 1 || !fx.mask[li] || !(m > 0)) continue;
+      if (fx.kind != 1 || !fx.mask[li] || !(m > R(0))) continue;
       for (int d = 0; d < 3; d++)
-        if (fx.set[d]) mb[d] += fx.c[d][0] * m;
+        if (fx.set[d]) mb[d] += (R)fx.c[d][0] * m;
     }
     // Grid::update_grid_velocities (src/grid.cpp:448-466)
-    for (int d = 0; d < 3; d++) vu[d] = m != 0 ? v[d] + dt * (f[d] + mb[d]) / m : v[d];
-    double T = 0, Tu = 0;
+#pragma unroll
+    for (int d = 0; d < 3; d++) vu[d] = m != R(0) ? v[d] + dt * (f[d] + mb[d]) * im : v[d];
+    R T = 0, Tu = 0;
     if (THERMAL) {
-      T = m > 0 ? s[o + 6] / m : 0.0;
-      Tu = m != 0 ? T + dt * (s[o + 8] + s[o + 7]) / m : T;  // src/grid.cpp:1354-1361
+      T = s[o + 6] * im;
+      Tu = m != R(0) ? T + dt * (s[o + 8] + s[o + 7]) * im : T;  // src/grid.cpp:1354-1361
     }
     // FixVelocityNodes::post_update_grid_state (src/fix_velocity_nodes.cpp:130-225)
     for (int k = a.fix_start[gi]; k < a.fix_start[gi] + a.fix_count[gi]; k++) {
       const FixDev &fx = a.fixes[k];
       if (fx.kind != 0 || !fx.mask[li]) continue;
       for (int d = 0; d < 3; d++)
-        if (fx.set[d]) { vu[d] = fix_value(fx, d, time); v[d] = fix_value(fx, d, time - dt); }
+        if (fx.set[d]) { vu[d] = (R)fix_value(fx, d, time); v[d] = (R)fix_value(fx, d, time - sc.dt); }
     }
     a.nodeA[node] = make_float4((float)v[0], (float)v[1], (float)v[2], (float)m);
     a.nodeB[node] = make_float4((float)vu[0], (float)vu[1], (float)vu[2], (float)Tu);
@@ -273,20 +336,22 @@ __global__ void __launch_bounds__(256) k_grid(GridArgs a) {
   }
   // GM_VEL: MUSL velocities_to_grid (+ BCs on v) and TL grid positions
   float4 A = a.nodeA[node];
-  double v[3] = {A.x, A.y, A.z};
+  R v[3] = {A.x, A.y, A.z};
   if (a.remap) {
     constexpr int Q = THERMAL ? 4 : 3;
-    double s[Q];
-    gather_partials<DIM, BASIS, Q>(a, g, li, ix, s);
-    double m = A.w;
-    for (int d = 0; d < 3; d++) v[d] = m > 0 ? s[d] / m : 0.0;
-    if (THERMAL) a.nodeT[node] = (float)(m > 0 ? s[3] / m : 0.0);
+    R s[Q];
+    gather_partials<DIM, BASIS, Q, R>(a, g, li, ix, s);
+    const R m = A.w;
+    const R im = m > R(0) ? R(1) / m : R(0);
+#pragma unroll
+    for (int d = 0; d < 3; d++) v[d] = s[d] * im;
+    if (THERMAL) a.nodeT[node] = (float)(s[3] * im);
     // FixVelocityNodes::post_velocities_to_grid (src/fix_velocity_nodes.cpp:227-271)
     for (int k = a.fix_start[gi]; k < a.fix_start[gi] + a.fix_count[gi]; k++) {
       const FixDev &fx = a.fixes[k];
       if (fx.kind != 0 || !fx.mask[li]) continue;
       for (int d = 0; d < 3; d++)
-        if (fx.set[d]) v[d] = fix_value(fx, d, time);
+        if (fx.set[d]) v[d] = (R)fix_value(fx, d, time);
     }
     a.nodeA[node] = make_float4((float)v[0], (float)v[1], (float)v[2], A.w);
   }
@@ -298,7 +363,6 @@ __global__ void __launch_bounds__(256) k_grid(GridArgs a) {
     a.nodeX[node] = X;
   }
 }
-
 
 // ============================================================== G2P
 template <int DIM, int BASIS> struct PAxes {
@@ -351,9 +415,11 @@ __global__ void __launch_bounds__(256) k_g2p1(PartArgs a) {
   constexpr int S = Stencil<BASIS>::S;
   constexpr int SY = DIM >= 2 ? S : 1, SZ = DIM == 3 ? S : 1;
   float vu[3] = {0, 0, 0}, dv[3] = {0, 0, 0}, Tp = 0.f;
+#pragma unroll
   for (int i = 0; i < S; i++) {
     const float sx = ax.ax[0].s[i];
     if (sx == 0.f) continue;
+#pragma unroll
     for (int j = 0; j < SY; j++) {
       const float sxy = sx * ax.ax[1].s[j];
       if (sxy == 0.f) continue;
@@ -421,9 +487,11 @@ __global__ void __launch_bounds__(256) k_g2p2(PartArgs a) {
     constexpr int SY = DIM >= 2 ? S : 1, SZ = DIM == 3 ? S : 1;
     float G[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
     float qg[3] = {0, 0, 0};
+#pragma unroll
     for (int i = 0; i < S; i++) {
       const float sx = ax.ax[0].s[i], dsx = ax.ax[0].ds[i];
       if (sx == 0.f) continue;
+#pragma unroll
       for (int j = 0; j < SY; j++) {
         const float sy = ax.ax[1].s[j], dsy = ax.ax[1].ds[j];
         if (sx * sy == 0.f) continue;
@@ -486,7 +554,7 @@ __global__ void __launch_bounds__(256) k_g2p2(PartArgs a) {
     float dmg = P[PF_DMG * ps + p];
     if (J <= 0.f && dmg < 1.f) raise_error(a.err, ERR_J, p, sc.ntimestep);
     const float vol0 = P[PF_VOL0 * ps + p];
-    const float rho = (float)m.rho0 / J;
+    const float rho = m.f_rho0 / J;
     float R[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
     Sym<float> D;
 #pragma unroll
@@ -524,7 +592,7 @@ __global__ void __launch_bounds__(256) k_g2p2(PartArgs a) {
     float PK1[9];
     bool have_pk1 = false;
     if (m.type == 0) {  // LINEAR
-      const float G2 = 2.f * (float)m.G, lam = (float)m.lambda;
+      const float G2 = 2.f * m.f_G, lam = m.f_lambda;
       const float trinc = dt * D.tr();
 #pragma unroll
       for (int k = 0; k < 6; k++) sig.a[k] += G2 * dt * D.a[k];
@@ -537,10 +605,13 @@ __global__ void __launch_bounds__(256) k_g2p2(PartArgs a) {
       float FiT[9];
 #pragma unroll
       for (int k = 0; k < 9; k++) FiT[k] = cofF[k] * iJ;
-      const float Gm = (float)m.G, lam = (float)m.lambda;
+      const float Gm = m.f_G, lam = m.f_lambda;
       const float lnJ = log1pf(Jm1);
+      // F - F^-T = H + F^-T H^T (no cancellation when F is close to I)
+      float FiTHt[9];
+      matmulT3(FiT, H, FiTHt);
 #pragma unroll
-      for (int k = 0; k < 9; k++) PK1[k] = Gm * (F[k] - FiT[k]) + lam * lnJ * FiT[k];
+      for (int k = 0; k < 9; k++) PK1[k] = Gm * (H[k] + FiTHt[k]) + lam * lnJ * FiT[k];
       have_pk1 = true;
       float FPt[9];
       matmulT3(F, PK1, FPt);  // F PK1^T
@@ -557,8 +628,8 @@ __global__ void __launch_bounds__(256) k_g2p2(PartArgs a) {
         P[(PF_STRAIN + 5) * ps + p] = 0.5f * FtF[5];
       }
     } else {  // EOS + strength (+ damage + temperature)
-      const bool hasT = m.cp != 0.0;
-      float T = hasT ? P[PF_T * ps + p] : 0.f;
+      const bool hasT = m.f_cp != 0.f;
+      float T = hasT ? a.T_ref + P[PF_T * ps + p] : 0.f;  // PF_T holds T - T_ref
       float epsp = P[PF_EPSP * ps + p], epsdot = P[PF_EPSDOT * ps + p];
       float dinit = m.damage >= 0 ? P[PF_DMGI * ps + p] : 0.f;
       float pH, dep;
@@ -578,24 +649,24 @@ __global__ void __launch_bounds__(256) k_g2p2(PartArgs a) {
         for (int k = 0; k < 6; k++) sdev.a[k] = (float)sdd.a[k];
       } else {
         pH = eos_pressure<float>(m, J, Jm1, rho, dmg, D.tr(), g.cellsize, T);
-        if (hasT) pH += (float)m.temp_p[3] * ((float)m.temp_p[4] - T);
+        if (hasT) pH += m.f_temp_p[3] * (m.f_temp_p[4] - T);
         sdev = strength_update<float>(m, dt, sig, D, dep, epsp, epsdot, dmg, T);
       }
       epsp += dep;
-      const float tav = 1000.f * g.cellsize / (float)m.signal_velocity;
+      const float tav = 1000.f * g.cellsize / m.f_signal_velocity;
       epsdot -= epsdot * dt / tav;
       epsdot += dep / tav;
       epsdot = fmaxf(0.f, epsdot);
       if (m.damage >= 0) {
-        float Tdm = a.thermal ? T : 0.f;
+        float Tdm = a.thermal ? a.T_ref + P[PF_T * ps + p] : 0.f;
         damage_update<float>(m, dinit, dmg, pH, sdev, epsdot, dep, Tdm);
         P[PF_DMGI * ps + p] = dinit;
         P[PF_DMG * ps + p] = dmg;
       }
       if (hasT) {
         const float flow = (float)KMPM_SQRT_3_OVER_2 * sdev.norm();
-        float gam = T < (float)m.temp_p[5] ? (float)m.temp_p[0] * flow * epsdot : 0.f;
-        gam *= (TL ? vol0 : J * vol0) * (float)m.invcp;
+        float gam = T < m.f_temp_p[5] ? m.f_temp_p[0] * flow * epsdot : 0.f;
+        gam *= (TL ? vol0 : J * vol0) * m.f_invcp;
         P[PF_GAMMA * ps + p] = gam;
       }
       P[PF_EPSP * ps + p] = epsp;
@@ -609,7 +680,7 @@ __global__ void __launch_bounds__(256) k_g2p2(PartArgs a) {
 #pragma unroll
         for (int k = 0; k < 3; k++) tre += P[(PF_STRAIN + k) * ps + p];
         const float tr3 = (dt * D.tr() + tre) / 3.f;
-        const float iG = dmg > 1e-10f ? 1.f / ((float)m.G * (1.f - dmg)) : 1.f / (float)m.G;
+        const float iG = dmg > 1e-10f ? 1.f / (m.f_G * (1.f - dmg)) : 1.f / m.f_G;
 #pragma unroll
         for (int k = 0; k < 6; k++) P[(PF_STRAIN + k) * ps + p] = sdev.a[k] * iG + (k < 3 ? tr3 : 0.f);
       }
@@ -634,14 +705,14 @@ __global__ void __launch_bounds__(256) k_g2p2(PartArgs a) {
       for (int k = 0; k < 6; k++) P[(PF_PK + k) * ps + p] = vol * sig.a[k];
     }
     if (THERMAL) {  // Solid::update_heat_flux (src/solid.cpp:2812-2839)
-      const float f = (TL ? vol0 : J * vol0) * (float)(m.invcp * m.kappa);
+      const float f = (TL ? vol0 : J * vol0) * (m.f_invcp * m.f_kappa);
 #pragma unroll
       for (int c = 0; c < 3; c++) P[(PF_Q + c) * ps + p] = qg[c] * f;
     }
     // ---- wave speed and h ratio (src/solid.cpp:1376-1437)
     if (dmg < 1.f) {
       const float vx = P[PF_V * ps + p], vy = P[(PF_V + 1) * ps + p], vz = P[(PF_V + 2) * ps + p];
-      const float c = sqrtf((float)(m.K + KMPM_FOUR_THIRD * m.G) / rho) + fmaxf(fmaxf(fabsf(vx), fabsf(vy)), fabsf(vz));
+      const float c = sqrtf(m.f_c2 / rho) + fmaxf(fmaxf(fabsf(vx), fabsf(vy)), fabsf(vz));
       if (isnan(c)) raise_error(a.err, ERR_NAN, p, sc.ntimestep);
       my_c = c;
       if (TL) my_h = fminf(1.f, min_abs_eig_real(H));
@@ -674,15 +745,18 @@ void fill_step_kernels(StepKernels &k) {
   k.p2g_ul_th = (void *)k_p2g<DIM, BASIS, P2G_UL, true>;
   k.p2g_vel = (void *)k_p2g<DIM, BASIS, P2G_VEL, false>;
   k.p2g_vel_th = (void *)k_p2g<DIM, BASIS, P2G_VEL, true>;
-  k.grid_mass = (void *)k_grid<DIM, BASIS, GM_MASS, true, false>;
-  k.grid_upd[0][0] = (void *)k_grid<DIM, BASIS, GM_UPDATE, false, false>;
-  k.grid_upd[0][1] = (void *)k_grid<DIM, BASIS, GM_UPDATE, false, true>;
-  k.grid_upd[1][0] = (void *)k_grid<DIM, BASIS, GM_UPDATE, true, false>;
-  k.grid_upd[1][1] = (void *)k_grid<DIM, BASIS, GM_UPDATE, true, true>;
-  k.grid_vel[0][0] = (void *)k_grid<DIM, BASIS, GM_VEL, false, false>;
-  k.grid_vel[0][1] = (void *)k_grid<DIM, BASIS, GM_VEL, false, true>;
-  k.grid_vel[1][0] = (void *)k_grid<DIM, BASIS, GM_VEL, true, false>;
-  k.grid_vel[1][1] = (void *)k_grid<DIM, BASIS, GM_VEL, true, true>;
+  k.grid_mass[0] = (void *)k_grid<DIM, BASIS, GM_MASS, true, false, float>;
+  k.grid_mass[1] = (void *)k_grid<DIM, BASIS, GM_MASS, true, false, double>;
+#define KMPM_GRID_SET(tl, th)                                                                  \
+  k.grid_upd[tl][th][0] = (void *)k_grid<DIM, BASIS, GM_UPDATE, tl, th, float>;                \
+  k.grid_upd[tl][th][1] = (void *)k_grid<DIM, BASIS, GM_UPDATE, tl, th, double>;               \
+  k.grid_vel[tl][th][0] = (void *)k_grid<DIM, BASIS, GM_VEL, tl, th, float>;                   \
+  k.grid_vel[tl][th][1] = (void *)k_grid<DIM, BASIS, GM_VEL, tl, th, double>;
+  KMPM_GRID_SET(false, false)
+  KMPM_GRID_SET(false, true)
+  KMPM_GRID_SET(true, false)
+  KMPM_GRID_SET(true, true)
+#undef KMPM_GRID_SET
   k.g2p1[0][0] = (void *)k_g2p1<DIM, BASIS, false, false>;
   k.g2p1[0][1] = (void *)k_g2p1<DIM, BASIS, false, true>;
   k.g2p1[1][0] = (void *)k_g2p1<DIM, BASIS, true, false>;
