@@ -185,6 +185,33 @@ int kmpm_launches_per_step(struct kmpm_ctx *ctx);
 int kmpm_profile(struct kmpm_ctx *ctx, int nsteps, double *phase_ms, int max_phases, int *nphases);
 const char *kmpm_profile_phase(struct kmpm_ctx *ctx, int i);
 
+/* Nodal mass without device allocation.  No counterpart in the reference.
+ *
+ * For callers that may not allocate device memory at the point where they
+ * need nodal masses: code running while a CUDA graph is being captured
+ * (cudaMalloc is not permitted during capture), or an application whose
+ * device memory belongs entirely to its own pool and budget.  The caller
+ * passes device buffers: x (n*3 floats, x y z per particle), mass (n floats)
+ * and node_mass (one float per node of the grid described by lo, cellsize,
+ * nnodes and nglobal, as in kmpm_add_grid); the result is what
+ * Solid::compute_mass_nodes (src/solid.cpp:317-335) computes, by the same
+ * deterministic scatter that kmpm_run uses.  Nothing is allocated: every
+ * intermediate array lives in one fixed-size device array of
+ * KMPM_NOALLOC_SCRATCH_BYTES that every GPU loading this library holds until
+ * the process exits.  Limits: at most KMPM_NOALLOC_MAX_PARTICLES particles and
+ * KMPM_NOALLOC_MAX_CELLS binning cells (larger problems return KMPM_ERR_ARG
+ * with a message in err).  The first call on a device looks up that array's
+ * device address: make it outside any stream capture.  Calls share the array;
+ * two calls that overlap on the GPU race on it.  Work is queued on `stream`
+ * (a cudaStream_t, may be 0); err (errlen bytes, may be NULL) receives the
+ * message of a failure. */
+#define KMPM_NOALLOC_MAX_PARTICLES 131072
+#define KMPM_NOALLOC_MAX_CELLS 262144
+#define KMPM_NOALLOC_SCRATCH_BYTES (24u << 20)
+int kmpm_p2g_mass_noalloc(const float *x, const float *mass, int n, int dim, int basis, const double lo[3],
+                          double cellsize, const int nnodes[3], const int nglobal[3], float *node_mass, void *stream,
+                          char *err, int errlen);
+
 #ifdef __cplusplus
 }
 #endif

@@ -29,7 +29,8 @@ GRID_FIELDS = {"mass": (0, 1), "v": (1, 3), "v_update": (2, 3), "x": (3, 3), "T"
 EXPORTED = ["kmpm_create", "kmpm_destroy", "kmpm_last_error", "kmpm_add_material", "kmpm_add_grid",
             "kmpm_add_solid", "kmpm_add_fix", "kmpm_run", "kmpm_run_time", "kmpm_scalars",
             "kmpm_download_particles", "kmpm_upload_particles", "kmpm_download_grid", "kmpm_energy",
-            "kmpm_stream", "kmpm_launches_per_step", "kmpm_profile", "kmpm_profile_phase"]
+            "kmpm_stream", "kmpm_launches_per_step", "kmpm_profile", "kmpm_profile_phase",
+            "kmpm_p2g_mass_noalloc"]
 
 
 class KmpmParams(ctypes.Structure):
@@ -81,6 +82,8 @@ def load(path: str = LIB_PATH):
     L.kmpm_profile.argtypes = [p, i, dp, i, ip]
     L.kmpm_profile_phase.restype = ctypes.c_char_p
     L.kmpm_profile_phase.argtypes = [p, i]
+    fp = ctypes.c_void_p
+    L.kmpm_p2g_mass_noalloc.argtypes = [fp, fp, i, i, i, dp, d, ip, ip, fp, p, ctypes.c_char_p, i]
     _lib = L
     return L
 

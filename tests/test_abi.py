@@ -10,7 +10,7 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 def declared_symbols():
     txt = open(os.path.join(ROOT, "include", "kmpm.h")).read()
-    return sorted(set(re.findall(r"\b(kmpm_[a-z_]+)\s*\(", txt)))
+    return sorted(set(re.findall(r"\b(kmpm_[a-z_0-9]+)\s*\(", txt)))
 
 
 def test_header_and_binding_agree():
