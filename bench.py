@@ -250,6 +250,43 @@ def bench_ours(args):
     print(json.dumps(line), flush=True)
 
 
+def bench_sweep(args):
+    """The batched sweep (benchmark list, configuration 5): args.instances
+    independent 2-D TLMPM tensile bars (Johnson-Cook + damage, seeded
+    parameters) in one launch per phase, particle-updates/s over all."""
+    import torch
+    from karamelo_gb300.batch import Batch, tensile_sweep
+    sims, _ = tensile_sweep(args.instances, seed=0)
+    t0 = time.perf_counter()
+    batch = Batch(sims, track_strain=False)
+    batch.run(1)
+    setup_s = time.perf_counter() - t0
+    n = batch.total_particles
+    be = batch.backend
+    be.run(args.warmup)
+    phases = be.profile(args.profile_steps)
+    stream = torch.cuda.ExternalStream(be.stream())
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    clocks = ClockSampler(0)
+    torch.cuda.synchronize()
+    clocks.start()
+    time.sleep(0.3)
+    e0.record(stream)
+    be.run(args.steps)
+    e1.record(stream)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1)
+    clk = clocks.stop()
+    line = {"metric": "particle-updates/s on 1 GB300 (batched TLMPM sweep)", "value": n * args.steps / (ms / 1e3),
+            "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seed 0)", "gpu_launches": be.launches_per_step() * args.steps,
+            "config": {"workload": f"tensile_sweep_2d_tlmpm_jc_damage instances={args.instances}", "particles": n,
+                       "setup_s": setup_s},
+            "phases_ms": phases, "clocks": clk}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -263,11 +300,15 @@ def main():
     ap.add_argument("--ref-steps", type=int, default=5)
     ap.add_argument("--ref-budget", type=float, default=60.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", default="taylor", choices=["taylor", "sweep"])
+    ap.add_argument("--instances", type=int, default=1024)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
         bench_reference(args)
+    elif args.workload == "sweep":
+        bench_sweep(args)
     else:
         bench_ours(args)
 

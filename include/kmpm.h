@@ -68,6 +68,9 @@ typedef struct {
   int precision;     /* KMPM_PREC_* */
   int sort_every;    /* ULMPM: particles are re-binned by cell every step; kept for ABI growth */
   int track_strain;  /* keep Solid::strain_el (needed by the strain-energy output) */
+  int independent;   /* TLMPM only: every solid is an independent simulation with its own
+                        dt and time (a batch of runs in one launch per phase); 0 = one
+                        simulation whose dt is the minimum over solids (adjust_dt) */
 } kmpm_params;
 
 /* One material: Mat (src/material.h:45-68) with its EOS / Strength / Damage /
@@ -156,6 +159,9 @@ int kmpm_run_time(struct kmpm_ctx *ctx, double maxtime, int *nsteps_done);
 
 /* Update::atime, Update::dt, Update::ntimestep. */
 int kmpm_scalars(struct kmpm_ctx *ctx, double *time, double *dt, long long *ntimestep);
+
+/* The same for one solid of an independent batch (kmpm_params.independent). */
+int kmpm_solid_scalars(struct kmpm_ctx *ctx, int solid, double *time, double *dt, long long *ntimestep);
 
 /* Download / upload one particle field of one solid in the caller's
  * particle order (the download before Output::write, src/output.cpp:128-200). */

@@ -96,6 +96,7 @@ struct kmpm_ctx {
   // temperatures are kept as T - T_ref in FP32 (T_ref: the first solid's
   // initial temperature in thermo-mechanical runs, 0 otherwise)
   double T_ref = 0;
+  bool indep() const { return prm.independent != 0; }
   bool TL() const { return prm.method == KMPM_TLMPM; }
   bool musl() const { return prm.scheme == KMPM_MUSL; }
 };
@@ -193,7 +194,7 @@ PartArgs part_args(kmpm_ctx *c) {
     a.boxlo[d] = (float)c->prm.boxlo[d];
     a.boxhi[d] = (float)c->prm.boxhi[d];
   }
-  a.indep = 0;
+  a.indep = c->indep();
   a.use_vu = c->musl() ? 0 : 1;
   a.thermal = c->prm.thermal;
   a.track_strain = c->prm.track_strain;
@@ -236,7 +237,7 @@ GridArgs grid_args(kmpm_ctx *c, int remap) {
   a.fix_start = c->d_fix_start;
   a.fix_count = c->d_fix_count;
   a.scalars = c->d_scalars;
-  a.indep = 0;
+  a.indep = c->indep();
   a.remap = remap;
   return a;
 }
@@ -251,7 +252,7 @@ DtArgs dt_args(kmpm_ctx *c) {
   a.scalars = c->d_scalars;
   a.err = c->d_err;
   a.nranges = (int)c->ranges.size();
-  a.indep = 0;
+  a.indep = c->indep();
   a.dt_constant = c->prm.dt_constant;
   a.dt_factor = c->prm.dt_factor;
   return a;
@@ -379,6 +380,8 @@ int build(kmpm_ctx *c) {
   }
   c->ps = pstart;
   c->nblk_p = (int)blk_range.size();
+  if (c->TL())  // per-grid clock of independent solids: the range of the solid owning the grid
+    for (size_t s = 0; s < c->hsolids.size(); s++) c->grids[c->hsolids[s].grid].solid0 = c->solid_range[s];
   // ---- device allocations
   DALLOC(c->buf[0], c->ps * PF_COUNT);
   DALLOC(c->buf[1], c->ps * PF_COUNT);
@@ -434,16 +437,17 @@ int build(kmpm_ctx *c) {
     c->pstride_tile = (size_t)NW * 10;
   }
   DALLOC(c->partial, c->pstride_tile * c->ntiles_total);
-  c->nscalars = 1;
+  c->nscalars = c->indep() ? (int)c->ranges.size() : 1;
   DALLOC(c->d_scalars, c->nscalars);
   {
-    StepScalars s{};
-    s.dt = c->prm.dt;
-    s.time = 0;
-    s.ntimestep = 0;
-    s.dtCFL = 1e22;
-    s.maxtime = 1e300;
-    CK(cudaMemcpyAsync(c->d_scalars, &s, sizeof(s), cudaMemcpyHostToDevice, c->st));
+    StepScalars s0{};
+    s0.dt = c->prm.dt;
+    s0.time = 0;
+    s0.ntimestep = 0;
+    s0.dtCFL = 1e22;
+    s0.maxtime = 1e300;
+    std::vector<StepScalars> sv(c->nscalars, s0);
+    CK(cudaMemcpy(c->d_scalars, sv.data(), sizeof(StepScalars) * sv.size(), cudaMemcpyHostToDevice));
   }
   DALLOC(c->d_dtcfl, c->ranges.size());
   DALLOC(c->d_err, 1);
@@ -457,35 +461,34 @@ int build(kmpm_ctx *c) {
   DALLOC(c->rtmp.v1, c->ps);
   DALLOC(c->rtmp.hist, 256 * ((c->ps + 2047) / 2048 + 1));
   DALLOC(c->rtmp.tot, 256);
-  // ---- particle upload (caller order within each solid)
+  // ---- particle upload (caller order within each solid), one field row at a time
   c->T_ref = c->prm.thermal ? c->hsolids[0].T0 : 0.0;
   {
-    std::vector<float> H((size_t)c->ps * PF_COUNT, 0.f);
-    auto at = [&](int f, int p) -> float & { return H[(size_t)f * c->ps + p]; };
-    for (size_t s = 0; s < c->hsolids.size(); s++) {
-      const auto &S = c->hsolids[s];
-      const RangeDev &r = c->ranges[c->TL() ? c->solid_range[s] : 0];
-      const int off = c->TL() ? r.start : r.start + c->solid_base[s];
-      for (int i = 0; i < S.n; i++) {
-        const int p = off + i;
-        for (int d = 0; d < 3; d++) {
-          at(PF_X0 + d, p) = (float)S.x0[3 * i + d];
+    std::vector<float> row(c->ps);
+    for (int f : active_fields(c)) {
+      std::fill(row.begin(), row.end(), 0.f);
+      for (size_t s = 0; s < c->hsolids.size(); s++) {
+        const auto &S = c->hsolids[s];
+        const RangeDev &r = c->ranges[c->TL() ? c->solid_range[s] : 0];
+        const int off = c->TL() ? r.start : r.start + c->solid_base[s];
+        for (int i = 0; i < S.n; i++) {
+          float &o = row[off + i];
+          if (f >= PF_X0 && f < PF_X0 + 3) o = (float)S.x0[3 * i + f - PF_X0];
           // positions are stored as the displacement from x0
-          at(PF_X + d, p) = (float)(S.x[3 * i + d] - S.x0[3 * i + d]);
-          if (!c->TL()) at(PF_XN + d, p) = at(PF_X + d, p);
-          at(PF_V + d, p) = (float)S.v[3 * i + d];
+          else if (f >= PF_X && f < PF_X + 3) o = (float)(S.x[3 * i + f - PF_X] - S.x0[3 * i + f - PF_X]);
+          else if (f >= PF_XN && f < PF_XN + 3) o = (float)(S.x[3 * i + f - PF_XN] - S.x0[3 * i + f - PF_XN]);
+          else if (f >= PF_V && f < PF_V + 3) o = (float)S.v[3 * i + f - PF_V];
+          else if (f == PF_MASS) o = (float)S.mass[i];
+          else if (f == PF_VOL0) o = (float)S.vol0[i];
+          // Solid::populate sets T = T0 only for thermo-mechanical runs; otherwise
+          // the vector is value-initialised (src/solid.cpp:2297-2306, 306-311)
+          else if (f == PF_T) o = c->prm.thermal ? (float)(S.T0 - c->T_ref) : 0.f;
+          else if (f == PF_ORIG) { int v = c->solid_base[s] + i; std::memcpy(&o, &v, 4); }
+          else if (f == PF_SID) { int v = (int)s; std::memcpy(&o, &v, 4); }
         }
-        at(PF_MASS, p) = (float)S.mass[i];
-        at(PF_VOL0, p) = (float)S.vol0[i];
-        // Solid::populate sets T = T0 only for thermo-mechanical runs; otherwise
-        // the vector is value-initialised (src/solid.cpp:2297-2306, 306-311)
-        at(PF_T, p) = c->prm.thermal ? (float)(S.T0 - c->T_ref) : 0.f;
-        int orig = c->solid_base[s] + i, sid = (int)s;
-        std::memcpy(&at(PF_ORIG, p), &orig, 4);
-        std::memcpy(&at(PF_SID, p), &sid, 4);
       }
+      CK(cudaMemcpy(c->buf[0] + (size_t)f * c->ps, row.data(), sizeof(float) * c->ps, cudaMemcpyHostToDevice));
     }
-    CK(cudaMemcpy(c->buf[0], H.data(), sizeof(float) * H.size(), cudaMemcpyHostToDevice));
   }
   // ---- kernel attributes
   const int modes[4] = {P2G_MASS, P2G_TL, P2G_UL, P2G_VEL};
@@ -750,6 +753,7 @@ int kmpm_create(const kmpm_params *params, kmpm_ctx **out) {
   if (p.scheme != KMPM_USL && p.scheme != KMPM_MUSL) return KMPM_ERR_ARG;
   if (p.basis < 0 || p.basis > 2 || p.dim < 1 || p.dim > 3) return KMPM_ERR_ARG;
   if (p.method == KMPM_ULMPM && p.basis == KMPM_BASIS_BERNSTEIN) return KMPM_ERR_ARG;
+  if (p.independent && p.method != KMPM_TLMPM) return KMPM_ERR_ARG;  // ULMPM solids share one grid
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return KMPM_ERR_CUDA;
   kmpm_ctx *c = new kmpm_ctx();
@@ -868,6 +872,7 @@ int kmpm_run(kmpm_ctx *c, int nsteps) {
 
 int kmpm_run_time(kmpm_ctx *c, double maxtime, int *nsteps_done) {
   if (!c) return KMPM_ERR_ARG;
+  if (c->indep()) return fail(c, KMPM_ERR_ARG, "run_time needs one clock: not available for independent solids");
   int r = prepare(c);
   if (r != KMPM_OK) return r;
   StepScalars s{};
@@ -909,6 +914,18 @@ int kmpm_scalars(kmpm_ctx *c, double *time, double *dt, long long *ntimestep) {
 
 // Copies the rows of the listed fields for slots [start, start+n) of the
 // current particle buffer into H (H[f][slot - start]).
+int kmpm_solid_scalars(kmpm_ctx *c, int solid, double *time, double *dt, long long *ntimestep) {
+  if (!c || solid < 0 || solid >= (int)c->hsolids.size()) return KMPM_ERR_ARG;
+  if (!c->built || !c->indep()) return kmpm_scalars(c, time, dt, ntimestep);
+  StepScalars s{};
+  CK(cudaMemcpyAsync(&s, c->d_scalars + c->solid_range[solid], sizeof(s), cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  if (time) *time = s.time;
+  if (dt) *dt = s.dt;
+  if (ntimestep) *ntimestep = s.ntimestep;
+  return KMPM_OK;
+}
+
 static int fetch_rows(kmpm_ctx *c, const std::vector<int> &fields, int start, int n,
                       std::vector<std::vector<float>> &H) {
   CK(cudaStreamSynchronize(c->st));

@@ -380,9 +380,9 @@ int p2g_smem_bytes(int dim, int basis, int mode, bool thermal) {
   const int L = t[0] / 8;
   const int WY = dim >= 2 ? (t[1] - 1) * SC + S : 1, WZ = dim == 3 ? (t[2] - 1) * SC + S : 1;
   const int NF = ((L - 1) * SC + S) * WY * WZ;
-  const int Q = p2g_nq(mode, thermal), QIN = p2g_nin(mode, thermal);
+  const int Q = p2g_nq(mode, thermal), QINP = (p2g_nin(mode, thermal) + 3) & ~3;
   const int slab = (Q * NF + 3) & ~3;
-  return 4 * 8 * (slab + 32 * (dim + QIN) + 32 * dim * S * 2);
+  return 4 * 8 * (slab + 32 * 4 + 32 * QINP + 32 * dim * S * 2);
 }
 
 }  // namespace kmpm

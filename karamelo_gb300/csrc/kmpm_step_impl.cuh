@@ -25,6 +25,33 @@ namespace kmpm {
 // slab footprint in shared memory.  After one barrier the slab footprints are
 // summed in warp order into the tile's slice of the partial buffer.  No float
 // atomics: the result is bit-reproducible.
+// Contribution of one staged particle to this lane's stencil nodes.
+template <int DIM, int S, int MODE, bool THERMAL, int Q, int QINP, int NSL, int NS, bool PAIR>
+__device__ __forceinline__ void p2g_particle(float (&accr)[NSL][Q], const float *spay_j, const float2 *bj,
+                                             const int (&soff)[NSL][3], int lane) {
+  float pay[QINP];
+#pragma unroll
+  for (int v = 0; v < QINP / 4; v++) {
+    const float4 t = reinterpret_cast<const float4 *>(spay_j)[v];
+    pay[4 * v] = t.x; pay[4 * v + 1] = t.y; pay[4 * v + 2] = t.z; pay[4 * v + 3] = t.w;
+  }
+  const float2 bx = bj[soff[0][0]];
+  const float2 by = DIM >= 2 ? bj[S + soff[0][1]] : make_float2(1.f, 0.f);
+  const float wxy = bx.x * by.x, gxy0 = bx.y * by.x, gxy1 = bx.x * by.y;
+#pragma unroll
+  for (int u = 0; u < NSL; u++) {
+    if (!PAIR && lane + 32 * u >= NS) continue;
+    const float2 bz = DIM == 3 ? bj[2 * S + soff[u][2]] : make_float2(1.f, 0.f);
+    const float w = wxy * bz.x;
+    // the reference keeps a particle-node pair only when every 1-D value is
+    // non-zero (src/tlmpm.cpp:263, src/ulmpm.cpp:259-272); the cubic spline
+    // at ntype 1 has a zero value but a non-zero slope
+    if (w == 0.f) continue;
+    const float gw[3] = {gxy0 * bz.x, gxy1 * bz.x, wxy * bz.y};
+    p2g_accumulate<MODE, THERMAL, Q>(accr[u], pay, w, gw);
+  }
+}
+
 template <int DIM, int BASIS, int MODE, bool THERMAL>
 __global__ void __launch_bounds__(256) k_p2g(P2GArgs a) {
   using TS = TileShape<DIM, BASIS>;
@@ -33,17 +60,18 @@ __global__ void __launch_bounds__(256) k_p2g(P2GArgs a) {
   constexpr int WX = TS::WX, WY = TS::WY, WZ = TS::WZ, FX = TS::FX, NW = TS::NW, NF = TS::NF, NS = TS::NS;
   constexpr int Q = p2g_nq(MODE, THERMAL);
   constexpr int QIN = p2g_nin(MODE, THERMAL);
+  constexpr int QINP = (QIN + 3) & ~3;  // staged payload row, padded for float4 access
   constexpr int NSL = (NS + 31) / 32;  // stencil nodes per lane
   constexpr bool PAIR = (DIM == 3 && S == 4);  // lane owns (a,b,c) and (a,b,c+2)
   constexpr int SLAB = (Q * NF + 3) & ~3;
-  constexpr int STAGE = 32 * (DIM + QIN) + 32 * DIM * S * 2;
+  constexpr int STAGE = 32 * 4 + 32 * QINP + 32 * DIM * S * 2;
 
   extern __shared__ __align__(16) float smem[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   float *slab = smem + warp * SLAB;                                // Q * NF
-  float *spos = smem + TS::NWARP * SLAB + warp * STAGE;            // 32 * DIM
-  float *spay = spos + 32 * DIM;                                   // 32 * QIN
-  float2 *sbas = reinterpret_cast<float2 *>(spay + 32 * QIN);      // 32 * DIM * S
+  float4 *spos = reinterpret_cast<float4 *>(smem + TS::NWARP * SLAB + warp * STAGE);  // 32
+  float *spay = reinterpret_cast<float *>(spos + 32);                                 // 32 * QINP
+  float2 *sbas = reinterpret_cast<float2 *>(spay + 32 * QINP);                        // 32 * DIM * S
 
   const int2 td = a.tiles[blockIdx.x];
   const GridDev g = a.grids[td.x];
@@ -120,10 +148,13 @@ __global__ void __launch_bounds__(256) k_p2g(P2GArgs a) {
       if (c0 > 0 && lane < cnt) KMPM_LOAD_PARTICLE(cstart + c0 + lane);  // cells with more than 32 particles
       // ---- stage (lane = particle)
       if (lane < cnt) {
+        spos[lane] = make_float4(ppos[0], DIM >= 2 ? ppos[DIM >= 2 ? 1 : 0] : 0.f, DIM == 3 ? ppos[DIM == 3 ? 2 : 0] : 0.f, 0.f);
 #pragma unroll
-        for (int d = 0; d < DIM; d++) spos[lane * DIM + d] = ppos[d];
-#pragma unroll
-        for (int q = 0; q < QIN; q++) spay[lane * QIN + q] = ppay[q];
+        for (int v = 0; v < QINP / 4; v++)
+          reinterpret_cast<float4 *>(spay + lane * QINP)[v] =
+              make_float4(ppay[4 * v], 4 * v + 1 < QIN ? ppay[min(4 * v + 1, QIN - 1)] : 0.f,
+                          4 * v + 2 < QIN ? ppay[min(4 * v + 2, QIN - 1)] : 0.f,
+                          4 * v + 3 < QIN ? ppay[min(4 * v + 3, QIN - 1)] : 0.f);
       }
       __syncwarp();
       // prefetch the next cell while this one is computed
@@ -140,7 +171,8 @@ __global__ void __launch_bounds__(256) k_p2g(P2GArgs a) {
           const int j = it / DIM, d = it % DIM;
           const int i0d = d == 0 ? i0[0] : (d == 1 ? i0[1] : i0[2]);
           const float lod = d == 0 ? glo0 : (d == 1 ? glo1 : glo2);
-          const float t = (spos[j * DIM + d] - lod) * ih;
+          const float4 pj = spos[j];
+          const float t = ((d == 0 ? pj.x : (d == 1 ? pj.y : pj.z)) - lod) * ih;
           float sv[4], dsv[4];
           cubic_weights(t - (float)(i0d + 1), ih, sv, dsv);
 #pragma unroll
@@ -157,33 +189,23 @@ __global__ void __launch_bounds__(256) k_p2g(P2GArgs a) {
         float sv = 0.f, dsv = 0.f;
         if (i >= 0 && i < nd) {
           const float xn = lod + (float)i * h;
-          const float r = (spos[j * DIM + d] - xn) * ih;
+          const float4 pj = spos[j];
+          const float r = ((d == 0 ? pj.x : (d == 1 ? pj.y : pj.z)) - xn) * ih;
           basis<BASIS>(r, node_type<BASIS>(i, ngd), ih, sv, dsv);
         }
         sbas[it] = make_float2(sv, dsv);
       }
       __syncwarp();
-      // ---- accumulate (lane = stencil node)
+      // ---- accumulate (lane = stencil node); two particles per iteration for ILP
       if (lane_active) {
-        for (int j = 0; j < cnt; j++) {
-          const float *pay = spay + j * QIN;
-          const float2 *bj = sbas + j * DIM * S;
-          const float2 bx = bj[soff[0][0]];
-          const float2 by = DIM >= 2 ? bj[S + soff[0][1]] : make_float2(1.f, 0.f);
-          const float wxy = bx.x * by.x, gxy0 = bx.y * by.x, gxy1 = bx.x * by.y;
-#pragma unroll
-          for (int u = 0; u < NSL; u++) {
-            if (!PAIR && lane + 32 * u >= NS) continue;
-            const float2 bz = DIM == 3 ? bj[2 * S + soff[u][2]] : make_float2(1.f, 0.f);
-            const float w = wxy * bz.x;
-            // the reference keeps a particle-node pair only when every 1-D
-            // value is non-zero (src/tlmpm.cpp:263, src/ulmpm.cpp:259-272); the
-            // cubic spline at ntype 1 has a zero value but a non-zero slope
-            if (w == 0.f) continue;
-            const float gw[3] = {gxy0 * bz.x, gxy1 * bz.x, wxy * bz.y};
-            p2g_accumulate<MODE, THERMAL, Q>(accr[u], pay, w, gw);
-          }
+        int j = 0;
+        for (; j + 1 < cnt; j += 2) {
+          p2g_particle<DIM, S, MODE, THERMAL, Q, QINP, NSL, NS, PAIR>(accr, spay + j * QINP, sbas + j * DIM * S, soff, lane);
+          p2g_particle<DIM, S, MODE, THERMAL, Q, QINP, NSL, NS, PAIR>(accr, spay + (j + 1) * QINP,
+                                                                      sbas + (j + 1) * DIM * S, soff, lane);
         }
+        if (j < cnt)
+          p2g_particle<DIM, S, MODE, THERMAL, Q, QINP, NSL, NS, PAIR>(accr, spay + j * QINP, sbas + j * DIM * S, soff, lane);
       }
       __syncwarp();
     }
@@ -394,7 +416,7 @@ __device__ __forceinline__ int range_particle(const PartArgs &a, RangeDev &rd) {
 
 // grid_to_points + advance_particles (src/solid.cpp:576-635, 786-790)
 template <int DIM, int BASIS, bool TL, bool THERMAL>
-__global__ void __launch_bounds__(256) k_g2p1(PartArgs a) {
+__global__ void __launch_bounds__(256, 4) k_g2p1(PartArgs a) {
   if (run_finished(a.scalars)) return;
   RangeDev rd;
   const int p = range_particle(a, rd);
@@ -414,22 +436,29 @@ __global__ void __launch_bounds__(256) k_g2p1(PartArgs a) {
   ax.eval(g, xp);
   constexpr int S = Stencil<BASIS>::S;
   constexpr int SY = DIM >= 2 ? S : 1, SZ = DIM == 3 ? S : 1;
+  // branch-free gather: per-axis node indices clamped into the grid (a node
+  // outside it has a zero value, so its clamped stand-in contributes nothing)
+  int cx[S], cy[SY], cz[SZ];
+#pragma unroll
+  for (int k = 0; k < S; k++) cx[k] = min(max(ax.ax[0].i0 + k, 0), g.n[0] - 1);
+#pragma unroll
+  for (int k = 0; k < SY; k++) cy[k] = min(max(ax.ax[1].i0 + k, 0), g.n[1] - 1);
+#pragma unroll
+  for (int k = 0; k < SZ; k++) cz[k] = min(max(ax.ax[2].i0 + k, 0), g.n[2] - 1);
+  const float4 *__restrict__ NA = a.nodeA + g.node_off;
+  const float4 *__restrict__ NB = a.nodeB + g.node_off;
   float vu[3] = {0, 0, 0}, dv[3] = {0, 0, 0}, Tp = 0.f;
 #pragma unroll
   for (int i = 0; i < S; i++) {
-    const float sx = ax.ax[0].s[i];
-    if (sx == 0.f) continue;
 #pragma unroll
     for (int j = 0; j < SY; j++) {
-      const float sxy = sx * ax.ax[1].s[j];
-      if (sxy == 0.f) continue;
+      const float sxy = ax.ax[0].s[i] * ax.ax[1].s[j];
+      const int row = (cx[i] * g.n[1] + cy[j]) * g.n[2];
 #pragma unroll
       for (int k = 0; k < SZ; k++) {
         const float w = sxy * ax.ax[2].s[k];
-        if (w == 0.f) continue;
-        const int node = g.node_off + ((ax.ax[0].i0 + i) * g.n[1] + (ax.ax[1].i0 + j)) * g.n[2] + ax.ax[2].i0 + k;
-        const float4 A = a.nodeA[node];
-        const float4 B = a.nodeB[node];
+        const float4 A = __ldg(NA + row + cz[k]);
+        const float4 B = __ldg(NB + row + cz[k]);
         vu[0] += w * B.x; vu[1] += w * B.y; vu[2] += w * B.z;
         dv[0] += w * (B.x - A.x); dv[1] += w * (B.y - A.y); dv[2] += w * (B.z - A.z);
         if (THERMAL) Tp += w * B.w;
@@ -464,7 +493,7 @@ __global__ void __launch_bounds__(256) k_g2p1(PartArgs a) {
 // rate of deformation + deformation gradient + stress + wave speed
 // (src/solid.cpp:798-936, 1155-1438)
 template <int DIM, int BASIS, bool TL, bool THERMAL, int PREC>
-__global__ void __launch_bounds__(256) k_g2p2(PartArgs a) {
+__global__ void __launch_bounds__(256, 3) k_g2p2(PartArgs a) {
   __shared__ float red_c[256], red_h[256];
   if (run_finished(a.scalars)) return;
   RangeDev rd;
@@ -487,28 +516,37 @@ __global__ void __launch_bounds__(256) k_g2p2(PartArgs a) {
     constexpr int SY = DIM >= 2 ? S : 1, SZ = DIM == 3 ? S : 1;
     float G[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
     float qg[3] = {0, 0, 0};
+    // branch-free gather (clamped indices, see k_g2p1); a pair with a zero
+    // weight is dropped as in the reference, so its slope is masked too
+    int cx[S], cy[SY], cz[SZ];
+#pragma unroll
+    for (int k = 0; k < S; k++) cx[k] = min(max(ax.ax[0].i0 + k, 0), g.n[0] - 1);
+#pragma unroll
+    for (int k = 0; k < SY; k++) cy[k] = min(max(ax.ax[1].i0 + k, 0), g.n[1] - 1);
+#pragma unroll
+    for (int k = 0; k < SZ; k++) cz[k] = min(max(ax.ax[2].i0 + k, 0), g.n[2] - 1);
+    const float4 *__restrict__ NV = (a.use_vu ? a.nodeB : a.nodeA) + g.node_off;
 #pragma unroll
     for (int i = 0; i < S; i++) {
       const float sx = ax.ax[0].s[i], dsx = ax.ax[0].ds[i];
-      if (sx == 0.f) continue;
 #pragma unroll
       for (int j = 0; j < SY; j++) {
         const float sy = ax.ax[1].s[j], dsy = ax.ax[1].ds[j];
-        if (sx * sy == 0.f) continue;
+        const float sxy = sx * sy, gx = dsx * sy, gy = sx * dsy;
+        const int row = (cx[i] * g.n[1] + cy[j]) * g.n[2];
 #pragma unroll
         for (int k = 0; k < SZ; k++) {
           const float sz = ax.ax[2].s[k], dsz = ax.ax[2].ds[k];
-          if (sx * sy * sz == 0.f) continue;
-          const float gw[3] = {dsx * sy * sz, sx * dsy * sz, sx * sy * dsz};
-          const int node = g.node_off + ((ax.ax[0].i0 + i) * g.n[1] + (ax.ax[1].i0 + j)) * g.n[2] + ax.ax[2].i0 + k;
-          const float4 V = a.use_vu ? a.nodeB[node] : a.nodeA[node];
+          const float on = (sxy * sz != 0.f) ? 1.f : 0.f;
+          const float gw[3] = {on * gx * sz, on * gy * sz, on * sxy * dsz};
+          const float4 V = __ldg(NV + row + cz[k]);
           const float vn[3] = {V.x, V.y, V.z};
 #pragma unroll
           for (int r = 0; r < DIM; r++)
 #pragma unroll
             for (int c = 0; c < DIM; c++) G[3 * r + c] += vn[r] * gw[c];
           if (THERMAL) {
-            const float Tn = a.use_vu ? V.w : a.nodeT[node];
+            const float Tn = a.use_vu ? V.w : a.nodeT[g.node_off + row + cz[k]];
 #pragma unroll
             for (int c = 0; c < 3; c++) qg[c] -= gw[c] * Tn;
           }

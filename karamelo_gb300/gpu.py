@@ -30,7 +30,7 @@ EXPORTED = ["kmpm_create", "kmpm_destroy", "kmpm_last_error", "kmpm_add_material
             "kmpm_add_solid", "kmpm_add_fix", "kmpm_run", "kmpm_run_time", "kmpm_scalars",
             "kmpm_download_particles", "kmpm_upload_particles", "kmpm_download_grid", "kmpm_energy",
             "kmpm_stream", "kmpm_launches_per_step", "kmpm_profile", "kmpm_profile_phase",
-            "kmpm_p2g_mass_noalloc"]
+            "kmpm_p2g_mass_noalloc", "kmpm_solid_scalars"]
 
 
 class KmpmParams(ctypes.Structure):
@@ -38,7 +38,7 @@ class KmpmParams(ctypes.Structure):
                 ("pic_flip", ctypes.c_double), ("thermal", ctypes.c_int), ("dt", ctypes.c_double),
                 ("dt_factor", ctypes.c_double), ("dt_constant", ctypes.c_int), ("boxlo", ctypes.c_double * 3),
                 ("boxhi", ctypes.c_double * 3), ("precision", ctypes.c_int), ("sort_every", ctypes.c_int),
-                ("track_strain", ctypes.c_int)]
+                ("track_strain", ctypes.c_int), ("independent", ctypes.c_int)]
 
 
 class KmpmError(RuntimeError):
@@ -72,6 +72,7 @@ def load(path: str = LIB_PATH):
     L.kmpm_run.argtypes = [p, i]
     L.kmpm_run_time.argtypes = [p, d, ip]
     L.kmpm_scalars.argtypes = [p, dp, dp, ctypes.POINTER(ctypes.c_longlong)]
+    L.kmpm_solid_scalars.argtypes = [p, i, dp, dp, ctypes.POINTER(ctypes.c_longlong)]
     L.kmpm_download_particles.argtypes = [p, i, i, dp]
     L.kmpm_upload_particles.argtypes = [p, i, i, dp]
     L.kmpm_download_grid.argtypes = [p, i, i, dp]
@@ -95,7 +96,7 @@ def _dp(a):
 class GpuBackend:
     """Runs a Scenario on the GPU through the C ABI."""
 
-    def __init__(self, s: sc.Scenario, precision: int = 0, track_strain: bool = True):
+    def __init__(self, s: sc.Scenario, precision: int = 0, track_strain: bool = True, independent: bool = False):
         L = load()
         self.L, self.s = L, s
         prm = KmpmParams()
@@ -107,6 +108,7 @@ class GpuBackend:
         prm.precision = precision
         prm.sort_every = 1
         prm.track_strain = int(track_strain)
+        prm.independent = int(independent)
         h = ctypes.c_void_p()
         r = L.kmpm_create(ctypes.byref(prm), ctypes.byref(h))
         if r != KMPM_OK:
@@ -160,6 +162,11 @@ class GpuBackend:
     def scalars(self):
         t, dt, n = ctypes.c_double(), ctypes.c_double(), ctypes.c_longlong()
         self._ck(self.L.kmpm_scalars(self.h, ctypes.byref(t), ctypes.byref(dt), ctypes.byref(n)))
+        return t.value, dt.value, n.value
+
+    def solid_scalars(self, si: int):
+        t, dt, n = ctypes.c_double(), ctypes.c_double(), ctypes.c_longlong()
+        self._ck(self.L.kmpm_solid_scalars(self.h, si, ctypes.byref(t), ctypes.byref(dt), ctypes.byref(n)))
         return t.value, dt.value, n.value
 
     def particles(self, si: int, field: str):

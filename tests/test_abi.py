@@ -23,12 +23,19 @@ def test_library_exports_all_symbols(gpu_lib):
         assert hasattr(gpu_lib, name), name
 
 
-def test_struct_layout_matches_header(gpu_lib):
+def test_struct_layout_matches_header(gpu_lib, tmp_path):
+    """The ctypes mirrors have the sizes a C compiler gives the header's structs."""
+    import subprocess
     from karamelo_gb300.gpu import KmpmParams
     from karamelo_gb300.scenario import MaterialParams
-    # kmpm_params: 4 ints, double, int, 2 doubles, int, 6 doubles, 3 ints
-    assert ctypes.sizeof(KmpmParams) == 120
-    assert ctypes.sizeof(MaterialParams) == 8 * (1 + 5 + 1 + 12 + 1 + 12 + 1 + 8 + 1 + 6)
+    src = tmp_path / "sz.c"
+    src.write_text('#include "kmpm.h"\n#include <stdio.h>\n'
+                   'int main(void){printf("%zu %zu\\n", sizeof(kmpm_params), sizeof(kmpm_material));return 0;}\n')
+    exe = tmp_path / "sz"
+    subprocess.check_call(["gcc", "-I" + os.path.join(ROOT, "include"), str(src), "-o", str(exe)])
+    p, m = map(int, subprocess.check_output([str(exe)]).split())
+    assert ctypes.sizeof(KmpmParams) == p
+    assert ctypes.sizeof(MaterialParams) == m
 
 
 def test_create_without_device_fails_loudly(gpu_lib):

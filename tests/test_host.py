@@ -79,3 +79,18 @@ def test_initial_velocity_applied_before_first_step():
     sim = W.two_disks()
     assert np.allclose(sim.s.solids[0].v[:, :2], 0.1)
     assert np.allclose(sim.s.solids[1].v[:, :2], -0.1)
+
+
+def test_batch_merges_scripts():
+    from karamelo_gb300.batch import Batch, tensile_sweep
+    sims, params = tensile_sweep(4, seed=3, nmin=500, nmax=4000)
+    got = {}
+    b = Batch(sims, backend_factory=lambda s: got.setdefault("s", s))
+    s = b.scenario
+    assert len(s.solids) == 4 and len(s.grids) == 4 and len(s.materials) == 4
+    assert [x.grid for x in s.solids] == [0, 1, 2, 3] and [x.mat for x in s.solids] == [0, 1, 2, 3]
+    assert sorted({f.grid for f in s.fixes}) == [0, 1, 2, 3]
+    counts = [x.np for x in s.solids]
+    assert min(counts) >= 300 and max(counts) <= 6000
+    d1 = [m.dam_p[0] for m in s.materials]
+    assert all(0.54 * 0.7 <= v <= 0.54 * 1.3 for v in d1) and len(set(d1)) == 4
