@@ -3,11 +3,17 @@
 
 Workload: the Taylor-bar impact (3-D TLMPM, MUSL, cubic B-spline, Johnson-Cook
 strength + linear EOS, copper bar R = 3.2 mm, L = 32.4 mm at 190 m/s on a rigid
-wall, 2x2x2 particles per cell), at cellsize 0.2 mm: 1,045,872 particles and
-177,507 grid nodes.  As in the reference script, one step runs before the wall
-fix is added; the timed steps follow.  Inputs are synthetic and deterministic
-(the populate lattice).  Particle state (~350 MB touched per step) is larger
-than the 129 MB L2, so no flush is needed between steps.
+wall, 2x2x2 particles per cell), at cellsize 0.1 mm: 8,354,016 particles and
+1,373,125 grid nodes (``--cellsize 0.2``: 1,045,872 and 177,507).  As in the
+reference script, one step runs before the wall fix is added; the timed steps
+follow.  Inputs are synthetic and deterministic (the populate lattice).
+Particle state (~2.9 GB touched per step) is far larger than the 129 MB L2, so
+no flush is needed between steps.
+
+The CPU leg (the FP64 oracle on the host cores) runs a bounded sample: a few
+steps of the same bar at ``--cpu-cellsize`` (0.2 mm by default, 1/8 of the
+particles; its frozen FP64 neighbour lists take ~5 GB there and ~40 GB at
+0.1 mm).  Its per-particle cost does not depend on the bar's resolution.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
@@ -105,6 +111,21 @@ def dist_env():
     return world, rank, local
 
 
+def aggregate_replicas(ms, units, device):
+    """Max of the timed milliseconds and sum of the processed units over all
+    ranks.  Replicas share no data; this reduction of two scalars after the
+    timed region is the only collective."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return float(ms), float(units)
+    t = torch.tensor([float(ms)], dtype=torch.float64, device=device)
+    u = torch.tensor([float(units)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dist.all_reduce(u, op=dist.ReduceOp.SUM)
+    return float(t.item()), float(u.item())
+
+
 def run_cpu_sample(cellsize, steps, time_budget, threads):
     """The oracle (FP64 CPU restatement of the reference step) on the host
     cores, over a bounded number of steps of the same workload.  Step 1
@@ -133,12 +154,13 @@ def bench_reference(args):
         return
     threads = os.cpu_count() or 1
     steps = max(1, min(args.steps, args.ref_steps))
-    v, n, done, dt = run_cpu_sample(args.cellsize, steps, args.ref_budget, threads)
-    sample = f"{done} steps of the {n}-particle bar (cellsize {args.cellsize} mm) after the untimed first step"
+    v, n, done, dt = run_cpu_sample(args.cpu_cellsize, steps, args.ref_budget, threads)
+    sample = f"{done} steps of the {n}-particle bar (cellsize {args.cpu_cellsize} mm) after the untimed first step"
     line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world, "steps": done, "warmup": 1,
             "ms_per_step": 1000 * dt / done, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f64", "data": "synthetic (populate lattice, deterministic)", "impl": "reference",
-            "config": {"workload": f"taylor_bar_tlmpm_musl_cubic_jc h={args.cellsize}mm particles={n}"},
+            "config": {"workload": f"taylor_bar_tlmpm_musl_cubic_jc h={args.cellsize}mm",
+                       "cpu_sample_cellsize_mm": args.cpu_cellsize, "cpu_sample_particles": n},
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -179,11 +201,8 @@ def bench_ours(args):
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1)
     clk = clocks.stop()
-    if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
-    value = world * n * args.steps / (ms / 1000.0)
+    ms, units = aggregate_replicas(ms, n * args.steps, "cuda")
+    value = units / (ms / 1000.0)
     launches = be.launches_per_step() * args.steps
 
     # end to end through the C ABI with host buffers: context creation and the
@@ -222,7 +241,7 @@ def bench_ours(args):
     tp = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(tp):
         with open(tp) as f:
-            traffic = json.load(f).get(dom)
+            traffic = json.load(f).get(f"taylor_bar h={args.cellsize:g}mm", {}).get(dom)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -244,14 +263,15 @@ def bench_ours(args):
     }
     if world == 1 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
-        v, npart, done_c, dtc = run_cpu_sample(args.cellsize, args.cpu_steps, args.ref_budget, threads)
+        v, npart, done_c, dtc = run_cpu_sample(args.cpu_cellsize, args.cpu_steps, args.ref_budget, threads)
         line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
-                                "sample": f"{done_c} oracle steps of the same {npart}-particle bar after its untimed first step"}
+                                "sample": f"{done_c} oracle steps of the same bar at cellsize {args.cpu_cellsize} mm "
+                                          f"({npart} particles) after its untimed first step"}
     print(json.dumps(line), flush=True)
 
 
 def bench_sweep(args):
-    """The batched sweep (benchmark list, configuration 5): args.instances
+    """The batched parameter sweep: args.instances
     independent 2-D TLMPM tensile bars (Johnson-Cook + damage, seeded
     parameters) in one launch per phase, particle-updates/s over all."""
     import torch
@@ -293,7 +313,8 @@ def main():
     ap.add_argument("--steps", type=int, default=500)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--cellsize", type=float, default=0.2)
+    ap.add_argument("--cellsize", type=float, default=0.1)
+    ap.add_argument("--cpu-cellsize", type=float, default=0.2)
     ap.add_argument("--precision", type=int, default=0)
     ap.add_argument("--profile-steps", type=int, default=5)
     ap.add_argument("--cpu-steps", type=int, default=3)

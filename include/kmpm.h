@@ -5,8 +5,7 @@
  * through src/style_method.h) and `usl/gpu` / `musl/gpu` (Scheme,
  * src/scheme.h:19-24); their code uploads the state that Karamelo's host
  * classes built (Domain, Grid::init, Solid::populate, Material, Group, Fix)
- * and then lets kmpm_run() execute whole time steps on the GPU.  The binding
- * is shown in INTEGRATION.md.
+ * and then lets kmpm_run() execute whole time steps on the GPU.
  *
  * Conventions
  *   - every function returns an int status: KMPM_OK (0) or a negative

@@ -74,7 +74,7 @@ class Batch:
 
 
 def tensile_sweep(n, seed=0, nmin=2000, nmax=64000, vmin=1.0, vmax=20.0, spread=0.3, build=None, **kw):
-    """The sweep of the benchmark list: n 2-D TLMPM tensile bars (aspect ratio
+    """A seeded parameter sweep: n 2-D TLMPM tensile bars (aspect ratio
     5:1, 2x2 particles per cell) with Johnson-Cook strength and damage, the
     damage constants D1..D5 drawn uniformly within +-spread of their nominal
     values, particle counts log-uniform in [nmin, nmax] (through the cell

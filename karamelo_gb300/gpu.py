@@ -1,8 +1,7 @@
 """ctypes driver of libkmpm.so (include/kmpm.h) for a :class:`Scenario`.
 
 This is the Python side of the drop-in boundary: it makes exactly the calls a
-Karamelo ``tlmpm/gpu`` / ``ulmpm/gpu`` method style makes from C++ (see
-INTEGRATION.md).  There is no fallback: if the library or a CUDA device is
+Karamelo ``tlmpm/gpu`` / ``ulmpm/gpu`` method style makes from C++.  There is no fallback: if the library or a CUDA device is
 missing, construction raises.
 """
 from __future__ import annotations

@@ -1,4 +1,4 @@
-"""Independent runs in one launch (the sweep of the benchmark list): every
+"""Independent runs in one launch (a seeded tensile-bar sweep): every
 instance of a batch must match the same script run alone on the oracle,
 including its own dt and time."""
 import numpy as np
