@@ -37,6 +37,7 @@ extern "C" {
 #define KMPM_ERR_NAN (-12)         /* nan wave speed / dtCFL, src/solid.cpp:1387-1397, src/tlmpm.cpp:498-508 */
 #define KMPM_ERR_POLDEC (-13)      /* polar decomposition failed, src/solid.cpp:1229-1236 */
 #define KMPM_ERR_DTCFL (-14)       /* dtCFL == 0, src/tlmpm.cpp:498-502 */
+#define KMPM_ERR_TIMEOUT (-15)     /* a bounded wait inside a tensor-core kernel ran out */
 
 /* method / scheme / basis (Update::create_method, src/update.cpp:108-196) */
 #define KMPM_TLMPM 0
@@ -189,6 +190,80 @@ int kmpm_launches_per_step(struct kmpm_ctx *ctx);
  * "g2p_advance", "p2g_velocity", "grid_velocity", "g2p_stress", "dt", ...). */
 int kmpm_profile(struct kmpm_ctx *ctx, int nsteps, double *phase_ms, int max_phases, int *nphases);
 const char *kmpm_profile_phase(struct kmpm_ctx *ctx, int i);
+
+/* ------------------------------------------------------------------------
+ * Learned Johnson-Cook return map.  No counterpart in the reference, which
+ * evaluates StrengthJohnsonCook::update_deviatoric_stress
+ * (src/strength_jc.cpp:100-184) in closed form.
+ *
+ * The network is an MLP 15 -> 128 -> 128 -> 128 -> 7 with ReLU hidden layers.
+ *   inputs  (KMPM_MLP_NIN): strain increment dt*D (6: xx yy zz xy xz yz, in the
+ *           corotational frame), Cauchy stress before the step (6), equivalent
+ *           plastic strain, temperature, log(1 + epsdot_p / epsdot0)
+ *   outputs (KMPM_MLP_NOUT): s_new - s_trial (6), plastic strain increment
+ * It is trained on the GPU in FP32 (kmpm_mlp_train) and evaluated inside the
+ * G2P stress kernel as BF16 tensor-core MMAs with FP32 accumulation
+ * (kmpm_set_surrogate).  Parameters are one flat FP32 vector of
+ * KMPM_MLP_NPARAMS values: W1[128x15] b1[128] W2[128x128] b2 W3[128x128] b3
+ * W4[7x128] b4[7] (row-major, out x in).  The normalisation vector holds
+ * in_mean[15] in_std[15] out_mean[7] out_scale[7] env_lo[15] env_hi[15];
+ * the envelope bounds are in normalised units.  Arrays named X and Y in the
+ * kmpm_mlp_* calls are DEVICE pointers, row-major, in physical units. */
+#define KMPM_MLP_NIN 15
+#define KMPM_MLP_NOUT 7
+#define KMPM_MLP_NPARAMS 35975
+#define KMPM_MLP_NNORM 74
+struct kmpm_mlp;
+typedef struct {
+  int batch;              /* rows per step, <= the batch given to kmpm_mlp_create */
+  long long steps;        /* optimiser steps (Adam, beta 0.9 / 0.999) */
+  double lr;              /* initial learning rate, cosine decay to lr * lr_final_ratio */
+  double lr_final_ratio;
+  unsigned long long seed;  /* batches are drawn with replacement by a hash of (seed, step, row) */
+  int report_every;       /* print the batch loss to stderr every this many steps (0: never) */
+} kmpm_train_opts;
+int kmpm_mlp_create(int batch, struct kmpm_mlp **out);
+void kmpm_mlp_destroy(struct kmpm_mlp *m);
+const char *kmpm_mlp_last_error(const struct kmpm_mlp *m);
+/* He-uniform weights from a seeded splitmix64 stream, zero biases, fresh optimiser state. */
+int kmpm_mlp_init(struct kmpm_mlp *m, unsigned long long seed);
+int kmpm_mlp_set_params(struct kmpm_mlp *m, const float *params);  /* host array */
+int kmpm_mlp_get_params(struct kmpm_mlp *m, float *params);
+int kmpm_mlp_set_norm(struct kmpm_mlp *m, const float *norm);      /* host array */
+int kmpm_mlp_get_norm(struct kmpm_mlp *m, float *norm);
+/* Mean squared error over n rows in normalised output units and its gradient
+ * (host outputs; grad has KMPM_MLP_NPARAMS values). */
+int kmpm_mlp_loss_grad(struct kmpm_mlp *m, const float *X, const float *Y, int n, float *loss, float *grad);
+int kmpm_mlp_train(struct kmpm_mlp *m, const float *X, const float *Y, long long n, const kmpm_train_opts *opts,
+                   float *final_loss);
+/* FP32 inference (the training kernels) and tensor-core inference (BF16
+ * operands, FP32 accumulation: the arithmetic of the learned G2P kernel);
+ * inside (may be NULL) receives 1 where every input lies in the envelope. */
+int kmpm_mlp_predict(struct kmpm_mlp *m, const float *X, long long n, float *Y);
+int kmpm_mlp_predict_tc(struct kmpm_mlp *m, const float *X, long long n, float *Y, signed char *inside);
+
+/* Training pairs from the plain GPU path: while logging is on, the stress
+ * kernel writes (15 inputs, 7 outputs) of a hashed fraction of the plastic
+ * particle-steps (undamaged Johnson-Cook particles) into a device buffer of
+ * capacity rows; kmpm_log_data returns its device address and the number of
+ * rows written.  TLMPM, 3-D, cubic B-spline, FP32, eos-strength materials
+ * with Johnson-Cook strength only (KMPM_ERR_ARG otherwise). */
+int kmpm_log_start(struct kmpm_ctx *ctx, long long capacity, double fraction, unsigned long long seed);
+int kmpm_log_stop(struct kmpm_ctx *ctx);
+int kmpm_log_data(struct kmpm_ctx *ctx, const float **rows, long long *n);
+/* Closed-form return map of one material on n input rows (device arrays):
+ * Y has 8 columns, the 7 outputs and a plastic flag (1 or 0). */
+int kmpm_jc_label(struct kmpm_ctx *ctx, int material, const float *X, long long n, float *Y);
+/* Replace the closed-form return map on plastic steps by the network (a copy
+ * of its current parameters is taken).  A network answer is used only where
+ * every input lies in the envelope and its yield-function, flow-rule and
+ * radial-direction residuals are all <= tol times the flow stress; the
+ * closed form is used everywhere else.  m == NULL restores the plain path.
+ * Same restrictions as kmpm_log_start. */
+int kmpm_set_surrogate(struct kmpm_ctx *ctx, struct kmpm_mlp *m, double tol);
+/* Particle-steps since kmpm_set_surrogate: out[0] plastic, out[1] served by
+ * the network, out[2] outside the envelope, out[3] residual above tol. */
+int kmpm_surrogate_stats(struct kmpm_ctx *ctx, long long out[4]);
 
 /* Nodal mass without device allocation.  No counterpart in the reference.
  *

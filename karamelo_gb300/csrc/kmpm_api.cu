@@ -6,6 +6,7 @@
 #include <cstddef>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <numeric>
 #include <string>
@@ -13,6 +14,7 @@
 
 #include "../../include/kmpm.h"
 #include "kmpm_kernels.cuh"
+#include "kmpm_learn.h"
 
 using namespace kmpm;
 
@@ -96,6 +98,16 @@ struct kmpm_ctx {
   // temperatures are kept as T - T_ref in FP32 (T_ref: the first solid's
   // initial temperature in thermo-mechanical runs, 0 otherwise)
   double T_ref = 0;
+  // learned return map: MODE_PLAIN, MODE_LOG (training pairs) or MODE_SUR
+  int learn_mode = MODE_PLAIN;
+  unsigned char *d_blob = nullptr;
+  float sur_tol = 0.f;
+  unsigned long long *d_lstats = nullptr, *d_log_count = nullptr;
+  float *d_log = nullptr;
+  long long log_cap = 0;
+  uint32_t log_thresh = 0;
+  unsigned long long log_seed = 0;
+  LearnKernels LK{};
   bool indep() const { return prm.independent != 0; }
   bool TL() const { return prm.method == KMPM_TLMPM; }
   bool musl() const { return prm.scheme == KMPM_MUSL; }
@@ -447,7 +459,8 @@ int build(kmpm_ctx *c) {
     s0.dtCFL = 1e22;
     s0.maxtime = 1e300;
     std::vector<StepScalars> sv(c->nscalars, s0);
-    CK(cudaMemcpy(c->d_scalars, sv.data(), sizeof(StepScalars) * sv.size(), cudaMemcpyHostToDevice));
+    CK(cudaMemcpyAsync(c->d_scalars, sv.data(), sizeof(StepScalars) * sv.size(), cudaMemcpyHostToDevice, c->st));
+    CK(cudaStreamSynchronize(c->st));
   }
   DALLOC(c->d_dtcfl, c->ranges.size());
   DALLOC(c->d_err, 1);
@@ -487,7 +500,8 @@ int build(kmpm_ctx *c) {
           else if (f == PF_SID) { int v = (int)s; std::memcpy(&o, &v, 4); }
         }
       }
-      CK(cudaMemcpy(c->buf[0] + (size_t)f * c->ps, row.data(), sizeof(float) * c->ps, cudaMemcpyHostToDevice));
+      CK(cudaMemcpyAsync(c->buf[0] + (size_t)f * c->ps, row.data(), sizeof(float) * c->ps, cudaMemcpyHostToDevice, c->st));
+      CK(cudaStreamSynchronize(c->st));
     }
   }
   // ---- kernel attributes
@@ -545,6 +559,45 @@ int build(kmpm_ctx *c) {
     c->ntiles_launch = (int)tiles.size();
     DALLOC(c->d_tiles, tiles.size());
     CK(cudaMemcpyAsync(c->d_tiles, tiles.data(), sizeof(int2) * tiles.size(), cudaMemcpyHostToDevice, c->st));
+    if (const char *ev = std::getenv("KMPM_CHECK_BINS"); ev && ev[0] == '1') {
+      // self-check of the binning (setup only): device ranges against the host's sorted keys
+      const size_t ncell = (size_t)c->ntiles_total * c->NCELL;
+      std::vector<int> cs(ncell), ce(ncell), ts(c->ntiles_total), te(c->ntiles_total), dk(c->ps);
+      CK(cudaMemcpyAsync(cs.data(), c->d_cs, sizeof(int) * ncell, cudaMemcpyDeviceToHost, c->st));
+      CK(cudaMemcpyAsync(ce.data(), c->d_ce, sizeof(int) * ncell, cudaMemcpyDeviceToHost, c->st));
+      CK(cudaMemcpyAsync(ts.data(), c->d_ts, sizeof(int) * ts.size(), cudaMemcpyDeviceToHost, c->st));
+      CK(cudaMemcpyAsync(te.data(), c->d_te, sizeof(int) * te.size(), cudaMemcpyDeviceToHost, c->st));
+      CK(cudaMemcpyAsync(dk.data(), c->d_keys, sizeof(int) * c->ps, cudaMemcpyDeviceToHost, c->st));
+      CK(cudaStreamSynchronize(c->st));
+      long long key_mismatch = 0, bad_cells = 0, total = 0, maxc = 0, bad_tiles = 0;
+      for (size_t i = 0; i < (size_t)c->ps; i++) key_mismatch += dk[i] != sorted[i];
+      std::vector<int> hs(ncell, 0), he(ncell, 0);
+      for (auto &r : c->ranges)
+        for (int i = 0; i < r.count; i++) {
+          const int k = sorted[r.start + i];
+          if (i == 0 || sorted[r.start + i - 1] != k) hs[k] = r.start + i;
+          he[k] = r.start + i + 1;
+        }
+      size_t first_bad = ncell;
+      for (size_t k = 0; k < ncell; k++) {
+        const long long n = (long long)ce[k] - cs[k];
+        total += n > 0 ? n : 0;
+        maxc = std::max(maxc, n);
+        if (cs[k] != hs[k] || ce[k] != he[k]) { bad_cells++; if (first_bad == ncell) first_bad = k; }
+      }
+      for (auto t : tiles) {
+        const int tg = c->grids[t.x].tile_off + t.y;
+        if (te[tg] <= ts[tg]) bad_tiles++;
+      }
+      std::fprintf(stderr,
+                   "[kmpm bins] ps %zu cells %zu tiles %d launched %d particles-in-cells %lld max/cell %lld "
+                   "key-mismatch %lld bad-cells %lld bad-tiles %lld",
+                   c->ps, ncell, c->ntiles_total, c->ntiles_launch, total, maxc, key_mismatch, bad_cells, bad_tiles);
+      if (first_bad < ncell)
+        std::fprintf(stderr, " first bad cell %zu: dev [%d,%d) host [%d,%d)", first_bad, cs[first_bad], ce[first_bad],
+                     hs[first_bad], he[first_bad]);
+      std::fprintf(stderr, "\n");
+    }
     // nodal mass, once (TLMPM::particles_to_grid, src/tlmpm.cpp:344-351)
     P2GArgs p = p2g_args(c);
     int nl = 0;
@@ -588,7 +641,8 @@ int upload_fixes(kmpm_ctx *c) {
       }
       uint8_t *m = nullptr;
       CK(cudaMalloc(&m, h.mask.size()));
-      CK(cudaMemcpy(m, h.mask.data(), h.mask.size(), cudaMemcpyHostToDevice));
+      CK(cudaMemcpyAsync(m, h.mask.data(), h.mask.size(), cudaMemcpyHostToDevice, c->st));
+      CK(cudaStreamSynchronize(c->st));
       c->d_masks.push_back(m);
       f.mask = m;
       fx.push_back(f);
@@ -596,11 +650,14 @@ int upload_fixes(kmpm_ctx *c) {
     count[gi] = (int)fx.size() - start[gi];
   }
   DALLOC(c->d_fixes, fx.size());
-  if (!fx.empty()) CK(cudaMemcpy(c->d_fixes, fx.data(), sizeof(FixDev) * fx.size(), cudaMemcpyHostToDevice));
+  if (!fx.empty())
+    CK(cudaMemcpyAsync(c->d_fixes, fx.data(), sizeof(FixDev) * fx.size(), cudaMemcpyHostToDevice, c->st));
   DALLOC(c->d_fix_start, start.size());
   DALLOC(c->d_fix_count, count.size());
-  CK(cudaMemcpy(c->d_fix_start, start.data(), sizeof(int) * start.size(), cudaMemcpyHostToDevice));
-  CK(cudaMemcpy(c->d_fix_count, count.data(), sizeof(int) * count.size(), cudaMemcpyHostToDevice));
+  CK(cudaMemcpyAsync(c->d_fix_start, start.data(), sizeof(int) * start.size(), cudaMemcpyHostToDevice, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  CK(cudaMemcpyAsync(c->d_fix_count, count.data(), sizeof(int) * count.size(), cudaMemcpyHostToDevice, c->st));
+  CK(cudaStreamSynchronize(c->st));
   c->fixes_dirty = false;
   c->graph_valid = false;
   return KMPM_OK;
@@ -659,7 +716,26 @@ int enqueue_step(kmpm_ctx *c) {
     MARK("grid_positions");
   }
   // compute_rate_deformation_gradient + update_deformation_gradient + update_stress
-  LAUNCH(c->K.g2p2[TL][th][prec], c->nblk_p, 256, 0, pa);
+  if (c->learn_mode == MODE_PLAIN) {
+    LAUNCH(c->K.g2p2[TL][th][prec], c->nblk_p, 256, 0, pa);
+  } else {
+    LearnArgs la{};
+    la.blob = c->d_blob;
+    la.tol = c->sur_tol;
+    la.stats = c->d_lstats;
+    la.log = c->d_log;
+    la.log_count = c->d_log_count;
+    la.log_cap = c->log_cap;
+    la.log_seed = c->log_seed;
+    la.log_thresh = c->log_thresh;
+    la.nblk = c->nblk_p;
+    void *args[] = {&pa, &la};
+    if (c->learn_mode == MODE_SUR)
+      CK(cudaLaunchKernel(c->LK.sur, dim3((c->nblk_p + 1) / 2), dim3(512), args, c->LK.sur_smem, c->st));
+    else
+      CK(cudaLaunchKernel(c->LK.log, dim3(c->nblk_p), dim3(256), args, 0, c->st));
+    nl++;
+  }
   MARK("g2p_stress");
   // update_time + adjust_dt
   DtArgs da = dt_args(c);
@@ -697,7 +773,8 @@ int check_error(kmpm_ctx *c) {
                      : "dtCFL == 0 or nan";
   std::snprintf(buf, sizeof(buf), "Error: %s (particle slot %d, step %lld)", what, e.particle, e.step);
   const int code = e.code == ERR_J ? KMPM_ERR_J : e.code == ERR_LEFT ? KMPM_ERR_LEFT_DOMAIN
-                   : e.code == ERR_NAN ? KMPM_ERR_NAN : e.code == ERR_POLDEC ? KMPM_ERR_POLDEC : KMPM_ERR_DTCFL;
+                   : e.code == ERR_NAN ? KMPM_ERR_NAN : e.code == ERR_POLDEC ? KMPM_ERR_POLDEC
+                   : e.code == ERR_TIMEOUT ? KMPM_ERR_TIMEOUT : KMPM_ERR_DTCFL;
   return fail(c, code, buf);
 }
 
@@ -777,6 +854,7 @@ int kmpm_destroy(kmpm_ctx *c) {
   dfree(c->nodeA); dfree(c->nodeB); dfree(c->nodeX); dfree(c->nodeT); dfree(c->d_tiles);
   dfree(c->d_cs); dfree(c->d_ce); dfree(c->d_ts); dfree(c->d_te); dfree(c->partial);
   dfree(c->d_fixes); dfree(c->d_fix_start); dfree(c->d_fix_count); dfree(c->d_scalars); dfree(c->d_dtcfl);
+  dfree(c->d_blob); dfree(c->d_lstats); dfree(c->d_log_count); dfree(c->d_log);
   dfree(c->d_err); dfree(c->d_blk_c); dfree(c->d_blk_h); dfree(c->d_eblk); dfree(c->d_eout);
   dfree(c->d_keys); dfree(c->d_vals); dfree(c->rtmp.k1); dfree(c->rtmp.v1); dfree(c->rtmp.hist); dfree(c->rtmp.tot);
   if (c->st) cudaStreamDestroy(c->st);
@@ -930,11 +1008,13 @@ static int fetch_rows(kmpm_ctx *c, const std::vector<int> &fields, int start, in
                       std::vector<std::vector<float>> &H) {
   CK(cudaStreamSynchronize(c->st));
   float *cur = nullptr;
-  CK(cudaMemcpy(&cur, c->d_pp, sizeof(float *), cudaMemcpyDeviceToHost));
+  CK(cudaMemcpyAsync(&cur, c->d_pp, sizeof(float *), cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
   H.assign(PF_COUNT, std::vector<float>());
   for (int f : fields) {
     H[f].resize(n);
-    CK(cudaMemcpy(H[f].data(), cur + (size_t)f * c->ps + start, sizeof(float) * n, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpyAsync(H[f].data(), cur + (size_t)f * c->ps + start, sizeof(float) * n, cudaMemcpyDeviceToHost, c->st));
+    CK(cudaStreamSynchronize(c->st));
   }
   return KMPM_OK;
 }
@@ -1106,10 +1186,12 @@ int kmpm_upload_particles(kmpm_ctx *c, int solid, int field, const double *in) {
     for (int d = 0; d < 3; d++) H[PF_V + d][q] = (float)in[3 * i + d];
   }
   float *cur = nullptr;
-  CK(cudaMemcpy(&cur, c->d_pp, sizeof(float *), cudaMemcpyDeviceToHost));
+  CK(cudaMemcpyAsync(&cur, c->d_pp, sizeof(float *), cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
   for (int d = 0; d < 3; d++)
-    CK(cudaMemcpy(cur + (size_t)(PF_V + d) * c->ps + rg.start, H[PF_V + d].data(), sizeof(float) * rg.count,
-                  cudaMemcpyHostToDevice));
+    CK(cudaMemcpyAsync(cur + (size_t)(PF_V + d) * c->ps + rg.start, H[PF_V + d].data(), sizeof(float) * rg.count,
+                       cudaMemcpyHostToDevice, c->st));
+  CK(cudaStreamSynchronize(c->st));
   return KMPM_OK;
 }
 
@@ -1121,11 +1203,16 @@ int kmpm_download_grid(kmpm_ctx *c, int grid, int field, double *out) {
   const int nn = g.n[0] * g.n[1] * g.n[2];
   std::vector<float4> A(nn), B(nn);
   std::vector<float> Tn(nn);
-  if (field == KMPM_G_MASS || field == KMPM_G_V) CK(cudaMemcpy(A.data(), c->nodeA + g.node_off, sizeof(float4) * nn, cudaMemcpyDeviceToHost));
-  else if (field == KMPM_G_V_UPDATE) CK(cudaMemcpy(A.data(), c->nodeB + g.node_off, sizeof(float4) * nn, cudaMemcpyDeviceToHost));
-  else if (field == KMPM_G_X) CK(cudaMemcpy(A.data(), c->nodeX + g.node_off, sizeof(float4) * nn, cudaMemcpyDeviceToHost));
-  else if (field == KMPM_G_T) CK(cudaMemcpy(Tn.data(), c->nodeT + g.node_off, sizeof(float) * nn, cudaMemcpyDeviceToHost));
+  if (field == KMPM_G_MASS || field == KMPM_G_V)
+    CK(cudaMemcpyAsync(A.data(), c->nodeA + g.node_off, sizeof(float4) * nn, cudaMemcpyDeviceToHost, c->st));
+  else if (field == KMPM_G_V_UPDATE)
+    CK(cudaMemcpyAsync(A.data(), c->nodeB + g.node_off, sizeof(float4) * nn, cudaMemcpyDeviceToHost, c->st));
+  else if (field == KMPM_G_X)
+    CK(cudaMemcpyAsync(A.data(), c->nodeX + g.node_off, sizeof(float4) * nn, cudaMemcpyDeviceToHost, c->st));
+  else if (field == KMPM_G_T)
+    CK(cudaMemcpyAsync(Tn.data(), c->nodeT + g.node_off, sizeof(float) * nn, cudaMemcpyDeviceToHost, c->st));
   else return fail(c, KMPM_ERR_ARG, "unknown grid field");
+  CK(cudaStreamSynchronize(c->st));
   for (int i = 0; i < nn; i++) {
     if (field == KMPM_G_MASS) out[i] = A[i].w;
     else if (field == KMPM_G_T) out[i] = c->T_ref + Tn[i];
@@ -1177,5 +1264,111 @@ const char *kmpm_profile_phase(kmpm_ctx *c, int i) {
 }
 
 int kmpm_launches_per_step(kmpm_ctx *c) { return c ? c->launches_per_step : 0; }
+
+// ---------------------------------------------------------------- learned return map
+static int learn_check(kmpm_ctx *c) {
+  if (!c->TL() || c->prm.dim != 3 || c->prm.basis != KMPM_BASIS_CUBIC)
+    return fail(c, KMPM_ERR_ARG, "the learned return map covers 3-D TLMPM with the cubic B-spline basis");
+  if (c->prm.precision != KMPM_PREC_FP32 || c->prm.thermal)
+    return fail(c, KMPM_ERR_ARG, "the learned return map needs FP32 and no thermo-mechanical coupling");
+  for (const MatDev &m : c->mats)
+    if (m.type != KMPM_MAT_EOS_STRENGTH || m.strength != 2)
+      return fail(c, KMPM_ERR_ARG, "the learned return map needs eos-strength materials with Johnson-Cook strength");
+  if (!c->LK.sur) get_learn_kernels(c->LK);
+  return KMPM_OK;
+}
+
+int kmpm_log_start(kmpm_ctx *c, long long capacity, double fraction, unsigned long long seed) {
+  if (!c || capacity < 1 || !(fraction > 0.0)) return KMPM_ERR_ARG;
+  int r = learn_check(c);
+  if (r != KMPM_OK) return r;
+  if (capacity != c->log_cap) {
+    dfree(c->d_log);
+    DALLOC(c->d_log, (size_t)capacity * (mlp_nin() + mlp_nout()));
+    c->log_cap = capacity;
+  }
+  if (!c->d_log_count) DALLOC(c->d_log_count, 1);
+  CK(cudaMemsetAsync(c->d_log_count, 0, sizeof(unsigned long long), c->st));
+  CK(cudaStreamSynchronize(c->st));
+  c->log_thresh = fraction >= 1.0 ? 0xFFFFFFFFu : (uint32_t)(fraction * 4294967296.0);
+  c->log_seed = seed;
+  c->learn_mode = MODE_LOG;
+  c->graph_valid = false;
+  return KMPM_OK;
+}
+
+int kmpm_log_stop(kmpm_ctx *c) {
+  if (!c) return KMPM_ERR_ARG;
+  if (c->learn_mode == MODE_LOG) {
+    c->learn_mode = MODE_PLAIN;
+    c->graph_valid = false;
+  }
+  return KMPM_OK;
+}
+
+int kmpm_log_data(kmpm_ctx *c, const float **rows, long long *n) {
+  if (!c || !rows || !n) return KMPM_ERR_ARG;
+  *rows = c->d_log;
+  *n = 0;
+  if (!c->d_log_count) return KMPM_OK;
+  unsigned long long cnt = 0;
+  CK(cudaMemcpyAsync(&cnt, c->d_log_count, sizeof(cnt), cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  *n = (long long)std::min<unsigned long long>(cnt, (unsigned long long)c->log_cap);
+  return KMPM_OK;
+}
+
+int kmpm_jc_label(kmpm_ctx *c, int material, const float *X, long long n, float *Y) {
+  if (!c || !X || !Y || n < 0 || material < 0 || material >= (int)c->mats.size()) return KMPM_ERR_ARG;
+  const MatDev &m = c->mats[material];
+  if (m.type != KMPM_MAT_EOS_STRENGTH || m.strength != 2) return fail(c, KMPM_ERR_ARG, "not a Johnson-Cook material");
+  int r = prepare(c);
+  if (r != KMPM_OK) return r;
+  if (!c->LK.label) get_learn_kernels(c->LK);
+  if (n == 0) return KMPM_OK;
+  const MatDev *mats = c->d_mats;
+  void *args[] = {(void *)&mats, &material, (void *)&X, &n, (void *)&Y};
+  CK(cudaLaunchKernel(c->LK.label, dim3((unsigned)((n + 255) / 256)), dim3(256), args, 0, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  return KMPM_OK;
+}
+
+int kmpm_set_surrogate(kmpm_ctx *c, kmpm_mlp *m, double tol) {
+  if (!c) return KMPM_ERR_ARG;
+  if (!m) {
+    if (c->learn_mode == MODE_SUR) {
+      c->learn_mode = MODE_PLAIN;
+      c->graph_valid = false;
+    }
+    return KMPM_OK;
+  }
+  if (!(tol > 0.0)) return fail(c, KMPM_ERR_ARG, "tol must be positive");
+  int r = learn_check(c);
+  if (r != KMPM_OK) return r;
+  const unsigned char *blob = nullptr;
+  r = mlp_device_blob(m, &blob);
+  if (r != KMPM_OK) return fail(c, r, std::string("network: ") + kmpm_mlp_last_error(m));
+  if (!c->d_blob) DALLOC(c->d_blob, (size_t)mlp_blob_bytes());
+  if (!c->d_lstats) DALLOC(c->d_lstats, 4);
+  CK(cudaMemcpyAsync(c->d_blob, blob, (size_t)mlp_blob_bytes(), cudaMemcpyDeviceToDevice, c->st));
+  CK(cudaMemsetAsync(c->d_lstats, 0, 4 * sizeof(unsigned long long), c->st));
+  CK(cudaStreamSynchronize(c->st));
+  CK(cudaFuncSetAttribute(c->LK.sur, cudaFuncAttributeMaxDynamicSharedMemorySize, c->LK.sur_smem));
+  c->sur_tol = (float)tol;
+  c->learn_mode = MODE_SUR;
+  c->graph_valid = false;
+  return KMPM_OK;
+}
+
+int kmpm_surrogate_stats(kmpm_ctx *c, long long out[4]) {
+  if (!c || !out) return KMPM_ERR_ARG;
+  unsigned long long v[4] = {0, 0, 0, 0};
+  if (c->d_lstats) {
+    CK(cudaMemcpyAsync(v, c->d_lstats, sizeof(v), cudaMemcpyDeviceToHost, c->st));
+    CK(cudaStreamSynchronize(c->st));
+  }
+  for (int k = 0; k < 4; k++) out[k] = (long long)v[k];
+  return KMPM_OK;
+}
 
 }  // extern "C"

@@ -121,6 +121,7 @@ enum ErrCode : int {
   ERR_NAN = 12,
   ERR_POLDEC = 13,
   ERR_DTCFL = 14,
+  ERR_TIMEOUT = 15,
 };
 struct ErrState {
   int code;
@@ -240,6 +241,13 @@ __device__ __forceinline__ void cubic_weights(float f, float ih, float *s, float
 
 // Per-axis stencil values of one particle: base node index i0 and, for each
 // stencil slot s, the basis value and derivative (0 where the node is absent).
+// The derivative is also set to 0 where the value is 0: the reference keeps a
+// particle-node pair only when every 1-D value is non-zero (src/tlmpm.cpp:263,
+// src/ulmpm.cpp:259-272), and with this masking every product of per-axis
+// values and slopes that forms w or grad w of such a pair is 0, so no kernel
+// needs a per-node test.  (The boundary-modified cubic spline at ntype 1 has a
+// zero value with a non-zero slope; interior cubic values are zero only where
+// their slope is zero too.)
 template <int BASIS> struct Axis {
   static constexpr int S = Stencil<BASIS>::S;
   int i0;
@@ -261,6 +269,7 @@ template <int BASIS> struct Axis {
       float xn = lo + (float)i * h;
       float r = (xp - xn) * ih;
       basis<BASIS>(r, node_type<BASIS>(i, ng), ih, s[k], ds[k]);
+      ds[k] = s[k] != 0.f ? ds[k] : 0.f;
     }
   }
   // 1-D (unused axis): weight 1, gradient 0, single slot at node 0
@@ -449,6 +458,24 @@ __device__ inline R eos_pressure(const MatDev &m, R J, R Jm1, R rho, R damage, R
 // src/strength_plastic.cpp:62-115, src/strength_jc.cpp:100-184,
 // src/strength_swift.cpp:77-147, src/strength_fluid.cpp:46-58).
 // sig: current sigma (full, symmetric storage), D: rate of deformation.
+// Johnson-Cook flow stress at the start of the step
+// (StrengthJohnsonCook::update_deviatoric_stress, src/strength_jc.cpp:120-150);
+// p = (G, A, B, n, epsdot0, C, m, Tr, Tm)
+template <typename R>
+__device__ __forceinline__ R jc_flow_stress(const R *p, R epsp, R epsdot, R T) {
+  R A = p[1], B = p[2], n = p[3], epsdot0 = p[4], C = p[5], mm = p[6], Tr = p[7], Tm = p[8];
+  R ratio = epsdot / epsdot0;
+  ratio = ratio > R(1) ? ratio : R(1);
+  R ys = epsp < R(1.0e-10) ? A : A + B * pow(epsp, n);
+  if (C != R(0)) ys *= pow(R(1) + ratio, C);
+  if (T < Tm) {
+    if (mm != R(0) && T >= Tr) ys *= R(1) - pow((T - Tr) / (Tm - Tr), mm);
+  } else {
+    ys = R(0);
+  }
+  return ys;
+}
+
 template <typename R>
 __device__ inline Sym<R> strength_update(const MatDev &m, R dt, const Sym<R> &sig, const Sym<R> &D, R &dep, R epsp,
                                          R epsdot, R damage, R T) {
@@ -492,16 +519,7 @@ __device__ inline Sym<R> strength_update(const MatDev &m, R dt, const Sym<R> &si
   }
   R G = p[0], ys;
   if (m.strength == 2) {
-    R A = p[1], B = p[2], n = p[3], epsdot0 = p[4], C = p[5], mm = p[6], Tr = p[7], Tm = p[8];
-    R ratio = epsdot / epsdot0;
-    ratio = ratio > R(1) ? ratio : R(1);
-    ys = epsp < R(1.0e-10) ? A : A + B * pow(epsp, n);
-    if (C != R(0)) ys *= pow(R(1) + ratio, C);
-    if (T < Tm) {
-      if (mm != R(0) && T >= Tr) ys *= R(1) - pow((T - Tr) / (Tm - Tr), mm);
-    } else {
-      ys = R(0);
-    }
+    ys = jc_flow_stress<R>(p, epsp, epsdot, T);
   } else {
     R A = p[1], B = p[2], C = p[3], n = p[4];
     ys = (epsp > R(1.0e-10) && epsp > C) ? A + B * pow(epsp - C, n) : A;

@@ -42,11 +42,9 @@ __device__ __forceinline__ void p2g_particle(float (&accr)[NSL][Q], const float 
   for (int u = 0; u < NSL; u++) {
     if (!PAIR && lane + 32 * u >= NS) continue;
     const float2 bz = DIM == 3 ? bj[2 * S + soff[u][2]] : make_float2(1.f, 0.f);
+    // a pair the reference drops has w = 0 and, through the masked per-axis
+    // slopes (Axis::eval), grad w = 0: it adds nothing, without a branch
     const float w = wxy * bz.x;
-    // the reference keeps a particle-node pair only when every 1-D value is
-    // non-zero (src/tlmpm.cpp:263, src/ulmpm.cpp:259-272); the cubic spline
-    // at ntype 1 has a zero value but a non-zero slope
-    if (w == 0.f) continue;
     const float gw[3] = {gxy0 * bz.x, gxy1 * bz.x, wxy * bz.y};
     p2g_accumulate<MODE, THERMAL, Q>(accr[u], pay, w, gw);
   }
@@ -192,6 +190,7 @@ __global__ void __launch_bounds__(256) k_p2g(P2GArgs a) {
           const float4 pj = spos[j];
           const float r = ((d == 0 ? pj.x : (d == 1 ? pj.y : pj.z)) - xn) * ih;
           basis<BASIS>(r, node_type<BASIS>(i, ngd), ih, sv, dsv);
+          dsv = sv != 0.f ? dsv : 0.f;  // as Axis::eval
         }
         sbas[it] = make_float2(sv, dsv);
       }
@@ -526,30 +525,44 @@ __global__ void __launch_bounds__(256, 3) k_g2p2(PartArgs a) {
 #pragma unroll
     for (int k = 0; k < SZ; k++) cz[k] = min(max(ax.ax[2].i0 + k, 0), g.n[2] - 1);
     const float4 *__restrict__ NV = (a.use_vu ? a.nodeB : a.nodeA) + g.node_off;
+    // sum factorisation over the z slots: for every (i, j), A = sum_k s_z V
+    // and B = sum_k ds_z V, then grad v += (ds_x s_y A, s_x ds_y A, s_x s_y B)
+    // (dropped pairs add 0: see Axis::eval)
 #pragma unroll
     for (int i = 0; i < S; i++) {
       const float sx = ax.ax[0].s[i], dsx = ax.ax[0].ds[i];
 #pragma unroll
       for (int j = 0; j < SY; j++) {
         const float sy = ax.ax[1].s[j], dsy = ax.ax[1].ds[j];
-        const float sxy = sx * sy, gx = dsx * sy, gy = sx * dsy;
         const int row = (cx[i] * g.n[1] + cy[j]) * g.n[2];
+        float A[3] = {0.f, 0.f, 0.f}, B[3] = {0.f, 0.f, 0.f}, AT = 0.f, BT = 0.f;
 #pragma unroll
         for (int k = 0; k < SZ; k++) {
           const float sz = ax.ax[2].s[k], dsz = ax.ax[2].ds[k];
-          const float on = (sxy * sz != 0.f) ? 1.f : 0.f;
-          const float gw[3] = {on * gx * sz, on * gy * sz, on * sxy * dsz};
           const float4 V = __ldg(NV + row + cz[k]);
           const float vn[3] = {V.x, V.y, V.z};
 #pragma unroll
-          for (int r = 0; r < DIM; r++)
-#pragma unroll
-            for (int c = 0; c < DIM; c++) G[3 * r + c] += vn[r] * gw[c];
+          for (int r = 0; r < DIM; r++) {
+            A[r] += sz * vn[r];
+            if (DIM == 3) B[r] += dsz * vn[r];
+          }
           if (THERMAL) {
             const float Tn = a.use_vu ? V.w : a.nodeT[g.node_off + row + cz[k]];
-#pragma unroll
-            for (int c = 0; c < 3; c++) qg[c] -= gw[c] * Tn;
+            AT += sz * Tn;
+            if (DIM == 3) BT += dsz * Tn;
           }
+        }
+        const float sxy = sx * sy, gx = dsx * sy, gy = sx * dsy;
+#pragma unroll
+        for (int r = 0; r < DIM; r++) {
+          G[3 * r] += gx * A[r];
+          if (DIM >= 2) G[3 * r + 1] += gy * A[r];
+          if (DIM == 3) G[3 * r + 2] += sxy * B[r];
+        }
+        if (THERMAL) {
+          qg[0] -= gx * AT;
+          qg[1] -= gy * AT;
+          qg[2] -= sxy * BT;
         }
       }
     }

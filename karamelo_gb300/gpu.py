@@ -29,7 +29,13 @@ EXPORTED = ["kmpm_create", "kmpm_destroy", "kmpm_last_error", "kmpm_add_material
             "kmpm_add_solid", "kmpm_add_fix", "kmpm_run", "kmpm_run_time", "kmpm_scalars",
             "kmpm_download_particles", "kmpm_upload_particles", "kmpm_download_grid", "kmpm_energy",
             "kmpm_stream", "kmpm_launches_per_step", "kmpm_profile", "kmpm_profile_phase",
-            "kmpm_p2g_mass_noalloc", "kmpm_solid_scalars"]
+            "kmpm_p2g_mass_noalloc", "kmpm_solid_scalars",
+            "kmpm_mlp_create", "kmpm_mlp_destroy", "kmpm_mlp_last_error", "kmpm_mlp_init", "kmpm_mlp_set_params",
+            "kmpm_mlp_get_params", "kmpm_mlp_set_norm", "kmpm_mlp_get_norm", "kmpm_mlp_loss_grad", "kmpm_mlp_train",
+            "kmpm_mlp_predict", "kmpm_mlp_predict_tc", "kmpm_log_start", "kmpm_log_stop", "kmpm_log_data",
+            "kmpm_jc_label", "kmpm_set_surrogate", "kmpm_surrogate_stats"]
+
+MLP_NIN, MLP_NOUT, MLP_NPARAMS, MLP_NNORM = 15, 7, 35975, 74
 
 
 class KmpmParams(ctypes.Structure):
@@ -38,6 +44,11 @@ class KmpmParams(ctypes.Structure):
                 ("dt_factor", ctypes.c_double), ("dt_constant", ctypes.c_int), ("boxlo", ctypes.c_double * 3),
                 ("boxhi", ctypes.c_double * 3), ("precision", ctypes.c_int), ("sort_every", ctypes.c_int),
                 ("track_strain", ctypes.c_int), ("independent", ctypes.c_int)]
+
+
+class TrainOpts(ctypes.Structure):
+    _fields_ = [("batch", ctypes.c_int), ("steps", ctypes.c_longlong), ("lr", ctypes.c_double),
+                ("lr_final_ratio", ctypes.c_double), ("seed", ctypes.c_ulonglong), ("report_every", ctypes.c_int)]
 
 
 class KmpmError(RuntimeError):
@@ -84,6 +95,28 @@ def load(path: str = LIB_PATH):
     L.kmpm_profile_phase.argtypes = [p, i]
     fp = ctypes.c_void_p
     L.kmpm_p2g_mass_noalloc.argtypes = [fp, fp, i, i, i, dp, d, ip, ip, fp, p, ctypes.c_char_p, i]
+    ll, ull = ctypes.c_longlong, ctypes.c_ulonglong
+    f32p = ctypes.POINTER(ctypes.c_float)
+    L.kmpm_mlp_create.argtypes = [i, ctypes.POINTER(p)]
+    L.kmpm_mlp_destroy.argtypes = [p]
+    L.kmpm_mlp_destroy.restype = None
+    L.kmpm_mlp_last_error.argtypes = [p]
+    L.kmpm_mlp_last_error.restype = ctypes.c_char_p
+    L.kmpm_mlp_init.argtypes = [p, ull]
+    L.kmpm_mlp_set_params.argtypes = [p, f32p]
+    L.kmpm_mlp_get_params.argtypes = [p, f32p]
+    L.kmpm_mlp_set_norm.argtypes = [p, f32p]
+    L.kmpm_mlp_get_norm.argtypes = [p, f32p]
+    L.kmpm_mlp_loss_grad.argtypes = [p, fp, fp, i, f32p, f32p]
+    L.kmpm_mlp_train.argtypes = [p, fp, fp, ll, ctypes.POINTER(TrainOpts), f32p]
+    L.kmpm_mlp_predict.argtypes = [p, fp, ll, fp]
+    L.kmpm_mlp_predict_tc.argtypes = [p, fp, ll, fp, fp]
+    L.kmpm_log_start.argtypes = [p, ll, d, ull]
+    L.kmpm_log_stop.argtypes = [p]
+    L.kmpm_log_data.argtypes = [p, ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(ll)]
+    L.kmpm_jc_label.argtypes = [p, i, fp, ll, fp]
+    L.kmpm_set_surrogate.argtypes = [p, p, d]
+    L.kmpm_surrogate_stats.argtypes = [p, ctypes.POINTER(ll)]
     _lib = L
     return L
 
@@ -197,6 +230,40 @@ class GpuBackend:
     def launches_per_step(self):
         return self.L.kmpm_launches_per_step(self.h)
 
+    # ---- learned return map (training pairs, surrogate)
+    def log_start(self, capacity: int, fraction: float, seed: int = 0):
+        self._ck(self.L.kmpm_log_start(self.h, int(capacity), float(fraction), int(seed)))
+
+    def log_stop(self):
+        self._ck(self.L.kmpm_log_stop(self.h))
+
+    def log_data(self):
+        """The logged pairs as a CUDA tensor [n, 22] (a copy: inputs then outputs)."""
+        import torch
+        ptr, n = ctypes.c_void_p(), ctypes.c_longlong()
+        self._ck(self.L.kmpm_log_data(self.h, ctypes.byref(ptr), ctypes.byref(n)))
+        if n.value == 0:
+            return torch.zeros((0, MLP_NIN + MLP_NOUT), dtype=torch.float32, device="cuda")
+        return device_view(ptr.value, (n.value, MLP_NIN + MLP_NOUT)).clone()
+
+    def jc_label(self, material: int, X):
+        """Closed-form return map of one material on input rows X (CUDA
+        float32 [n, 15]): [n, 8] = 7 outputs and the plastic flag."""
+        import torch
+        X = X.contiguous()
+        Y = torch.empty((X.shape[0], MLP_NOUT + 1), dtype=torch.float32, device=X.device)
+        torch.cuda.synchronize()
+        self._ck(self.L.kmpm_jc_label(self.h, int(material), X.data_ptr(), X.shape[0], Y.data_ptr()))
+        return Y
+
+    def set_surrogate(self, mlp, tol: float = 1e-3):
+        self._ck(self.L.kmpm_set_surrogate(self.h, mlp.h if mlp is not None else None, float(tol)))
+
+    def surrogate_stats(self):
+        out = (ctypes.c_longlong * 4)()
+        self._ck(self.L.kmpm_surrogate_stats(self.h, out))
+        return dict(plastic=out[0], network=out[1], outside=out[2], residual=out[3])
+
     def profile(self, nsteps: int):
         """Mean device time (ms) of every phase of a step, from CUDA events on
         the library's stream (eager launches, not the captured graph)."""
@@ -204,3 +271,113 @@ class GpuBackend:
         n = ctypes.c_int(0)
         self._ck(self.L.kmpm_profile(self.h, int(nsteps), _dp(out), 32, ctypes.byref(n)))
         return {self.L.kmpm_profile_phase(self.h, k).decode(): float(out[k]) for k in range(n.value)}
+
+
+class _CudaArray:
+    def __init__(self, ptr, shape):
+        self.__cuda_array_interface__ = {"shape": tuple(shape), "typestr": "<f4", "data": (int(ptr), False),
+                                         "version": 3, "strides": None}
+
+
+def device_view(ptr, shape):
+    """A torch view (no copy) of a float32 device array owned by the library."""
+    import torch
+    return torch.as_tensor(_CudaArray(ptr, shape), device="cuda")
+
+
+class Mlp:
+    """The learned return map's network (kmpm_mlp_*): FP32 training on the
+    GPU, FP32 and tensor-core inference.  X / Y are CUDA float32 tensors in
+    physical units ([n, 15] / [n, 7])."""
+
+    def __init__(self, batch: int = 8192, seed: int = 0):
+        L = load()
+        self.L = L
+        h = ctypes.c_void_p()
+        r = L.kmpm_mlp_create(int(batch), ctypes.byref(h))
+        if r != KMPM_OK:
+            raise KmpmError(r, "kmpm_mlp_create failed (no CUDA device?)")
+        self.h = h
+        self.batch = batch
+        self._ck(L.kmpm_mlp_init(h, int(seed)))
+
+    def _ck(self, r):
+        if r != KMPM_OK:
+            raise KmpmError(r, self.L.kmpm_mlp_last_error(self.h).decode())
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            self.L.kmpm_mlp_destroy(self.h)
+            self.h = None
+
+    @staticmethod
+    def _f32(a):
+        a = np.ascontiguousarray(a, np.float32)
+        return a, a.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+
+    def init(self, seed: int):
+        self._ck(self.L.kmpm_mlp_init(self.h, int(seed)))
+
+    @property
+    def params(self):
+        out = np.empty(MLP_NPARAMS, np.float32)
+        self._ck(self.L.kmpm_mlp_get_params(self.h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_float))))
+        return out
+
+    @params.setter
+    def params(self, v):
+        a, ptr = self._f32(v)
+        assert a.size == MLP_NPARAMS
+        self._ck(self.L.kmpm_mlp_set_params(self.h, ptr))
+
+    @property
+    def norm(self):
+        out = np.empty(MLP_NNORM, np.float32)
+        self._ck(self.L.kmpm_mlp_get_norm(self.h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_float))))
+        return out
+
+    @norm.setter
+    def norm(self, v):
+        a, ptr = self._f32(v)
+        assert a.size == MLP_NNORM
+        self._ck(self.L.kmpm_mlp_set_norm(self.h, ptr))
+
+    def loss_grad(self, X, Y):
+        import torch
+        X, Y = X.contiguous(), Y.contiguous()
+        torch.cuda.synchronize()
+        loss = ctypes.c_float()
+        g = np.empty(MLP_NPARAMS, np.float32)
+        self._ck(self.L.kmpm_mlp_loss_grad(self.h, X.data_ptr(), Y.data_ptr(), X.shape[0], ctypes.byref(loss),
+                                           g.ctypes.data_as(ctypes.POINTER(ctypes.c_float))))
+        return float(loss.value), g
+
+    def train(self, X, Y, steps: int, batch: int = None, lr: float = 1e-3, lr_final_ratio: float = 0.01,
+              seed: int = 0, report_every: int = 0) -> float:
+        import torch
+        X, Y = X.contiguous(), Y.contiguous()
+        torch.cuda.synchronize()
+        o = TrainOpts(batch=int(batch or self.batch), steps=int(steps), lr=float(lr),
+                      lr_final_ratio=float(lr_final_ratio), seed=int(seed), report_every=int(report_every))
+        loss = ctypes.c_float()
+        self._ck(self.L.kmpm_mlp_train(self.h, X.data_ptr(), Y.data_ptr(), X.shape[0], ctypes.byref(o),
+                                       ctypes.byref(loss)))
+        return float(loss.value)
+
+    def predict(self, X):
+        import torch
+        X = X.contiguous()
+        Y = torch.empty((X.shape[0], MLP_NOUT), dtype=torch.float32, device=X.device)
+        torch.cuda.synchronize()
+        self._ck(self.L.kmpm_mlp_predict(self.h, X.data_ptr(), X.shape[0], Y.data_ptr()))
+        return Y
+
+    def predict_tc(self, X):
+        """Tensor-core inference: (Y [n, 7], inside-envelope flags [n] int8)."""
+        import torch
+        X = X.contiguous()
+        Y = torch.empty((X.shape[0], MLP_NOUT), dtype=torch.float32, device=X.device)
+        ins = torch.empty((X.shape[0],), dtype=torch.int8, device=X.device)
+        torch.cuda.synchronize()
+        self._ck(self.L.kmpm_mlp_predict_tc(self.h, X.data_ptr(), X.shape[0], Y.data_ptr(), ins.data_ptr()))
+        return Y, ins

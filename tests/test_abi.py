@@ -26,16 +26,21 @@ def test_library_exports_all_symbols(gpu_lib):
 def test_struct_layout_matches_header(gpu_lib, tmp_path):
     """The ctypes mirrors have the sizes a C compiler gives the header's structs."""
     import subprocess
-    from karamelo_gb300.gpu import KmpmParams
+    from karamelo_gb300.gpu import KmpmParams, TrainOpts
     from karamelo_gb300.scenario import MaterialParams
     src = tmp_path / "sz.c"
     src.write_text('#include "kmpm.h"\n#include <stdio.h>\n'
-                   'int main(void){printf("%zu %zu\\n", sizeof(kmpm_params), sizeof(kmpm_material));return 0;}\n')
+                   'int main(void){printf("%zu %zu %zu %d %d %d %d\\n", sizeof(kmpm_params), sizeof(kmpm_material),'
+                   ' sizeof(kmpm_train_opts), KMPM_MLP_NIN, KMPM_MLP_NOUT, KMPM_MLP_NPARAMS, KMPM_MLP_NNORM);'
+                   'return 0;}\n')
     exe = tmp_path / "sz"
     subprocess.check_call(["gcc", "-I" + os.path.join(ROOT, "include"), str(src), "-o", str(exe)])
-    p, m = map(int, subprocess.check_output([str(exe)]).split())
+    p, m, t, nin, nout, npar, nnorm = map(int, subprocess.check_output([str(exe)]).split())
     assert ctypes.sizeof(KmpmParams) == p
     assert ctypes.sizeof(MaterialParams) == m
+    assert ctypes.sizeof(TrainOpts) == t
+    from karamelo_gb300 import gpu
+    assert (gpu.MLP_NIN, gpu.MLP_NOUT, gpu.MLP_NPARAMS, gpu.MLP_NNORM) == (nin, nout, npar, nnorm)
 
 
 def test_create_without_device_fails_loudly(gpu_lib):
