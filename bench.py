@@ -35,7 +35,8 @@ import time
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-METRIC = "particle-updates/s on 1 GB300 (Taylor-bar TLMPM MUSL step)"
+METRIC = "particle-updates/s on 1 GB300: learned/FP32 vs plain GPU, at <=1e-3 rel err"
+NETWORK = os.path.join(ROOT, "karamelo_gb300", "data", "taylor_copper_mlp.npz")
 UNIT = "particle-updates/s"
 
 # Algorithmic bytes of every phase (FP32 = 4 B): particle fields read or
@@ -201,6 +202,8 @@ def bench_ours(args):
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1)
     clk = clocks.stop()
+    plain_sigma, plain_x = sim.particles(0, "sigma"), sim.particles(0, "x")
+    learned = None if args.no_learned else bench_learned(args, be, plain_sigma, plain_x, n, ms)
     ms, units = aggregate_replicas(ms, n * args.steps, "cuda")
     value = units / (ms / 1000.0)
     launches = be.launches_per_step() * args.steps
@@ -261,6 +264,8 @@ def bench_ours(args):
         "phases_ms": phases,
         "clocks": clk,
     }
+    if learned is not None:
+        line["learned"] = learned
     if world == 1 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
         v, npart, done_c, dtc = run_cpu_sample(args.cpu_cellsize, args.cpu_steps, args.ref_budget, threads)
@@ -268,6 +273,51 @@ def bench_ours(args):
                                 "sample": f"{done_c} oracle steps of the same bar at cellsize {args.cpu_cellsize} mm "
                                           f"({npart} particles) after its untimed first step"}
     print(json.dumps(line), flush=True)
+
+
+def bench_learned(args, plain_backend, plain_sigma, plain_x, n, plain_ms):
+    """The same bar and the same steps with the learned return map
+    (kmpm_set_surrogate, residual tolerance 1e-3): throughput, share of
+    plastic particle-steps the network answered, and the final stress and bar
+    length against the plain FP32 run."""
+    import numpy as np
+    import torch
+    from karamelo_gb300 import workloads as W
+    from karamelo_gb300.gpu import GpuBackend
+    from karamelo_gb300.surrogate import load_network
+    if not os.path.exists(NETWORK):
+        return {"unavailable": f"no trained network at {os.path.relpath(NETWORK, ROOT)}"}
+    mlp, meta = load_network(NETWORK)
+    sim = W.taylor_bar(None, cellsize=args.cellsize)
+    sim.backend = GpuBackend(sim.s, precision=args.precision, track_strain=False)
+    sim.run(1)
+    W.taylor_bar_wall(sim)
+    be = sim.backend
+    be.set_surrogate(mlp, args.tol)
+    be.run(args.warmup)
+    be.profile(args.profile_steps)
+    stream = torch.cuda.ExternalStream(be.stream())
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    be.run(args.steps)
+    e1.record(stream)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1)
+    st = be.surrogate_stats()
+    sig, x = sim.particles(0, "sigma"), sim.particles(0, "x")
+    length = lambda a: float(a[:, 0].max() - a[:, 0].min())
+    value = n * args.steps / (ms / 1000.0)
+    return {"value": value, "unit": UNIT, "ms_per_step": ms / args.steps, "plain_ms_per_step": plain_ms / args.steps,
+            "learned_over_plain": (plain_ms / ms), "tol": args.tol,
+            "rel_l2_sigma_vs_plain": float(np.linalg.norm(sig - plain_sigma) / np.linalg.norm(plain_sigma)),
+            "rel_l2_x_vs_plain": float(np.linalg.norm(x - plain_x) / np.linalg.norm(plain_x)),
+            "bar_length_rel_err_vs_plain": abs(length(x) - length(plain_x)) / length(plain_x),
+            "plastic_particle_steps": st["plastic"], "served_by_network": st["network"],
+            "outside_envelope": st["outside"], "residual_above_tol": st["residual"],
+            "network": {"file": os.path.relpath(NETWORK, ROOT), "n_pairs": meta.get("n_pairs"),
+                        "train_steps": meta.get("steps"), "holdout_tc_pass": meta.get("tc_pass")},
+            "gpu_launches": be.launches_per_step() * args.steps}
 
 
 def bench_sweep(args):
@@ -323,6 +373,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", default="taylor", choices=["taylor", "sweep"])
     ap.add_argument("--instances", type=int, default=1024)
+    ap.add_argument("--tol", type=float, default=1e-3)
+    ap.add_argument("--no-learned", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -255,11 +255,13 @@ int kmpm_log_data(struct kmpm_ctx *ctx, const float **rows, long long *n);
  * Y has 8 columns, the 7 outputs and a plastic flag (1 or 0). */
 int kmpm_jc_label(struct kmpm_ctx *ctx, int material, const float *X, long long n, float *Y);
 /* Replace the closed-form return map on plastic steps by the network (a copy
- * of its current parameters is taken).  A network answer is used only where
- * every input lies in the envelope and its yield-function, flow-rule and
- * radial-direction residuals are all <= tol times the flow stress; the
- * closed form is used everywhere else.  m == NULL restores the plain path.
- * Same restrictions as kmpm_log_start. */
+ * of its current parameters is taken).  The predicted stress correction is
+ * kept through its component along the trial deviator (J2 flow is radial).
+ * A network answer is used only where every input lies in the envelope and
+ * its yield-function residual |s_eq(new) - flow stress| and flow-rule
+ * residual |s_eq(trial) - s_eq(new) - 3 G dep| are both <= tol times the flow
+ * stress; the closed form is used everywhere else.  m == NULL restores the
+ * plain path.  Same restrictions as kmpm_log_start. */
 int kmpm_set_surrogate(struct kmpm_ctx *ctx, struct kmpm_mlp *m, double tol);
 /* Particle-steps since kmpm_set_surrogate: out[0] plastic, out[1] served by
  * the network, out[2] outside the envelope, out[3] residual above tol. */

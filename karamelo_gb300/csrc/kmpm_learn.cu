@@ -7,7 +7,8 @@
 //             (src/strength_jc.cpp:100-184) replaced on plastic steps by the
 //             tensor-core MLP (kmpm_mlp.cuh), falling back to the closed form
 //             where the inputs leave the training envelope or the network's
-//             answer misses the yield / flow-rule residual tolerance
+//             answer (its stress correction kept along the trial deviator)
+//             misses the yield-function or flow-rule residual tolerance
 //
 // Both cover TLMPM with materials of type eos-strength whose strength is
 // Johnson-Cook (the host checks this), FP32, no nodal temperature field.
@@ -199,23 +200,28 @@ __global__ void __launch_bounds__(MODE == MODE_SUR ? 512 : 256, MODE == MODE_SUR
       if (!mlp::tile_forward<NTILE>(tcx, y)) {
         if (threadIdx.x == 0) raise_error(a.err, ERR_TIMEOUT, -1, step);
       } else if (cand && inside) {
-        // residuals of the network's answer, relative to the flow stress:
-        // yield function at the new state, flow rule (stress drop = 3 G dep)
-        // and radial direction
+        // J2 flow returns along the trial deviator, so the predicted
+        // correction is kept through its component along s_trial:
+        // s_new = (1 + a) s_trial, a = <ds, s_trial> / <s_trial, s_trial>
+        float dsn = 0.f, ss = 0.f;
+#pragma unroll
+        for (int k = 0; k < 6; k++) {
+          const float wk = k < 3 ? 1.f : 2.f;
+          dsn += wk * y[k] * str.a[k];
+          ss += wk * str.a[k] * str.a[k];
+        }
+        const float f1 = 1.f + dsn / ss;
         Sym<float> sn;
 #pragma unroll
-        for (int k = 0; k < 6; k++) sn.a[k] = str.a[k] + y[k];
-        const float J2n = (float)KMPM_SQRT_3_OVER_2 * sn.norm();
+        for (int k = 0; k < 6; k++) sn.a[k] = f1 * str.a[k];
+        const float J2n = J2tr * fabsf(f1);
         const float depn = y[6];
+        // residuals relative to the flow stress: the yield function at the new
+        // state and the flow rule (stress drop = 3 G dep)
         const float iys = 1.f / ys;
         const float r_yield = fabsf(J2n - ys) * iys;
         const float r_flow = fabsf(J2tr - J2n - 3.f * Gd * depn) * iys;
-        Sym<float> dd;
-        const float ratio = J2n / J2tr;
-#pragma unroll
-        for (int k = 0; k < 6; k++) dd.a[k] = sn.a[k] - ratio * str.a[k];
-        const float r_dir = (float)KMPM_SQRT_3_OVER_2 * dd.norm() * iys;
-        if (depn >= 0.f && r_yield <= l.tol && r_flow <= l.tol && r_dir <= l.tol) {
+        if (depn >= 0.f && f1 > 0.f && r_yield <= l.tol && r_flow <= l.tol) {
           use_net = true;
           sdev = sn;
           dep = depn;

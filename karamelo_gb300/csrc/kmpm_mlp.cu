@@ -205,9 +205,21 @@ void build_blob(const float *params, const float *norm, std::vector<unsigned cha
     const uint16_t b = bf16_bits(v);
     std::memcpy(&blob[off + canon_off(r, k, K)], &b, 2);
   };
+  auto bf = [](float v) {
+    const uint32_t u = (uint32_t)bf16_bits(v) << 16;
+    float f;
+    std::memcpy(&f, &u, 4);
+    return f;
+  };
   for (int r = 0; r < HID; r++) {
-    for (int k = 0; k < NIN; k++) put(W1_OFF, r, k, K1, params[O_W1 + r * NIN + k]);
-    put(W1_OFF, r, NIN, K1, params[O_B1 + r]);
+    // layer 1, hi/lo split (kmpm_mlp.cuh): [w_hi, b_hi | w_hi, 0 | w_lo, b_lo]
+    for (int k = 0; k <= NIN; k++) {
+      const float w = k < NIN ? params[O_W1 + r * NIN + k] : params[O_B1 + r];
+      const float whi = bf(w), wlo = w - whi;
+      put(W1_OFF, r, k, K1, whi);
+      if (k < NIN) put(W1_OFF, r, 16 + k, K1, whi);
+      put(W1_OFF, r, 32 + k, K1, wlo);
+    }
     for (int k = 0; k < HID; k++) {
       put(W2_OFF, r, k, HID, params[O_W2 + r * HID + k]);
       put(W3_OFF, r, k, HID, params[O_W3 + r * HID + k]);

@@ -25,22 +25,29 @@ namespace kmpm {
 namespace mlp {
 
 constexpr int NIN = 15, NOUT = 7, HID = 128;
-constexpr int K1 = 16;  // layer-1 K: 15 features + a constant 1 (bias column)
+// Layer 1 runs at ~16-bit input precision with BF16 operands: each normalised
+// input x and weight w is split into hi = bf16(x) and lo = bf16(x - hi), and
+// the product is accumulated as w_hi x_hi + w_hi x_lo + w_lo x_hi (the lo*lo
+// term is below FP32 rounding of the sum).  The K = 48 row of the A operand is
+//   [x_hi (15), 1 | x_lo (15), 0 | x_hi (15), 1]
+// against the weight row [w_hi, b_hi | w_hi, 0 | w_lo, b_lo].
+constexpr int K1 = 48;
 constexpr int N4 = 16;  // layer-4 N: 7 outputs padded to the minimum MMA N
 constexpr int NPARAMS = HID * NIN + HID + HID * HID + HID + HID * HID + HID + NOUT * HID + NOUT;  // 35975
 // normalisation block: in_mean[15] in_std[15] out_mean[7] out_scale[7] env_lo[15] env_hi[15]
 constexpr int NNORM = 4 * NIN + 2 * NOUT;  // 74
 
 // ---- device image of the network (global blob == shared-memory image)
-constexpr int W1_OFF = 0;                          // [128 x 16]  BF16
+constexpr int W1_OFF = 0;                          // [128 x 48]  BF16
 constexpr int W2_OFF = W1_OFF + HID * K1 * 2;      // [128 x 128] BF16
 constexpr int W3_OFF = W2_OFF + HID * HID * 2;     // [128 x 128] BF16
 constexpr int W4_OFF = W3_OFF + HID * HID * 2;     // [16 x 128]  BF16
 constexpr int PAR_OFF = W4_OFF + N4 * HID * 2;     // FP32 block below
 constexpr int P_B2 = 0, P_B3 = 128, P_B4 = 256, P_IN_MEAN = 272, P_IN_ISTD = 288, P_OUT_MEAN = 304,
               P_OUT_SCALE = 312, P_ENV_LO = 320, P_ENV_HI = 336, NPAR = 352;
-constexpr int BLOB_BYTES = PAR_OFF + NPAR * 4;     // 75136
+constexpr int BLOB_BYTES = PAR_OFF + NPAR * 4;     // 83328
 static_assert(BLOB_BYTES % 64 == 0, "blob copied in four 16-byte-multiple pieces");
+static_assert(K1 * 128 * 2 <= HID * HID * 2, "layer-1 operand fits the activation buffer");
 // ---- shared memory of a tile CTA
 constexpr int ACT_OFF = (BLOB_BYTES + 1023) & ~1023;  // per M-tile: [128 x 128] BF16 = 32 KB
 constexpr int ACT_BYTES = HID * HID * 2;
@@ -213,29 +220,35 @@ __device__ __forceinline__ void tile_end(TileCtx &t) {
   if (threadIdx.x < 32) tmem_dealloc(t.tmem, NTILE * 128);
 }
 
-// This thread's feature row (layer-1 A operand): normalised inputs in BF16,
-// column 15 = 1 (carries the layer-1 bias).  Returns whether every
-// normalised input lies inside the training envelope.
+// This thread's feature row (layer-1 A operand, hi/lo split as above).
+// Returns whether every normalised input lies inside the training envelope.
 __device__ __forceinline__ bool tile_put_features(TileCtx &t, const float (&x)[NIN], bool active) {
   const float *par = reinterpret_cast<const float *>(t.smem + PAR_OFF);
-  float xn[K1];
+  float hi[16], lo[16];
   bool inside = true;
 #pragma unroll
   for (int j = 0; j < NIN; j++) {
-    xn[j] = active ? (x[j] - par[P_IN_MEAN + j]) * par[P_IN_ISTD + j] : 0.f;
-    inside = inside && xn[j] >= par[P_ENV_LO + j] && xn[j] <= par[P_ENV_HI + j];
+    const float xn = active ? (x[j] - par[P_IN_MEAN + j]) * par[P_IN_ISTD + j] : 0.f;
+    inside = inside && xn >= par[P_ENV_LO + j] && xn <= par[P_ENV_HI + j];
+    hi[j] = __bfloat162float(__float2bfloat16_rn(xn));
+    lo[j] = xn - hi[j];
   }
-  xn[NIN] = 1.f;
+  hi[NIN] = 1.f;
+  lo[NIN] = 0.f;
   const int tile = threadIdx.x >> 7, row = threadIdx.x & 127;
   unsigned char *act = t.smem + ACT_OFF + tile * ACT_BYTES;
 #pragma unroll
-  for (int c = 0; c < 2; c++) {
-    uint4 v;
-    v.x = pack_bf16(xn[8 * c + 0], xn[8 * c + 1]);
-    v.y = pack_bf16(xn[8 * c + 2], xn[8 * c + 3]);
-    v.z = pack_bf16(xn[8 * c + 4], xn[8 * c + 5]);
-    v.w = pack_bf16(xn[8 * c + 6], xn[8 * c + 7]);
-    *reinterpret_cast<uint4 *>(act + canon_off(row, 8 * c, K1)) = v;
+  for (int part = 0; part < 3; part++) {
+    const float *v16 = part == 1 ? lo : hi;
+#pragma unroll
+    for (int c = 0; c < 2; c++) {
+      uint4 v;
+      v.x = pack_bf16(v16[8 * c + 0], v16[8 * c + 1]);
+      v.y = pack_bf16(v16[8 * c + 2], v16[8 * c + 3]);
+      v.z = pack_bf16(v16[8 * c + 4], v16[8 * c + 5]);
+      v.w = pack_bf16(v16[8 * c + 6], v16[8 * c + 7]);
+      *reinterpret_cast<uint4 *>(act + canon_off(row, 16 * part + 8 * c, K1)) = v;
+    }
   }
   fence_proxy_async();
   return inside;

@@ -52,17 +52,24 @@ def _bf16(t):
 
 
 def _tc_reference(params, norm, X):
-    """PyTorch FP32 reference of the tensor-core arithmetic: BF16 operands
+    """PyTorch reference of the tensor-core arithmetic: BF16 operands
     (weights, normalised inputs, hidden activations), FP32 accumulation,
-    FP32 bias + ReLU epilogue, the layer-1 bias carried as a BF16 column."""
+    FP32 bias + ReLU epilogue; layer 1 as hi/lo BF16 pairs with the bias
+    carried as a column."""
     p = [(torch.tensor(W, dtype=torch.float32), torch.tensor(b, dtype=torch.float32)) for W, b in MO.unpack(params)]
     nm = torch.tensor(norm, dtype=torch.float32)
     in_mean, in_std, out_mean, out_scale = nm[:15], nm[15:30], nm[30:37], nm[37:44]
     istd = torch.where(in_std > 0, 1.0 / torch.where(in_std > 0, in_std, torch.ones_like(in_std)), 0 * in_std)
     xn = (torch.tensor(X) - in_mean) * istd
-    a = _bf16(torch.cat([xn, torch.ones(xn.shape[0], 1)], 1))
-    W1 = _bf16(torch.cat([p[0][0], p[0][1][:, None]], 1))
-    h = _bf16(torch.relu(a.double() @ W1.double().T).float())
+    # layer 1 with the hi/lo split of inputs and weights (bias as a column)
+    x = torch.cat([xn, torch.ones(xn.shape[0], 1)], 1)
+    xh = _bf16(x)
+    xl = _bf16(x - xh)
+    W = torch.cat([p[0][0], p[0][1][:, None]], 1)
+    Wh = _bf16(W)
+    Wl = _bf16(W - Wh)
+    z = xh.double() @ Wh.double().T + xl.double() @ Wh.double().T + xh.double() @ Wl.double().T
+    h = _bf16(torch.relu(z).float())
     for li in (1, 2):
         h = _bf16(torch.relu((h.double() @ _bf16(p[li][0]).double().T).float() + p[li][1]))
     y = (h.double() @ _bf16(p[3][0]).double().T).float() + p[3][1]
@@ -163,7 +170,7 @@ def trained(gpu_lib):
     from karamelo_gb300 import surrogate as S
     sims, _ = S.taylor_training_runs(cellsize=0.8, instances=6, spread=0.2, seed=0)
     X, Y, raw, _ = S.collect_pairs(sims, steps=2500, capacity=2_000_000, fraction=0.5, seed=1)
-    mlp, stats = S.train_surrogate(X, Y, steps=6000, batch=4096, lr=2e-3, seed=0)
+    mlp, stats = S.train_surrogate(X, Y, steps=20000, batch=4096, lr=2e-3, seed=0)
     return mlp, stats, X, Y
 
 
