@@ -108,6 +108,9 @@ struct kmpm_ctx {
   uint32_t log_thresh = 0;
   unsigned long long log_seed = 0;
   LearnKernels LK{};
+  // device buffer of kmpm_download_particles (one field of one solid, FP64)
+  double *d_dump = nullptr;
+  size_t dump_cap = 0;
   bool indep() const { return prm.independent != 0; }
   bool TL() const { return prm.method == KMPM_TLMPM; }
   bool musl() const { return prm.scheme == KMPM_MUSL; }
@@ -477,30 +480,56 @@ int build(kmpm_ctx *c) {
   // ---- particle upload (caller order within each solid), one field row at a time
   c->T_ref = c->prm.thermal ? c->hsolids[0].T0 : 0.0;
   {
+    // only the fields that are not zero at the start are copied: the buffer
+    // was zeroed on the context stream (H = F - I, sigma, eps_p, ... are 0)
+    std::vector<int> up;
+    for (int d = 0; d < 3; d++) up.push_back(PF_X0 + d);
+    for (int d = 0; d < 3; d++) up.push_back(PF_X + d);
+    if (!c->TL())
+      for (int d = 0; d < 3; d++) up.push_back(PF_XN + d);
+    for (int d = 0; d < 3; d++) up.push_back(PF_V + d);
+    up.insert(up.end(), {PF_MASS, PF_VOL0, PF_ORIG, PF_SID});
+    if (c->prm.thermal) up.push_back(PF_T);
     std::vector<float> row(c->ps);
-    for (int f : active_fields(c)) {
+    for (int f : up) {
       std::fill(row.begin(), row.end(), 0.f);
+      bool nonzero = false;
       for (size_t s = 0; s < c->hsolids.size(); s++) {
         const auto &S = c->hsolids[s];
         const RangeDev &r = c->ranges[c->TL() ? c->solid_range[s] : 0];
-        const int off = c->TL() ? r.start : r.start + c->solid_base[s];
-        for (int i = 0; i < S.n; i++) {
-          float &o = row[off + i];
-          if (f >= PF_X0 && f < PF_X0 + 3) o = (float)S.x0[3 * i + f - PF_X0];
+        float *o = row.data() + (c->TL() ? r.start : r.start + c->solid_base[s]);
+        const int n = S.n;
+        if (f >= PF_X0 && f < PF_X0 + 3) {
+          const int d = f - PF_X0;
+          for (int i = 0; i < n; i++) o[i] = (float)S.x0[3 * i + d];
+        } else if ((f >= PF_X && f < PF_X + 3) || (f >= PF_XN && f < PF_XN + 3)) {
           // positions are stored as the displacement from x0
-          else if (f >= PF_X && f < PF_X + 3) o = (float)(S.x[3 * i + f - PF_X] - S.x0[3 * i + f - PF_X]);
-          else if (f >= PF_XN && f < PF_XN + 3) o = (float)(S.x[3 * i + f - PF_XN] - S.x0[3 * i + f - PF_XN]);
-          else if (f >= PF_V && f < PF_V + 3) o = (float)S.v[3 * i + f - PF_V];
-          else if (f == PF_MASS) o = (float)S.mass[i];
-          else if (f == PF_VOL0) o = (float)S.vol0[i];
+          const int d = (f >= PF_XN) ? f - PF_XN : f - PF_X;
+          for (int i = 0; i < n; i++) o[i] = (float)(S.x[3 * i + d] - S.x0[3 * i + d]);
+        } else if (f >= PF_V && f < PF_V + 3) {
+          const int d = f - PF_V;
+          for (int i = 0; i < n; i++) o[i] = (float)S.v[3 * i + d];
+        } else if (f == PF_MASS) {
+          for (int i = 0; i < n; i++) o[i] = (float)S.mass[i];
+        } else if (f == PF_VOL0) {
+          for (int i = 0; i < n; i++) o[i] = (float)S.vol0[i];
+        } else if (f == PF_T) {
           // Solid::populate sets T = T0 only for thermo-mechanical runs; otherwise
           // the vector is value-initialised (src/solid.cpp:2297-2306, 306-311)
-          else if (f == PF_T) o = c->prm.thermal ? (float)(S.T0 - c->T_ref) : 0.f;
-          else if (f == PF_ORIG) { int v = c->solid_base[s] + i; std::memcpy(&o, &v, 4); }
-          else if (f == PF_SID) { int v = (int)s; std::memcpy(&o, &v, 4); }
+          const float t = (float)(S.T0 - c->T_ref);
+          for (int i = 0; i < n; i++) o[i] = t;
+        } else if (f == PF_ORIG) {
+          for (int i = 0; i < n; i++) { const int v = c->solid_base[s] + i; std::memcpy(o + i, &v, 4); }
+        } else if (f == PF_SID) {
+          const int v = (int)s;
+          for (int i = 0; i < n; i++) std::memcpy(o + i, &v, 4);
         }
       }
-      CK(cudaMemcpyAsync(c->buf[0] + (size_t)f * c->ps, row.data(), sizeof(float) * c->ps, cudaMemcpyHostToDevice, c->st));
+      if (f == PF_ORIG || f == PF_SID) nonzero = true;  // integer bit patterns: always copied
+      for (size_t i = 0; i < row.size() && !nonzero; i++) nonzero = row[i] != 0.f;
+      if (!nonzero) continue;
+      CK(cudaMemcpyAsync(c->buf[0] + (size_t)f * c->ps, row.data(), sizeof(float) * c->ps, cudaMemcpyHostToDevice,
+                         c->st));
       CK(cudaStreamSynchronize(c->st));
     }
   }
@@ -521,46 +550,56 @@ int build(kmpm_ctx *c) {
   // ---- TLMPM: bin once by x0 (static connectivity, src/tlmpm.cpp:339) and compute the nodal mass
   if (c->TL()) {
     PartArgs pa = part_args(c);
-    launch_cell_keys(pa, c->nblk_p, c->d_keys, 1, c->st);
-    std::vector<int> keys(c->ps);
-    CK(cudaMemcpyAsync(keys.data(), c->d_keys, sizeof(int) * c->ps, cudaMemcpyDeviceToHost, c->st));
-    CK(cudaStreamSynchronize(c->st));
-    std::vector<int> perm(c->ps, 0), sorted(c->ps, 0);
+    // grids in range order keep the keys of range r below those of range r+1
+    bool ordered = true;
+    for (size_t r = 1; r < c->ranges.size(); r++) ordered = ordered && c->ranges[r].grid > c->ranges[r - 1].grid;
     std::vector<int2> tiles;
-    for (auto &r : c->ranges) {
-      std::vector<int> idx(r.count);
-      std::iota(idx.begin(), idx.end(), 0);
-      const int *kb = keys.data() + r.start;
-      std::stable_sort(idx.begin(), idx.end(), [&](int a, int b) { return kb[a] < kb[b]; });
-      for (int i = 0; i < r.count; i++) {
-        perm[r.start + i] = idx[i];
-        sorted[r.start + i] = kb[idx[i]];
-      }
-      int last = -1;
-      for (int i = 0; i < r.count; i++) {
-        int t = sorted[r.start + i] / c->NCELL;
-        if (t != last) {
-          const GridDev &g = c->grids[r.grid];
-          tiles.push_back(make_int2(r.grid, t - g.tile_off));
-          last = t;
-        }
+    if (ordered) {
+      // one stable LSD radix sort of every slot on the device: the same
+      // permutation as a stable sort of each range by cell key (padding
+      // slots carry their grid's last key and stay at the end of their range)
+      launch_cell_keys(pa, c->nblk_p, c->d_keys, 1, c->st, 1);
+      launch_iota(c->d_vals, (int)c->ps, c->st);
+      radix_sort(c->d_keys, c->d_vals, (int)c->ps, c->key_bits, c->rtmp, c->st);
+      std::vector<int> fl;
+      for (int f : active_fields(c)) fl.push_back((f << 8) | f);
+      launch_permute(c->d_pp, c->d_pp + 1, c->ps, c->d_vals, 0, (int)c->ps, fl.data(), (int)fl.size(), c->st);
+    } else {
+      // grids out of range order: sort range by range
+      launch_cell_keys(pa, c->nblk_p, c->d_keys, 1, c->st, 0);
+      std::vector<int> fl;
+      for (int f : active_fields(c)) fl.push_back((f << 8) | f);
+      for (auto &r : c->ranges) {
+        launch_iota(c->d_vals + r.start, r.count, c->st);
+        radix_sort(c->d_keys + r.start, c->d_vals + r.start, r.count, c->key_bits, c->rtmp, c->st);
+        launch_permute(c->d_pp, c->d_pp + 1, c->ps, c->d_vals + r.start, r.start, r.count, fl.data(), (int)fl.size(),
+                       c->st);
       }
     }
-    CK(cudaMemcpyAsync(c->d_vals, perm.data(), sizeof(int) * c->ps, cudaMemcpyHostToDevice, c->st));
-    CK(cudaMemcpyAsync(c->d_keys, sorted.data(), sizeof(int) * c->ps, cudaMemcpyHostToDevice, c->st));
-    std::vector<int> fl;
-    for (int f : active_fields(c)) fl.push_back((f << 8) | f);
-    for (auto &r : c->ranges)
-      launch_permute(c->d_pp, c->d_pp + 1, c->ps, c->d_vals + r.start, r.start, r.count, fl.data(), (int)fl.size(), c->st);
     launch_swap_ptrs(c->d_pp, c->st);
     std::swap(c->buf[0], c->buf[1]);
     for (auto &r : c->ranges)
       launch_cell_ranges(c->d_keys + r.start, r.start, r.count, c->NCELL, c->d_cs, c->d_ce, c->d_ts, c->d_te, c->st);
+    CK(cudaGetLastError());
+    // the non-empty tiles, in grid then tile order
+    {
+      std::vector<int> ts(c->ntiles_total), te(c->ntiles_total);
+      CK(cudaMemcpyAsync(ts.data(), c->d_ts, sizeof(int) * ts.size(), cudaMemcpyDeviceToHost, c->st));
+      CK(cudaMemcpyAsync(te.data(), c->d_te, sizeof(int) * te.size(), cudaMemcpyDeviceToHost, c->st));
+      CK(cudaStreamSynchronize(c->st));
+      for (auto &r : c->ranges) {
+        const GridDev &g = c->grids[r.grid];
+        const int nt = g.ntile[0] * g.ntile[1] * g.ntile[2];
+        for (int t = 0; t < nt; t++)
+          if (te[g.tile_off + t] > ts[g.tile_off + t]) tiles.push_back(make_int2(r.grid, t));
+      }
+    }
     c->ntiles_launch = (int)tiles.size();
     DALLOC(c->d_tiles, tiles.size());
     CK(cudaMemcpyAsync(c->d_tiles, tiles.data(), sizeof(int2) * tiles.size(), cudaMemcpyHostToDevice, c->st));
     if (const char *ev = std::getenv("KMPM_CHECK_BINS"); ev && ev[0] == '1') {
-      // self-check of the binning (setup only): device ranges against the host's sorted keys
+      // self-check of the binning (setup only): sorted keys and the device cell
+      // ranges against ranges recomputed on the host
       const size_t ncell = (size_t)c->ntiles_total * c->NCELL;
       std::vector<int> cs(ncell), ce(ncell), ts(c->ntiles_total), te(c->ntiles_total), dk(c->ps);
       CK(cudaMemcpyAsync(cs.data(), c->d_cs, sizeof(int) * ncell, cudaMemcpyDeviceToHost, c->st));
@@ -570,12 +609,12 @@ int build(kmpm_ctx *c) {
       CK(cudaMemcpyAsync(dk.data(), c->d_keys, sizeof(int) * c->ps, cudaMemcpyDeviceToHost, c->st));
       CK(cudaStreamSynchronize(c->st));
       long long key_mismatch = 0, bad_cells = 0, total = 0, maxc = 0, bad_tiles = 0;
-      for (size_t i = 0; i < (size_t)c->ps; i++) key_mismatch += dk[i] != sorted[i];
       std::vector<int> hs(ncell, 0), he(ncell, 0);
       for (auto &r : c->ranges)
         for (int i = 0; i < r.count; i++) {
-          const int k = sorted[r.start + i];
-          if (i == 0 || sorted[r.start + i - 1] != k) hs[k] = r.start + i;
+          const int k = dk[r.start + i];
+          if (i > 0 && dk[r.start + i - 1] > k) key_mismatch++;  // unsorted within a range
+          if (i == 0 || dk[r.start + i - 1] != k) hs[k] = r.start + i;
           he[k] = r.start + i + 1;
         }
       size_t first_bad = ncell;
@@ -591,7 +630,7 @@ int build(kmpm_ctx *c) {
       }
       std::fprintf(stderr,
                    "[kmpm bins] ps %zu cells %zu tiles %d launched %d particles-in-cells %lld max/cell %lld "
-                   "key-mismatch %lld bad-cells %lld bad-tiles %lld",
+                   "unsorted %lld bad-cells %lld bad-tiles %lld",
                    c->ps, ncell, c->ntiles_total, c->ntiles_launch, total, maxc, key_mismatch, bad_cells, bad_tiles);
       if (first_bad < ncell)
         std::fprintf(stderr, " first bad cell %zu: dev [%d,%d) host [%d,%d)", first_bad, cs[first_bad], ce[first_bad],
@@ -796,27 +835,6 @@ int read_scalars(kmpm_ctx *c, StepScalars &s) {
   return KMPM_OK;
 }
 
-// Newton polar rotation in double (host), for the rotated-stress download
-void polar_host(const double *F, double *R) {
-  double X[9];
-  for (int k = 0; k < 9; k++) X[k] = F[k];
-  for (int it = 0; it < 40; it++) {
-    double C[9];
-    C[0] = X[4] * X[8] - X[5] * X[7]; C[1] = X[5] * X[6] - X[3] * X[8]; C[2] = X[3] * X[7] - X[4] * X[6];
-    C[3] = X[2] * X[7] - X[1] * X[8]; C[4] = X[0] * X[8] - X[2] * X[6]; C[5] = X[1] * X[6] - X[0] * X[7];
-    C[6] = X[1] * X[5] - X[2] * X[4]; C[7] = X[2] * X[3] - X[0] * X[5]; C[8] = X[0] * X[4] - X[1] * X[3];
-    double d = X[0] * C[0] + X[1] * C[1] + X[2] * C[2];
-    double g = std::cbrt(1.0 / std::fabs(d)), gi = 1.0 / (g * d), diff = 0;
-    for (int k = 0; k < 9; k++) {
-      double xn = 0.5 * (g * X[k] + gi * C[k]);
-      diff += (xn - X[k]) * (xn - X[k]);
-      X[k] = xn;
-    }
-    if (diff < 1e-30) break;
-  }
-  for (int k = 0; k < 9; k++) R[k] = X[k];
-}
-
 }  // namespace
 
 // ================================================================ C ABI
@@ -854,6 +872,7 @@ int kmpm_destroy(kmpm_ctx *c) {
   dfree(c->nodeA); dfree(c->nodeB); dfree(c->nodeX); dfree(c->nodeT); dfree(c->d_tiles);
   dfree(c->d_cs); dfree(c->d_ce); dfree(c->d_ts); dfree(c->d_te); dfree(c->partial);
   dfree(c->d_fixes); dfree(c->d_fix_start); dfree(c->d_fix_count); dfree(c->d_scalars); dfree(c->d_dtcfl);
+  dfree(c->d_dump);
   dfree(c->d_blob); dfree(c->d_lstats); dfree(c->d_log_count); dfree(c->d_log);
   dfree(c->d_err); dfree(c->d_blk_c); dfree(c->d_blk_h); dfree(c->d_eblk); dfree(c->d_eout);
   dfree(c->d_keys); dfree(c->d_vals); dfree(c->rtmp.k1); dfree(c->rtmp.v1); dfree(c->rtmp.hist); dfree(c->rtmp.tot);
@@ -1047,35 +1066,6 @@ static int slot_map(kmpm_ctx *c, const RangeDev &rg, std::vector<int> &orig, std
   return KMPM_OK;
 }
 
-static std::vector<int> fields_for(kmpm_ctx *c, int field) {
-  switch (field) {
-    case KMPM_P_X: return c->TL() ? std::vector<int>{PF_X0, PF_X0 + 1, PF_X0 + 2, PF_X, PF_X + 1, PF_X + 2}
-                                  : std::vector<int>{PF_X0, PF_X0 + 1, PF_X0 + 2, PF_XN, PF_XN + 1, PF_XN + 2};
-    case KMPM_P_X0: return {PF_X0, PF_X0 + 1, PF_X0 + 2};
-    case KMPM_P_V: return {PF_V, PF_V + 1, PF_V + 2};
-    case KMPM_P_SIGMA: return {PF_SIG, PF_SIG + 1, PF_SIG + 2, PF_SIG + 3, PF_SIG + 4, PF_SIG + 5};
-    case KMPM_P_SIGMA_ROT: {
-      std::vector<int> f = {PF_SIG, PF_SIG + 1, PF_SIG + 2, PF_SIG + 3, PF_SIG + 4, PF_SIG + 5};
-      if (c->TL()) for (int k = 0; k < 9; k++) f.push_back(PF_H + k);
-      return f;
-    }
-    case KMPM_P_F: case KMPM_P_J: case KMPM_P_VOL: {
-      std::vector<int> f;
-      for (int k = 0; k < 9; k++) f.push_back(PF_H + k);
-      f.push_back(PF_VOL0);
-      return f;
-    }
-    case KMPM_P_EPS_P: return {PF_EPSP};
-    case KMPM_P_EPSDOT_P: return {PF_EPSDOT};
-    case KMPM_P_DAMAGE: return {PF_DMG};
-    case KMPM_P_DAMAGE_INIT: return {PF_DMGI};
-    case KMPM_P_T: return {PF_T};
-    case KMPM_P_STRAIN_EL: return {PF_STRAIN, PF_STRAIN + 1, PF_STRAIN + 2, PF_STRAIN + 3, PF_STRAIN + 4, PF_STRAIN + 5};
-    case KMPM_P_MASS: return {PF_MASS};
-    default: return {};
-  }
-}
-
 int kmpm_download_particles(kmpm_ctx *c, int solid, int field, double *out) {
   if (!c || !out || solid < 0 || solid >= (int)c->hsolids.size()) return KMPM_ERR_ARG;
   const auto &S = c->hsolids[solid];
@@ -1090,78 +1080,24 @@ int kmpm_download_particles(kmpm_ctx *c, int solid, int field, double *out) {
   }
   if (field == KMPM_P_STRAIN_EL && !c->prm.track_strain)
     return fail(c, KMPM_ERR_STATE, "strain_el is tracked only with track_strain");
-  const std::vector<int> fl = fields_for(c, field);
-  if (fl.empty()) return fail(c, KMPM_ERR_ARG, "unknown particle field");
-  const RangeDev &rg = c->ranges[c->TL() ? c->solid_range[solid] : 0];
-  std::vector<int> orig, sid;
-  int r = slot_map(c, rg, orig, sid);
-  if (r != KMPM_OK) return r;
-  std::vector<std::vector<float>> H;
-  r = fetch_rows(c, fl, rg.start, rg.count, H);
-  if (r != KMPM_OK) return r;
-  const int base = c->solid_base[solid];
-  for (int q = 0; q < rg.count; q++) {
-    if (sid[q] != solid) continue;
-    const int i = orig[q] - base;
-    auto f = [&](int fld) { return (double)H[fld][q]; };
-    auto sym = [&](int b, double *m) {
-      const int map[9] = {0, 3, 4, 3, 1, 5, 4, 5, 2};
-      for (int k = 0; k < 9; k++) m[k] = f(b + map[k]);
-    };
-    switch (field) {
-      case KMPM_P_X:
-        for (int d = 0; d < 3; d++) out[3 * i + d] = f(PF_X0 + d) + (c->TL() ? f(PF_X + d) : f(PF_XN + d));
-        break;
-      case KMPM_P_X0:
-        for (int d = 0; d < 3; d++) out[3 * i + d] = f(PF_X0 + d);
-        break;
-      case KMPM_P_V:
-        for (int d = 0; d < 3; d++) out[3 * i + d] = f(PF_V + d);
-        break;
-      case KMPM_P_SIGMA:
-        sym(PF_SIG, out + 9 * i);
-        break;
-      case KMPM_P_SIGMA_ROT: {
-        double sg[9], F[9], R[9], RS[9];
-        sym(PF_SIG, sg);
-        // ULMPM stores sigma in the current frame; TLMPM rotates it, except for
-        // neo-Hookean solids, whose R stays the identity (src/solid.cpp:1220)
-        if (!c->TL() || c->mats[S.mat].type == KMPM_MAT_NEO_HOOKEAN) {
-          for (int k = 0; k < 9; k++) out[9 * i + k] = sg[k];
-          break;
-        }
-        for (int k = 0; k < 9; k++) F[k] = f(PF_H + k) + (k % 4 == 0 ? 1.0 : 0.0);
-        polar_host(F, R);
-        for (int a = 0; a < 3; a++)
-          for (int b = 0; b < 3; b++) RS[3 * a + b] = R[3 * a] * sg[b] + R[3 * a + 1] * sg[3 + b] + R[3 * a + 2] * sg[6 + b];
-        for (int a = 0; a < 3; a++)
-          for (int b = 0; b < 3; b++)
-            out[9 * i + 3 * a + b] = RS[3 * a] * R[3 * b] + RS[3 * a + 1] * R[3 * b + 1] + RS[3 * a + 2] * R[3 * b + 2];
-        break;
-      }
-      case KMPM_P_F:
-        for (int k = 0; k < 9; k++) out[9 * i + k] = f(PF_H + k) + (k % 4 == 0 ? 1.0 : 0.0);
-        break;
-      case KMPM_P_EPS_P: out[i] = f(PF_EPSP); break;
-      case KMPM_P_EPSDOT_P: out[i] = f(PF_EPSDOT); break;
-      case KMPM_P_DAMAGE: out[i] = f(PF_DMG); break;
-      case KMPM_P_DAMAGE_INIT: out[i] = f(PF_DMGI); break;
-      case KMPM_P_T: out[i] = c->T_ref + f(PF_T); break;
-      case KMPM_P_J:
-      case KMPM_P_VOL: {
-        double Hd[9];
-        for (int k = 0; k < 9; k++) Hd[k] = f(PF_H + k);
-        double jm1 = (Hd[0] + Hd[4] + Hd[8]) +
-                     (Hd[0] * Hd[4] - Hd[1] * Hd[3] + Hd[0] * Hd[8] - Hd[2] * Hd[6] + Hd[4] * Hd[8] - Hd[5] * Hd[7]) +
-                     (Hd[0] * (Hd[4] * Hd[8] - Hd[5] * Hd[7]) - Hd[1] * (Hd[3] * Hd[8] - Hd[5] * Hd[6]) +
-                      Hd[2] * (Hd[3] * Hd[7] - Hd[4] * Hd[6]));
-        out[i] = field == KMPM_P_J ? 1.0 + jm1 : (1.0 + jm1) * f(PF_VOL0);
-        break;
-      }
-      case KMPM_P_STRAIN_EL: sym(PF_STRAIN, out + 9 * i); break;
-      case KMPM_P_MASS: out[i] = f(PF_MASS); break;
-    }
+  const int w = dump_width(field);
+  if (w == 0) return fail(c, KMPM_ERR_ARG, "unknown particle field");
+  // gathered into caller order and FP64 on the device (kmpm_dump.cu), then one copy
+  const size_t need = (size_t)S.n * w;
+  if (need > c->dump_cap) {
+    dfree(c->d_dump);
+    DALLOC(c->d_dump, need);
+    c->dump_cap = need;
   }
+  const int ri = c->TL() ? c->solid_range[solid] : 0;
+  // TLMPM keeps sigma unrotated, except for neo-Hookean solids, whose R stays
+  // the identity (src/solid.cpp:1220); ULMPM stores it in the current frame
+  const int rotate = c->TL() && c->mats[S.mat].type != KMPM_MAT_NEO_HOOKEAN;
+  launch_dump(part_args(c), ri, c->ranges[ri].count, solid, c->solid_base[solid], field, c->TL() ? 1 : 0, rotate,
+              c->T_ref, c->d_dump, c->st);
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(out, c->d_dump, sizeof(double) * need, cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
   return KMPM_OK;
 }
 

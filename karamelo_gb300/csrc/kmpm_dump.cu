@@ -1,0 +1,124 @@
+// Particle downloads for dumps, on the device: one solid's field gathered into
+// the caller's particle order and converted to FP64 (the download before
+// Output::write, src/output.cpp:128-200, and the fields DumpParticle writes,
+// src/dump_particle.cpp:52-161), so a dump is one kernel and one copy.
+#include "../../include/kmpm.h"
+#include "kmpm_kernels.cuh"
+
+namespace kmpm {
+
+// R of F = R U in FP64 (the scaled Newton iteration of the stress kernel's
+// polar_rotation, here to FP64 convergence; N. J. Higham, SIAM J. Sci. Stat.
+// Comput. 7, 1986)
+__device__ void polar_rotation_fp64(const double *F, double *R) {
+  double X[9];
+  for (int k = 0; k < 9; k++) X[k] = F[k];
+  for (int it = 0; it < 40; it++) {
+    double C[9];
+    C[0] = X[4] * X[8] - X[5] * X[7]; C[1] = X[5] * X[6] - X[3] * X[8]; C[2] = X[3] * X[7] - X[4] * X[6];
+    C[3] = X[2] * X[7] - X[1] * X[8]; C[4] = X[0] * X[8] - X[2] * X[6]; C[5] = X[1] * X[6] - X[0] * X[7];
+    C[6] = X[1] * X[5] - X[2] * X[4]; C[7] = X[2] * X[3] - X[0] * X[5]; C[8] = X[0] * X[4] - X[1] * X[3];
+    const double d = X[0] * C[0] + X[1] * C[1] + X[2] * C[2];
+    const double g = cbrt(1.0 / fabs(d)), gi = 1.0 / (g * d);
+    double diff = 0;
+    for (int k = 0; k < 9; k++) {
+      const double xn = 0.5 * (g * X[k] + gi * C[k]);
+      diff += (xn - X[k]) * (xn - X[k]);
+      X[k] = xn;
+    }
+    if (diff < 1e-30) break;
+  }
+  for (int k = 0; k < 9; k++) R[k] = X[k];
+}
+
+struct DumpArgs {
+  int ri, solid, base, field, TL, rotate;
+  double T_ref;
+  double *out;
+};
+
+__global__ void k_dump(PartArgs a, DumpArgs d) {
+  const RangeDev rd = a.ranges[d.ri];
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= rd.count) return;
+  const int p = rd.start + q;
+  const float *P = *a.Pp;
+  const size_t ps = a.ps;
+  if (__float_as_int(P[PF_SID * ps + p]) != d.solid) return;
+  const size_t i = (size_t)(__float_as_int(P[PF_ORIG * ps + p]) - d.base);
+  auto f = [&](int fld) { return (double)P[fld * ps + p]; };
+  double *o = d.out;
+  const int sm[9] = {0, 3, 4, 3, 1, 5, 4, 5, 2};  // symmetric 6 -> 3x3 row-major
+  switch (d.field) {
+    case KMPM_P_X:
+      for (int k = 0; k < 3; k++) o[3 * i + k] = f(PF_X0 + k) + (d.TL ? f(PF_X + k) : f(PF_XN + k));
+      break;
+    case KMPM_P_X0:
+      for (int k = 0; k < 3; k++) o[3 * i + k] = f(PF_X0 + k);
+      break;
+    case KMPM_P_V:
+      for (int k = 0; k < 3; k++) o[3 * i + k] = f(PF_V + k);
+      break;
+    case KMPM_P_SIGMA:
+      for (int k = 0; k < 9; k++) o[9 * i + k] = f(PF_SIG + sm[k]);
+      break;
+    case KMPM_P_STRAIN_EL:
+      for (int k = 0; k < 9; k++) o[9 * i + k] = f(PF_STRAIN + sm[k]);
+      break;
+    case KMPM_P_SIGMA_ROT: {
+      double sg[9];
+      for (int k = 0; k < 9; k++) sg[k] = f(PF_SIG + sm[k]);
+      if (!d.rotate) {
+        for (int k = 0; k < 9; k++) o[9 * i + k] = sg[k];
+        break;
+      }
+      double F[9], R[9], RS[9];
+      for (int k = 0; k < 9; k++) F[k] = f(PF_H + k) + (k % 4 == 0 ? 1.0 : 0.0);
+      polar_rotation_fp64(F, R);
+      for (int r = 0; r < 3; r++)
+        for (int c = 0; c < 3; c++) RS[3 * r + c] = R[3 * r] * sg[c] + R[3 * r + 1] * sg[3 + c] + R[3 * r + 2] * sg[6 + c];
+      for (int r = 0; r < 3; r++)
+        for (int c = 0; c < 3; c++)
+          o[9 * i + 3 * r + c] = RS[3 * r] * R[3 * c] + RS[3 * r + 1] * R[3 * c + 1] + RS[3 * r + 2] * R[3 * c + 2];
+      break;
+    }
+    case KMPM_P_F:
+      for (int k = 0; k < 9; k++) o[9 * i + k] = f(PF_H + k) + (k % 4 == 0 ? 1.0 : 0.0);
+      break;
+    case KMPM_P_J:
+    case KMPM_P_VOL: {
+      double H[9];
+      for (int k = 0; k < 9; k++) H[k] = f(PF_H + k);
+      const double jm1 = (H[0] + H[4] + H[8]) +
+                         (H[0] * H[4] - H[1] * H[3] + H[0] * H[8] - H[2] * H[6] + H[4] * H[8] - H[5] * H[7]) +
+                         (H[0] * (H[4] * H[8] - H[5] * H[7]) - H[1] * (H[3] * H[8] - H[5] * H[6]) +
+                          H[2] * (H[3] * H[7] - H[4] * H[6]));
+      o[i] = d.field == KMPM_P_J ? 1.0 + jm1 : (1.0 + jm1) * f(PF_VOL0);
+      break;
+    }
+    case KMPM_P_EPS_P: o[i] = f(PF_EPSP); break;
+    case KMPM_P_EPSDOT_P: o[i] = f(PF_EPSDOT); break;
+    case KMPM_P_DAMAGE: o[i] = f(PF_DMG); break;
+    case KMPM_P_DAMAGE_INIT: o[i] = f(PF_DMGI); break;
+    case KMPM_P_T: o[i] = d.T_ref + f(PF_T); break;
+    case KMPM_P_MASS: o[i] = f(PF_MASS); break;
+  }
+}
+
+int dump_width(int field) {
+  switch (field) {
+    case KMPM_P_X: case KMPM_P_X0: case KMPM_P_V: return 3;
+    case KMPM_P_SIGMA: case KMPM_P_SIGMA_ROT: case KMPM_P_F: case KMPM_P_STRAIN_EL: return 9;
+    case KMPM_P_EPS_P: case KMPM_P_EPSDOT_P: case KMPM_P_DAMAGE: case KMPM_P_DAMAGE_INIT: case KMPM_P_T:
+    case KMPM_P_J: case KMPM_P_VOL: case KMPM_P_MASS: return 1;
+    default: return 0;
+  }
+}
+
+void launch_dump(const PartArgs &a, int ri, int count, int solid, int base, int field, int TL, int rotate,
+                 double T_ref, double *out, cudaStream_t st) {
+  DumpArgs d{ri, solid, base, field, TL, rotate, T_ref, out};
+  if (count > 0) k_dump<<<(count + 255) / 256, 256, 0, st>>>(a, d);
+}
+
+}  // namespace kmpm

@@ -91,10 +91,15 @@ struct StepKernels {
 };
 
 void get_step_kernels(int dim, int basis, StepKernels &k);
+// particle downloads (kmpm_dump.cu): values per particle of a KMPM_P_* field
+// (0 if unknown) and the gather of one solid's field into caller order, FP64
+int dump_width(int field);
+void launch_dump(const PartArgs &a, int ri, int count, int solid, int base, int field, int TL, int rotate,
+                 double T_ref, double *out, cudaStream_t st);
 int p2g_smem_bytes(int dim, int basis, int mode, bool thermal);
 
 // kmpm_misc.cu
-void launch_cell_keys(const PartArgs &a, int nblk, int *keys, int use_x0, cudaStream_t st);
+void launch_cell_keys(const PartArgs &a, int nblk, int *keys, int use_x0, cudaStream_t st, int pad_last = 0);
 void launch_cell_ranges(const int *sorted_keys, int start, int n, int ncell_per_tile, int *cell_start, int *cell_end,
                         int *tile_start, int *tile_end, cudaStream_t st);
 void launch_dt(const DtArgs &a, cudaStream_t st);

@@ -13,15 +13,21 @@ namespace kmpm {
 // ------------------------------------------------------------------ keys
 // key = global tile * cells_per_tile + cell within tile, from the FP32
 // position the kernels use (TL: x0, UL: x0 + the moved displacement PF_XN)
-__global__ void k_cell_keys(PartArgs a, int *keys, int use_x0) {
+__global__ void k_cell_keys(PartArgs a, int *keys, int use_x0, int pad_last) {
   if (a.scalars != nullptr && run_finished(a.scalars)) return;
   const int ri = a.blk_range[blockIdx.x];
   const RangeDev rd = a.ranges[ri];
   const int p = rd.start + (blockIdx.x - rd.blk0) * 256 + threadIdx.x;
-  if (p >= rd.start + rd.count) return;
-  const float *P = *a.Pp;
   const GridDev g = a.grids[rd.grid];
   const int *T = a.tile_t;
+  if (p >= rd.start + rd.count) {
+    // padding slot: the last key of its grid, so that a stable sort of all
+    // slots keeps every range's particles first and its padding last
+    if (pad_last)
+      keys[p] = (g.tile_off + g.ntile[0] * g.ntile[1] * g.ntile[2]) * (T[0] * T[1] * T[2]) - 1;
+    return;
+  }
+  const float *P = *a.Pp;
   int c[3] = {0, 0, 0};
   for (int d = 0; d < a.dim; d++) {
     const float xp = P[(PF_X0 + d) * a.ps + p] + (use_x0 ? 0.f : P[(PF_XN + d) * a.ps + p]);
@@ -36,8 +42,8 @@ __global__ void k_cell_keys(PartArgs a, int *keys, int use_x0) {
   keys[p] = (g.tile_off + tl) * ncpt + lc;
 }
 
-void launch_cell_keys(const PartArgs &a, int nblk, int *keys, int use_x0, cudaStream_t st) {
-  k_cell_keys<<<nblk, 256, 0, st>>>(a, keys, use_x0);
+void launch_cell_keys(const PartArgs &a, int nblk, int *keys, int use_x0, cudaStream_t st, int pad_last) {
+  k_cell_keys<<<nblk, 256, 0, st>>>(a, keys, use_x0, pad_last);
 }
 
 // first / last particle of every cell and tile in sorted keys (arrays zeroed before)
