@@ -262,6 +262,7 @@ def bench_ours(args):
         "step_roofline": {"alg_bytes_per_step": step_bytes, "achieved_gbs": step_bytes / (ms / args.steps * 1e-3) / 1e9,
                           "frac": step_bytes / (ms / args.steps * 1e-3) / 1e9 / peak},
         "phases_ms": phases,
+        "autotune": be.tuning(),
         "clocks": clk,
     }
     if learned is not None:
@@ -353,7 +354,7 @@ def bench_sweep(args):
             "data": "synthetic (seed 0)", "gpu_launches": be.launches_per_step() * args.steps,
             "config": {"workload": f"tensile_sweep_2d_tlmpm_jc_damage instances={args.instances}", "particles": n,
                        "setup_s": setup_s},
-            "phases_ms": phases, "clocks": clk}
+            "phases_ms": phases, "autotune": be.tuning(), "clocks": clk}
     print(json.dumps(line), flush=True)
 
 

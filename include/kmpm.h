@@ -71,6 +71,9 @@ typedef struct {
   int independent;   /* TLMPM only: every solid is an independent simulation with its own
                         dt and time (a batch of runs in one launch per phase); 0 = one
                         simulation whose dt is the minimum over solids (adjust_dt) */
+  int autotune;      /* 1: at the first kmpm_run / kmpm_run_time after at least one step,
+                        time every launch shape of the gather kernels on a scratch copy of
+                        the particle state and keep the fastest (kmpm_tuning reports it) */
 } kmpm_params;
 
 /* One material: Mat (src/material.h:45-68) with its EOS / Strength / Damage /
@@ -182,6 +185,11 @@ void *kmpm_stream(struct kmpm_ctx *ctx);
 
 /* Number of kernel launches one time step issues (for launch accounting). */
 int kmpm_launches_per_step(struct kmpm_ctx *ctx);
+
+/* The autotuner's record (no counterpart in the reference): a JSON object
+ * with the candidate launch shapes of each gather kernel, their times in ms
+ * and the one chosen; "{}" before tuning. */
+const char *kmpm_tuning(struct kmpm_ctx *ctx);
 
 /* Profiling (no counterpart in the reference): runs nsteps steps launched
  * eagerly with a CUDA event recorded on the context's stream after every

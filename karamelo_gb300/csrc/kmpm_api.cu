@@ -108,6 +108,11 @@ struct kmpm_ctx {
   uint32_t log_thresh = 0;
   unsigned long long log_seed = 0;
   LearnKernels LK{};
+  // autotuner: chosen launch-shape variant of each gather kernel, its record
+  int var_g2p1 = 0, var_g2p2 = 0;
+  bool tuned = false;
+  long long runs = 0;
+  std::string tuning = "{}";
   // device buffer of kmpm_download_particles (one field of one solid, FP64)
   double *d_dump = nullptr;
   size_t dump_cap = 0;
@@ -553,6 +558,7 @@ int build(kmpm_ctx *c) {
     // grids in range order keep the keys of range r below those of range r+1
     bool ordered = true;
     for (size_t r = 1; r < c->ranges.size(); r++) ordered = ordered && c->ranges[r].grid > c->ranges[r - 1].grid;
+    if (const char *ev = std::getenv("KMPM_SORT_PER_RANGE"); ev && ev[0] == '1') ordered = false;
     std::vector<int2> tiles;
     if (ordered) {
       // one stable LSD radix sort of every slot on the device: the same
@@ -740,7 +746,7 @@ int enqueue_step(kmpm_ctx *c) {
   LAUNCH(c->K.grid_upd[TL][th][prec], c->nblk_g, 256, 0, g1);
   MARK("grid_update");
   // grid_to_points + advance_particles
-  LAUNCH(c->K.g2p1[TL][th], c->nblk_p, 256, 0, pa);
+  LAUNCH(th ? c->K.g2p1[TL][th] : c->K.g2p1_v[TL][c->var_g2p1], c->nblk_p, 256, 0, pa);
   MARK("g2p_advance");
   if (musl) {
     // velocities_to_grid + post_velocities_to_grid (+ TL grid positions)
@@ -756,7 +762,7 @@ int enqueue_step(kmpm_ctx *c) {
   }
   // compute_rate_deformation_gradient + update_deformation_gradient + update_stress
   if (c->learn_mode == MODE_PLAIN) {
-    LAUNCH(c->K.g2p2[TL][th][prec], c->nblk_p, 256, 0, pa);
+    LAUNCH((th || prec) ? c->K.g2p2[TL][th][prec] : c->K.g2p2_v[TL][c->var_g2p2], c->nblk_p, 256, 0, pa);
   } else {
     LearnArgs la{};
     la.blob = c->d_blob;
@@ -826,6 +832,75 @@ int prepare(kmpm_ctx *c) {
     int r = upload_fixes(c);
     if (r != KMPM_OK) return r;
   }
+  return ensure_graph(c);
+}
+
+// ---------------------------------------------------------------- autotuner
+// Launch shape of the two gathers: resident blocks per SM, i.e. the register
+// budget of k_g2p1 / k_g2p2 (G2P1_MINB / G2P2_MINB).  Every candidate runs on
+// a scratch copy of the live particle state (the spare buffer), interleaved,
+// three timed launches each after one untimed; the fastest mean is kept for
+// the rest of the run.  The live state and the dt partials of the next step
+// are untouched.
+int autotune(kmpm_ctx *c) {
+  c->tuned = true;
+  if (c->prm.thermal || c->prm.precision != KMPM_PREC_FP32) return KMPM_OK;  // candidates exist for FP32 mechanics
+  const double big = 1e300;
+  CK(cudaMemcpyAsync((char *)c->d_scalars + offsetof(StepScalars, maxtime), &big, sizeof(double),
+                     cudaMemcpyHostToDevice, c->st));
+  float *pp[2] = {nullptr, nullptr};
+  CK(cudaMemcpyAsync(pp, c->d_pp, sizeof(pp), cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  CK(cudaMemcpyAsync(pp[1], pp[0], sizeof(float) * c->ps * PF_COUNT, cudaMemcpyDeviceToDevice, c->st));
+  launch_swap_ptrs(c->d_pp, c->st);  // the candidates read and write the copy
+  const bool TL = c->TL();
+  PartArgs pa = part_args(c);
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  double t[2][G2P_NVAR] = {{0}};
+  for (int rep = 0; rep < 4; rep++)
+    for (int k = 0; k < 2; k++)
+      for (int v = 0; v < G2P_NVAR; v++) {
+        void *fn = k == 0 ? c->K.g2p1_v[TL][v] : c->K.g2p2_v[TL][v];
+        CK(cudaEventRecord(e0, c->st));
+        int r = launch(c, fn, dim3(c->nblk_p), dim3(256), 0, &pa);
+        if (r != KMPM_OK) return r;
+        CK(cudaEventRecord(e1, c->st));
+        CK(cudaEventSynchronize(e1));
+        float ms = 0.f;
+        CK(cudaEventElapsedTime(&ms, e0, e1));
+        if (rep > 0) t[k][v] += ms / 3.0;
+      }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  launch_swap_ptrs(c->d_pp, c->st);
+  CK(cudaMemsetAsync(c->d_err, 0, sizeof(ErrState), c->st));
+  CK(cudaStreamSynchronize(c->st));
+  int best[2] = {0, 0};
+  for (int k = 0; k < 2; k++)
+    for (int v = 1; v < G2P_NVAR; v++)
+      if (t[k][v] < t[k][best[k]]) best[k] = v;
+  c->var_g2p1 = best[0];
+  c->var_g2p2 = best[1];
+  char buf[512];
+  std::snprintf(buf, sizeof(buf),
+                "{\"g2p_advance\": {\"min_blocks\": [%d, %d, %d], \"ms\": [%.4f, %.4f, %.4f], \"chosen\": %d}, "
+                "\"g2p_stress\": {\"min_blocks\": [%d, %d, %d], \"ms\": [%.4f, %.4f, %.4f], \"chosen\": %d}}",
+                G2P1_MINB[0], G2P1_MINB[1], G2P1_MINB[2], t[0][0], t[0][1], t[0][2], G2P1_MINB[best[0]],
+                G2P2_MINB[0], G2P2_MINB[1], G2P2_MINB[2], t[1][0], t[1][1], t[1][2], G2P2_MINB[best[1]]);
+  c->tuning = buf;
+  c->graph_valid = false;
+  return KMPM_OK;
+}
+
+// tune once, at the first run after at least one step (a state with motion)
+int maybe_tune(kmpm_ctx *c) {
+  const bool due = c->prm.autotune && !c->tuned && c->runs > 0;
+  c->runs++;
+  if (!due) return KMPM_OK;
+  int r = autotune(c);
+  if (r != KMPM_OK) return r;
   return ensure_graph(c);
 }
 
@@ -961,6 +1036,10 @@ int kmpm_run(kmpm_ctx *c, int nsteps) {
   if (!c || nsteps < 0) return KMPM_ERR_ARG;
   int r = prepare(c);
   if (r != KMPM_OK) return r;
+  if (nsteps > 0) {
+    r = maybe_tune(c);
+    if (r != KMPM_OK) return r;
+  }
   r = set_maxtime(c, 1e300);
   if (r != KMPM_OK) return r;
   for (int i = 0; i < nsteps; i++) CK(cudaGraphLaunch(c->gexec, c->st));
@@ -971,6 +1050,8 @@ int kmpm_run_time(kmpm_ctx *c, double maxtime, int *nsteps_done) {
   if (!c) return KMPM_ERR_ARG;
   if (c->indep()) return fail(c, KMPM_ERR_ARG, "run_time needs one clock: not available for independent solids");
   int r = prepare(c);
+  if (r != KMPM_OK) return r;
+  r = maybe_tune(c);
   if (r != KMPM_OK) return r;
   StepScalars s{};
   r = read_scalars(c, s);
@@ -1200,6 +1281,8 @@ const char *kmpm_profile_phase(kmpm_ctx *c, int i) {
 }
 
 int kmpm_launches_per_step(kmpm_ctx *c) { return c ? c->launches_per_step : 0; }
+
+const char *kmpm_tuning(kmpm_ctx *c) { return c ? c->tuning.c_str() : "{}"; }
 
 // ---------------------------------------------------------------- learned return map
 static int learn_check(kmpm_ctx *c) {

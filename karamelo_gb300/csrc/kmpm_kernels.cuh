@@ -88,7 +88,13 @@ struct StepKernels {
   void *p2g_mass, *p2g_tl, *p2g_tl_th, *p2g_ul, *p2g_ul_th, *p2g_vel, *p2g_vel_th;
   void *grid_mass[2], *grid_upd[2][2][2], *grid_vel[2][2][2];
   void *g2p1[2][2], *g2p2[2][2][2];
+  // launch-shape candidates [TL][variant] of the gathers (FP32, no thermal):
+  // __launch_bounds__(256, G2P1_MINB[v] / G2P2_MINB[v]); variant 0 is the default
+  void *g2p1_v[2][3], *g2p2_v[2][3];
 };
+constexpr int G2P_NVAR = 3;
+constexpr int G2P1_MINB[G2P_NVAR] = {4, 3, 6};
+constexpr int G2P2_MINB[G2P_NVAR] = {3, 2, 4};
 
 void get_step_kernels(int dim, int basis, StepKernels &k);
 // particle downloads (kmpm_dump.cu): values per particle of a KMPM_P_* field

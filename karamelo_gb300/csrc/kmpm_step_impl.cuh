@@ -414,8 +414,10 @@ __device__ __forceinline__ int range_particle(const PartArgs &a, RangeDev &rd) {
 }
 
 // grid_to_points + advance_particles (src/solid.cpp:576-635, 786-790)
-template <int DIM, int BASIS, bool TL, bool THERMAL>
-__global__ void __launch_bounds__(256, 4) k_g2p1(PartArgs a) {
+// MINB: resident blocks per SM the register budget is set for (launch shape
+// picked per run by the autotuner, kmpm_api.cu)
+template <int DIM, int BASIS, bool TL, bool THERMAL, int MINB = 4>
+__global__ void __launch_bounds__(256, MINB) k_g2p1(PartArgs a) {
   if (run_finished(a.scalars)) return;
   RangeDev rd;
   const int p = range_particle(a, rd);
@@ -491,8 +493,8 @@ __global__ void __launch_bounds__(256, 4) k_g2p1(PartArgs a) {
 
 // rate of deformation + deformation gradient + stress + wave speed
 // (src/solid.cpp:798-936, 1155-1438)
-template <int DIM, int BASIS, bool TL, bool THERMAL, int PREC>
-__global__ void __launch_bounds__(256, 3) k_g2p2(PartArgs a) {
+template <int DIM, int BASIS, bool TL, bool THERMAL, int PREC, int MINB = 3>
+__global__ void __launch_bounds__(256, MINB) k_g2p2(PartArgs a) {
   __shared__ float red_c[256], red_h[256];
   if (run_finished(a.scalars)) return;
   RangeDev rd;
@@ -820,6 +822,17 @@ void fill_step_kernels(StepKernels &k) {
   k.g2p2[0][1][1] = (void *)k_g2p2<DIM, BASIS, false, true, 1>;
   k.g2p2[1][0][1] = (void *)k_g2p2<DIM, BASIS, true, false, 1>;
   k.g2p2[1][1][1] = (void *)k_g2p2<DIM, BASIS, true, true, 1>;
+  // launch-shape candidates of the FP32 mechanical path (variant 0 = default)
+#define KMPM_VAR_SET(tl)                                                                       \
+  k.g2p1_v[tl][0] = (void *)k_g2p1<DIM, BASIS, tl, false, G2P1_MINB[0]>;                      \
+  k.g2p1_v[tl][1] = (void *)k_g2p1<DIM, BASIS, tl, false, G2P1_MINB[1]>;                      \
+  k.g2p1_v[tl][2] = (void *)k_g2p1<DIM, BASIS, tl, false, G2P1_MINB[2]>;                      \
+  k.g2p2_v[tl][0] = (void *)k_g2p2<DIM, BASIS, tl, false, 0, G2P2_MINB[0]>;                   \
+  k.g2p2_v[tl][1] = (void *)k_g2p2<DIM, BASIS, tl, false, 0, G2P2_MINB[1]>;                   \
+  k.g2p2_v[tl][2] = (void *)k_g2p2<DIM, BASIS, tl, false, 0, G2P2_MINB[2]>;
+  KMPM_VAR_SET(false)
+  KMPM_VAR_SET(true)
+#undef KMPM_VAR_SET
 }
 
 }  // namespace kmpm

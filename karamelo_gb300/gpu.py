@@ -33,7 +33,7 @@ EXPORTED = ["kmpm_create", "kmpm_destroy", "kmpm_last_error", "kmpm_add_material
             "kmpm_mlp_create", "kmpm_mlp_destroy", "kmpm_mlp_last_error", "kmpm_mlp_init", "kmpm_mlp_set_params",
             "kmpm_mlp_get_params", "kmpm_mlp_set_norm", "kmpm_mlp_get_norm", "kmpm_mlp_loss_grad", "kmpm_mlp_train",
             "kmpm_mlp_predict", "kmpm_mlp_predict_tc", "kmpm_log_start", "kmpm_log_stop", "kmpm_log_data",
-            "kmpm_jc_label", "kmpm_set_surrogate", "kmpm_surrogate_stats"]
+            "kmpm_jc_label", "kmpm_set_surrogate", "kmpm_surrogate_stats", "kmpm_tuning"]
 
 MLP_NIN, MLP_NOUT, MLP_NPARAMS, MLP_NNORM = 15, 7, 35975, 74
 
@@ -43,7 +43,7 @@ class KmpmParams(ctypes.Structure):
                 ("pic_flip", ctypes.c_double), ("thermal", ctypes.c_int), ("dt", ctypes.c_double),
                 ("dt_factor", ctypes.c_double), ("dt_constant", ctypes.c_int), ("boxlo", ctypes.c_double * 3),
                 ("boxhi", ctypes.c_double * 3), ("precision", ctypes.c_int), ("sort_every", ctypes.c_int),
-                ("track_strain", ctypes.c_int), ("independent", ctypes.c_int)]
+                ("track_strain", ctypes.c_int), ("independent", ctypes.c_int), ("autotune", ctypes.c_int)]
 
 
 class TrainOpts(ctypes.Structure):
@@ -117,6 +117,8 @@ def load(path: str = LIB_PATH):
     L.kmpm_jc_label.argtypes = [p, i, fp, ll, fp]
     L.kmpm_set_surrogate.argtypes = [p, p, d]
     L.kmpm_surrogate_stats.argtypes = [p, ctypes.POINTER(ll)]
+    L.kmpm_tuning.argtypes = [p]
+    L.kmpm_tuning.restype = ctypes.c_char_p
     _lib = L
     return L
 
@@ -128,7 +130,8 @@ def _dp(a):
 class GpuBackend:
     """Runs a Scenario on the GPU through the C ABI."""
 
-    def __init__(self, s: sc.Scenario, precision: int = 0, track_strain: bool = True, independent: bool = False):
+    def __init__(self, s: sc.Scenario, precision: int = 0, track_strain: bool = True, independent: bool = False,
+                 autotune: bool = True):
         L = load()
         self.L, self.s = L, s
         prm = KmpmParams()
@@ -141,6 +144,7 @@ class GpuBackend:
         prm.sort_every = 1
         prm.track_strain = int(track_strain)
         prm.independent = int(independent)
+        prm.autotune = int(autotune)
         h = ctypes.c_void_p()
         r = L.kmpm_create(ctypes.byref(prm), ctypes.byref(h))
         if r != KMPM_OK:
@@ -229,6 +233,11 @@ class GpuBackend:
 
     def launches_per_step(self):
         return self.L.kmpm_launches_per_step(self.h)
+
+    def tuning(self):
+        """The autotuner's record (launch shapes tried, their ms, the choice)."""
+        import json
+        return json.loads(self.L.kmpm_tuning(self.h).decode())
 
     # ---- learned return map (training pairs, surrogate)
     def log_start(self, capacity: int, fraction: float, seed: int = 0):
