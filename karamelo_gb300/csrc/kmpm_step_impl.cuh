@@ -38,6 +38,40 @@ __device__ __forceinline__ void p2g_particle(float (&accr)[NSL][Q], const float 
   const float2 bx = bj[soff[0][0]];
   const float2 by = DIM >= 2 ? bj[S + soff[0][1]] : make_float2(1.f, 0.f);
   const float wxy = bx.x * by.x, gxy0 = bx.y * by.x, gxy1 = bx.x * by.y;
+  if ((MODE == P2G_TL || MODE == P2G_UL) && !THERMAL) {
+    // the lane's nodes share (a, b): with w = wxy s_z and grad w =
+    // (gxy0 s_z, gxy1 s_z, wxy s'_z), every term factors into a per-particle
+    // part and s_z or s'_z:  m v w = s_z (wxy m v),
+    // f_r -= s_z (T_r0 gxy0 + T_r1 gxy1) + s'_z (T_r2 wxy)  (T = vol0 PK1 or vol sigma)
+    constexpr int OM = MODE == P2G_UL ? 1 : 0;  // UL payload and sums start with the mass
+    float q[4], t[3], t2[3];
+#pragma unroll
+    for (int d = 0; d < 3 + OM; d++) q[d] = wxy * pay[d];
+#pragma unroll
+    for (int r = 0; r < 3; r++) {
+      float T0, T1, T2;
+      if (MODE == P2G_TL) {
+        T0 = pay[3 + 3 * r]; T1 = pay[4 + 3 * r]; T2 = pay[5 + 3 * r];
+      } else {  // symmetric sigma: xx yy zz xy xz yz
+        const float *sg = pay + 4;
+        T0 = r == 0 ? sg[0] : (r == 1 ? sg[3] : sg[4]);
+        T1 = r == 0 ? sg[3] : (r == 1 ? sg[1] : sg[5]);
+        T2 = r == 0 ? sg[4] : (r == 1 ? sg[5] : sg[2]);
+      }
+      t[r] = T0 * gxy0 + T1 * gxy1;
+      t2[r] = T2 * wxy;
+    }
+#pragma unroll
+    for (int u = 0; u < NSL; u++) {
+      if (!PAIR && lane + 32 * u >= NS) continue;
+      const float2 bz = DIM == 3 ? bj[2 * S + soff[u][2]] : make_float2(1.f, 0.f);
+#pragma unroll
+      for (int d = 0; d < 3 + OM; d++) accr[u][d] = fmaf(bz.x, q[d], accr[u][d]);
+#pragma unroll
+      for (int r = 0; r < 3; r++) accr[u][3 + OM + r] = fmaf(-bz.x, t[r], fmaf(-bz.y, t2[r], accr[u][3 + OM + r]));
+    }
+    return;
+  }
 #pragma unroll
   for (int u = 0; u < NSL; u++) {
     if (!PAIR && lane + 32 * u >= NS) continue;
