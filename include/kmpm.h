@@ -48,6 +48,11 @@ extern "C" {
 #define KMPM_BASIS_CUBIC 1
 #define KMPM_BASIS_BERNSTEIN 2
 
+/* kmpm_params.transfer: the method's sub-type (Update::create_method,
+ * src/update.cpp:129-149) */
+#define KMPM_TRANSFER_FLIP 0
+#define KMPM_TRANSFER_APIC 1
+
 /* kmpm_params.precision: arithmetic of the three places that the FP32 bulk
  * may promote (nodal v = p/m, det/inverse of F, the constitutive return) */
 #define KMPM_PREC_FP32 0
@@ -74,6 +79,9 @@ typedef struct {
   int autotune;      /* 1: at the first kmpm_run / kmpm_run_time after at least one step,
                         time every launch shape of the gather kernels on a scratch copy of
                         the particle state and keep the fastest (kmpm_tuning reports it) */
+  int transfer;      /* KMPM_TRANSFER_FLIP (PIC/FLIP blend by pic_flip) or KMPM_TRANSFER_APIC
+                        (method(..., APIC, ...): affine transfers, src/solid.cpp:392-426 and
+                        1006-1153; cubic spline, mechanical runs; sets pic_flip = 0) */
 } kmpm_params;
 
 /* One material: Mat (src/material.h:45-68) with its EOS / Strength / Damage /

@@ -117,6 +117,8 @@ struct kmpm_ctx {
   double *d_dump = nullptr;
   size_t dump_cap = 0;
   bool indep() const { return prm.independent != 0; }
+  bool apic() const { return prm.transfer == KMPM_TRANSFER_APIC; }
+  int smem_apic[3] = {0, 0, 0};  // dynamic shared memory of the APIC scatters (TL, UL, VEL)
   bool TL() const { return prm.method == KMPM_TLMPM; }
   bool musl() const { return prm.scheme == KMPM_MUSL; }
 };
@@ -218,6 +220,7 @@ PartArgs part_args(kmpm_ctx *c) {
   a.use_vu = c->musl() ? 0 : 1;
   a.thermal = c->prm.thermal;
   a.track_strain = c->prm.track_strain;
+  a.apic = c->apic() ? 1 : 0;
   a.dim = c->prm.dim;
   for (int d = 0; d < 3; d++) a.tile_t[d] = c->tdim[d];
   return a;
@@ -237,6 +240,7 @@ P2GArgs p2g_args(kmpm_ctx *c) {
   a.tile_start = c->d_ts;
   a.tile_end = c->d_te;
   a.scalars = c->d_scalars;
+  a.apic_pos = -1;
   return a;
 }
 
@@ -321,6 +325,7 @@ std::vector<int> active_fields(kmpm_ctx *c) {
   if (thermal) { add(PF_T, 2); add(PF_Q, 3); }
   if (c->prm.track_strain) add(PF_STRAIN, 6);
   if (!c->TL()) add(PF_XN, 3);
+  if (c->apic()) add(PF_C, 9);
   return f;
 }
 
@@ -547,6 +552,14 @@ int build(kmpm_ctx *c) {
       c->smem[m][t] = p2g_smem_bytes(dim, basis, modes[m], t == 1);
       CK(cudaFuncSetAttribute(fns[m][t], cudaFuncAttributeMaxDynamicSharedMemorySize, c->smem[m][t]));
     }
+  if (c->apic()) {
+    const int am[3] = {P2G_TL_APIC, P2G_UL_APIC, P2G_VEL_APIC};
+    void *af[3] = {c->K.p2g_tl_apic, c->K.p2g_ul_apic, c->K.p2g_vel_apic};
+    for (int m = 0; m < 3; m++) {
+      c->smem_apic[m] = p2g_smem_bytes(dim, basis, am[m], false);
+      CK(cudaFuncSetAttribute(af[m], cudaFuncAttributeMaxDynamicSharedMemorySize, c->smem_apic[m]));
+    }
+  }
   c->ul_fields.clear();
   for (int f : active_fields(c)) {
     int src = (f >= PF_X && f < PF_X + 3) ? PF_XN + (f - PF_X) : f;
@@ -738,8 +751,11 @@ int enqueue_step(kmpm_ctx *c) {
   }
   P2GArgs p = p2g_args(c);
   GridArgs g1 = grid_args(c, 0);
-  // particles_to_grid
-  if (TL) LAUNCH(th ? c->K.p2g_tl_th : c->K.p2g_tl, c->ntiles_launch, 256, c->smem[1][th], p);
+  const bool apic = c->apic();
+  // particles_to_grid (APIC: compute_velocity_nodes_APIC with x_p = x0 (TL) or x (UL))
+  p.apic_pos = TL ? -1 : PF_X;
+  if (apic) LAUNCH(TL ? c->K.p2g_tl_apic : c->K.p2g_ul_apic, c->ntiles_launch, 256, c->smem_apic[TL ? 0 : 1], p);
+  else if (TL) LAUNCH(th ? c->K.p2g_tl_th : c->K.p2g_tl, c->ntiles_launch, 256, c->smem[1][th], p);
   else LAUNCH(th ? c->K.p2g_ul_th : c->K.p2g_ul, c->ntiles_launch, 256, c->smem[2][th], p);
   MARK("p2g");
   // update_grid_state + fixes
@@ -750,7 +766,11 @@ int enqueue_step(kmpm_ctx *c) {
   MARK("g2p_advance");
   if (musl) {
     // velocities_to_grid + post_velocities_to_grid (+ TL grid positions)
-    LAUNCH(th ? c->K.p2g_vel_th : c->K.p2g_vel, c->ntiles_launch, 256, c->smem[3][th], p);
+    // APIC re-map: ULMPM takes x_p after the move, with this step's weights
+    P2GArgs pv = p;
+    pv.apic_pos = TL ? -1 : PF_XN;
+    if (apic) LAUNCH(c->K.p2g_vel_apic, c->ntiles_launch, 256, c->smem_apic[2], pv);
+    else LAUNCH(th ? c->K.p2g_vel_th : c->K.p2g_vel, c->ntiles_launch, 256, c->smem[3][th], pv);
     MARK("p2g_velocity");
     GridArgs g2 = grid_args(c, 1);
     LAUNCH(c->K.grid_vel[TL][th][prec], c->nblk_g, 256, 0, g2);
@@ -924,10 +944,14 @@ int kmpm_create(const kmpm_params *params, kmpm_ctx **out) {
   if (p.basis < 0 || p.basis > 2 || p.dim < 1 || p.dim > 3) return KMPM_ERR_ARG;
   if (p.method == KMPM_ULMPM && p.basis == KMPM_BASIS_BERNSTEIN) return KMPM_ERR_ARG;
   if (p.independent && p.method != KMPM_TLMPM) return KMPM_ERR_ARG;  // ULMPM solids share one grid
+  if (p.transfer != KMPM_TRANSFER_FLIP && p.transfer != KMPM_TRANSFER_APIC) return KMPM_ERR_ARG;
+  // APIC: the cubic spline (Di = 3/h^2), mechanical runs
+  if (p.transfer == KMPM_TRANSFER_APIC && (p.basis != KMPM_BASIS_CUBIC || p.thermal)) return KMPM_ERR_ARG;
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return KMPM_ERR_CUDA;
   kmpm_ctx *c = new kmpm_ctx();
   c->prm = p;
+  if (c->apic()) c->prm.pic_flip = 0;  // APIC updates v = v_update (src/tlmpm.cpp:82-84, src/ulmpm.cpp:79-82)
   if (cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking) != cudaSuccess) {
     delete c;
     return KMPM_ERR_CUDA;
@@ -1288,8 +1312,8 @@ const char *kmpm_tuning(kmpm_ctx *c) { return c ? c->tuning.c_str() : "{}"; }
 static int learn_check(kmpm_ctx *c) {
   if (!c->TL() || c->prm.dim != 3 || c->prm.basis != KMPM_BASIS_CUBIC)
     return fail(c, KMPM_ERR_ARG, "the learned return map covers 3-D TLMPM with the cubic B-spline basis");
-  if (c->prm.precision != KMPM_PREC_FP32 || c->prm.thermal)
-    return fail(c, KMPM_ERR_ARG, "the learned return map needs FP32 and no thermo-mechanical coupling");
+  if (c->prm.precision != KMPM_PREC_FP32 || c->prm.thermal || c->apic())
+    return fail(c, KMPM_ERR_ARG, "the learned return map needs FP32, FLIP/PIC transfers and no thermo-mechanical coupling");
   for (const MatDev &m : c->mats)
     if (m.type != KMPM_MAT_EOS_STRENGTH || m.strength != 2)
       return fail(c, KMPM_ERR_ARG, "the learned return map needs eos-strength materials with Johnson-Cook strength");

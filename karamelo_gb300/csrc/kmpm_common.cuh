@@ -40,7 +40,8 @@ enum PField : int {
   PF_XN = 50,       // 3: ULMPM displacement after this step's move (weights use PF_X)
   PF_ORIG = 53,     // caller index (int bits)
   PF_SID = 54,      // solid id (int bits), ULMPM only
-  PF_COUNT = 55
+  PF_C = 55,        // APIC affine matrix (9, row-major): Fdot (TL) or L (UL) of the last stress update
+  PF_COUNT = 64
 };
 
 // symmetric storage order: xx yy zz xy xz yz

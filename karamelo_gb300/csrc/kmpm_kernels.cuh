@@ -10,14 +10,29 @@ enum P2GMode : int {
   P2G_TL = 1,    // p, f_int (TL)          (+ mT, Qext, Qint when thermal)
   P2G_UL = 2,    // m, p, f_int (UL)       (+ mT, Qext, Qint)
   P2G_VEL = 3,   // p                      (MUSL re-map; + mT)
+  // APIC (Solid::compute_velocity_nodes_APIC, src/solid.cpp:392-426): the
+  // same sums with the particle velocity v + C (x_node - x_p); the payload
+  // adds m C (9) and x_p (3)
+  P2G_TL_APIC = 4,
+  P2G_UL_APIC = 5,
+  P2G_VEL_APIC = 6,
 };
+__host__ __device__ constexpr int p2g_base(int mode) { return mode >= P2G_TL_APIC ? mode - 3 : mode; }
+__host__ __device__ constexpr bool p2g_apic(int mode) { return mode >= P2G_TL_APIC; }
 enum GridMode : int { GM_MASS = 0, GM_UPDATE = 1, GM_VEL = 2 };
 
 __host__ __device__ constexpr int p2g_nq(int mode, bool th) {
-  return mode == P2G_MASS ? 1 : mode == P2G_TL ? (th ? 9 : 6) : mode == P2G_UL ? (th ? 10 : 7) : (th ? 4 : 3);
+  return p2g_base(mode) == P2G_MASS  ? 1
+         : p2g_base(mode) == P2G_TL ? (th ? 9 : 6)
+         : p2g_base(mode) == P2G_UL ? (th ? 10 : 7)
+                                    : (th ? 4 : 3);
 }
 __host__ __device__ constexpr int p2g_nin(int mode, bool th) {
-  return mode == P2G_MASS ? 1 : mode == P2G_TL ? (th ? 17 : 12) : mode == P2G_UL ? (th ? 15 : 10) : (th ? 4 : 3);
+  return (p2g_base(mode) == P2G_MASS  ? 1
+          : p2g_base(mode) == P2G_TL ? (th ? 17 : 12)
+          : p2g_base(mode) == P2G_UL ? (th ? 15 : 10)
+                                     : (th ? 4 : 3)) +
+         (p2g_apic(mode) ? 12 : 0);
 }
 
 struct P2GArgs {
@@ -31,6 +46,7 @@ struct P2GArgs {
   size_t pstride_tile;       // floats per tile slice
   const int *tile_start, *tile_end;  // particle range of every tile (empty tiles are skipped)
   const StepScalars *scalars;
+  int apic_pos;              // APIC: displacement field added to x0 for x_p (PF_X, PF_XN) or -1 (TL: x0)
 };
 
 struct GridArgs {
@@ -66,6 +82,7 @@ struct PartArgs {
   float boxlo[3], boxhi[3];
   int indep, use_vu, thermal, track_strain, dim;
   int tile_t[3];
+  int apic;                  // APIC transfers: k_g2p2 forms grad v from moments and stores PF_C
 };
 
 struct DtArgs {
@@ -86,6 +103,7 @@ struct LaunchSet {
 // kernel entry points of one (dim, basis) instantiation
 struct StepKernels {
   void *p2g_mass, *p2g_tl, *p2g_tl_th, *p2g_ul, *p2g_ul_th, *p2g_vel, *p2g_vel_th;
+  void *p2g_tl_apic, *p2g_ul_apic, *p2g_vel_apic;  // cubic spline only (nullptr otherwise)
   void *grid_mass[2], *grid_upd[2][2][2], *grid_vel[2][2][2];
   void *g2p1[2][2], *g2p2[2][2][2];
   // launch-shape candidates [TL][variant] of the gathers (FP32, no thermal):
@@ -122,8 +140,9 @@ void launch_permute(float *const *src_pp, float *const *dst_pp, size_t ps, const
 void launch_swap_ptrs(float **pp, cudaStream_t st);
 
 // ---- payload staged per particle for the scatter
-template <int MODE, bool TH>
+template <int MODE_, bool TH>
 __device__ __forceinline__ void p2g_payload(const P2GArgs &a, const float *P, int p, float *pay) {
+  constexpr int MODE = p2g_base(MODE_);
   const size_t ps = a.ps;
   const float m = P[PF_MASS * ps + p];
   if (MODE == P2G_MASS) { pay[0] = m; return; }
@@ -146,11 +165,19 @@ __device__ __forceinline__ void p2g_payload(const P2GArgs &a, const float *P, in
       for (int d = 0; d < 3; d++) pay[o++] = P[(PF_Q + d) * ps + p];
     }
   }
+  if (p2g_apic(MODE_)) {
+#pragma unroll
+    for (int k = 0; k < 9; k++) pay[o++] = m * P[(PF_C + k) * ps + p];
+#pragma unroll
+    for (int d = 0; d < 3; d++)
+      pay[o++] = P[(PF_X0 + d) * ps + p] + (a.apic_pos >= 0 ? P[(a.apic_pos + d) * ps + p] : 0.f);
+  }
 }
 
 // ---- contribution of one particle to one node
-template <int MODE, bool TH, int Q>
+template <int MODE_, bool TH, int Q>
 __device__ __forceinline__ void p2g_accumulate(float *acc, const float *pay, float w, const float *gw) {
+  constexpr int MODE = p2g_base(MODE_);  // APIC modes never take this path (no thermal APIC)
   if (MODE == P2G_MASS) { acc[0] += w * pay[0]; return; }
   int o = 0, i = 0;
   if (MODE == P2G_UL) acc[o++] += w * pay[i++];

@@ -28,7 +28,9 @@ namespace kmpm {
 // Contribution of one staged particle to this lane's stencil nodes.
 template <int DIM, int S, int MODE, bool THERMAL, int Q, int QINP, int NSL, int NS, bool PAIR>
 __device__ __forceinline__ void p2g_particle(float (&accr)[NSL][Q], const float *spay_j, const float2 *bj,
-                                             const int (&soff)[NSL][3], int lane) {
+                                             const int (&soff)[NSL][3], const float (&nco)[NSL][3], int lane) {
+  constexpr int BM = p2g_base(MODE);
+  constexpr bool AP = p2g_apic(MODE);
   float pay[QINP];
 #pragma unroll
   for (int v = 0; v < QINP / 4; v++) {
@@ -38,28 +40,43 @@ __device__ __forceinline__ void p2g_particle(float (&accr)[NSL][Q], const float 
   const float2 bx = bj[soff[0][0]];
   const float2 by = DIM >= 2 ? bj[S + soff[0][1]] : make_float2(1.f, 0.f);
   const float wxy = bx.x * by.x, gxy0 = bx.y * by.x, gxy1 = bx.x * by.y;
-  if ((MODE == P2G_TL || MODE == P2G_UL) && !THERMAL) {
+  if ((BM == P2G_TL || BM == P2G_UL || AP) && !THERMAL) {
     // the lane's nodes share (a, b): with w = wxy s_z and grad w =
     // (gxy0 s_z, gxy1 s_z, wxy s'_z), every term factors into a per-particle
     // part and s_z or s'_z:  m v w = s_z (wxy m v),
-    // f_r -= s_z (T_r0 gxy0 + T_r1 gxy1) + s'_z (T_r2 wxy)  (T = vol0 PK1 or vol sigma)
-    constexpr int OM = MODE == P2G_UL ? 1 : 0;  // UL payload and sums start with the mass
-    float q[4], t[3], t2[3];
+    // f_r -= s_z (T_r0 gxy0 + T_r1 gxy1) + s'_z (T_r2 wxy)  (T = vol0 PK1 or vol sigma).
+    // APIC adds m C (x_node - x_p) to m v: its x and y parts join the
+    // per-particle term, its z part s_z (z_node - z_p) (wxy m C_r2) is per node.
+    constexpr int OM = BM == P2G_UL ? 1 : 0;  // UL payload and sums start with the mass
+    constexpr bool FORCE = BM != P2G_VEL;
+    constexpr int NB = p2g_nin(BM, false);    // APIC: m C (9) and x_p (3) follow the base payload
+    float q[4], t[3], t2[3], qc[3];
 #pragma unroll
     for (int d = 0; d < 3 + OM; d++) q[d] = wxy * pay[d];
+    if (AP) {
+      const float *mC = pay + NB, *xp = pay + NB + 9;
+      const float dxa = nco[0][0] - xp[0], dyb = DIM >= 2 ? nco[0][1] - xp[1] : 0.f;
 #pragma unroll
-    for (int r = 0; r < 3; r++) {
-      float T0, T1, T2;
-      if (MODE == P2G_TL) {
-        T0 = pay[3 + 3 * r]; T1 = pay[4 + 3 * r]; T2 = pay[5 + 3 * r];
-      } else {  // symmetric sigma: xx yy zz xy xz yz
-        const float *sg = pay + 4;
-        T0 = r == 0 ? sg[0] : (r == 1 ? sg[3] : sg[4]);
-        T1 = r == 0 ? sg[3] : (r == 1 ? sg[1] : sg[5]);
-        T2 = r == 0 ? sg[4] : (r == 1 ? sg[5] : sg[2]);
+      for (int r = 0; r < 3; r++) {
+        q[OM + r] = fmaf(wxy, mC[3 * r] * dxa + mC[3 * r + 1] * dyb, q[OM + r]);
+        qc[r] = wxy * mC[3 * r + 2];
       }
-      t[r] = T0 * gxy0 + T1 * gxy1;
-      t2[r] = T2 * wxy;
+    }
+    if (FORCE) {
+#pragma unroll
+      for (int r = 0; r < 3; r++) {
+        float T0, T1, T2;
+        if (BM == P2G_TL) {
+          T0 = pay[3 + 3 * r]; T1 = pay[4 + 3 * r]; T2 = pay[5 + 3 * r];
+        } else {  // symmetric sigma: xx yy zz xy xz yz
+          const float *sg = pay + 4;
+          T0 = r == 0 ? sg[0] : (r == 1 ? sg[3] : sg[4]);
+          T1 = r == 0 ? sg[3] : (r == 1 ? sg[1] : sg[5]);
+          T2 = r == 0 ? sg[4] : (r == 1 ? sg[5] : sg[2]);
+        }
+        t[r] = T0 * gxy0 + T1 * gxy1;
+        t2[r] = T2 * wxy;
+      }
     }
 #pragma unroll
     for (int u = 0; u < NSL; u++) {
@@ -67,8 +84,14 @@ __device__ __forceinline__ void p2g_particle(float (&accr)[NSL][Q], const float 
       const float2 bz = DIM == 3 ? bj[2 * S + soff[u][2]] : make_float2(1.f, 0.f);
 #pragma unroll
       for (int d = 0; d < 3 + OM; d++) accr[u][d] = fmaf(bz.x, q[d], accr[u][d]);
+      if (AP && DIM == 3) {
+        const float bzd = bz.x * (nco[u][2] - pay[NB + 9 + 2]);
 #pragma unroll
-      for (int r = 0; r < 3; r++) accr[u][3 + OM + r] = fmaf(-bz.x, t[r], fmaf(-bz.y, t2[r], accr[u][3 + OM + r]));
+        for (int r = 0; r < 3; r++) accr[u][OM + r] = fmaf(bzd, qc[r], accr[u][OM + r]);
+      }
+      if (FORCE)
+#pragma unroll
+        for (int r = 0; r < 3; r++) accr[u][3 + OM + r] = fmaf(-bz.x, t[r], fmaf(-bz.y, t2[r], accr[u][3 + OM + r]));
     }
     return;
   }
@@ -168,6 +191,14 @@ __global__ void __launch_bounds__(256) k_p2g(P2GArgs a) {
     const int tco[3] = {tc[0] * TX, tc[1] * TY, tc[2] * TZ};
 #pragma unroll
     for (int d = 0; d < 3; d++) i0[d] = (d < DIM) ? (tco[d] + lc[d]) * SC - LO : 0;
+    // coordinates of this lane's nodes (APIC: x_node - x_p)
+    float nco[NSL][3];
+#pragma unroll
+    for (int u = 0; u < NSL; u++) {
+      nco[u][0] = glo0 + (float)(i0[0] + soff[u][0]) * h;
+      nco[u][1] = glo1 + (float)(i0[1] + soff[u][1]) * h;
+      nco[u][2] = glo2 + (float)(i0[2] + soff[u][2]) * h;
+    }
 
     float accr[NSL][Q];
 #pragma unroll
@@ -233,12 +264,14 @@ __global__ void __launch_bounds__(256) k_p2g(P2GArgs a) {
       if (lane_active) {
         int j = 0;
         for (; j + 1 < cnt; j += 2) {
-          p2g_particle<DIM, S, MODE, THERMAL, Q, QINP, NSL, NS, PAIR>(accr, spay + j * QINP, sbas + j * DIM * S, soff, lane);
+          p2g_particle<DIM, S, MODE, THERMAL, Q, QINP, NSL, NS, PAIR>(accr, spay + j * QINP, sbas + j * DIM * S, soff,
+                                                                      nco, lane);
           p2g_particle<DIM, S, MODE, THERMAL, Q, QINP, NSL, NS, PAIR>(accr, spay + (j + 1) * QINP,
-                                                                      sbas + (j + 1) * DIM * S, soff, lane);
+                                                                      sbas + (j + 1) * DIM * S, soff, nco, lane);
         }
         if (j < cnt)
-          p2g_particle<DIM, S, MODE, THERMAL, Q, QINP, NSL, NS, PAIR>(accr, spay + j * QINP, sbas + j * DIM * S, soff, lane);
+          p2g_particle<DIM, S, MODE, THERMAL, Q, QINP, NSL, NS, PAIR>(accr, spay + j * QINP, sbas + j * DIM * S, soff,
+                                                                      nco, lane);
       }
       __syncwarp();
     }
@@ -549,6 +582,22 @@ __global__ void __launch_bounds__(256, MINB) k_g2p2(PartArgs a) {
     ax.eval(g, xp);
     constexpr int S = Stencil<BASIS>::S;
     constexpr int SY = DIM >= 2 ? S : 1, SZ = DIM == 3 ? S : 1;
+    if (BASIS == 1 && a.apic) {
+      // APIC (compute_rate_deformation_gradient_{TL,UL}_APIC,
+      // src/solid.cpp:1006-1153): grad v = sum w v_node (x_node - x_p)^T Di with
+      // Di = 3 / cellsize^2 (Solid::compute_inertia_tensor, src/solid.cpp:1440-1478).
+      // The per-axis moment s (x_node - x_p) Di takes the place of the slope;
+      // x_p is x0 (TL), and for ULMPM the position the reference holds at this
+      // point: before the move (USL) or after it (MUSL)
+      const float Di = 3.f * g.inv_cellsize * g.inv_cellsize;
+#pragma unroll
+      for (int d = 0; d < DIM; d++) {
+        const float pd = P[(PF_X0 + d) * ps + p] + (TL ? 0.f : P[((a.use_vu ? PF_X : PF_XN) + d) * ps + p]);
+#pragma unroll
+        for (int k = 0; k < S; k++)
+          ax.ax[d].ds[k] = ax.ax[d].s[k] * (g.lo[d] + (float)(ax.ax[d].i0 + k) * g.cellsize - pd) * Di;
+      }
+    }
     float G[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
     float qg[3] = {0, 0, 0};
     // branch-free gather (clamped indices, see k_g2p1); a pair with a zero
@@ -602,6 +651,9 @@ __global__ void __launch_bounds__(256, MINB) k_g2p2(PartArgs a) {
         }
       }
     }
+    if (BASIS == 1 && a.apic)
+#pragma unroll
+      for (int k = 0; k < 9; k++) P[(PF_C + k) * ps + p] = G[k];  // C of the next transfers
     // ---- deformation gradient (src/solid.cpp:1155-1244), stored as H = F - I
     float H[9];
 #pragma unroll
@@ -832,6 +884,13 @@ void fill_step_kernels(StepKernels &k) {
   k.p2g_ul_th = (void *)k_p2g<DIM, BASIS, P2G_UL, true>;
   k.p2g_vel = (void *)k_p2g<DIM, BASIS, P2G_VEL, false>;
   k.p2g_vel_th = (void *)k_p2g<DIM, BASIS, P2G_VEL, true>;
+  if constexpr (BASIS == 1) {  // APIC runs with the cubic spline
+    k.p2g_tl_apic = (void *)k_p2g<DIM, BASIS, P2G_TL_APIC, false>;
+    k.p2g_ul_apic = (void *)k_p2g<DIM, BASIS, P2G_UL_APIC, false>;
+    k.p2g_vel_apic = (void *)k_p2g<DIM, BASIS, P2G_VEL_APIC, false>;
+  } else {
+    k.p2g_tl_apic = k.p2g_ul_apic = k.p2g_vel_apic = nullptr;
+  }
   k.grid_mass[0] = (void *)k_grid<DIM, BASIS, GM_MASS, true, false, float>;
   k.grid_mass[1] = (void *)k_grid<DIM, BASIS, GM_MASS, true, false, double>;
 #define KMPM_GRID_SET(tl, th)                                                                  \

@@ -43,7 +43,8 @@ class KmpmParams(ctypes.Structure):
                 ("pic_flip", ctypes.c_double), ("thermal", ctypes.c_int), ("dt", ctypes.c_double),
                 ("dt_factor", ctypes.c_double), ("dt_constant", ctypes.c_int), ("boxlo", ctypes.c_double * 3),
                 ("boxhi", ctypes.c_double * 3), ("precision", ctypes.c_int), ("sort_every", ctypes.c_int),
-                ("track_strain", ctypes.c_int), ("independent", ctypes.c_int), ("autotune", ctypes.c_int)]
+                ("track_strain", ctypes.c_int), ("independent", ctypes.c_int), ("autotune", ctypes.c_int),
+                ("transfer", ctypes.c_int)]
 
 
 class TrainOpts(ctypes.Structure):
@@ -145,6 +146,7 @@ class GpuBackend:
         prm.track_strain = int(track_strain)
         prm.independent = int(independent)
         prm.autotune = int(autotune)
+        prm.transfer = int(getattr(s, "transfer", 0))
         h = ctypes.c_void_p()
         r = L.kmpm_create(ctypes.byref(prm), ctypes.byref(h))
         if r != KMPM_OK:

@@ -94,18 +94,25 @@ class MPM:
         if self._backend_factory is None and not style.endswith("/gpu"):
             raise KarameloError(f"method style {style} is the reference's CPU method; use {base}/gpu")
         self.s.method = sc.TLMPM if base == "tlmpm" else sc.ULMPM
+        self.s.transfer = 0
         if sub == "PIC":
             self.s.pic_flip = 0.0
         elif sub == "FLIP":
             if not rest:
                 raise KarameloError("Illegal method command: FLIP needs the PIC/FLIP ratio")
+        elif sub == "APIC":
+            # APIC sets PIC_FLIP = 0 (src/tlmpm.cpp:82-84, src/ulmpm.cpp:79-82)
+            self.s.transfer = 1
+            self.s.pic_flip = 0.0
         else:
-            raise KarameloError(f"method type {sub} not supported on the GPU path (PIC or FLIP)")
+            raise KarameloError(f"method type {sub} not supported on the GPU path (PIC, FLIP or APIC)")
         if basis not in sc.BASIS_NAMES:
             raise KarameloError(f"shape function {basis} not supported: linear, cubic-spline, Bernstein-quadratic")
         self.s.basis = sc.BASIS_NAMES[basis]
         if self.s.basis == sc.BERNSTEIN and self.s.method == sc.ULMPM:
             raise KarameloError("Bernstein-quadratic shape functions are only supported with TLMPM")
+        if self.s.transfer == 1 and self.s.basis != sc.CUBIC:
+            raise KarameloError("APIC on the GPU path runs with the cubic spline")
         rest = list(rest)
         if sub == "FLIP":
             self.s.pic_flip = float(rest.pop(0))

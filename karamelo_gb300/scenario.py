@@ -138,6 +138,7 @@ class Scenario:
     basis: int = LINEAR
     dim: int = 3
     pic_flip: float = 0.99
+    transfer: int = 0            # 0: PIC/FLIP blend, 1: APIC (kmpm_params.transfer)
     thermal: bool = False
     dt: float = 1e-16            # Update::Update, src/update.cpp:38
     dt_factor: float = 0.9

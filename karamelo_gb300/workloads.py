@@ -46,21 +46,57 @@ def two_disks(backend_factory=None, cellsize=0.05, ppc=2, v0=0.1, method="ulmpm/
     return sim
 
 
+def spinning_disk(backend_factory=None, cellsize=0.05, ppc=2, omega=1.0, method="ulmpm/gpu", scheme="musl",
+                  sub="APIC", pic_flip=0.99, dt=1e-3):
+    """A linear-elastic disk (R = 0.2 m at the centre of a unit square, cubic
+    spline) in rigid rotation at omega rad/s: the case that separates APIC,
+    which transfers the rotation without loss, from PIC, which damps it."""
+    import numpy as np
+    sim = MPM(backend_factory)
+    _method(sim, method, sub, "cubic-spline", pic_flip)
+    sim.scheme(scheme)
+    sim.dimension(2, 0, 1, 0, 1, cellsize)
+    sim.region("rDisk", "cylinder", 0.5, 0.5, 0.2)
+    sim.material("mat1", "linear", 1000, 1e4, 0.3)
+    sim.solid("sDisk", "region", "rDisk", ppc, "mat1", cellsize, 0)
+    sol = sim.s.solids[0]
+    r = sol.x0 - np.array([0.5, 0.5, 0.0])
+    sol.v[:, 0] = -omega * r[:, 1]
+    sol.v[:, 1] = omega * r[:, 0]
+    sim.set_dt(dt)
+    return sim
+
+
+def angular_momentum(sim, centre=(0.5, 0.5)):
+    """L_z of solid 0 about centre: sum m ((x - xc) v_y - (y - yc) v_x)."""
+    import numpy as np
+    x, v = sim.particles(0, "x"), sim.particles(0, "v")
+    m = sim.s.solids[0].mass
+    return float(np.sum(m * ((x[:, 0] - centre[0]) * v[:, 1] - (x[:, 1] - centre[1]) * v[:, 0])))
+
+
 # Copper, units GPa / mm / ms.  E = 115 GPa and nu = 0.31 give the shear
 # modulus the Johnson-Cook law needs (examples/Taylor-bar/.../cylindrical_taylor_bar.mpm:5-8).
 COPPER = dict(E=115.0, nu=0.31, rho=8.94e-6, K=137.0, A=0.09, B=0.292, n=0.31, C=0.025, epsdot0=1e-3,
               m=0.0, Tr=25.0, Tm=1600.0)
 
 
+def _method(sim, method, sub, basis, pic_flip):
+    if sub == "FLIP":
+        sim.method(method, sub, basis, pic_flip)
+    else:
+        sim.method(method, sub, basis)
+
+
 def taylor_bar(backend_factory=None, cellsize=0.2, R=3.2, L=32.4, ppc=2, v0=190.0, method="tlmpm/gpu",
-               scheme="musl", basis="cubic-spline", pic_flip=0.99, dt_factor=0.1, params=None):
+               scheme="musl", basis="cubic-spline", pic_flip=0.99, dt_factor=0.1, params=None, sub="FLIP"):
     p = dict(COPPER)
     if params:
         p.update(params)
     G = p["E"] / (2 * (1 + p["nu"]))
     hL = L / 2
     sim = MPM(backend_factory)
-    sim.method(method, "FLIP", basis, pic_flip)
+    _method(sim, method, sub, basis, pic_flip)
     sim.scheme(scheme)
     x_wall = hL
     Df = 2.5 * R
@@ -85,9 +121,9 @@ def taylor_bar_wall(sim):
 
 def dam_break(backend_factory=None, cellsize=0.005, Lx=1.6, Ly=0.4, Lz=0.8, wx=0.4, wy=0.4, wz=0.8, ppc=2,
               method="ulmpm/gpu", scheme="musl", basis="cubic-spline", pic_flip=0.99, dt_factor=0.1,
-              K=2e6, gamma=7.0, rho0=1000.0, mu=1e-3, g=-9.81):
+              K=2e6, gamma=7.0, rho0=1000.0, mu=1e-3, g=-9.81, sub="FLIP"):
     sim = MPM(backend_factory)
-    sim.method(method, "FLIP", basis, pic_flip)
+    _method(sim, method, sub, basis, pic_flip)
     sim.scheme(scheme)
     sim.dimension(3, 0, Lx, 0, Ly, 0, Lz, cellsize)
     sim.eos("eosf", "fluid", rho0, K, gamma)

@@ -337,6 +337,7 @@ struct Solid {
   std::vector<std::vector<double>> wf_pn, wf_np;
   std::vector<std::vector<double>> wfd_pn, wfd_np;  // 3 per entry
   double dtCFL;
+  double Di[3] = {1, 1, 1};  // APIC inertia tensor inverse (diagonal), Solid::compute_inertia_tensor
 };
 
 enum { FIX_VEL_NODES = 0, FIX_BODY_FORCE = 1 };
@@ -350,6 +351,7 @@ struct Fix {
 struct Sim {
   int method, scheme, basis, dim;
   double pic_flip;
+  bool apic = false;  // sub-method APIC (src/update.cpp:129-149, src/tlmpm.cpp:82-84, src/ulmpm.cpp:79-82)
   bool thermal;
   double dt, dt_factor;
   bool dt_constant;
@@ -433,8 +435,16 @@ void grid_init(Sim &s, Grid &g, const double *boundlo, const double *boundhi, do
 // TLMPM/ULMPM::compute_grid_weight_functions_and_gradients,
 // src/tlmpm.cpp:87-340 and src/ulmpm.cpp:88-337.  TL uses x0 relative to the
 // solid's lower bound, UL uses x relative to the box.
+// Solid::compute_inertia_tensor, src/solid.cpp:1440-1478, cubic spline:
+// Di = 3 / cellsize^2 on the active dimensions, 1 on the others
+void compute_inertia_tensor(const Sim &s, Solid &S) {
+  const double c = s.grids[S.grid].cellsize;
+  for (int d = 0; d < 3; d++) S.Di[d] = d < s.dim ? 3.0 / (c * c) : 1.0;
+}
+
 void build_neighbours(Sim &s, Solid &S) {
   Grid &g = s.grids[S.grid];
+  if (s.apic) compute_inertia_tensor(s, S);
   const std::vector<double> &xp = (s.method == TLMPM) ? S.x0 : S.x;
   const double *lo = (s.method == TLMPM) ? g.lo : s.boxlo;
   double ih = 1.0 / g.cellsize;
@@ -511,8 +521,13 @@ void compute_mass_nodes(Solid &S, Grid &g, bool reset) {
   }
 }
 
-// Solid::compute_velocity_nodes, src/solid.cpp:337-390
-void compute_velocity_nodes(Solid &S, Grid &g, bool reset) {
+// Solid::compute_velocity_nodes, src/solid.cpp:337-390, and with APIC
+// Solid::compute_velocity_nodes_APIC, src/solid.cpp:392-426: the particle
+// velocity plus C (x0_node - x_p), C = Fdot (TL) or L (UL), x_p = x0 (TL) or x (UL)
+void compute_velocity_nodes(const Sim &s, Solid &S, Grid &g, bool reset) {
+  const bool TL = s.method == TLMPM;
+  const std::vector<double> &pos = TL ? S.x0 : S.x;
+  const std::vector<M3> &C = TL ? S.Fdot : S.L;
 #pragma omp parallel for schedule(static)
   for (int in = 0; in < g.nn; in++) {
     if (reset) for (int d = 0; d < 3; d++) g.v[3 * in + d] = 0;
@@ -521,7 +536,13 @@ void compute_velocity_nodes(Solid &S, Grid &g, bool reset) {
       for (size_t j = 0; j < S.neigh_np[in].size(); j++) {
         int ip = S.neigh_np[in][j];
         double wm = S.wf_np[in][j] * S.mass[ip];
-        for (int d = 0; d < 3; d++) vt[d] += wm * S.v[3 * ip + d];
+        double vp[3] = {S.v[3 * ip], S.v[3 * ip + 1], S.v[3 * ip + 2]};
+        if (s.apic) {
+          double dx[3];
+          for (int d = 0; d < 3; d++) dx[d] = g.x0[3 * in + d] - pos[3 * ip + d];
+          for (int d = 0; d < 3; d++) vp[d] += C[ip](d, 0) * dx[0] + C[ip](d, 1) * dx[1] + C[ip](d, 2) * dx[2];
+        }
+        for (int d = 0; d < 3; d++) vt[d] += wm * vp[d];
       }
       for (int d = 0; d < 3; d++) g.v[3 * in + d] += vt[d] / g.mass[in];
     }
@@ -862,7 +883,7 @@ bool step(Sim &s) {
     }
     for (auto &S : s.solids) {
       Grid &g = s.grids[S.grid];
-      compute_velocity_nodes(S, g, true);
+      compute_velocity_nodes(s, S, g, true);
       compute_external_forces_nodes(S, g, true);
       compute_internal_forces_nodes_TL(S, g);
       if (s.thermal) {
@@ -874,7 +895,7 @@ bool step(Sim &s) {
     Grid &g = s.grids[0];
     for (size_t i = 0; i < s.solids.size(); i++) compute_mass_nodes(s.solids[i], g, i == 0);
     for (size_t i = 0; i < s.solids.size(); i++) {
-      compute_velocity_nodes(s.solids[i], g, i == 0);
+      compute_velocity_nodes(s, s.solids[i], g, i == 0);
       compute_forces_nodes_UL(s.solids[i], g, i == 0);
       if (s.thermal) {
         compute_temperature_nodes(s.solids[i], g, i == 0);
@@ -921,14 +942,28 @@ bool step(Sim &s) {
   auto rate = [&](Solid &S, bool doublemapping) {
     Grid &g = s.grids[S.grid];
     const std::vector<double> &vn = doublemapping ? g.v : g.vu;
+    const std::vector<double> &pos = TL ? S.x0 : S.x;
 #pragma omp parallel for schedule(static)
     for (int ip = 0; ip < S.np; ip++) {
       M3 G = zero3();
-      for (size_t j = 0; j < S.neigh_pn[ip].size(); j++) {
-        int in = S.neigh_pn[ip][j];
-        const double *gw = &S.wfd_pn[ip][3 * j];
-        for (int a = 0; a < s.dim; a++)
-          for (int b = 0; b < s.dim; b++) G(a, b) += vn[3 * in + a] * gw[b];
+      if (s.apic) {
+        // compute_rate_deformation_gradient_{TL,UL}_APIC, src/solid.cpp:1006-1153:
+        // sum w v_node (x0_node - x_p)^T, times Di
+        for (size_t j = 0; j < S.neigh_pn[ip].size(); j++) {
+          int in = S.neigh_pn[ip][j];
+          const double w = S.wf_pn[ip][j];
+          for (int a = 0; a < s.dim; a++)
+            for (int b = 0; b < s.dim; b++) G(a, b) += vn[3 * in + a] * (g.x0[3 * in + b] - pos[3 * ip + b]) * w;
+        }
+        for (int a = 0; a < 3; a++)
+          for (int b = 0; b < 3; b++) G(a, b) *= S.Di[b];
+      } else {
+        for (size_t j = 0; j < S.neigh_pn[ip].size(); j++) {
+          int in = S.neigh_pn[ip][j];
+          const double *gw = &S.wfd_pn[ip][3 * j];
+          for (int a = 0; a < s.dim; a++)
+            for (int b = 0; b < s.dim; b++) G(a, b) += vn[3 * in + a] * gw[b];
+        }
       }
       if (TL) S.Fdot[ip] = G;  // src/solid.cpp:798-858
       else S.L[ip] = G;        // src/solid.cpp:860-936
@@ -984,12 +1019,12 @@ bool step(Sim &s) {
     // velocities_to_grid: src/tlmpm.cpp:440-452, src/ulmpm.cpp:476-496
     if (TL) {
       for (auto &S : s.solids) {
-        compute_velocity_nodes(S, s.grids[S.grid], true);
+        compute_velocity_nodes(s, S, s.grids[S.grid], true);
         if (s.thermal) compute_temperature_nodes(S, s.grids[S.grid], true);
       }
     } else {
       for (size_t i = 0; i < s.solids.size(); i++) {
-        compute_velocity_nodes(s.solids[i], s.grids[0], i == 0);
+        compute_velocity_nodes(s, s.solids[i], s.grids[0], i == 0);
         if (s.thermal) compute_temperature_nodes(s.solids[i], s.grids[0], i == 0);
       }
     }
@@ -1046,6 +1081,15 @@ void *om_create(int method, int scheme, int basis, int dim, double pic_flip, int
   return s;
 }
 void om_destroy(void *h) { delete (Sim *)h; }
+// sub-method APIC: PIC velocity update (PIC_FLIP = 0) and affine transfers;
+// the reference supports it with the cubic spline (and linear TLMPM)
+int om_set_apic(void *h, int on) {
+  Sim *s = (Sim *)h;
+  if (on && s->basis != CUBIC) { s->err = "APIC is restated for the cubic spline"; return -1; }
+  s->apic = on != 0;
+  if (s->apic) s->pic_flip = 0;
+  return 0;
+}
 const char *om_error(void *h) { return ((Sim *)h)->err.c_str(); }
 
 int om_add_material(void *h, const om_material *m) {

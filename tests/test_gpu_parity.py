@@ -30,7 +30,8 @@ def pair(oracle_mod, build, steps, **kw):
 
 
 def _cpu(build):
-    return {W.taylor_bar: "tlmpm", W.two_disks: "ulmpm", W.dam_break: "ulmpm", W.tensile_bar_2d: "tlmpm"}[build]
+    return {W.taylor_bar: "tlmpm", W.two_disks: "ulmpm", W.dam_break: "ulmpm", W.tensile_bar_2d: "tlmpm",
+            W.spinning_disk: "ulmpm"}[build]
 
 
 def check(g, o, tol, solid=0):
@@ -239,3 +240,32 @@ def test_shock_eos_artificial_viscosity(gpu_lib, oracle_mod):
 def test_hyperelastic_and_linear_materials(gpu_lib, oracle_mod, kind):
     g, o = _pair_block(oracle_mod, 150, strength="linear", mat_kind=kind, v0=30.0)
     check(g, o, {"x": 1e-6, "v": 1e-3, "sigma": 1e-3})
+
+
+# ---------------------------------------------------------------- APIC (§8(f) next row 1)
+@pytest.mark.parametrize("scheme", ["musl", "usl"])
+def test_taylor_bar_apic(gpu_lib, oracle_mod, scheme):
+    """TLMPM with APIC transfers (compute_velocity_nodes_APIC and
+    compute_rate_deformation_gradient_TL_APIC, src/solid.cpp:392-426,
+    1006-1080): the Johnson-Cook bar at the wall, cubic spline."""
+    g, o = pair(oracle_mod, W.taylor_bar, [1, W.taylor_bar_wall, 50], cellsize=0.8, scheme=scheme,
+                method="tlmpm/gpu", sub="APIC")
+    check(g, o, {"x": 1e-6, "v": 1e-4, "sigma": 1e-4, "eps_p": 1e-4, "F": 1e-6})
+
+
+@pytest.mark.parametrize("method,scheme", [("ulmpm/gpu", "musl"), ("ulmpm/gpu", "usl"), ("tlmpm/gpu", "musl")])
+def test_spinning_disk_apic(gpu_lib, oracle_mod, method, scheme):
+    """A spinning linear-elastic disk with APIC (ULMPM takes x_p before the
+    move for USL and after it for MUSL): state and angular momentum.  The
+    stress is the small centrifugal load (rho omega^2 R^2 = 40 Pa against
+    E = 1e4 Pa), so its FP32 relative error is larger than in the loaded cases."""
+    g, o = pair(oracle_mod, W.spinning_disk, [1, 150], method=method, scheme=scheme)
+    check(g, o, {"x": 1e-6, "v": 1e-4, "sigma": 3e-3})
+    Lg, Lo = W.angular_momentum(g), W.angular_momentum(o)
+    assert abs(Lg / Lo - 1) < 1e-4
+
+
+def test_dam_break_apic(gpu_lib, oracle_mod):
+    """The ULMPM dam break (fluid EOS, viscosity, gravity, slip walls) with APIC."""
+    g, o = pair(oracle_mod, W.dam_break, [60], cellsize=0.05, method="ulmpm/gpu", sub="APIC")
+    check(g, o, {"x": 1e-6, "v": 1e-4, "sigma": 1e-3})
