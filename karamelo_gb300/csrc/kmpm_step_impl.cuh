@@ -118,6 +118,11 @@ __global__ void __launch_bounds__(256) k_p2g(P2GArgs a) {
   constexpr int QINP = (QIN + 3) & ~3;  // staged payload row, padded for float4 access
   constexpr int NSL = (NS + 31) / 32;  // stencil nodes per lane
   constexpr bool PAIR = (DIM == 3 && S == 4);  // lane owns (a,b,c) and (a,b,c+2)
+  // stencils of at most 16 nodes: the warp splits into NG lane groups of GS
+  // lanes on the same nodes; group g takes particles g, g + NG, ... of the
+  // cell, and a fixed butterfly of shuffles adds the groups before the flush
+  constexpr int GS = PAIR ? 32 : (NS <= 4 ? 4 : (NS <= 8 ? 8 : (NS <= 16 ? 16 : 32)));
+  constexpr int NG = 32 / GS;
   constexpr int SLAB = (Q * NF + 3) & ~3;
   constexpr int STAGE = 32 * 4 + 32 * QINP + 32 * DIM * S * 2;
 
@@ -152,13 +157,14 @@ __global__ void __launch_bounds__(256) k_p2g(P2GArgs a) {
     if (PAIR) {
       soff[u][0] = (lane & 15) >> 2; soff[u][1] = lane & 3; soff[u][2] = (lane >> 4) + 2 * u;
     } else {
-      const int sidx = lane + 32 * u;
+      const int sidx = (NG > 1 ? lane % GS : lane) + 32 * u;
       if (DIM == 3) { soff[u][0] = sidx / (S * S); soff[u][1] = (sidx / S) % S; soff[u][2] = sidx % S; }
       else if (DIM == 2) { soff[u][0] = sidx / S; soff[u][1] = sidx % S; soff[u][2] = 0; }
       else { soff[u][0] = sidx; soff[u][1] = 0; soff[u][2] = 0; }
     }
   }
-  const bool lane_active = PAIR || lane < NS;
+  const bool lane_active = PAIR || (NG > 1 ? lane % GS : lane) < NS;
+  const int grp = lane / GS;
 
   // the k-th cell of this warp's slab: local cell index (lx*TY + ly)*TZ + lz
   const int cell_base = tile_global * TS::NCELL + warp * L * TY * TZ;
@@ -262,21 +268,44 @@ __global__ void __launch_bounds__(256) k_p2g(P2GArgs a) {
       __syncwarp();
       // ---- accumulate (lane = stencil node); two particles per iteration for ILP
       if (lane_active) {
-        int j = 0;
-        for (; j + 1 < cnt; j += 2) {
-          p2g_particle<DIM, S, MODE, THERMAL, Q, QINP, NSL, NS, PAIR>(accr, spay + j * QINP, sbas + j * DIM * S, soff,
-                                                                      nco, lane);
-          p2g_particle<DIM, S, MODE, THERMAL, Q, QINP, NSL, NS, PAIR>(accr, spay + (j + 1) * QINP,
-                                                                      sbas + (j + 1) * DIM * S, soff, nco, lane);
+        const int nl = NG > 1 ? lane % GS : lane;  // node slot of this lane
+        if (NG == 1) {
+          int j = 0;
+          for (; j + 1 < cnt; j += 2) {
+            p2g_particle<DIM, S, MODE, THERMAL, Q, QINP, NSL, NS, PAIR>(accr, spay + j * QINP, sbas + j * DIM * S,
+                                                                        soff, nco, nl);
+            p2g_particle<DIM, S, MODE, THERMAL, Q, QINP, NSL, NS, PAIR>(accr, spay + (j + 1) * QINP,
+                                                                        sbas + (j + 1) * DIM * S, soff, nco, nl);
+          }
+          if (j < cnt)
+            p2g_particle<DIM, S, MODE, THERMAL, Q, QINP, NSL, NS, PAIR>(accr, spay + j * QINP, sbas + j * DIM * S,
+                                                                        soff, nco, nl);
+        } else {
+          int j = grp;
+          for (; j + NG < cnt; j += 2 * NG) {
+            p2g_particle<DIM, S, MODE, THERMAL, Q, QINP, NSL, NS, PAIR>(accr, spay + j * QINP, sbas + j * DIM * S,
+                                                                        soff, nco, nl);
+            p2g_particle<DIM, S, MODE, THERMAL, Q, QINP, NSL, NS, PAIR>(accr, spay + (j + NG) * QINP,
+                                                                        sbas + (j + NG) * DIM * S, soff, nco, nl);
+          }
+          if (j < cnt)
+            p2g_particle<DIM, S, MODE, THERMAL, Q, QINP, NSL, NS, PAIR>(accr, spay + j * QINP, sbas + j * DIM * S,
+                                                                        soff, nco, nl);
         }
-        if (j < cnt)
-          p2g_particle<DIM, S, MODE, THERMAL, Q, QINP, NSL, NS, PAIR>(accr, spay + j * QINP, sbas + j * DIM * S, soff,
-                                                                      nco, lane);
       }
       __syncwarp();
     }
+    // ---- add the lane groups (fixed butterfly: the same order on every run)
+    if (NG > 1) {
+#pragma unroll
+      for (int u = 0; u < NSL; u++)
+#pragma unroll
+        for (int q = 0; q < Q; q++)
+#pragma unroll
+          for (int o = GS; o < 32; o <<= 1) accr[u][q] += __shfl_xor_sync(0xffffffffu, accr[u][q], o);
+    }
     // ---- add into this warp's slab footprint (only this warp writes it)
-    if (lane_active) {
+    if (lane_active && grp == 0) {
 #pragma unroll
       for (int u = 0; u < NSL; u++) {
         if (!PAIR && lane + 32 * u >= NS) continue;
