@@ -179,6 +179,15 @@ int kmpm_solid_scalars(struct kmpm_ctx *ctx, int solid, double *time, double *dt
 int kmpm_download_particles(struct kmpm_ctx *ctx, int solid, int field, double *out);
 int kmpm_upload_particles(struct kmpm_ctx *ctx, int solid, int field, const double *in);
 
+/* Asynchronous download (no counterpart in the reference; the dump path of
+ * SURVEY's next rows): the field is gathered on the context's stream in
+ * order with the steps, then copied to `out` on a second stream while later
+ * kmpm_run calls proceed.  `out` must be page-locked host memory
+ * (cudaHostAlloc / cudaHostRegister) of n*width doubles and stays owned by
+ * the caller; its content is valid after kmpm_sync_downloads. */
+int kmpm_download_particles_async(struct kmpm_ctx *ctx, int solid, int field, double *out);
+int kmpm_sync_downloads(struct kmpm_ctx *ctx);
+
 /* Download one grid field (n*1 or n*3 doubles, reference node order). */
 int kmpm_download_grid(struct kmpm_ctx *ctx, int grid, int field, double *out);
 

@@ -116,6 +116,16 @@ struct kmpm_ctx {
   // device buffer of kmpm_download_particles (one field of one solid, FP64)
   double *d_dump = nullptr;
   size_t dump_cap = 0;
+  // asynchronous downloads: gathers on the step stream, copies on cst, one
+  // device buffer per download in flight (reused once its copy has ended)
+  cudaStream_t cst = nullptr;
+  struct AsyncBuf {
+    double *buf = nullptr;
+    size_t cap = 0;
+    cudaEvent_t gathered = nullptr, copied = nullptr;
+    bool busy = false;
+  };
+  std::vector<AsyncBuf> abufs;
   bool indep() const { return prm.independent != 0; }
   bool apic() const { return prm.transfer == KMPM_TRANSFER_APIC; }
   int smem_apic[3] = {0, 0, 0};  // dynamic shared memory of the APIC scatters (TL, UL, VEL)
@@ -972,6 +982,13 @@ int kmpm_destroy(kmpm_ctx *c) {
   dfree(c->d_cs); dfree(c->d_ce); dfree(c->d_ts); dfree(c->d_te); dfree(c->partial);
   dfree(c->d_fixes); dfree(c->d_fix_start); dfree(c->d_fix_count); dfree(c->d_scalars); dfree(c->d_dtcfl);
   dfree(c->d_dump);
+  if (c->cst) cudaStreamSynchronize(c->cst);
+  for (auto &b : c->abufs) {
+    dfree(b.buf);
+    if (b.gathered) cudaEventDestroy(b.gathered);
+    if (b.copied) cudaEventDestroy(b.copied);
+  }
+  if (c->cst) cudaStreamDestroy(c->cst);
   dfree(c->d_blob); dfree(c->d_lstats); dfree(c->d_log_count); dfree(c->d_log);
   dfree(c->d_err); dfree(c->d_blk_c); dfree(c->d_blk_h); dfree(c->d_eblk); dfree(c->d_eout);
   dfree(c->d_keys); dfree(c->d_vals); dfree(c->rtmp.k1); dfree(c->rtmp.v1); dfree(c->rtmp.hist); dfree(c->rtmp.tot);
@@ -1203,6 +1220,51 @@ int kmpm_download_particles(kmpm_ctx *c, int solid, int field, double *out) {
   CK(cudaGetLastError());
   CK(cudaMemcpyAsync(out, c->d_dump, sizeof(double) * need, cudaMemcpyDeviceToHost, c->st));
   CK(cudaStreamSynchronize(c->st));
+  return KMPM_OK;
+}
+
+int kmpm_download_particles_async(kmpm_ctx *c, int solid, int field, double *out) {
+  if (!c || !out || solid < 0 || solid >= (int)c->hsolids.size()) return KMPM_ERR_ARG;
+  if (!c->built) return fail(c, KMPM_ERR_STATE, "no particle state before the first run");
+  if (field == KMPM_P_STRAIN_EL && !c->prm.track_strain)
+    return fail(c, KMPM_ERR_STATE, "strain_el is tracked only with track_strain");
+  const int w = dump_width(field);
+  if (w == 0) return fail(c, KMPM_ERR_ARG, "unknown particle field");
+  const auto &S = c->hsolids[solid];
+  const size_t need = (size_t)S.n * w;
+  if (!c->cst) CK(cudaStreamCreateWithFlags(&c->cst, cudaStreamNonBlocking));
+  // a free buffer: one whose copy has ended, else a new one
+  kmpm_ctx::AsyncBuf *b = nullptr;
+  for (auto &x : c->abufs)
+    if (!x.busy || cudaEventQuery(x.copied) == cudaSuccess) { x.busy = false; b = &x; break; }
+  if (!b) {
+    c->abufs.emplace_back();
+    b = &c->abufs.back();
+    CK(cudaEventCreateWithFlags(&b->gathered, cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&b->copied, cudaEventDisableTiming));
+  }
+  if (need > b->cap) {
+    dfree(b->buf);
+    DALLOC(b->buf, need);
+    b->cap = need;
+  }
+  const int ri = c->TL() ? c->solid_range[solid] : 0;
+  const int rotate = c->TL() && c->mats[S.mat].type != KMPM_MAT_NEO_HOOKEAN;
+  launch_dump(part_args(c), ri, c->ranges[ri].count, solid, c->solid_base[solid], field, c->TL() ? 1 : 0, rotate,
+              c->T_ref, b->buf, c->st);
+  CK(cudaGetLastError());
+  CK(cudaEventRecord(b->gathered, c->st));
+  CK(cudaStreamWaitEvent(c->cst, b->gathered, 0));
+  CK(cudaMemcpyAsync(out, b->buf, sizeof(double) * need, cudaMemcpyDeviceToHost, c->cst));
+  CK(cudaEventRecord(b->copied, c->cst));
+  b->busy = true;
+  return KMPM_OK;
+}
+
+int kmpm_sync_downloads(kmpm_ctx *c) {
+  if (!c) return KMPM_ERR_ARG;
+  if (c->cst) CK(cudaStreamSynchronize(c->cst));
+  for (auto &b : c->abufs) b.busy = false;
   return KMPM_OK;
 }
 

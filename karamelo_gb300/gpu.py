@@ -33,7 +33,8 @@ EXPORTED = ["kmpm_create", "kmpm_destroy", "kmpm_last_error", "kmpm_add_material
             "kmpm_mlp_create", "kmpm_mlp_destroy", "kmpm_mlp_last_error", "kmpm_mlp_init", "kmpm_mlp_set_params",
             "kmpm_mlp_get_params", "kmpm_mlp_set_norm", "kmpm_mlp_get_norm", "kmpm_mlp_loss_grad", "kmpm_mlp_train",
             "kmpm_mlp_predict", "kmpm_mlp_predict_tc", "kmpm_log_start", "kmpm_log_stop", "kmpm_log_data",
-            "kmpm_jc_label", "kmpm_set_surrogate", "kmpm_surrogate_stats", "kmpm_tuning"]
+            "kmpm_jc_label", "kmpm_set_surrogate", "kmpm_surrogate_stats", "kmpm_tuning",
+            "kmpm_download_particles_async", "kmpm_sync_downloads"]
 
 MLP_NIN, MLP_NOUT, MLP_NPARAMS, MLP_NNORM = 15, 7, 35975, 74
 
@@ -119,6 +120,8 @@ def load(path: str = LIB_PATH):
     L.kmpm_set_surrogate.argtypes = [p, p, d]
     L.kmpm_surrogate_stats.argtypes = [p, ctypes.POINTER(ll)]
     L.kmpm_tuning.argtypes = [p]
+    L.kmpm_download_particles_async.argtypes = [p, i, i, fp]
+    L.kmpm_sync_downloads.argtypes = [p]
     L.kmpm_tuning.restype = ctypes.c_char_p
     _lib = L
     return L
@@ -213,6 +216,18 @@ class GpuBackend:
         out = np.zeros(n * w)
         self._ck(self.L.kmpm_download_particles(self.h, si, code, _dp(out)))
         return out.reshape(n, 3, 3) if w == 9 else (out.reshape(n, 3) if w == 3 else out)
+
+    def particles_async(self, si: int, field: str, out):
+        """Queue the download of one field into ``out``, a page-locked float64
+        torch tensor of n*width values (torch.empty(..., pin_memory=True));
+        valid after :meth:`sync_downloads`."""
+        code, w = PARTICLE_FIELDS[field]
+        assert out.dtype.is_floating_point and out.element_size() == 8 and out.is_pinned()
+        assert out.numel() == self.s.solids[si].np * w
+        self._ck(self.L.kmpm_download_particles_async(self.h, si, code, out.data_ptr()))
+
+    def sync_downloads(self):
+        self._ck(self.L.kmpm_sync_downloads(self.h))
 
     def upload_velocity(self, si: int, v):
         v = np.ascontiguousarray(v, float)

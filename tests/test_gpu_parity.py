@@ -269,3 +269,25 @@ def test_dam_break_apic(gpu_lib, oracle_mod):
     """The ULMPM dam break (fluid EOS, viscosity, gravity, slip walls) with APIC."""
     g, o = pair(oracle_mod, W.dam_break, [60], cellsize=0.05, method="ulmpm/gpu", sub="APIC")
     check(g, o, {"x": 1e-6, "v": 1e-4, "sigma": 1e-3})
+
+
+def test_async_downloads_match_sync(gpu_lib):
+    """A download queued between runs holds the state of that moment, while
+    later steps run on (gather in stream order, copy on a second stream)."""
+    import torch
+    g = W.taylor_bar(None, cellsize=0.8)
+    g._ensure_backend()
+    g.run(1)
+    W.taylor_bar_wall(g)
+    g.run(20)
+    be = g.backend
+    ref = {f: be.particles(0, f) for f in ("x", "sigma", "eps_p")}
+    n = g.s.solids[0].np
+    out = {f: torch.empty(n * w, dtype=torch.float64, pin_memory=True) for f, w in (("x", 3), ("sigma", 9), ("eps_p", 1))}
+    for f, t in out.items():
+        be.particles_async(0, f, t)
+    g.run(30)
+    be.sync_downloads()
+    for f in ref:
+        assert np.array_equal(out[f].numpy().reshape(ref[f].shape), ref[f]), f
+    assert not np.array_equal(be.particles(0, "x"), ref["x"])
