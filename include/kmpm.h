@@ -44,6 +44,7 @@ extern "C" {
 #define KMPM_ULMPM 1
 #define KMPM_USL 0
 #define KMPM_MUSL 1
+#define KMPM_USF 2       /* USF::run, src/usf.cpp:34-95 (FLIP/PIC transfers, mechanical runs) */
 #define KMPM_BASIS_LINEAR 0
 #define KMPM_BASIS_CUBIC 1
 #define KMPM_BASIS_BERNSTEIN 2
@@ -60,7 +61,7 @@ extern "C" {
 
 typedef struct {
   int method;        /* KMPM_TLMPM / KMPM_ULMPM */
-  int scheme;        /* KMPM_USL / KMPM_MUSL (src/update.cpp:42-45 default MUSL) */
+  int scheme;        /* KMPM_USL / KMPM_MUSL / KMPM_USF (src/update.cpp:42-45 default MUSL) */
   int basis;         /* KMPM_BASIS_* */
   int dim;           /* 1, 2 or 3 (Domain::dimension) */
   double pic_flip;   /* Update::PIC_FLIP (0 for PIC) */

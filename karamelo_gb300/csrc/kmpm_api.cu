@@ -131,6 +131,7 @@ struct kmpm_ctx {
   int smem_apic[3] = {0, 0, 0};  // dynamic shared memory of the APIC scatters (TL, UL, VEL)
   bool TL() const { return prm.method == KMPM_TLMPM; }
   bool musl() const { return prm.scheme == KMPM_MUSL; }
+  bool usf() const { return prm.scheme == KMPM_USF; }
 };
 
 namespace {
@@ -771,6 +772,34 @@ int enqueue_step(kmpm_ctx *c) {
   // update_grid_state + fixes
   LAUNCH(c->K.grid_upd[TL][th][prec], c->nblk_g, 256, 0, g1);
   MARK("grid_update");
+  if (c->usf()) {
+    // USF::run (src/usf.cpp:43-86): the stress from the grid velocities of the
+    // first scatter (compute_rate_deformation_gradient(true)), then the
+    // forces of the new stress, the grid update and the particle update
+    PartArgs ps = pa;
+    ps.use_vu = 0;
+    LAUNCH((th || prec) ? c->K.g2p2[TL][th][prec] : c->K.g2p2_v[TL][c->var_g2p2], c->nblk_p, 256, 0, ps);
+    MARK("g2p_stress");
+    if (TL) LAUNCH(c->K.p2g_tl, c->ntiles_launch, 256, c->smem[1][0], p);
+    else LAUNCH(c->K.p2g_ul, c->ntiles_launch, 256, c->smem[2][0], p);
+    MARK("p2g_forces");
+    LAUNCH(c->K.grid_upd[TL][th][prec], c->nblk_g, 256, 0, g1);
+    MARK("grid_update2");
+    LAUNCH(c->K.g2p1_v[TL][c->var_g2p1], c->nblk_p, 256, 0, pa);
+    MARK("g2p_advance");
+    if (TL) {
+      GridArgs g2 = grid_args(c, 0);
+      LAUNCH(c->K.grid_vel[TL][th][prec], c->nblk_g, 256, 0, g2);
+      MARK("grid_positions");
+    }
+    DtArgs da = dt_args(c);
+    launch_dt(da, c->st);
+    nl += 2;
+    MARK("dt");
+    CK(cudaGetLastError());
+    c->launches_per_step = nl;
+    return KMPM_OK;
+  }
   // grid_to_points + advance_particles
   LAUNCH(th ? c->K.g2p1[TL][th] : c->K.g2p1_v[TL][c->var_g2p1], c->nblk_p, 256, 0, pa);
   MARK("g2p_advance");
@@ -950,7 +979,8 @@ int kmpm_create(const kmpm_params *params, kmpm_ctx **out) {
   *out = nullptr;
   const kmpm_params &p = *params;
   if (p.method != KMPM_TLMPM && p.method != KMPM_ULMPM) return KMPM_ERR_ARG;
-  if (p.scheme != KMPM_USL && p.scheme != KMPM_MUSL) return KMPM_ERR_ARG;
+  if (p.scheme != KMPM_USL && p.scheme != KMPM_MUSL && p.scheme != KMPM_USF) return KMPM_ERR_ARG;
+  if (p.scheme == KMPM_USF && (p.transfer != KMPM_TRANSFER_FLIP || p.thermal)) return KMPM_ERR_ARG;
   if (p.basis < 0 || p.basis > 2 || p.dim < 1 || p.dim > 3) return KMPM_ERR_ARG;
   if (p.method == KMPM_ULMPM && p.basis == KMPM_BASIS_BERNSTEIN) return KMPM_ERR_ARG;
   if (p.independent && p.method != KMPM_TLMPM) return KMPM_ERR_ARG;  // ULMPM solids share one grid
@@ -1374,8 +1404,9 @@ const char *kmpm_tuning(kmpm_ctx *c) { return c ? c->tuning.c_str() : "{}"; }
 static int learn_check(kmpm_ctx *c) {
   if (!c->TL() || c->prm.dim != 3 || c->prm.basis != KMPM_BASIS_CUBIC)
     return fail(c, KMPM_ERR_ARG, "the learned return map covers 3-D TLMPM with the cubic B-spline basis");
-  if (c->prm.precision != KMPM_PREC_FP32 || c->prm.thermal || c->apic())
-    return fail(c, KMPM_ERR_ARG, "the learned return map needs FP32, FLIP/PIC transfers and no thermo-mechanical coupling");
+  if (c->prm.precision != KMPM_PREC_FP32 || c->prm.thermal || c->apic() || c->usf())
+    return fail(c, KMPM_ERR_ARG,
+                "the learned return map needs FP32, FLIP/PIC transfers, USL or MUSL and no thermo-mechanical coupling");
   for (const MatDev &m : c->mats)
     if (m.type != KMPM_MAT_EOS_STRENGTH || m.strength != 2)
       return fail(c, KMPM_ERR_ARG, "the learned return map needs eos-strength materials with Johnson-Cook strength");

@@ -135,8 +135,10 @@ class MPM:
             self.s.scheme = sc.USL
         elif base == "musl":
             self.s.scheme = sc.MUSL
+        elif base == "usf":
+            self.s.scheme = sc.USF
         else:
-            raise KarameloError(f"Illegal scheme style {style}: usl or musl")
+            raise KarameloError(f"Illegal scheme style {style}: usl, musl or usf")
 
     def set_dt(self, dt):
         """Update::set_dt, src/update.cpp:58-65."""

@@ -16,7 +16,7 @@ import numpy as np
 
 # method / scheme / basis codes (src/update.h:78-90 names)
 TLMPM, ULMPM = 0, 1
-USL, MUSL = 0, 1
+USL, MUSL, USF = 0, 1, 2
 LINEAR, CUBIC, BERNSTEIN = 0, 1, 2
 BASIS_NAMES = {"linear": LINEAR, "cubic-spline": CUBIC, "Bernstein-quadratic": BERNSTEIN}
 

@@ -256,7 +256,7 @@ double dbf_bern(double rs, int nt, double ih) {
 
 // ---------------------------------------------------------------- model
 enum { TLMPM = 0, ULMPM = 1 };
-enum { USL = 0, MUSL = 1 };
+enum { USL = 0, MUSL = 1, USF = 2 };
 enum { LINEAR = 0, CUBIC = 1, BERNSTEIN = 2 };
 enum { MAT_LINEAR = 0, MAT_NEO_HOOKEAN = 1, MAT_EOS_STRENGTH = 2 };
 enum { EOS_LINEAR = 0, EOS_SHOCK = 1, EOS_FLUID = 2 };
@@ -875,7 +875,9 @@ bool step(Sim &s) {
     S.dtCFL = 1.0e22;
     std::fill(S.mbp.begin(), S.mbp.end(), 0.0);
   }
-  // particles_to_grid: src/tlmpm.cpp:342-366, src/ulmpm.cpp:338-378
+  // particles_to_grid (src/tlmpm.cpp:342-366, src/ulmpm.cpp:338-378), body
+  // forces, update_grid_state and the velocity fixes
+  auto p2g_grid = [&]() {
   if (TL) {
     if (s.update_mass_nodes) {
       for (auto &S : s.solids) compute_mass_nodes(S, s.grids[S.grid], true);
@@ -938,6 +940,7 @@ bool step(Sim &s) {
         for (int d = 0; d < 3; d++)
           if (fx.set[d]) { g.vu[3 * in + d] = vnow[d]; g.v[3 * in + d] = vold[d]; }
   }
+  };
   // USL: compute_rate_deformation_gradient(false) before grid_to_points
   auto rate = [&](Solid &S, bool doublemapping) {
     Grid &g = s.grids[S.grid];
@@ -969,8 +972,8 @@ bool step(Sim &s) {
       else S.L[ip] = G;        // src/solid.cpp:860-936
     }
   };
-  if (!musl)
-    for (auto &S : s.solids) rate(S, false);
+  // grid_to_points and advance_particles
+  auto g2p = [&]() -> bool {
   // grid_to_points: Solid::compute_particle_accelerations_velocities_and_positions src/solid.cpp:576-635
   int left = -1;
   for (auto &S : s.solids) {
@@ -1015,6 +1018,43 @@ bool step(Sim &s) {
     for (int ip = 0; ip < S.np; ip++)
       for (int d = 0; d < 3; d++)
         S.v[3 * ip + d] = (1 - s.pic_flip) * S.vu[3 * ip + d] + s.pic_flip * (S.v[3 * ip + d] + s.dt * S.a[3 * ip + d]);
+    return true;
+  };
+  // update_time and adjust_dt
+  auto finish = [&]() -> bool {
+    // update_time: src/update.cpp:201-206
+    s.time += s.dt;
+    // adjust_dt: src/tlmpm.cpp:489-514, src/ulmpm.cpp:525-551
+    if (!s.dt_constant) {
+      double dtCFL = 1.0e22;
+      for (auto &S : s.solids) {
+        dtCFL = std::min(dtCFL, S.dtCFL);
+        if (dtCFL == 0 || std::isnan(dtCFL)) return fail(s, "dtCFL == 0 or nan");
+      }
+      s.dt = dtCFL * s.dt_factor;
+    }
+    return true;
+  };
+  if (s.scheme == USF) {
+    // USF::run, src/usf.cpp:43-86: velocities to the grid, stress from the
+    // grid velocities, then the forces of the new stress
+    p2g_grid();
+    for (auto &S : s.solids) rate(S, true);
+    for (auto &S : s.solids)
+      if (!update_deformation_gradient(s, S)) return false;
+    for (auto &S : s.solids)
+      if (!update_stress(s, S)) return false;
+    p2g_grid();
+    if (!g2p()) return false;
+    if (TL)
+      for (auto &g : s.grids)
+        for (int q = 0; q < 3 * g.nn; q++) g.x[q] += s.dt * g.v[q];
+    return finish();
+  }
+  p2g_grid();
+  if (!musl)
+    for (auto &S : s.solids) rate(S, false);
+  if (!g2p()) return false;
   if (musl) {
     // velocities_to_grid: src/tlmpm.cpp:440-452, src/ulmpm.cpp:476-496
     if (TL) {
@@ -1050,18 +1090,7 @@ bool step(Sim &s) {
     if (!update_stress(s, S)) return false;
     if (s.thermal) update_heat_flux(s, S, musl);
   }
-  // update_time: src/update.cpp:201-206
-  s.time += s.dt;
-  // adjust_dt: src/tlmpm.cpp:489-514, src/ulmpm.cpp:525-551
-  if (!s.dt_constant) {
-    double dtCFL = 1.0e22;
-    for (auto &S : s.solids) {
-      dtCFL = std::min(dtCFL, S.dtCFL);
-      if (dtCFL == 0 || std::isnan(dtCFL)) return fail(s, "dtCFL == 0 or nan");
-    }
-    s.dt = dtCFL * s.dt_factor;
-  }
-  return true;
+  return finish();
 }
 
 }  // namespace

@@ -291,3 +291,28 @@ def test_async_downloads_match_sync(gpu_lib):
     for f in ref:
         assert np.array_equal(out[f].numpy().reshape(ref[f].shape), ref[f]), f
     assert not np.array_equal(be.particles(0, "x"), ref["x"])
+
+
+# ---------------------------------------------------------------- USF (§8(f) next row 4)
+@pytest.mark.parametrize("basis", ["cubic-spline", "linear"])
+def test_taylor_bar_usf(gpu_lib, oracle_mod, basis):
+    """USF::run (src/usf.cpp:34-95): stress from the first scatter's grid
+    velocities, then the forces of the new stress (TLMPM, Johnson-Cook bar)."""
+    g, o = pair(oracle_mod, W.taylor_bar, [1, W.taylor_bar_wall, 50], cellsize=0.8, basis=basis, scheme="usf",
+                method="tlmpm/gpu")
+    tol = dict(TAYLOR_TOL)
+    if basis == "linear":
+        tol.pop("eps_p")
+    check(g, o, tol)
+    assert abs(g.dt / o.dt - 1) < 1e-5
+
+
+def test_dam_break_usf(gpu_lib, oracle_mod):
+    g, o = pair(oracle_mod, W.dam_break, [60], cellsize=0.05, method="ulmpm/gpu", scheme="usf")
+    check(g, o, {"x": 1e-6, "v": 1e-4, "sigma": 1e-3})
+
+
+def test_tensile_bar_usf(gpu_lib, oracle_mod):
+    """2-D TLMPM tensile bar with Johnson-Cook damage under USF."""
+    g, o = pair(oracle_mod, W.tensile_bar_2d, [400], cellsize=0.5, scheme="usf", vend=20.0, ramp=False)
+    check(g, o, {"x": 1e-6, "v": 1e-3, "sigma": 1e-3})
