@@ -48,6 +48,7 @@ extern "C" {
 #define KMPM_BASIS_LINEAR 0
 #define KMPM_BASIS_CUBIC 1
 #define KMPM_BASIS_BERNSTEIN 2
+#define KMPM_BASIS_QUADRATIC 3  /* quadratic B-spline, src/basis_functions.h:140-241 */
 
 /* kmpm_params.transfer: the method's sub-type (Update::create_method,
  * src/update.cpp:129-149) */
@@ -82,7 +83,7 @@ typedef struct {
                         the particle state and keep the fastest (kmpm_tuning reports it) */
   int transfer;      /* KMPM_TRANSFER_FLIP (PIC/FLIP blend by pic_flip) or KMPM_TRANSFER_APIC
                         (method(..., APIC, ...): affine transfers, src/solid.cpp:392-426 and
-                        1006-1153; cubic spline, mechanical runs; sets pic_flip = 0) */
+                        1006-1153; cubic or quadratic spline, mechanical runs; sets pic_flip = 0) */
 } kmpm_params;
 
 /* One material: Mat (src/material.h:45-68) with its EOS / Strength / Damage /

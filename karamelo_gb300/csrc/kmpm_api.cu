@@ -981,12 +981,14 @@ int kmpm_create(const kmpm_params *params, kmpm_ctx **out) {
   if (p.method != KMPM_TLMPM && p.method != KMPM_ULMPM) return KMPM_ERR_ARG;
   if (p.scheme != KMPM_USL && p.scheme != KMPM_MUSL && p.scheme != KMPM_USF) return KMPM_ERR_ARG;
   if (p.scheme == KMPM_USF && (p.transfer != KMPM_TRANSFER_FLIP || p.thermal)) return KMPM_ERR_ARG;
-  if (p.basis < 0 || p.basis > 2 || p.dim < 1 || p.dim > 3) return KMPM_ERR_ARG;
+  if (p.basis < 0 || p.basis > 3 || p.dim < 1 || p.dim > 3) return KMPM_ERR_ARG;
   if (p.method == KMPM_ULMPM && p.basis == KMPM_BASIS_BERNSTEIN) return KMPM_ERR_ARG;
   if (p.independent && p.method != KMPM_TLMPM) return KMPM_ERR_ARG;  // ULMPM solids share one grid
   if (p.transfer != KMPM_TRANSFER_FLIP && p.transfer != KMPM_TRANSFER_APIC) return KMPM_ERR_ARG;
   // APIC: the cubic spline (Di = 3/h^2), mechanical runs
-  if (p.transfer == KMPM_TRANSFER_APIC && (p.basis != KMPM_BASIS_CUBIC || p.thermal)) return KMPM_ERR_ARG;
+  if (p.transfer == KMPM_TRANSFER_APIC &&
+      ((p.basis != KMPM_BASIS_CUBIC && p.basis != KMPM_BASIS_QUADRATIC) || p.thermal))
+    return KMPM_ERR_ARG;
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return KMPM_ERR_CUDA;
   kmpm_ctx *c = new kmpm_ctx();

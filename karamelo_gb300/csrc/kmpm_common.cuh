@@ -140,6 +140,8 @@ template <int BASIS> struct Stencil;
 template <> struct Stencil<0> { static constexpr int S = 2, LO = 0, SC = 1, C = 2; };
 template <> struct Stencil<1> { static constexpr int S = 4, LO = 1, SC = 1, C = 4; };
 template <> struct Stencil<2> { static constexpr int S = 3, LO = 0, SC = 2, C = 2; };
+// quadratic B-spline: the cubic stencil (src/ulmpm.cpp:204-207, src/tlmpm.cpp:209-245)
+template <> struct Stencil<3> { static constexpr int S = 4, LO = 1, SC = 1, C = 4; };
 
 // Tiles of TX x TY x TZ cells.  The scatter kernel gives every warp of the
 // tile an x-slab of L = TX / NWARP cell layers; the warp accumulates its slab
@@ -169,13 +171,13 @@ __host__ __device__ inline void tile_dims(int dim, int basis, int *t) {
   t[1] = dim == 3 ? 4 : (dim == 2 ? 16 : 1);
   t[2] = dim == 3 ? 4 : 1;
 }
-__host__ __device__ inline int stencil_width(int basis) { return basis == 0 ? 2 : (basis == 1 ? 4 : 3); }
-__host__ __device__ inline int stencil_lo(int basis) { return basis == 1 ? 1 : 0; }
+__host__ __device__ inline int stencil_width(int basis) { return basis == 0 ? 2 : (basis == 2 ? 3 : 4); }
+__host__ __device__ inline int stencil_lo(int basis) { return (basis == 1 || basis == 3) ? 1 : 0; }
 __host__ __device__ inline int stencil_sc(int basis) { return basis == 2 ? 2 : 1; }
 
 // ntype of a node along one axis (Grid::init, src/grid.cpp:228-240)
 template <int BASIS> __device__ __forceinline__ int node_type(int i, int ng) {
-  if (BASIS == 1) return min(2, i) - min(ng - 1 - i, 2);
+  if (BASIS == 1 || BASIS == 3) return min(2, i) - min(ng - 1 - i, 2);
   if (BASIS == 2) return i & 1;
   return 0;
 }
@@ -221,6 +223,31 @@ template <> __device__ __forceinline__ void basis<2>(float r, int nt, float ih, 
   } else {
     s = (1.f - a) * (1.f - a);
     ds = r > 0.f ? -2.f * (1.f - r) * ih : 2.f * (1.f + r) * ih;
+  }
+}
+
+// BasisFunction::quadratic_spline and its derivative, src/basis_functions.h:140-241
+template <> __device__ __forceinline__ void basis<3>(float r, int nt, float ih, float &s, float &ds) {
+  s = 0.f;
+  ds = 0.f;
+  if (nt == 0) {
+    if (r >= 0.5f && r < 1.5f) { s = (0.5f * r - 1.5f) * r + 1.125f; ds = ih * (r - 1.5f); }
+    else if (r >= -0.5f && r < 0.5f) { s = -r * r + 0.75f; ds = -2.f * ih * r; }
+    else if (r >= -1.5f && r < 0.5f) { s = (0.5f * r + 1.5f) * r + 1.125f; ds = ih * (r + 1.5f); }
+  } else if (nt == -2) {
+    if (r >= 0.f && r < 0.5f) { s = 1.f - r; ds = -ih; }
+    else if (r >= 0.5f && r < 1.5f) { s = (0.5f * r - 1.5f) * r + 1.125f; ds = ih * (r - 1.5f); }
+  } else if (nt == -1) {
+    if (r >= -1.f && r < -0.5f) { s = 1.f + r; ds = ih; }
+    else if (r >= -0.5f && r < 0.5f) { s = -r * r + 0.75f; ds = -2.f * ih * r; }
+    else if (r >= 0.5f && r < 1.5f) { s = (0.5f * r - 1.5f) * r + 1.125f; ds = ih * (r - 1.5f); }
+  } else if (nt == 1) {
+    if (r >= -1.5f && r < -0.5f) { s = (0.5f * r + 1.5f) * r + 1.125f; ds = ih * (r + 1.5f); }
+    else if (r >= -0.5f && r < 0.5f) { s = -r * r + 0.75f; ds = -2.f * ih * r; }
+    else if (r >= 0.5f && r < 1.f) { s = 1.f - r; ds = -ih; }
+  } else {
+    if (r >= -1.5f && r < -0.5f) { s = (0.5f * r + 1.5f) * r + 1.125f; ds = ih * (r + 1.5f); }
+    else if (r >= -0.5f && r <= 0.f) { s = 1.f + r; ds = ih; }
   }
 }
 

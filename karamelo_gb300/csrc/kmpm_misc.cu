@@ -370,12 +370,16 @@ void get_step_kernels_2_2(StepKernels &k);
 void get_step_kernels_3_0(StepKernels &k);
 void get_step_kernels_3_1(StepKernels &k);
 void get_step_kernels_3_2(StepKernels &k);
+void get_step_kernels_1_3(StepKernels &k);
+void get_step_kernels_2_3(StepKernels &k);
+void get_step_kernels_3_3(StepKernels &k);
 
 void get_step_kernels(int dim, int basis, StepKernels &k) {
   typedef void (*F)(StepKernels &);
-  static const F tab[3][3] = {{get_step_kernels_1_0, get_step_kernels_1_1, get_step_kernels_1_2},
-                              {get_step_kernels_2_0, get_step_kernels_2_1, get_step_kernels_2_2},
-                              {get_step_kernels_3_0, get_step_kernels_3_1, get_step_kernels_3_2}};
+  static const F tab[3][4] = {
+      {get_step_kernels_1_0, get_step_kernels_1_1, get_step_kernels_1_2, get_step_kernels_1_3},
+      {get_step_kernels_2_0, get_step_kernels_2_1, get_step_kernels_2_2, get_step_kernels_2_3},
+      {get_step_kernels_3_0, get_step_kernels_3_1, get_step_kernels_3_2, get_step_kernels_3_3}};
   tab[dim - 1][basis](k);
 }
 

@@ -611,14 +611,15 @@ __global__ void __launch_bounds__(256, MINB) k_g2p2(PartArgs a) {
     ax.eval(g, xp);
     constexpr int S = Stencil<BASIS>::S;
     constexpr int SY = DIM >= 2 ? S : 1, SZ = DIM == 3 ? S : 1;
-    if (BASIS == 1 && a.apic) {
+    if ((BASIS == 1 || BASIS == 3) && a.apic) {
       // APIC (compute_rate_deformation_gradient_{TL,UL}_APIC,
       // src/solid.cpp:1006-1153): grad v = sum w v_node (x_node - x_p)^T Di with
-      // Di = 3 / cellsize^2 (Solid::compute_inertia_tensor, src/solid.cpp:1440-1478).
+      // Di = 3 / cellsize^2 (cubic) or 4 / cellsize^2 (quadratic)
+      // (Solid::compute_inertia_tensor, src/solid.cpp:1440-1478).
       // The per-axis moment s (x_node - x_p) Di takes the place of the slope;
       // x_p is x0 (TL), and for ULMPM the position the reference holds at this
       // point: before the move (USL) or after it (MUSL)
-      const float Di = 3.f * g.inv_cellsize * g.inv_cellsize;
+      const float Di = (BASIS == 3 ? 4.f : 3.f) * g.inv_cellsize * g.inv_cellsize;
 #pragma unroll
       for (int d = 0; d < DIM; d++) {
         const float pd = P[(PF_X0 + d) * ps + p] + (TL ? 0.f : P[((a.use_vu ? PF_X : PF_XN) + d) * ps + p]);
@@ -680,7 +681,7 @@ __global__ void __launch_bounds__(256, MINB) k_g2p2(PartArgs a) {
         }
       }
     }
-    if (BASIS == 1 && a.apic)
+    if ((BASIS == 1 || BASIS == 3) && a.apic)
 #pragma unroll
       for (int k = 0; k < 9; k++) P[(PF_C + k) * ps + p] = G[k];  // C of the next transfers
     // ---- deformation gradient (src/solid.cpp:1155-1244), stored as H = F - I
@@ -913,7 +914,7 @@ void fill_step_kernels(StepKernels &k) {
   k.p2g_ul_th = (void *)k_p2g<DIM, BASIS, P2G_UL, true>;
   k.p2g_vel = (void *)k_p2g<DIM, BASIS, P2G_VEL, false>;
   k.p2g_vel_th = (void *)k_p2g<DIM, BASIS, P2G_VEL, true>;
-  if constexpr (BASIS == 1) {  // APIC runs with the cubic spline
+  if constexpr (BASIS == 1 || BASIS == 3) {  // APIC runs with the cubic and quadratic splines
     k.p2g_tl_apic = (void *)k_p2g<DIM, BASIS, P2G_TL_APIC, false>;
     k.p2g_ul_apic = (void *)k_p2g<DIM, BASIS, P2G_UL_APIC, false>;
     k.p2g_vel_apic = (void *)k_p2g<DIM, BASIS, P2G_VEL_APIC, false>;

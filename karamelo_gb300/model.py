@@ -107,12 +107,13 @@ class MPM:
         else:
             raise KarameloError(f"method type {sub} not supported on the GPU path (PIC, FLIP or APIC)")
         if basis not in sc.BASIS_NAMES:
-            raise KarameloError(f"shape function {basis} not supported: linear, cubic-spline, Bernstein-quadratic")
+            raise KarameloError(f"shape function {basis} not supported: linear, cubic-spline, quadratic-spline, "
+                                "Bernstein-quadratic")
         self.s.basis = sc.BASIS_NAMES[basis]
         if self.s.basis == sc.BERNSTEIN and self.s.method == sc.ULMPM:
             raise KarameloError("Bernstein-quadratic shape functions are only supported with TLMPM")
-        if self.s.transfer == 1 and self.s.basis != sc.CUBIC:
-            raise KarameloError("APIC on the GPU path runs with the cubic spline")
+        if self.s.transfer == 1 and self.s.basis not in (sc.CUBIC, sc.QUADRATIC):
+            raise KarameloError("APIC on the GPU path runs with the cubic or quadratic spline")
         rest = list(rest)
         if sub == "FLIP":
             self.s.pic_flip = float(rest.pop(0))

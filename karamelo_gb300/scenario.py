@@ -17,8 +17,9 @@ import numpy as np
 # method / scheme / basis codes (src/update.h:78-90 names)
 TLMPM, ULMPM = 0, 1
 USL, MUSL, USF = 0, 1, 2
-LINEAR, CUBIC, BERNSTEIN = 0, 1, 2
-BASIS_NAMES = {"linear": LINEAR, "cubic-spline": CUBIC, "Bernstein-quadratic": BERNSTEIN}
+LINEAR, CUBIC, BERNSTEIN, QUADRATIC = 0, 1, 2, 3
+BASIS_NAMES = {"linear": LINEAR, "cubic-spline": CUBIC, "Bernstein-quadratic": BERNSTEIN,
+               "quadratic-spline": QUADRATIC}
 
 # Mat::type (src/material.h:114-119) -- RIGID is not supported on the GPU path
 MAT_LINEAR, MAT_NEO_HOOKEAN, MAT_EOS_STRENGTH = 0, 1, 2

@@ -47,13 +47,13 @@ def two_disks(backend_factory=None, cellsize=0.05, ppc=2, v0=0.1, method="ulmpm/
 
 
 def spinning_disk(backend_factory=None, cellsize=0.05, ppc=2, omega=1.0, method="ulmpm/gpu", scheme="musl",
-                  sub="APIC", pic_flip=0.99, dt=1e-3):
-    """A linear-elastic disk (R = 0.2 m at the centre of a unit square, cubic
-    spline) in rigid rotation at omega rad/s: the case that separates APIC,
+                  sub="APIC", pic_flip=0.99, dt=1e-3, basis="cubic-spline"):
+    """A linear-elastic disk (R = 0.2 m at the centre of a unit square) in
+    rigid rotation at omega rad/s: the case that separates APIC,
     which transfers the rotation without loss, from PIC, which damps it."""
     import numpy as np
     sim = MPM(backend_factory)
-    _method(sim, method, sub, "cubic-spline", pic_flip)
+    _method(sim, method, sub, basis, pic_flip)
     sim.scheme(scheme)
     sim.dimension(2, 0, 1, 0, 1, cellsize)
     sim.region("rDisk", "cylinder", 0.5, 0.5, 0.2)

@@ -241,6 +241,65 @@ double dbf_cubic(double r, int nt, double ih) {
   if (r >= -2 && r < -1) return ih * ((0.5 * r + 2) * r + 2);
   return 0;
 }
+// BasisFunction::quadratic_spline / derivative_quadratic_spline,
+// src/basis_functions.h:140-241 (ranges restated as in the reference)
+double bf_quad(double r, int nt) {
+  if (nt == 0) {
+    if (r >= 0.5 && r < 1.5) return (0.5 * r - 1.5) * r + 1.125;
+    if (r >= -0.5 && r < 0.5) return -r * r + 0.75;
+    if (r >= -1.5 && r < 0.5) return (0.5 * r + 1.5) * r + 1.125;
+    return 0;
+  }
+  if (nt == -2) {
+    if (r >= 0. && r < 0.5) return 1 - r;
+    if (r >= 0.5 && r < 1.5) return (0.5 * r - 1.5) * r + 1.125;
+    return 0;
+  }
+  if (nt == -1) {
+    if (r >= -1. && r < -0.5) return 1 + r;
+    if (r >= -0.5 && r < 0.5) return -r * r + 0.75;
+    if (r >= 0.5 && r < 1.5) return (0.5 * r - 1.5) * r + 1.125;
+    return 0;
+  }
+  if (nt == 1) {
+    if (r >= -1.5 && r < -0.5) return (0.5 * r + 1.5) * r + 1.125;
+    if (r >= -0.5 && r < 0.5) return -r * r + 0.75;
+    if (r >= 0.5 && r < 1.) return 1 - r;
+    return 0;
+  }
+  if (r >= -1.5 && r < -0.5) return (0.5 * r + 1.5) * r + 1.125;
+  if (r >= -0.5 && r <= 0.) return 1 + r;
+  return 0;
+}
+double dbf_quad(double r, int nt, double ih) {
+  if (nt == 0) {
+    if (r >= 0.5 && r < 1.5) return ih * (r - 1.5);
+    if (r >= -0.5 && r < 0.5) return -2 * ih * r;
+    if (r >= -1.5 && r < 0.5) return ih * (r + 1.5);
+    return 0;
+  }
+  if (nt == -2) {
+    if (r >= 0. && r < 0.5) return -ih;
+    if (r >= 0.5 && r < 1.5) return ih * (r - 1.5);
+    return 0;
+  }
+  if (nt == -1) {
+    if (r >= -1. && r < -0.5) return ih;
+    if (r >= -0.5 && r < 0.5) return -2 * ih * r;
+    if (r >= 0.5 && r < 1.5) return ih * (r - 1.5);
+    return 0;
+  }
+  if (nt == 1) {
+    if (r >= -1.5 && r < -0.5) return ih * (r + 1.5);
+    if (r >= -0.5 && r < 0.5) return -2 * ih * r;
+    if (r >= 0.5 && r < 1.) return -ih;
+    return 0;
+  }
+  if (r >= -1.5 && r < -0.5) return ih * (r + 1.5);
+  if (r >= -0.5 && r <= 0.) return ih;
+  return 0;
+}
+
 double bf_bern(double r_, int nt) {
   double r = std::fabs(r_);
   if (r >= 1.0) return 0;
@@ -257,7 +316,7 @@ double dbf_bern(double rs, int nt, double ih) {
 // ---------------------------------------------------------------- model
 enum { TLMPM = 0, ULMPM = 1 };
 enum { USL = 0, MUSL = 1, USF = 2 };
-enum { LINEAR = 0, CUBIC = 1, BERNSTEIN = 2 };
+enum { LINEAR = 0, CUBIC = 1, BERNSTEIN = 2, QUADRATIC = 3 };
 enum { MAT_LINEAR = 0, MAT_NEO_HOOKEAN = 1, MAT_EOS_STRENGTH = 2 };
 enum { EOS_LINEAR = 0, EOS_SHOCK = 1, EOS_FLUID = 2 };
 enum { STR_LINEAR = 0, STR_PLASTIC = 1, STR_JC = 2, STR_SWIFT = 3, STR_FLUID = 4 };
@@ -417,7 +476,7 @@ void grid_init(Sim &s, Grid &g, const double *boundlo, const double *boundhi, do
           g.ntype[3 * l + 0] = i % 2;
           g.ntype[3 * l + 1] = j % 2;
           g.ntype[3 * l + 2] = k % 2;
-        } else if (s.basis == CUBIC) {
+        } else if (s.basis == CUBIC || s.basis == QUADRATIC) {
           g.ntype[3 * l + 0] = std::min(2, i) - std::min(g.nxg - 1 - i, 2);
           g.ntype[3 * l + 1] = std::min(2, j) - std::min(g.nyg - 1 - j, 2);
           g.ntype[3 * l + 2] = std::min(2, k) - std::min(g.nzg - 1 - k, 2);
@@ -435,11 +494,12 @@ void grid_init(Sim &s, Grid &g, const double *boundlo, const double *boundhi, do
 // TLMPM/ULMPM::compute_grid_weight_functions_and_gradients,
 // src/tlmpm.cpp:87-340 and src/ulmpm.cpp:88-337.  TL uses x0 relative to the
 // solid's lower bound, UL uses x relative to the box.
-// Solid::compute_inertia_tensor, src/solid.cpp:1440-1478, cubic spline:
-// Di = 3 / cellsize^2 on the active dimensions, 1 on the others
+// Solid::compute_inertia_tensor, src/solid.cpp:1440-1478: Di = 3 / cellsize^2
+// (cubic) or 4 / cellsize^2 (quadratic) on the active dimensions, 1 on the others
 void compute_inertia_tensor(const Sim &s, Solid &S) {
   const double c = s.grids[S.grid].cellsize;
-  for (int d = 0; d < 3; d++) S.Di[d] = d < s.dim ? 3.0 / (c * c) : 1.0;
+  const double k = s.basis == QUADRATIC ? 4.0 : 3.0;
+  for (int d = 0; d < 3; d++) S.Di[d] = d < s.dim ? k / (c * c) : 1.0;
 }
 
 void build_neighbours(Sim &s, Solid &S) {
@@ -1107,6 +1167,7 @@ void *om_create(int method, int scheme, int basis, int dim, double pic_flip, int
   for (int d = 0; d < 3; d++) { s->boxlo[d] = boxlo[d]; s->boxhi[d] = boxhi[d]; }
   if (basis == CUBIC) { s->bf = bf_cubic; s->dbf = dbf_cubic; }
   else if (basis == BERNSTEIN) { s->bf = bf_bern; s->dbf = dbf_bern; }
+  else if (basis == QUADRATIC) { s->bf = bf_quad; s->dbf = dbf_quad; }
   return s;
 }
 void om_destroy(void *h) { delete (Sim *)h; }
@@ -1114,7 +1175,10 @@ void om_destroy(void *h) { delete (Sim *)h; }
 // the reference supports it with the cubic spline (and linear TLMPM)
 int om_set_apic(void *h, int on) {
   Sim *s = (Sim *)h;
-  if (on && s->basis != CUBIC) { s->err = "APIC is restated for the cubic spline"; return -1; }
+  if (on && s->basis != CUBIC && s->basis != QUADRATIC) {
+    s->err = "APIC is restated for the cubic and quadratic splines";
+    return -1;
+  }
   s->apic = on != 0;
   if (s->apic) s->pic_flip = 0;
   return 0;
@@ -1275,6 +1339,7 @@ void om_energy(void *h, double *out) {
 double om_basis(int basis, int kind, double r, int ntype, double icellsize) {
   if (basis == LINEAR) return kind ? dbf_linear(r, ntype, icellsize) : bf_linear(r, ntype);
   if (basis == CUBIC) return kind ? dbf_cubic(r, ntype, icellsize) : bf_cubic(r, ntype);
+  if (basis == QUADRATIC) return kind ? dbf_quad(r, ntype, icellsize) : bf_quad(r, ntype);
   return kind ? dbf_bern(r, ntype, icellsize) : bf_bern(r, ntype);
 }
 // Constitutive kernels exposed for unit checks (strength + EOS on one state).

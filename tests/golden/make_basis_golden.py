@@ -23,7 +23,7 @@ def main():
                                   np.array([-1e-12, 1e-12, 0.999999999, -0.999999999, 1.999999999])]))
     out = {"r": r}
     icell = 2.5
-    for basis, ntypes in ((0, [0]), (1, [-2, -1, 0, 1, 2]), (2, [0, 1])):
+    for basis, ntypes in ((0, [0]), (1, [-2, -1, 0, 1, 2]), (2, [0, 1]), (3, [-2, -1, 0, 1, 2])):
         for nt in ntypes:
             for kind in (0, 1):
                 out[f"b{basis}_n{nt}_k{kind}"] = np.array([L.ref_basis(basis, kind, float(x), nt, icell) for x in r])

@@ -44,7 +44,8 @@ TAYLOR_TOL = {"x": 1e-6, "v": 1e-4, "sigma": 1e-4, "eps_p": 1e-4}
 
 
 @pytest.mark.parametrize("basis,scheme", [("cubic-spline", "musl"), ("cubic-spline", "usl"), ("linear", "usl"),
-                                          ("linear", "musl"), ("Bernstein-quadratic", "musl")])
+                                          ("linear", "musl"), ("Bernstein-quadratic", "musl"),
+                                          ("quadratic-spline", "musl"), ("quadratic-spline", "usl")])
 def test_taylor_bar_tlmpm(gpu_lib, oracle_mod, basis, scheme):
     """3-D TLMPM Johnson-Cook + linear EOS bar hitting the wall (the benchmark's
     physics at cellsize 0.8 mm): 1 step, wall fix, 50 steps."""
@@ -316,3 +317,17 @@ def test_tensile_bar_usf(gpu_lib, oracle_mod):
     """2-D TLMPM tensile bar with Johnson-Cook damage under USF."""
     g, o = pair(oracle_mod, W.tensile_bar_2d, [400], cellsize=0.5, scheme="usf", vend=20.0, ramp=False)
     check(g, o, {"x": 1e-6, "v": 1e-3, "sigma": 1e-3})
+
+
+# ---------------------------------------------------------------- quadratic spline (§8(f) next row 4)
+def test_dam_break_quadratic(gpu_lib, oracle_mod):
+    """ULMPM dam break with the quadratic B-spline (src/basis_functions.h:140-241)."""
+    g, o = pair(oracle_mod, W.dam_break, [60], cellsize=0.05, method="ulmpm/gpu", basis="quadratic-spline")
+    check(g, o, {"x": 1e-6, "v": 1e-4, "sigma": 1e-3})
+
+
+def test_spinning_disk_apic_quadratic(gpu_lib, oracle_mod):
+    """APIC with the quadratic spline (Di = 4 / h^2)."""
+    g, o = pair(oracle_mod, W.spinning_disk, [1, 150], method="ulmpm/gpu", scheme="musl", basis="quadratic-spline")
+    check(g, o, {"x": 1e-6, "v": 1e-4, "sigma": 3e-3})
+    assert abs(W.angular_momentum(g) / W.angular_momentum(o) - 1) < 1e-4

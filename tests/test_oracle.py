@@ -25,7 +25,7 @@ def test_basis_matches_reference_golden(oracle_mod):
         mine = np.array([oracle_mod.basis(basis, kind, x, ntype, icell) for x in r])
         np.testing.assert_array_equal(mine, g[key], err_msg=key)
         n += 1
-    assert n == 16
+    assert n == 26
 
 
 def test_basis_live_reference_if_present(oracle_mod):
@@ -34,8 +34,8 @@ def test_basis_live_reference_if_present(oracle_mod):
         pytest.skip("reference tree not present (golden vectors cover this)")
     rng = np.random.default_rng(0)
     for _ in range(2000):
-        basis = int(rng.integers(0, 3))
-        nt = int(rng.choice([-2, -1, 0, 1, 2] if basis == 1 else ([0, 1] if basis == 2 else [0])))
+        basis = int(rng.integers(0, 4))
+        nt = int(rng.choice([-2, -1, 0, 1, 2] if basis in (1, 3) else ([0, 1] if basis == 2 else [0])))
         x = float(rng.uniform(-2.5, 2.5))
         for kind in (0, 1):
             assert oracle_mod.basis(basis, kind, x, nt, 3.0) == L.ref_basis(basis, kind, x, nt, 3.0)
