@@ -54,6 +54,9 @@ extern "C" {
  * src/update.cpp:129-149) */
 #define KMPM_TRANSFER_FLIP 0
 #define KMPM_TRANSFER_APIC 1
+#define KMPM_TRANSFER_AFLIP 2   /* ULMPM: affine transfers with the FLIP blend; TLMPM: as FLIP */
+#define KMPM_TRANSFER_ASFLIP 3  /* AFLIP with positions moved by the blended velocity (ULMPM) */
+#define KMPM_TRANSFER_MLS 4     /* ULMPM only: APIC with internal forces from moments */
 
 /* kmpm_params.precision: arithmetic of the three places that the FP32 bulk
  * may promote (nodal v = p/m, det/inverse of F, the constitutive return) */
@@ -81,9 +84,10 @@ typedef struct {
   int autotune;      /* 1: at the first kmpm_run / kmpm_run_time after at least one step,
                         time every launch shape of the gather kernels on a scratch copy of
                         the particle state and keep the fastest (kmpm_tuning reports it) */
-  int transfer;      /* KMPM_TRANSFER_FLIP (PIC/FLIP blend by pic_flip) or KMPM_TRANSFER_APIC
-                        (method(..., APIC, ...): affine transfers, src/solid.cpp:392-426 and
-                        1006-1153; cubic or quadratic spline, mechanical runs; sets pic_flip = 0) */
+  int transfer;      /* KMPM_TRANSFER_*: the method's sub-type.  FLIP: PIC/FLIP blend by pic_flip.
+                        APIC (and for ULMPM AFLIP, ASFLIP, MLS): affine transfers,
+                        src/solid.cpp:392-426, 524-574, 1006-1153; cubic or quadratic spline,
+                        mechanical runs; APIC and MLS set pic_flip = 0 */
 } kmpm_params;
 
 /* One material: Mat (src/material.h:45-68) with its EOS / Strength / Damage /

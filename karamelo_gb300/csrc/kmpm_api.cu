@@ -127,7 +127,12 @@ struct kmpm_ctx {
   };
   std::vector<AsyncBuf> abufs;
   bool indep() const { return prm.independent != 0; }
-  bool apic() const { return prm.transfer == KMPM_TRANSFER_APIC; }
+  // affine transfers: APIC, and for ULMPM also AFLIP / ASFLIP / MLS
+  // (src/ulmpm.cpp:79-85; TLMPM takes the affine path for APIC only, src/tlmpm.cpp:354)
+  bool apic() const {
+    return prm.transfer == KMPM_TRANSFER_APIC ||
+           (prm.method == KMPM_ULMPM && prm.transfer >= KMPM_TRANSFER_AFLIP && prm.transfer <= KMPM_TRANSFER_MLS);
+  }
   int smem_apic[3] = {0, 0, 0};  // dynamic shared memory of the APIC scatters (TL, UL, VEL)
   bool TL() const { return prm.method == KMPM_TLMPM; }
   bool musl() const { return prm.scheme == KMPM_MUSL; }
@@ -232,6 +237,7 @@ PartArgs part_args(kmpm_ctx *c) {
   a.thermal = c->prm.thermal;
   a.track_strain = c->prm.track_strain;
   a.apic = c->apic() ? 1 : 0;
+  a.asflip = (!c->TL() && c->prm.transfer == KMPM_TRANSFER_ASFLIP) ? 1 : 0;
   a.dim = c->prm.dim;
   for (int d = 0; d < 3; d++) a.tile_t[d] = c->tdim[d];
   return a;
@@ -252,6 +258,11 @@ P2GArgs p2g_args(kmpm_ctx *c) {
   a.tile_end = c->d_te;
   a.scalars = c->d_scalars;
   a.apic_pos = -1;
+  a.mls = (!c->TL() && c->prm.transfer == KMPM_TRANSFER_MLS) ? 1 : 0;
+  {
+    const double cs = c->hgrids.empty() ? 1.0 : c->hgrids[0].cellsize;
+    a.mls_di = (float)((c->prm.basis == KMPM_BASIS_QUADRATIC ? 4.0 : 3.0) / (cs * cs));
+  }
   return a;
 }
 
@@ -984,16 +995,19 @@ int kmpm_create(const kmpm_params *params, kmpm_ctx **out) {
   if (p.basis < 0 || p.basis > 3 || p.dim < 1 || p.dim > 3) return KMPM_ERR_ARG;
   if (p.method == KMPM_ULMPM && p.basis == KMPM_BASIS_BERNSTEIN) return KMPM_ERR_ARG;
   if (p.independent && p.method != KMPM_TLMPM) return KMPM_ERR_ARG;  // ULMPM solids share one grid
-  if (p.transfer != KMPM_TRANSFER_FLIP && p.transfer != KMPM_TRANSFER_APIC) return KMPM_ERR_ARG;
-  // APIC: the cubic spline (Di = 3/h^2), mechanical runs
-  if (p.transfer == KMPM_TRANSFER_APIC &&
-      ((p.basis != KMPM_BASIS_CUBIC && p.basis != KMPM_BASIS_QUADRATIC) || p.thermal))
-    return KMPM_ERR_ARG;
+  if (p.transfer < KMPM_TRANSFER_FLIP || p.transfer > KMPM_TRANSFER_MLS) return KMPM_ERR_ARG;
+  if (p.transfer == KMPM_TRANSFER_MLS && p.method != KMPM_ULMPM) return KMPM_ERR_ARG;  // MLS is a ULMPM path
+  {
+    // affine transfers: the cubic or quadratic spline, mechanical runs
+    const bool affine = p.transfer == KMPM_TRANSFER_APIC || (p.method == KMPM_ULMPM && p.transfer >= KMPM_TRANSFER_AFLIP);
+    if (affine && ((p.basis != KMPM_BASIS_CUBIC && p.basis != KMPM_BASIS_QUADRATIC) || p.thermal)) return KMPM_ERR_ARG;
+  }
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return KMPM_ERR_CUDA;
   kmpm_ctx *c = new kmpm_ctx();
   c->prm = p;
-  if (c->apic()) c->prm.pic_flip = 0;  // APIC updates v = v_update (src/tlmpm.cpp:82-84, src/ulmpm.cpp:79-82)
+  // APIC and MLS update v = v_update (src/tlmpm.cpp:82-84, src/ulmpm.cpp:79-82)
+  if (p.transfer == KMPM_TRANSFER_APIC || p.transfer == KMPM_TRANSFER_MLS) c->prm.pic_flip = 0;
   if (cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking) != cudaSuccess) {
     delete c;
     return KMPM_ERR_CUDA;

@@ -47,6 +47,8 @@ struct P2GArgs {
   const int *tile_start, *tile_end;  // particle range of every tile (empty tiles are skipped)
   const StepScalars *scalars;
   int apic_pos;              // APIC: displacement field added to x0 for x_p (PF_X, PF_XN) or -1 (TL: x0)
+  int mls;                   // ULMPM MLS: internal forces from moments, Di = mls_di
+  float mls_di;
 };
 
 struct GridArgs {
@@ -83,6 +85,7 @@ struct PartArgs {
   int indep, use_vu, thermal, track_strain, dim;
   int tile_t[3];
   int apic;                  // APIC transfers: k_g2p2 forms grad v from moments and stores PF_C
+  int asflip;                // ULMPM ASFLIP: positions move with the blended velocity
 };
 
 struct DtArgs {

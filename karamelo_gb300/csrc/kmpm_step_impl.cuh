@@ -244,6 +244,11 @@ __global__ void __launch_bounds__(256) k_p2g(P2GArgs a) {
           const float t = ((d == 0 ? pj.x : (d == 1 ? pj.y : pj.z)) - lod) * ih;
           float sv[4], dsv[4];
           cubic_weights(t - (float)(i0d + 1), ih, sv, dsv);
+          if (a.mls) {  // MLS forces: the moment s (x_node - x_p) Di in place of the slope
+            const float xp = d == 0 ? pj.x : (d == 1 ? pj.y : pj.z);
+#pragma unroll
+            for (int kk = 0; kk < 4; kk++) dsv[kk] = sv[kk] * (lod + (float)(i0d + kk) * h - xp) * a.mls_di;
+          }
 #pragma unroll
           for (int kk = 0; kk < 4; kk++) sbas[it * S + kk] = make_float2(sv[kk], dsv[kk]);
         }
@@ -262,6 +267,9 @@ __global__ void __launch_bounds__(256) k_p2g(P2GArgs a) {
           const float r = ((d == 0 ? pj.x : (d == 1 ? pj.y : pj.z)) - xn) * ih;
           basis<BASIS>(r, node_type<BASIS>(i, ngd), ih, sv, dsv);
           dsv = sv != 0.f ? dsv : 0.f;  // as Axis::eval
+          // MLS forces (compute_external_and_internal_forces_nodes_UL_MLS,
+          // src/solid.cpp:524-574): w Di (x_node - x_p) in place of grad w
+          if (a.mls) dsv = sv * (xn - (d == 0 ? pj.x : (d == 1 ? pj.y : pj.z))) * a.mls_di;
         }
         sbas[it] = make_float2(sv, dsv);
       }
@@ -569,15 +577,19 @@ __global__ void __launch_bounds__(256, MINB) k_g2p1(PartArgs a) {
     // x += dt * v_update.  Positions are kept as the displacement u = x - x0
     // (FP32 rounding then scales with the displacement, not with |x|).  UL
     // writes the moved displacement to PF_XN: this step's weights keep PF_X.
-    if (TL) P[(PF_X + d) * ps + p] = up[d] + dt * vu[d];
-    else {
-      const float un = up[d] + dt * vu[d];
-      P[(PF_XN + d) * ps + p] = un;
-      xn[d] = P[(PF_X0 + d) * ps + p] + un;
-    }
     const float v = P[(PF_V + d) * ps + p];
     // v = (1-alpha) v_update + alpha (v + dt a), with dt a = sum w (v_update - v)
-    P[(PF_V + d) * ps + p] = (1.f - alpha) * vu[d] + alpha * (v + dv[d]);
+    const float vnew = (1.f - alpha) * vu[d] + alpha * (v + dv[d]);
+    if (TL) P[(PF_X + d) * ps + p] = up[d] + dt * vu[d];
+    else {
+      // ASFLIP moves the particle with the blended velocity
+      // (update_particle_velocities_and_positions, src/solid.cpp:791-796) and
+      // checks the box on the position before the move (src/solid.cpp:676-686)
+      const float un = up[d] + dt * (a.asflip ? vnew : vu[d]);
+      P[(PF_XN + d) * ps + p] = un;
+      xn[d] = P[(PF_X0 + d) * ps + p] + (a.asflip ? up[d] : un);
+    }
+    P[(PF_V + d) * ps + p] = vnew;
   }
   if (THERMAL) P[PF_T * ps + p] = Tp;
   if (!TL) {

@@ -100,22 +100,30 @@ class MPM:
         elif sub == "FLIP":
             if not rest:
                 raise KarameloError("Illegal method command: FLIP needs the PIC/FLIP ratio")
-        elif sub == "APIC":
-            # APIC sets PIC_FLIP = 0 (src/tlmpm.cpp:82-84, src/ulmpm.cpp:79-82)
-            self.s.transfer = 1
+        elif sub in ("APIC", "MLS"):
+            # APIC and MLS set PIC_FLIP = 0 (src/tlmpm.cpp:82-84, src/ulmpm.cpp:79-82)
+            if sub == "MLS" and self.s.method != sc.ULMPM:
+                raise KarameloError("MLS is a ULMPM method type")
+            self.s.transfer = 1 if sub == "APIC" else 4
             self.s.pic_flip = 0.0
+        elif sub in ("AFLIP", "ASFLIP"):
+            if not rest:
+                raise KarameloError(f"Illegal method command: {sub} needs the PIC/FLIP ratio")
+            self.s.transfer = 2 if sub == "AFLIP" else 3
         else:
-            raise KarameloError(f"method type {sub} not supported on the GPU path (PIC, FLIP or APIC)")
+            raise KarameloError(f"method type {sub} not supported on the GPU path "
+                                "(PIC, FLIP, APIC, AFLIP, ASFLIP or MLS)")
         if basis not in sc.BASIS_NAMES:
             raise KarameloError(f"shape function {basis} not supported: linear, cubic-spline, quadratic-spline, "
                                 "Bernstein-quadratic")
         self.s.basis = sc.BASIS_NAMES[basis]
         if self.s.basis == sc.BERNSTEIN and self.s.method == sc.ULMPM:
             raise KarameloError("Bernstein-quadratic shape functions are only supported with TLMPM")
-        if self.s.transfer == 1 and self.s.basis not in (sc.CUBIC, sc.QUADRATIC):
-            raise KarameloError("APIC on the GPU path runs with the cubic or quadratic spline")
+        affine = self.s.transfer == 1 or (self.s.method == sc.ULMPM and self.s.transfer >= 2)
+        if affine and self.s.basis not in (sc.CUBIC, sc.QUADRATIC):
+            raise KarameloError(f"{sub} on the GPU path runs with the cubic or quadratic spline")
         rest = list(rest)
-        if sub == "FLIP":
+        if sub in ("FLIP", "AFLIP", "ASFLIP"):
             self.s.pic_flip = float(rest.pop(0))
         if rest:
             kw = rest.pop(0)

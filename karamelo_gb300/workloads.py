@@ -82,7 +82,7 @@ COPPER = dict(E=115.0, nu=0.31, rho=8.94e-6, K=137.0, A=0.09, B=0.292, n=0.31, C
 
 
 def _method(sim, method, sub, basis, pic_flip):
-    if sub == "FLIP":
+    if sub in ("FLIP", "AFLIP", "ASFLIP"):
         sim.method(method, sub, basis, pic_flip)
     else:
         sim.method(method, sub, basis)

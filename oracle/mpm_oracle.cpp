@@ -410,7 +410,9 @@ struct Fix {
 struct Sim {
   int method, scheme, basis, dim;
   double pic_flip;
-  bool apic = false;  // sub-method APIC (src/update.cpp:129-149, src/tlmpm.cpp:82-84, src/ulmpm.cpp:79-82)
+  bool apic = false;  // affine transfers: APIC, and for ULMPM AFLIP / ASFLIP / MLS (src/ulmpm.cpp:79-85)
+  bool asflip = false;  // ULMPM ASFLIP: positions move with the blended velocity (src/ulmpm.cpp:453-473)
+  bool mls = false;     // ULMPM MLS: internal forces from moments (src/solid.cpp:524-574)
   bool thermal;
   double dt, dt_factor;
   bool dt_constant;
@@ -638,14 +640,21 @@ void compute_internal_forces_nodes_TL(Solid &S, Grid &g) {
 }
 
 // Solid::compute_external_and_internal_forces_nodes_UL, src/solid.cpp:482-522
-void compute_forces_nodes_UL(Solid &S, Grid &g, bool reset) {
+void compute_forces_nodes_UL(const Sim &s, Solid &S, Grid &g, bool reset) {
 #pragma omp parallel for schedule(static)
   for (int in = 0; in < g.nn; in++) {
     if (reset) for (int d = 0; d < 3; d++) { g.f[3 * in + d] = 0; g.mb[3 * in + d] = 0; }
     for (size_t j = 0; j < S.neigh_np[in].size(); j++) {
       int ip = S.neigh_np[in][j];
       const M3 &sg = S.sigma[ip];
-      const double *gw = &S.wfd_np[in][3 * j];
+      double gw[3];
+      if (s.mls) {
+        // compute_external_and_internal_forces_nodes_UL_MLS, src/solid.cpp:524-574:
+        // w Di (x0_node - x_p) in place of grad w
+        for (int d = 0; d < 3; d++) gw[d] = S.wf_np[in][j] * S.Di[d] * (g.x0[3 * in + d] - S.x[3 * ip + d]);
+      } else {
+        for (int d = 0; d < 3; d++) gw[d] = S.wfd_np[in][3 * j + d];
+      }
       for (int d = 0; d < 3; d++) {
         g.f[3 * in + d] -= S.vol[ip] * (sg(d, 0) * gw[0] + sg(d, 1) * gw[1] + sg(d, 2) * gw[2]);
         g.mb[3 * in + d] += S.wf_np[in][j] * S.mbp[3 * ip + d];
@@ -958,7 +967,7 @@ bool step(Sim &s) {
     for (size_t i = 0; i < s.solids.size(); i++) compute_mass_nodes(s.solids[i], g, i == 0);
     for (size_t i = 0; i < s.solids.size(); i++) {
       compute_velocity_nodes(s, s.solids[i], g, i == 0);
-      compute_forces_nodes_UL(s.solids[i], g, i == 0);
+      compute_forces_nodes_UL(s, s.solids[i], g, i == 0);
       if (s.thermal) {
         compute_temperature_nodes(s.solids[i], g, i == 0);
         compute_temperature_forces(s.solids[i], g, i == 0);
@@ -1054,7 +1063,8 @@ bool step(Sim &s) {
         S.vu[3 * ip + d] = vu[d];
         S.a[3 * ip + d] = a[d] * inv_dt;
         S.f[3 * ip + d] = S.a[3 * ip + d] * S.mass[ip];
-        S.x[3 * ip + d] += s.dt * vu[d];
+        // ASFLIP: Solid::compute_particle_accelerations_velocities leaves x
+        if (!s.asflip) S.x[3 * ip + d] += s.dt * vu[d];
       }
       if (!TL) {
         const double *x = &S.x[3 * ip];
@@ -1076,8 +1086,11 @@ bool step(Sim &s) {
   for (auto &S : s.solids)
 #pragma omp parallel for schedule(static)
     for (int ip = 0; ip < S.np; ip++)
-      for (int d = 0; d < 3; d++)
+      for (int d = 0; d < 3; d++) {
         S.v[3 * ip + d] = (1 - s.pic_flip) * S.vu[3 * ip + d] + s.pic_flip * (S.v[3 * ip + d] + s.dt * S.a[3 * ip + d]);
+        // ASFLIP: Solid::update_particle_velocities_and_positions, src/solid.cpp:791-796
+        if (s.asflip) S.x[3 * ip + d] += s.dt * S.v[3 * ip + d];
+      }
     return true;
   };
   // update_time and adjust_dt
@@ -1173,14 +1186,22 @@ void *om_create(int method, int scheme, int basis, int dim, double pic_flip, int
 void om_destroy(void *h) { delete (Sim *)h; }
 // sub-method APIC: PIC velocity update (PIC_FLIP = 0) and affine transfers;
 // the reference supports it with the cubic spline (and linear TLMPM)
-int om_set_apic(void *h, int on) {
+// kind: 0 PIC/FLIP, 1 APIC, 2 AFLIP, 3 ASFLIP, 4 MLS (Update::create_method,
+// src/update.cpp:129-149).  TLMPM takes the affine path for APIC only
+// (src/tlmpm.cpp:82-84, 354); ULMPM for all four (src/ulmpm.cpp:79-85).
+int om_set_transfer(void *h, int kind) {
   Sim *s = (Sim *)h;
-  if (on && s->basis != CUBIC && s->basis != QUADRATIC) {
-    s->err = "APIC is restated for the cubic and quadratic splines";
+  const bool TL = s->method == TLMPM;
+  if (kind < 0 || kind > 4 || (kind == 4 && TL)) { s->err = "unsupported sub-method"; return -1; }
+  const bool affine = kind == 1 || (!TL && kind >= 2);
+  if (affine && s->basis != CUBIC && s->basis != QUADRATIC) {
+    s->err = "affine transfers are restated for the cubic and quadratic splines";
     return -1;
   }
-  s->apic = on != 0;
-  if (s->apic) s->pic_flip = 0;
+  s->apic = affine;
+  s->asflip = !TL && kind == 3;
+  s->mls = !TL && kind == 4;
+  if (kind == 1 || kind == 4) s->pic_flip = 0;
   return 0;
 }
 const char *om_error(void *h) { return ((Sim *)h)->err.c_str(); }

@@ -45,7 +45,7 @@ def lib():
         L.om_create.restype = p
         L.om_create.argtypes = [i, i, i, i, d, i, d, d, i, dp, dp]
         L.om_destroy.argtypes = [p]
-        L.om_set_apic.argtypes = [p, i]
+        L.om_set_transfer.argtypes = [p, i]
         L.om_error.restype = ctypes.c_char_p
         L.om_error.argtypes = [p]
         L.om_add_material.argtypes = [p, p]
@@ -91,7 +91,7 @@ class OracleBackend:
         self.h = L.om_create(s.method, s.scheme, s.basis, s.dim, s.pic_flip, int(s.thermal), s.dt, s.dt_factor,
                              int(s.dt_constant), _dp(lo), _dp(hi))
         self.L = L
-        if getattr(s, "transfer", 0) == 1 and L.om_set_apic(self.h, 1) != 0:
+        if getattr(s, "transfer", 0) != 0 and L.om_set_transfer(self.h, int(s.transfer)) != 0:
             raise RuntimeError(L.om_error(self.h).decode())
         for m in s.materials:
             L.om_add_material(self.h, ctypes.byref(m))

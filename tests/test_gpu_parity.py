@@ -331,3 +331,21 @@ def test_spinning_disk_apic_quadratic(gpu_lib, oracle_mod):
     g, o = pair(oracle_mod, W.spinning_disk, [1, 150], method="ulmpm/gpu", scheme="musl", basis="quadratic-spline")
     check(g, o, {"x": 1e-6, "v": 1e-4, "sigma": 3e-3})
     assert abs(W.angular_momentum(g) / W.angular_momentum(o) - 1) < 1e-4
+
+
+# ---------------------------------------------------------------- AFLIP / ASFLIP / MLS (§8(f) next row 1)
+@pytest.mark.parametrize("sub", ["AFLIP", "ASFLIP", "MLS"])
+def test_dam_break_affine_submethods(gpu_lib, oracle_mod, sub):
+    """ULMPM dam break with the other affine sub-methods: AFLIP and ASFLIP
+    (affine transfers with the FLIP blend; ASFLIP moves particles with the
+    blended velocity, src/ulmpm.cpp:453-473) and MLS (internal forces from
+    moments, src/solid.cpp:524-574)."""
+    g, o = pair(oracle_mod, W.dam_break, [60], cellsize=0.05, method="ulmpm/gpu", sub=sub)
+    check(g, o, {"x": 1e-6, "v": 1e-4, "sigma": 1e-3})
+
+
+@pytest.mark.parametrize("sub", ["ASFLIP", "MLS"])
+def test_spinning_disk_affine_submethods(gpu_lib, oracle_mod, sub):
+    g, o = pair(oracle_mod, W.spinning_disk, [1, 150], method="ulmpm/gpu", scheme="musl", sub=sub)
+    check(g, o, {"x": 1e-6, "v": 1e-4, "sigma": 3e-3})
+    assert abs(W.angular_momentum(g) / W.angular_momentum(o) - 1) < 1e-4
