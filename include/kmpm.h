@@ -167,6 +167,30 @@ int kmpm_add_solid(struct kmpm_ctx *ctx, int grid, int mat, int n, const double 
 int kmpm_add_fix(struct kmpm_ctx *ctx, int kind, int grid, const unsigned char *node_mask, const int set[3],
                  const double coef[12]);
 
+/* Contact fixes between two solids, evaluated at the start of every step
+ * (Modify::initial_integrate): each particle pair closer than Rp1 + Rp2
+ * (Rp = half the cube root of the current volume in 3-D, half its square
+ * root in 2-D) adds equal and opposite forces to the external force vector
+ * mbp of its two particles, which the scatter then adds to the node forces.
+ * Pairs are found on a hashed cell list of the current positions with the
+ * larger of the two grids' cellsizes as its cell; each particle sums its
+ * own pairs, so the result does not depend on scheduling.
+ *   KMPM_CONTACT_MIN_PENETRATION: FixContactMinPenetration::initial_integrate
+ *     (src/fix_contact_min_penetration.cpp:83-235), with Coulomb friction mu
+ *     and, in thermo-mechanical runs, frictional heating;
+ *   KMPM_CONTACT_HERTZ: FixContactHertz::initial_integrate
+ *     (src/fix_contact_hertz.cpp:82-197); mu is ignored.
+ * Both solids must differ; independent batches take no contact.  Returns the
+ * contact's id (>= 0). */
+#define KMPM_CONTACT_MIN_PENETRATION 0
+#define KMPM_CONTACT_HERTZ 1
+int kmpm_add_contact(struct kmpm_ctx *ctx, int kind, int solid1, int solid2, double mu);
+
+/* Total contact force of the last step (the variables <id>_x, <id>_y, <id>_z
+ * the reference fix sets): the sum over all pairs of the force on solid1
+ * (min-penetration) or on solid2 (Hertz).  Zero before the first step. */
+int kmpm_contact_force(struct kmpm_ctx *ctx, int contact, double out[3]);
+
 /* Scheme::run for nsteps steps (USL::run src/usl.cpp:34-94, MUSL::run
  * src/musl.cpp:34-95), each step fully on the GPU. */
 int kmpm_run(struct kmpm_ctx *ctx, int nsteps);

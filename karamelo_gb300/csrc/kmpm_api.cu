@@ -47,6 +47,18 @@ struct kmpm_ctx {
   };
   std::vector<HFix> hfixes;
   bool built = false, fixes_dirty = true;
+  // contact fixes: the pairs of solids, and their device state
+  struct HContact {
+    int kind, s1, s2;
+    double mu;
+  };
+  std::vector<HContact> hcontacts;
+  std::vector<double> mat_E, mat_nu;  // Mat::E, Mat::nu (derived from K and G for EOS materials)
+  std::vector<ContactDev> contacts;
+  float *d_mbp = nullptr;             // external particle forces, 3 rows of ps floats
+  bool contacts_dirty = false;
+  int smem_ext[2][2] = {{0}};         // dynamic shared memory of the scatters with mbp: [UL][thermal]
+  int smem_apic_ext[2] = {0, 0};      // [UL]
   // ---- device layout
   size_t ps = 0;
   int nblk_p = 0;
@@ -259,6 +271,7 @@ P2GArgs p2g_args(kmpm_ctx *c) {
   a.scalars = c->d_scalars;
   a.apic_pos = -1;
   a.mls = (!c->TL() && c->prm.transfer == KMPM_TRANSFER_MLS) ? 1 : 0;
+  a.mbp = c->d_mbp;
   {
     const double cs = c->hgrids.empty() ? 1.0 : c->hgrids[0].cellsize;
     a.mls_di = (float)((c->prm.basis == KMPM_BASIS_QUADRATIC ? 4.0 : 3.0) / (cs * cs));
@@ -301,6 +314,8 @@ DtArgs dt_args(kmpm_ctx *c) {
   a.indep = c->indep();
   a.dt_constant = c->prm.dt_constant;
   a.dt_factor = c->prm.dt_factor;
+  a.max_nblk = 0;
+  for (const auto &r : c->ranges) a.max_nblk = std::max(a.max_nblk, r.nblk);
   return a;
 }
 
@@ -743,6 +758,94 @@ int upload_fixes(kmpm_ctx *c) {
   return KMPM_OK;
 }
 
+void free_contacts(kmpm_ctx *c) {
+  for (auto &d : c->contacts) {
+    dfree(d.keys); dfree(d.vals); dfree(d.bstart); dfree(d.bend);
+    dfree(d.ra); dfree(d.rb); dfree(d.rc); dfree(d.blk); dfree(d.ftot);
+  }
+  c->contacts.clear();
+  dfree(c->d_mbp);
+}
+
+// device state of the contact fixes: member lists, hash buckets and the mbp rows
+int setup_contacts(kmpm_ctx *c) {
+  free_contacts(c);
+  c->contacts_dirty = false;
+  c->graph_valid = false;
+  if (c->hcontacts.empty()) return KMPM_OK;
+  const int dim = c->prm.dim, basis = c->prm.basis;
+  if (dim >= 2) {
+    // the force scatters with external particle forces
+    void *fx[2][2] = {{c->K.p2g_tl_ext[0], c->K.p2g_tl_ext[1]}, {c->K.p2g_ul_ext[0], c->K.p2g_ul_ext[1]}};
+    for (int ul = 0; ul < 2; ul++)
+      for (int th = 0; th < 2; th++) {
+        c->smem_ext[ul][th] = p2g_smem_bytes(dim, basis, (ul ? P2G_UL : P2G_TL) | P2G_EXT, th == 1);
+        CK(cudaFuncSetAttribute(fx[ul][th], cudaFuncAttributeMaxDynamicSharedMemorySize, c->smem_ext[ul][th]));
+      }
+    if (c->apic()) {
+      void *fa[2] = {c->K.p2g_tl_apic_ext, c->K.p2g_ul_apic_ext};
+      for (int ul = 0; ul < 2; ul++) {
+        c->smem_apic_ext[ul] = p2g_smem_bytes(dim, basis, (ul ? P2G_UL_APIC : P2G_TL_APIC) | P2G_EXT, false);
+        CK(cudaFuncSetAttribute(fa[ul], cudaFuncAttributeMaxDynamicSharedMemorySize, c->smem_apic_ext[ul]));
+      }
+    }
+  }
+  DALLOC(c->d_mbp, 3 * c->ps);
+  CK(cudaMemsetAsync(c->d_mbp, 0, sizeof(float) * 3 * c->ps, c->st));
+  for (const auto &h : c->hcontacts) {
+    ContactDev d{};
+    d.kind = h.kind;
+    d.dim = dim;
+    d.thermal = c->prm.thermal;
+    d.ul = c->TL() ? 0 : 1;
+    d.sid1 = h.s1;
+    d.sid2 = h.s2;
+    if (c->TL()) {
+      const RangeDev &r1 = c->ranges[c->solid_range[h.s1]], &r2 = c->ranges[c->solid_range[h.s2]];
+      d.start1 = r1.start; d.n1 = r1.count;
+      d.start2 = r2.start; d.n2 = r2.count;
+      d.nmem = r1.count + r2.count;
+    } else {
+      const RangeDev &r = c->ranges[0];
+      d.start1 = r.start; d.n1 = r.count;
+      d.start2 = 0; d.n2 = 0;
+      d.nmem = r.count;
+    }
+    d.nb = 1024;
+    while (d.nb < d.nmem) d.nb <<= 1;
+    d.key_bits = 1;
+    while ((1 << d.key_bits) <= d.nb) d.key_bits++;  // bucket nb marks non-members
+    const int m1 = c->hsolids[h.s1].mat, m2 = c->hsolids[h.s2].mat;
+    const double E1 = c->mat_E[m1], E2 = c->mat_E[m2], nu1 = c->mat_nu[m1], nu2 = c->mat_nu[m2];
+    d.estar = (float)(1.0 / ((1 - nu1 * nu1) / E1 + (1 - nu2 * nu2) / E2));
+    d.alpha = (float)(c->mats[m1].kappa / (c->mats[m1].kappa + c->mats[m2].kappa));
+    d.invcp1 = (float)c->mats[m1].invcp;
+    d.invcp2 = (float)c->mats[m2].invcp;
+    d.mu = (float)h.mu;
+    // four_thirds = 1.333333333 in both reference fixes; 0.25 pi in 2-D Hertz
+    d.hcoef = (float)(dim == 3 ? 1.333333333 : 0.25 * M_PI);
+    const double cmax = std::max(c->hgrids[c->hsolids[h.s1].grid].cellsize, c->hgrids[c->hsolids[h.s2].grid].cellsize);
+    d.cmax = (float)cmax;
+    d.inv_cmax = (float)(1.0 / cmax);
+    for (int k = 0; k < 3; k++) d.boxlo[k] = (float)c->prm.boxlo[k];
+    const int nblk = (d.nmem + 255) / 256;
+    DALLOC(d.keys, std::max(d.nmem, 1));
+    DALLOC(d.vals, std::max(d.nmem, 1));
+    DALLOC(d.bstart, d.nb);
+    DALLOC(d.bend, d.nb);
+    DALLOC(d.ra, std::max(d.nmem, 1));
+    DALLOC(d.rb, std::max(d.nmem, 1));
+    DALLOC(d.rc, std::max(d.nmem, 1));
+    DALLOC(d.blk, 3 * std::max(nblk, 1));
+    DALLOC(d.ftot, 3);
+    CK(cudaMemsetAsync(d.ftot, 0, 3 * sizeof(double), c->st));
+    d.mbp = c->d_mbp;
+    c->contacts.push_back(d);
+  }
+  CK(cudaStreamSynchronize(c->st));
+  return KMPM_OK;
+}
+
 // ---------------------------------------------------------------- one step
 // USL::run (src/usl.cpp:43-92) / MUSL::run (src/musl.cpp:43-93)
 int enqueue_step(kmpm_ctx *c) {
@@ -771,12 +874,24 @@ int enqueue_step(kmpm_ctx *c) {
     nl += 5 + 3 * ((c->key_bits + 7) / 8);
     MARK("bin_sort");
   }
+  // reset() + initial_integrate: the contact fixes fill mbp from the current
+  // positions (src/musl.cpp:48-49, src/usl.cpp:48-49, src/usf.cpp:48-49)
+  const bool ext = !c->contacts.empty() && c->prm.dim >= 2;
+  if (ext) {
+    CK(cudaMemsetAsync(c->d_mbp, 0, sizeof(float) * 3 * c->ps, c->st));
+    for (const auto &cd : c->contacts) nl += launch_contact(pa, cd, c->rtmp, c->st);
+    MARK("contact");
+  }
   P2GArgs p = p2g_args(c);
   GridArgs g1 = grid_args(c, 0);
   const bool apic = c->apic();
   // particles_to_grid (APIC: compute_velocity_nodes_APIC with x_p = x0 (TL) or x (UL))
   p.apic_pos = TL ? -1 : PF_X;
-  if (apic) LAUNCH(TL ? c->K.p2g_tl_apic : c->K.p2g_ul_apic, c->ntiles_launch, 256, c->smem_apic[TL ? 0 : 1], p);
+  if (ext) {
+    // the same scatters with w mbp added to the node forces
+    if (apic) LAUNCH(TL ? c->K.p2g_tl_apic_ext : c->K.p2g_ul_apic_ext, c->ntiles_launch, 256, c->smem_apic_ext[TL ? 0 : 1], p);
+    else LAUNCH(TL ? c->K.p2g_tl_ext[th] : c->K.p2g_ul_ext[th], c->ntiles_launch, 256, c->smem_ext[TL ? 0 : 1][th], p);
+  } else if (apic) LAUNCH(TL ? c->K.p2g_tl_apic : c->K.p2g_ul_apic, c->ntiles_launch, 256, c->smem_apic[TL ? 0 : 1], p);
   else if (TL) LAUNCH(th ? c->K.p2g_tl_th : c->K.p2g_tl, c->ntiles_launch, 256, c->smem[1][th], p);
   else LAUNCH(th ? c->K.p2g_ul_th : c->K.p2g_ul, c->ntiles_launch, 256, c->smem[2][th], p);
   MARK("p2g");
@@ -791,7 +906,8 @@ int enqueue_step(kmpm_ctx *c) {
     ps.use_vu = 0;
     LAUNCH((th || prec) ? c->K.g2p2[TL][th][prec] : c->K.g2p2_v[TL][c->var_g2p2], c->nblk_p, 256, 0, ps);
     MARK("g2p_stress");
-    if (TL) LAUNCH(c->K.p2g_tl, c->ntiles_launch, 256, c->smem[1][0], p);
+    if (ext) LAUNCH(TL ? c->K.p2g_tl_ext[0] : c->K.p2g_ul_ext[0], c->ntiles_launch, 256, c->smem_ext[TL ? 0 : 1][0], p);
+    else if (TL) LAUNCH(c->K.p2g_tl, c->ntiles_launch, 256, c->smem[1][0], p);
     else LAUNCH(c->K.p2g_ul, c->ntiles_launch, 256, c->smem[2][0], p);
     MARK("p2g_forces");
     LAUNCH(c->K.grid_upd[TL][th][prec], c->nblk_g, 256, 0, g1);
@@ -900,6 +1016,10 @@ int prepare(kmpm_ctx *c) {
   }
   if (c->fixes_dirty) {
     int r = upload_fixes(c);
+    if (r != KMPM_OK) return r;
+  }
+  if (c->contacts_dirty) {
+    int r = setup_contacts(c);
     if (r != KMPM_OK) return r;
   }
   return ensure_graph(c);
@@ -1028,6 +1148,7 @@ int kmpm_destroy(kmpm_ctx *c) {
   dfree(c->d_cs); dfree(c->d_ce); dfree(c->d_ts); dfree(c->d_te); dfree(c->partial);
   dfree(c->d_fixes); dfree(c->d_fix_start); dfree(c->d_fix_count); dfree(c->d_scalars); dfree(c->d_dtcfl);
   dfree(c->d_dump);
+  free_contacts(c);
   if (c->cst) cudaStreamSynchronize(c->cst);
   for (auto &b : c->abufs) {
     dfree(b.buf);
@@ -1057,6 +1178,15 @@ int kmpm_add_material(kmpm_ctx *c, const kmpm_material *m) {
       return fail(c, KMPM_ERR_ARG, "Error: reference temperature Tr equals melting temperature Tm");
   }
   c->mats.push_back(to_dev(*m));
+  // Mat::Mat (src/material.cpp:720-747): E and nu of an EOS material from K and G
+  if (m->type == KMPM_MAT_EOS_STRENGTH) {
+    const double K = m->eos_p[1], G = m->str_p[0];
+    c->mat_E.push_back(9 * K * G / (3 * K + G));
+    c->mat_nu.push_back((3 * K - 2 * G) / (2 * (3 * K + G)));
+  } else {
+    c->mat_E.push_back(m->E);
+    c->mat_nu.push_back(m->nu);
+  }
   return (int)c->mats.size() - 1;
 }
 
@@ -1110,6 +1240,30 @@ int kmpm_add_fix(kmpm_ctx *c, int kind, int grid, const unsigned char *node_mask
   c->hfixes.push_back(std::move(f));
   c->fixes_dirty = true;
   return (int)c->hfixes.size() - 1;
+}
+
+int kmpm_add_contact(kmpm_ctx *c, int kind, int solid1, int solid2, double mu) {
+  if (!c) return KMPM_ERR_ARG;
+  if (kind != KMPM_CONTACT_MIN_PENETRATION && kind != KMPM_CONTACT_HERTZ)
+    return fail(c, KMPM_ERR_ARG, "unsupported contact style");
+  const int ns = (int)c->hsolids.size();
+  if (solid1 < 0 || solid1 >= ns || solid2 < 0 || solid2 >= ns) return fail(c, KMPM_ERR_ARG, "Error: solid unknown.");
+  if (solid1 == solid2) return fail(c, KMPM_ERR_ARG, "a contact needs two different solids");
+  if (c->indep()) return fail(c, KMPM_ERR_ARG, "independent batches take no contact fix");
+  c->hcontacts.push_back({kind, solid1, solid2, kind == KMPM_CONTACT_MIN_PENETRATION ? mu : 0.0});
+  c->contacts_dirty = true;
+  return (int)c->hcontacts.size() - 1;
+}
+
+int kmpm_contact_force(kmpm_ctx *c, int k, double out[3]) {
+  if (!c || !out || k < 0 || k >= (int)c->hcontacts.size()) return KMPM_ERR_ARG;
+  if (k >= (int)c->contacts.size()) {
+    out[0] = out[1] = out[2] = 0;
+    return KMPM_OK;
+  }
+  CK(cudaMemcpyAsync(out, c->contacts[k].ftot, 3 * sizeof(double), cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  return KMPM_OK;
 }
 
 static int set_maxtime(kmpm_ctx *c, double maxtime) {

@@ -276,10 +276,16 @@ __device__ __forceinline__ void cubic_weights(float f, float ih, float *s, float
 // needs a per-node test.  (The boundary-modified cubic spline at ntype 1 has a
 // zero value with a non-zero slope; interior cubic values are zero only where
 // their slope is zero too.)
+//
+// o[k] = (x_node - x_p) / h, formed from the same rounded operands as the
+// value: the affine moments s (x_node - x_p) built from it keep the spline's
+// linear reproduction sum_k s_k o_k = 0 to the rounding of s, where node and
+// particle coordinates subtracted in FP32 would leave an error of one ulp of
+// |x| (relative to h), which APIC transfers feed back step after step.
 template <int BASIS> struct Axis {
   static constexpr int S = Stencil<BASIS>::S;
   int i0;
-  float s[S], ds[S];
+  float s[S], ds[S], o[S];
   __device__ __forceinline__ void eval(float xp, float lo, float ih, float h, int n, int ng) {
     // the reference truncates (src/tlmpm.cpp:145); the clamp keeps indices of a
     // non-finite or far-away position in range (such a particle raises an error)
@@ -287,24 +293,28 @@ template <int BASIS> struct Axis {
     int c = (int)t;
     i0 = c * Stencil<BASIS>::SC - Stencil<BASIS>::LO;
     if (BASIS == 1 && cubic_interior(i0, n, ng)) {
-      cubic_weights(t - (float)c, ih, s, ds);
+      const float f = t - (float)c;
+      cubic_weights(f, ih, s, ds);
+#pragma unroll
+      for (int k = 0; k < S; k++) o[k] = (float)(k - 1) - f;
       return;
     }
 #pragma unroll
     for (int k = 0; k < S; k++) {
       int i = i0 + k;
-      if (i < 0 || i >= n) { s[k] = 0.f; ds[k] = 0.f; continue; }
+      if (i < 0 || i >= n) { s[k] = 0.f; ds[k] = 0.f; o[k] = 0.f; continue; }
       float xn = lo + (float)i * h;
       float r = (xp - xn) * ih;
       basis<BASIS>(r, node_type<BASIS>(i, ng), ih, s[k], ds[k]);
       ds[k] = s[k] != 0.f ? ds[k] : 0.f;
+      o[k] = -r;
     }
   }
   // 1-D (unused axis): weight 1, gradient 0, single slot at node 0
   __device__ __forceinline__ void unit() {
     i0 = 0;
 #pragma unroll
-    for (int k = 0; k < S; k++) { s[k] = k == 0 ? 1.f : 0.f; ds[k] = 0.f; }
+    for (int k = 0; k < S; k++) { s[k] = k == 0 ? 1.f : 0.f; ds[k] = 0.f; o[k] = 0.f; }
   }
 };
 

@@ -12,13 +12,20 @@ enum P2GMode : int {
   P2G_VEL = 3,   // p                      (MUSL re-map; + mT)
   // APIC (Solid::compute_velocity_nodes_APIC, src/solid.cpp:392-426): the
   // same sums with the particle velocity v + C (x_node - x_p); the payload
-  // adds m C (9) and x_p (3)
+  // adds m C (9) and x_w - x_p (3), x_w the position of the weights
   P2G_TL_APIC = 4,
   P2G_UL_APIC = 5,
   P2G_VEL_APIC = 6,
+  // flag on the force modes: the particle's external force mbp (3, contact
+  // fixes) joins the payload and w mbp the force sums -- the grid's
+  // f + mb of Grid::update_grid_velocities (src/grid.cpp:456), filled by
+  // Solid::compute_external_forces_nodes (src/solid.cpp:428-449)
+  P2G_EXT = 8,
 };
-__host__ __device__ constexpr int p2g_base(int mode) { return mode >= P2G_TL_APIC ? mode - 3 : mode; }
-__host__ __device__ constexpr bool p2g_apic(int mode) { return mode >= P2G_TL_APIC; }
+__host__ __device__ constexpr int p2g_kind(int mode) { return mode & 7; }
+__host__ __device__ constexpr int p2g_base(int mode) { return p2g_kind(mode) >= P2G_TL_APIC ? p2g_kind(mode) - 3 : p2g_kind(mode); }
+__host__ __device__ constexpr bool p2g_apic(int mode) { return p2g_kind(mode) >= P2G_TL_APIC; }
+__host__ __device__ constexpr bool p2g_ext(int mode) { return (mode & P2G_EXT) != 0; }
 enum GridMode : int { GM_MASS = 0, GM_UPDATE = 1, GM_VEL = 2 };
 
 __host__ __device__ constexpr int p2g_nq(int mode, bool th) {
@@ -32,7 +39,7 @@ __host__ __device__ constexpr int p2g_nin(int mode, bool th) {
           : p2g_base(mode) == P2G_TL ? (th ? 17 : 12)
           : p2g_base(mode) == P2G_UL ? (th ? 15 : 10)
                                      : (th ? 4 : 3)) +
-         (p2g_apic(mode) ? 12 : 0);
+         (p2g_apic(mode) ? 12 : 0) + (p2g_ext(mode) ? 3 : 0);
 }
 
 struct P2GArgs {
@@ -47,8 +54,10 @@ struct P2GArgs {
   const int *tile_start, *tile_end;  // particle range of every tile (empty tiles are skipped)
   const StepScalars *scalars;
   int apic_pos;              // APIC: displacement field added to x0 for x_p (PF_X, PF_XN) or -1 (TL: x0)
+                             // (pos_field is that of the weights)
   int mls;                   // ULMPM MLS: internal forces from moments, Di = mls_di
   float mls_di;
+  const float *mbp;          // P2G_EXT: external particle forces, 3 rows of ps floats
 };
 
 struct GridArgs {
@@ -97,6 +106,7 @@ struct DtArgs {
   ErrState *err;
   int nranges, indep, dt_constant;
   double dt_factor;
+  int max_nblk;              // largest range, in 256-particle blocks (picks the reduction width)
 };
 
 struct LaunchSet {
@@ -107,6 +117,8 @@ struct LaunchSet {
 struct StepKernels {
   void *p2g_mass, *p2g_tl, *p2g_tl_th, *p2g_ul, *p2g_ul_th, *p2g_vel, *p2g_vel_th;
   void *p2g_tl_apic, *p2g_ul_apic, *p2g_vel_apic;  // cubic spline only (nullptr otherwise)
+  // the force scatters with external particle forces (P2G_EXT): [thermal]
+  void *p2g_tl_ext[2], *p2g_ul_ext[2], *p2g_tl_apic_ext, *p2g_ul_apic_ext;
   void *grid_mass[2], *grid_upd[2][2][2], *grid_vel[2][2][2];
   void *g2p1[2][2], *g2p2[2][2][2];
   // launch-shape candidates [TL][variant] of the gathers (FP32, no thermal):
@@ -125,6 +137,26 @@ void launch_dump(const PartArgs &a, int ri, int count, int solid, int base, int 
                  double T_ref, double *out, cudaStream_t st);
 int p2g_smem_bytes(int dim, int basis, int mode, bool thermal);
 
+// kmpm_contact.cu: one contact fix between two solids (device form)
+struct ContactDev {
+  int kind;                  // KMPM_CONTACT_*
+  int dim, thermal;
+  int ul;                    // ULMPM: members are the slots of one range, told apart by PF_SID
+  int sid1, sid2;            // solid ids (ULMPM member test)
+  int start1, n1, start2, n2;  // TLMPM: the two solids' slot ranges; ULMPM: start1, n1 = the range
+  int nmem;                  // members (n1 + n2 TLMPM, n1 ULMPM)
+  int nb, key_bits;          // hash buckets (a power of two) and sort key bits (bucket nb = not a member)
+  float mu, estar, alpha, hcoef, cmax, inv_cmax;
+  float invcp1, invcp2;
+  float boxlo[3];
+  int *keys, *vals;          // bucket of every member, sorted with the member index
+  int *bstart, *bend;        // member range of every bucket in sorted order
+  float4 *ra, *rb;           // per member: (x, Rp), (v, m)
+  int4 *rc;                  // per member: cell (3), tag (0 solid1, 1 solid2, -1 neither)
+  double *blk, *ftot;        // per-block partial sums of the pair forces, their total
+  float *mbp;                // 3 rows of ps floats: external particle forces
+};
+
 // kmpm_misc.cu
 void launch_cell_keys(const PartArgs &a, int nblk, int *keys, int use_x0, cudaStream_t st, int pad_last = 0);
 void launch_cell_ranges(const int *sorted_keys, int start, int n, int ncell_per_tile, int *cell_start, int *cell_end,
@@ -137,6 +169,8 @@ struct RadixTemp {
   int max_blocks;
 };
 void radix_sort(int *keys, int *vals, int n, int key_bits, RadixTemp &tmp, cudaStream_t st);
+// kmpm_contact.cu: launches one contact's kernels on st; returns the number of launches
+int launch_contact(const PartArgs &a, const ContactDev &c, RadixTemp &rt, cudaStream_t st);
 void launch_iota(int *v, int n, cudaStream_t st);
 void launch_permute(float *const *src_pp, float *const *dst_pp, size_t ps, const int *perm, int start, int n,
                     const int *fields, int nfields, cudaStream_t st);
@@ -171,9 +205,16 @@ __device__ __forceinline__ void p2g_payload(const P2GArgs &a, const float *P, in
   if (p2g_apic(MODE_)) {
 #pragma unroll
     for (int k = 0; k < 9; k++) pay[o++] = m * P[(PF_C + k) * ps + p];
+    // x_w - x_p: the weights' position minus the affine one (ULMPM re-map:
+    // u - u_moved; 0 where both are the same)
 #pragma unroll
     for (int d = 0; d < 3; d++)
-      pay[o++] = P[(PF_X0 + d) * ps + p] + (a.apic_pos >= 0 ? P[(a.apic_pos + d) * ps + p] : 0.f);
+      pay[o++] = (a.apic_pos >= 0 && a.apic_pos != a.pos_field)
+                     ? P[(a.pos_field + d) * ps + p] - P[(a.apic_pos + d) * ps + p] : 0.f;
+  }
+  if (p2g_ext(MODE_)) {
+#pragma unroll
+    for (int d = 0; d < 3; d++) pay[o++] = a.mbp[d * ps + p];
   }
 }
 
@@ -206,7 +247,14 @@ __device__ __forceinline__ void p2g_accumulate(float *acc, const float *pay, flo
     if (MODE != P2G_VEL) {
       acc[o++] += w * pay[i++];  // Qext: w gamma
       acc[o++] += gw[0] * pay[i] + gw[1] * pay[i + 1] + gw[2] * pay[i + 2];  // Qint: grad w . q
+      i += 3;
     }
+  }
+  if (p2g_ext(MODE_)) {
+    // f += w mbp (the force sums follow the momentum: index 3 TL, 4 UL)
+    constexpr int FO = MODE == P2G_UL ? 4 : 3;
+#pragma unroll
+    for (int d = 0; d < 3; d++) acc[FO + d] += w * pay[i + d];
   }
 }
 

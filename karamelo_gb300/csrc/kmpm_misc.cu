@@ -225,19 +225,29 @@ __device__ __forceinline__ void raise_error_m(ErrState *e, int code, int p, long
 }
 
 // per range: dtCFL = cellsize * min_h_ratio / max_p_wave_speed (src/solid.cpp:1430)
-__global__ void k_dt_range(DtArgs a) {
-  __shared__ float rc[256], rh[256];
+template <int BS>
+__global__ void __launch_bounds__(BS) k_dt_range(DtArgs a) {
+  __shared__ float rc[BS], rh[BS];
   if (run_finished(a.scalars)) return;
   const RangeDev rd = a.ranges[blockIdx.x];
   float c = 0.f, h = 1.f;
-  for (int b = rd.blk0 + threadIdx.x; b < rd.blk0 + rd.nblk; b += blockDim.x) {
+  // four independent loads in flight per thread (max / min are order-free)
+  const int end = rd.blk0 + rd.nblk;
+  int b = rd.blk0 + threadIdx.x;
+  for (; b + 3 * BS < end; b += 4 * BS) {
+    const float c0 = a.blk_c[b], c1 = a.blk_c[b + BS], c2 = a.blk_c[b + 2 * BS], c3 = a.blk_c[b + 3 * BS];
+    const float h0 = a.blk_h[b], h1 = a.blk_h[b + BS], h2 = a.blk_h[b + 2 * BS], h3 = a.blk_h[b + 3 * BS];
+    c = fmaxf(c, fmaxf(fmaxf(c0, c1), fmaxf(c2, c3)));
+    h = fminf(h, fminf(fminf(h0, h1), fminf(h2, h3)));
+  }
+  for (; b < end; b += BS) {
     c = fmaxf(c, a.blk_c[b]);
     h = fminf(h, a.blk_h[b]);
   }
   rc[threadIdx.x] = c;
   rh[threadIdx.x] = h;
   __syncthreads();
-  for (int s = 128; s > 0; s >>= 1) {
+  for (int s = BS / 2; s > 0; s >>= 1) {
     if (threadIdx.x < s) {
       rc[threadIdx.x] = fmaxf(rc[threadIdx.x], rc[threadIdx.x + s]);
       rh[threadIdx.x] = fminf(rh[threadIdx.x], rh[threadIdx.x + s]);
@@ -282,7 +292,9 @@ __global__ void k_step_begin(StepScalars *s, int n) {
 }
 
 void launch_dt(const DtArgs &a, cudaStream_t st) {
-  k_dt_range<<<a.nranges, 256, 0, st>>>(a);
+  // wide CTAs for few large ranges, narrow ones for many small ranges
+  if (a.max_nblk > 4096) k_dt_range<1024><<<a.nranges, 1024, 0, st>>>(a);
+  else k_dt_range<256><<<a.nranges, 256, 0, st>>>(a);
   k_dt_final<<<1, 256, 0, st>>>(a);
 }
 
@@ -392,7 +404,8 @@ int p2g_smem_bytes(int dim, int basis, int mode, bool thermal) {
   const int NF = ((L - 1) * SC + S) * WY * WZ;
   const int Q = p2g_nq(mode, thermal), QINP = (p2g_nin(mode, thermal) + 3) & ~3;
   const int slab = (Q * NF + 3) & ~3;
-  return 4 * 8 * (slab + 32 * 4 + 32 * QINP + 32 * dim * S * 2);
+  // affine modes also stage the per-slot offsets (x_node - x_p) / h
+  return 4 * 8 * (slab + 32 * 4 + 32 * QINP + 32 * dim * S * (p2g_apic(mode) ? 3 : 2));
 }
 
 }  // namespace kmpm

@@ -28,7 +28,7 @@ namespace kmpm {
 // Contribution of one staged particle to this lane's stencil nodes.
 template <int DIM, int S, int MODE, bool THERMAL, int Q, int QINP, int NSL, int NS, bool PAIR>
 __device__ __forceinline__ void p2g_particle(float (&accr)[NSL][Q], const float *spay_j, const float2 *bj,
-                                             const int (&soff)[NSL][3], const float (&nco)[NSL][3], int lane) {
+                                             const float *oj, float h, const int (&soff)[NSL][3], int lane) {
   constexpr int BM = p2g_base(MODE);
   constexpr bool AP = p2g_apic(MODE);
   float pay[QINP];
@@ -44,18 +44,20 @@ __device__ __forceinline__ void p2g_particle(float (&accr)[NSL][Q], const float 
     // the lane's nodes share (a, b): with w = wxy s_z and grad w =
     // (gxy0 s_z, gxy1 s_z, wxy s'_z), every term factors into a per-particle
     // part and s_z or s'_z:  m v w = s_z (wxy m v),
-    // f_r -= s_z (T_r0 gxy0 + T_r1 gxy1) + s'_z (T_r2 wxy)  (T = vol0 PK1 or vol sigma).
+    // f_r -= s_z (T_r0 gxy0 + T_r1 gxy1) + s'_z (T_r2 wxy)  (T = vol0 PK1 or vol sigma),
+    // and with external particle forces f_r += s_z (wxy mbp_r).
     // APIC adds m C (x_node - x_p) to m v: its x and y parts join the
-    // per-particle term, its z part s_z (z_node - z_p) (wxy m C_r2) is per node.
+    // per-particle term, its z part s_z (z_node - z_p) (wxy m C_r2) is per node;
+    // x_node - x_p = h o + (x_w - x_p) with the staged offsets o of the weights.
     constexpr int OM = BM == P2G_UL ? 1 : 0;  // UL payload and sums start with the mass
     constexpr bool FORCE = BM != P2G_VEL;
-    constexpr int NB = p2g_nin(BM, false);    // APIC: m C (9) and x_p (3) follow the base payload
+    constexpr int NB = p2g_nin(BM, false);    // APIC: m C (9) and x_w - x_p (3) follow the base payload
     float q[4], t[3], t2[3], qc[3];
 #pragma unroll
     for (int d = 0; d < 3 + OM; d++) q[d] = wxy * pay[d];
     if (AP) {
-      const float *mC = pay + NB, *xp = pay + NB + 9;
-      const float dxa = nco[0][0] - xp[0], dyb = DIM >= 2 ? nco[0][1] - xp[1] : 0.f;
+      const float *mC = pay + NB, *dw = pay + NB + 9;
+      const float dxa = fmaf(oj[soff[0][0]], h, dw[0]), dyb = DIM >= 2 ? fmaf(oj[S + soff[0][1]], h, dw[1]) : 0.f;
 #pragma unroll
       for (int r = 0; r < 3; r++) {
         q[OM + r] = fmaf(wxy, mC[3 * r] * dxa + mC[3 * r + 1] * dyb, q[OM + r]);
@@ -75,6 +77,8 @@ __device__ __forceinline__ void p2g_particle(float (&accr)[NSL][Q], const float 
           T2 = r == 0 ? sg[4] : (r == 1 ? sg[5] : sg[2]);
         }
         t[r] = T0 * gxy0 + T1 * gxy1;
+        // external particle force: f_r += s_z (wxy mbp_r)
+        if (p2g_ext(MODE)) t[r] = fmaf(-wxy, pay[p2g_nin(MODE & ~P2G_EXT, false) + r], t[r]);
         t2[r] = T2 * wxy;
       }
     }
@@ -85,7 +89,7 @@ __device__ __forceinline__ void p2g_particle(float (&accr)[NSL][Q], const float 
 #pragma unroll
       for (int d = 0; d < 3 + OM; d++) accr[u][d] = fmaf(bz.x, q[d], accr[u][d]);
       if (AP && DIM == 3) {
-        const float bzd = bz.x * (nco[u][2] - pay[NB + 9 + 2]);
+        const float bzd = bz.x * fmaf(oj[2 * S + soff[u][2]], h, pay[NB + 9 + 2]);
 #pragma unroll
         for (int r = 0; r < 3; r++) accr[u][OM + r] = fmaf(bzd, qc[r], accr[u][OM + r]);
       }
@@ -124,7 +128,8 @@ __global__ void __launch_bounds__(256) k_p2g(P2GArgs a) {
   constexpr int GS = PAIR ? 32 : (NS <= 4 ? 4 : (NS <= 8 ? 8 : (NS <= 16 ? 16 : 32)));
   constexpr int NG = 32 / GS;
   constexpr int SLAB = (Q * NF + 3) & ~3;
-  constexpr int STAGE = 32 * 4 + 32 * QINP + 32 * DIM * S * 2;
+  constexpr bool AP = p2g_apic(MODE);
+  constexpr int STAGE = 32 * 4 + 32 * QINP + 32 * DIM * S * (AP ? 3 : 2);
 
   extern __shared__ __align__(16) float smem[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -132,6 +137,7 @@ __global__ void __launch_bounds__(256) k_p2g(P2GArgs a) {
   float4 *spos = reinterpret_cast<float4 *>(smem + TS::NWARP * SLAB + warp * STAGE);  // 32
   float *spay = reinterpret_cast<float *>(spos + 32);                                 // 32 * QINP
   float2 *sbas = reinterpret_cast<float2 *>(spay + 32 * QINP);                        // 32 * DIM * S
+  float *sofs = reinterpret_cast<float *>(sbas + 32 * DIM * S);  // affine modes: 32 * DIM * S offsets
 
   const int2 td = a.tiles[blockIdx.x];
   const GridDev g = a.grids[td.x];
@@ -197,14 +203,6 @@ __global__ void __launch_bounds__(256) k_p2g(P2GArgs a) {
     const int tco[3] = {tc[0] * TX, tc[1] * TY, tc[2] * TZ};
 #pragma unroll
     for (int d = 0; d < 3; d++) i0[d] = (d < DIM) ? (tco[d] + lc[d]) * SC - LO : 0;
-    // coordinates of this lane's nodes (APIC: x_node - x_p)
-    float nco[NSL][3];
-#pragma unroll
-    for (int u = 0; u < NSL; u++) {
-      nco[u][0] = glo0 + (float)(i0[0] + soff[u][0]) * h;
-      nco[u][1] = glo1 + (float)(i0[1] + soff[u][1]) * h;
-      nco[u][2] = glo2 + (float)(i0[2] + soff[u][2]) * h;
-    }
 
     float accr[NSL][Q];
 #pragma unroll
@@ -243,11 +241,17 @@ __global__ void __launch_bounds__(256) k_p2g(P2GArgs a) {
           const float4 pj = spos[j];
           const float t = ((d == 0 ? pj.x : (d == 1 ? pj.y : pj.z)) - lod) * ih;
           float sv[4], dsv[4];
-          cubic_weights(t - (float)(i0d + 1), ih, sv, dsv);
-          if (a.mls) {  // MLS forces: the moment s (x_node - x_p) Di in place of the slope
-            const float xp = d == 0 ? pj.x : (d == 1 ? pj.y : pj.z);
+          const float f = t - (float)(i0d + 1);
+          cubic_weights(f, ih, sv, dsv);
+          // (x_node - x_p) / h of the slots from the same f (see Axis::eval)
+          if (AP) {
 #pragma unroll
-            for (int kk = 0; kk < 4; kk++) dsv[kk] = sv[kk] * (lod + (float)(i0d + kk) * h - xp) * a.mls_di;
+            for (int kk = 0; kk < 4; kk++) {
+              const float o = (float)(kk - 1) - f;
+              sofs[it * S + kk] = o;
+              // MLS forces: the moment s (x_node - x_p) Di in place of the slope
+              if (a.mls) dsv[kk] = sv[kk] * (o * h) * a.mls_di;
+            }
           }
 #pragma unroll
           for (int kk = 0; kk < 4; kk++) sbas[it * S + kk] = make_float2(sv[kk], dsv[kk]);
@@ -260,18 +264,20 @@ __global__ void __launch_bounds__(256) k_p2g(P2GArgs a) {
         const int nd = d == 0 ? gn0 : (d == 1 ? gn1 : gn2);
         const int ngd = d == 0 ? gng0 : (d == 1 ? gng1 : gng2);
         const float lod = d == 0 ? glo0 : (d == 1 ? glo1 : glo2);
-        float sv = 0.f, dsv = 0.f;
+        float sv = 0.f, dsv = 0.f, ov = 0.f;
         if (i >= 0 && i < nd) {
           const float xn = lod + (float)i * h;
           const float4 pj = spos[j];
           const float r = ((d == 0 ? pj.x : (d == 1 ? pj.y : pj.z)) - xn) * ih;
           basis<BASIS>(r, node_type<BASIS>(i, ngd), ih, sv, dsv);
           dsv = sv != 0.f ? dsv : 0.f;  // as Axis::eval
+          ov = -r;
           // MLS forces (compute_external_and_internal_forces_nodes_UL_MLS,
           // src/solid.cpp:524-574): w Di (x_node - x_p) in place of grad w
-          if (a.mls) dsv = sv * (xn - (d == 0 ? pj.x : (d == 1 ? pj.y : pj.z))) * a.mls_di;
+          if (AP && a.mls) dsv = sv * (ov * h) * a.mls_di;
         }
         sbas[it] = make_float2(sv, dsv);
+        if (AP) sofs[it] = ov;
       }
       __syncwarp();
       // ---- accumulate (lane = stencil node); two particles per iteration for ILP
@@ -281,24 +287,24 @@ __global__ void __launch_bounds__(256) k_p2g(P2GArgs a) {
           int j = 0;
           for (; j + 1 < cnt; j += 2) {
             p2g_particle<DIM, S, MODE, THERMAL, Q, QINP, NSL, NS, PAIR>(accr, spay + j * QINP, sbas + j * DIM * S,
-                                                                        soff, nco, nl);
-            p2g_particle<DIM, S, MODE, THERMAL, Q, QINP, NSL, NS, PAIR>(accr, spay + (j + 1) * QINP,
-                                                                        sbas + (j + 1) * DIM * S, soff, nco, nl);
+                                                                        sofs + j * DIM * S, h, soff, nl);
+            p2g_particle<DIM, S, MODE, THERMAL, Q, QINP, NSL, NS, PAIR>(accr, spay + (j + 1) * QINP, sbas + (j + 1) * DIM * S,
+                                                                        sofs + (j + 1) * DIM * S, h, soff, nl);
           }
           if (j < cnt)
             p2g_particle<DIM, S, MODE, THERMAL, Q, QINP, NSL, NS, PAIR>(accr, spay + j * QINP, sbas + j * DIM * S,
-                                                                        soff, nco, nl);
+                                                                        sofs + j * DIM * S, h, soff, nl);
         } else {
           int j = grp;
           for (; j + NG < cnt; j += 2 * NG) {
             p2g_particle<DIM, S, MODE, THERMAL, Q, QINP, NSL, NS, PAIR>(accr, spay + j * QINP, sbas + j * DIM * S,
-                                                                        soff, nco, nl);
-            p2g_particle<DIM, S, MODE, THERMAL, Q, QINP, NSL, NS, PAIR>(accr, spay + (j + NG) * QINP,
-                                                                        sbas + (j + NG) * DIM * S, soff, nco, nl);
+                                                                        sofs + j * DIM * S, h, soff, nl);
+            p2g_particle<DIM, S, MODE, THERMAL, Q, QINP, NSL, NS, PAIR>(accr, spay + (j + NG) * QINP, sbas + (j + NG) * DIM * S,
+                                                                        sofs + (j + NG) * DIM * S, h, soff, nl);
           }
           if (j < cnt)
             p2g_particle<DIM, S, MODE, THERMAL, Q, QINP, NSL, NS, PAIR>(accr, spay + j * QINP, sbas + j * DIM * S,
-                                                                        soff, nco, nl);
+                                                                        sofs + j * DIM * S, h, soff, nl);
         }
       }
       __syncwarp();
@@ -631,13 +637,15 @@ __global__ void __launch_bounds__(256, MINB) k_g2p2(PartArgs a) {
       // The per-axis moment s (x_node - x_p) Di takes the place of the slope;
       // x_p is x0 (TL), and for ULMPM the position the reference holds at this
       // point: before the move (USL) or after it (MUSL)
+      // x_node - x_p = h o_k + (x_w - x_p): o_k from the weights (Axis::eval)
+      // and, for ULMPM MUSL, the move x_w - x_p = u - u_moved of this step
       const float Di = (BASIS == 3 ? 4.f : 3.f) * g.inv_cellsize * g.inv_cellsize;
 #pragma unroll
       for (int d = 0; d < DIM; d++) {
-        const float pd = P[(PF_X0 + d) * ps + p] + (TL ? 0.f : P[((a.use_vu ? PF_X : PF_XN) + d) * ps + p]);
+        const float dw = (TL || a.use_vu) ? 0.f : P[(PF_X + d) * ps + p] - P[(PF_XN + d) * ps + p];
 #pragma unroll
         for (int k = 0; k < S; k++)
-          ax.ax[d].ds[k] = ax.ax[d].s[k] * (g.lo[d] + (float)(ax.ax[d].i0 + k) * g.cellsize - pd) * Di;
+          ax.ax[d].ds[k] = ax.ax[d].s[k] * fmaf(ax.ax[d].o[k], g.cellsize, dw) * Di;
       }
     }
     float G[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
@@ -932,6 +940,21 @@ void fill_step_kernels(StepKernels &k) {
     k.p2g_vel_apic = (void *)k_p2g<DIM, BASIS, P2G_VEL_APIC, false>;
   } else {
     k.p2g_tl_apic = k.p2g_ul_apic = k.p2g_vel_apic = nullptr;
+  }
+  if constexpr (DIM >= 2) {  // contact fixes act in 2-D and 3-D runs
+    k.p2g_tl_ext[0] = (void *)k_p2g<DIM, BASIS, P2G_TL | P2G_EXT, false>;
+    k.p2g_tl_ext[1] = (void *)k_p2g<DIM, BASIS, P2G_TL | P2G_EXT, true>;
+    k.p2g_ul_ext[0] = (void *)k_p2g<DIM, BASIS, P2G_UL | P2G_EXT, false>;
+    k.p2g_ul_ext[1] = (void *)k_p2g<DIM, BASIS, P2G_UL | P2G_EXT, true>;
+    if constexpr (BASIS == 1 || BASIS == 3) {
+      k.p2g_tl_apic_ext = (void *)k_p2g<DIM, BASIS, P2G_TL_APIC | P2G_EXT, false>;
+      k.p2g_ul_apic_ext = (void *)k_p2g<DIM, BASIS, P2G_UL_APIC | P2G_EXT, false>;
+    } else {
+      k.p2g_tl_apic_ext = k.p2g_ul_apic_ext = nullptr;
+    }
+  } else {
+    k.p2g_tl_ext[0] = k.p2g_tl_ext[1] = k.p2g_ul_ext[0] = k.p2g_ul_ext[1] = nullptr;
+    k.p2g_tl_apic_ext = k.p2g_ul_apic_ext = nullptr;
   }
   k.grid_mass[0] = (void *)k_grid<DIM, BASIS, GM_MASS, true, false, float>;
   k.grid_mass[1] = (void *)k_grid<DIM, BASIS, GM_MASS, true, false, double>;

@@ -34,7 +34,7 @@ EXPORTED = ["kmpm_create", "kmpm_destroy", "kmpm_last_error", "kmpm_add_material
             "kmpm_mlp_get_params", "kmpm_mlp_set_norm", "kmpm_mlp_get_norm", "kmpm_mlp_loss_grad", "kmpm_mlp_train",
             "kmpm_mlp_predict", "kmpm_mlp_predict_tc", "kmpm_log_start", "kmpm_log_stop", "kmpm_log_data",
             "kmpm_jc_label", "kmpm_set_surrogate", "kmpm_surrogate_stats", "kmpm_tuning",
-            "kmpm_download_particles_async", "kmpm_sync_downloads"]
+            "kmpm_download_particles_async", "kmpm_sync_downloads", "kmpm_add_contact", "kmpm_contact_force"]
 
 MLP_NIN, MLP_NOUT, MLP_NPARAMS, MLP_NNORM = 15, 7, 35975, 74
 
@@ -123,6 +123,8 @@ def load(path: str = LIB_PATH):
     L.kmpm_download_particles_async.argtypes = [p, i, i, fp]
     L.kmpm_sync_downloads.argtypes = [p]
     L.kmpm_tuning.restype = ctypes.c_char_p
+    L.kmpm_add_contact.argtypes = [p, i, i, i, d]
+    L.kmpm_contact_force.argtypes = [p, i, dp]
     _lib = L
     return L
 
@@ -171,6 +173,8 @@ class GpuBackend:
                                       sol.T0), allow_id=True)
         for f in s.fixes:
             self.add_fix(f)
+        for c in s.contacts:
+            self.add_contact(c)
 
     def _ck(self, r, allow_id=False):
         if r < 0 or (r != KMPM_OK and not allow_id):
@@ -191,6 +195,14 @@ class GpuBackend:
         coef = np.ascontiguousarray(f.coef, float).ravel()
         self._ck(self.L.kmpm_add_fix(self.h, f.kind, f.grid, mask.ctypes.data_as(ctypes.POINTER(ctypes.c_ubyte)),
                                      st, _dp(coef)), allow_id=True)
+
+    def add_contact(self, c: sc.ContactSpec) -> int:
+        return self._ck(self.L.kmpm_add_contact(self.h, c.kind, c.solid1, c.solid2, c.mu), allow_id=True)
+
+    def contact_force(self, k: int):
+        out = np.zeros(3)
+        self._ck(self.L.kmpm_contact_force(self.h, int(k), _dp(out)))
+        return out
 
     def run(self, n: int):
         self._ck(self.L.kmpm_run(self.h, int(n)))

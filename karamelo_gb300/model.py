@@ -80,6 +80,7 @@ class MPM:
         self.solid_ids: Dict[str, int] = {}
         self.groups: Dict[str, dict] = {}
         self.energy_fixes: Dict[str, str] = {}
+        self.contact_ids: Dict[str, int] = {}
         self.np_total = 0
         self.method_set = False
         self.dim_set = False
@@ -376,6 +377,27 @@ class MPM:
     def fix(self, name, kind, group, *vals):
         """Modify::add_fix for the fixes the GPU method lowers; any other fix is an error
         (the GPU path has no CPU fallback)."""
+        if kind in sc.CONTACT_STYLES:
+            # fix(ID, contact/minimize_penetration, solid1, solid2, mu) and
+            # fix(ID, contact/hertz, solid1, solid2): the third argument is a solid
+            # (src/fix_contact_min_penetration.cpp:55-73, src/fix_contact_hertz.cpp:52-70)
+            code = sc.CONTACT_STYLES[kind]
+            args = [group] + list(vals)
+            need = 3 if code == sc.CONTACT_MIN_PENETRATION else 2
+            if len(args) < need:
+                raise KarameloError("Error: not enough arguments.")
+            ids = []
+            for nm in args[:2]:
+                if nm not in self.solid_ids:
+                    raise KarameloError(f"Error: solid {nm} unknown.")
+                ids.append(self.solid_ids[nm])
+            mu = float(args[2]) if code == sc.CONTACT_MIN_PENETRATION else 0.0
+            c = sc.ContactSpec(kind=code, solid1=ids[0], solid2=ids[1], mu=mu, name=name)
+            self.s.contacts.append(c)
+            self.contact_ids[name] = len(self.s.contacts) - 1
+            if self.backend is not None:
+                self.backend.add_contact(c)
+            return
         if kind not in _SUPPORTED_FIXES:
             raise KarameloError(f"fix {kind} is not supported by the GPU method")
         if group != "all" and group not in self.groups:
@@ -450,6 +472,10 @@ class MPM:
     def energies(self):
         """(Ek, Es): FixKineticEnergy / ComputeStrainEnergy over all solids."""
         return self._ensure_backend().energies()
+
+    def contact_force(self, name):
+        """The contact fix's variables (ID_x, ID_y, ID_z) after the last step."""
+        return self._ensure_backend().contact_force(self.contact_ids[name])
 
     @property
     def time(self):

@@ -29,6 +29,8 @@ DAMAGE_NONE, DAMAGE_JC = -1, 0
 TEMP_NONE, TEMP_PLASTIC_WORK = -1, 0
 
 FIX_VELOCITY_NODES, FIX_BODY_FORCE = 0, 1
+CONTACT_MIN_PENETRATION, CONTACT_HERTZ = 0, 1
+CONTACT_STYLES = {"contact/minimize_penetration": CONTACT_MIN_PENETRATION, "contact/hertz": CONTACT_HERTZ}
 
 
 class MaterialParams(ctypes.Structure):
@@ -133,6 +135,18 @@ class FixSpec:
 
 
 @dataclass
+class ContactSpec:
+    """A contact fix between two solids (``fix(ID, contact/minimize_penetration,
+    solid1, solid2, mu)``, src/fix_contact_min_penetration.cpp:33-73, or
+    ``fix(ID, contact/hertz, solid1, solid2)``, src/fix_contact_hertz.cpp:33-70)."""
+    kind: int
+    solid1: int
+    solid2: int
+    mu: float = 0.0
+    name: str = ""
+
+
+@dataclass
 class Scenario:
     method: int = TLMPM
     scheme: int = MUSL
@@ -150,6 +164,7 @@ class Scenario:
     grids: List[GridSpec] = field(default_factory=list)
     solids: List[SolidSpec] = field(default_factory=list)
     fixes: List[FixSpec] = field(default_factory=list)
+    contacts: List[ContactSpec] = field(default_factory=list)
 
     @property
     def total_particles(self) -> int:

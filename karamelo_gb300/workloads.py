@@ -186,3 +186,67 @@ def tensile_bar_2d(backend_factory=None, cellsize=0.4, hLx=10.0, hLy=2.0, ppc=2,
         sim.fix("BC_right", "velocity_nodes", "gr", vend, None)
     sim.dt_factor(dt_factor)
     return sim
+
+
+def bouncing_balls(backend_factory=None, method="tlmpm/gpu", sub="FLIP", basis="linear", pic_flip=0.99,
+                   contact="contact/minimize_penetration", mu=0.0, N=40, ppc=2, v=0.1, R=0.2, centre=0.3,
+                   offset=0.0, dt=1e-3, E=1e3, scheme="musl", vy=None):
+    """Two linear-elastic balls meeting through a contact fix
+    (examples/Bouncing_balls/TLMPM/FLIP/bouncing_balls2.mpm:1-68: 2-D unit box,
+    N = 40 cells per side, R = 0.2, 2x2 particles per cell, +-v per axis,
+    E = 1e3, nu = 0.3, rho = 1000, dt = 1e-3).  The balls sit at +-(centre,
+    centre); ``offset`` shifts both across the line of approach (+-offset along
+    (1, -1)/sqrt 2) for an oblique impact; ``vy`` replaces the y velocity."""
+    L = 1.0
+    hL = 0.5 * L
+    cellsize = L / N
+    sim = MPM(backend_factory)
+    _method(sim, method, sub, basis, pic_flip)
+    sim.scheme(scheme)
+    sim.dimension(2, -hL, hL, -hL, hL, cellsize)
+    s = offset / np.sqrt(2.0)
+    sim.region("rBall1", "cylinder", -centre + s, -centre - s, R)
+    sim.region("rBall2", "cylinder", centre - s, centre + s, R)
+    sim.material("mat1", "linear", 1000, E, 0.3)
+    sim.solid("sBall1", "region", "rBall1", ppc, "mat1", cellsize, 0)
+    sim.solid("sBall2", "region", "rBall2", ppc, "mat1", cellsize, 0)
+    sim.group("gBall1", "particles", "region", "rBall1", "solid", "sBall1")
+    sim.group("gBall2", "particles", "region", "rBall2", "solid", "sBall2")
+    vy = v if vy is None else vy
+    sim.fix("v0Ball1", "initial_velocity_particles", "gBall1", v, vy, None)
+    sim.fix("v0Ball2", "initial_velocity_particles", "gBall2", -v, -vy, None)
+    if contact == "contact/hertz":
+        sim.fix("contact", contact, "sBall1", "sBall2")
+    elif contact:
+        sim.fix("contact", contact, "sBall1", "sBall2", mu)
+    sim.fix("Ek", "kinetic_energy", "all")
+    sim.fix("Es", "strain_energy", "all")
+    sim.set_dt(dt)
+    return sim
+
+
+def hertz_spheres(backend_factory=None, method="tlmpm/gpu", sub="FLIP", basis="cubic-spline", pic_flip=0.99,
+                  contact="contact/hertz", mu=0.0, cellsize=0.05, ppc=2, v=0.5, R=0.1, gap=0.01, dt=2e-4,
+                  E=1e4, scheme="musl"):
+    """Two linear-elastic spheres approaching along x in a 3-D box, in contact
+    through a contact fix (the 3-D branch of both fixes)."""
+    sim = MPM(backend_factory)
+    _method(sim, method, sub, basis, pic_flip)
+    sim.scheme(scheme)
+    sim.dimension(3, -0.5, 0.5, -0.25, 0.25, -0.25, 0.25, cellsize)
+    c = R + 0.5 * gap
+    sim.region("rA", "sphere", -c, 0.0, 0.0, R)
+    sim.region("rB", "sphere", c, 0.0, 0.0, R)
+    sim.material("mat1", "linear", 1000, E, 0.3)
+    sim.solid("sA", "region", "rA", ppc, "mat1", cellsize, 0)
+    sim.solid("sB", "region", "rB", ppc, "mat1", cellsize, 0)
+    sim.group("gA", "particles", "region", "rA", "solid", "sA")
+    sim.group("gB", "particles", "region", "rB", "solid", "sB")
+    sim.fix("vA", "initial_velocity_particles", "gA", v, 0.0, 0.0)
+    sim.fix("vB", "initial_velocity_particles", "gB", -v, 0.0, 0.0)
+    if contact == "contact/hertz":
+        sim.fix("contact", contact, "sA", "sB")
+    else:
+        sim.fix("contact", contact, "sA", "sB", mu)
+    sim.set_dt(dt)
+    return sim

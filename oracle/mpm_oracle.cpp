@@ -346,12 +346,15 @@ struct Mat {
   om_material d;
   int type;
   double rho0, K, G, lambda, signal_velocity, cp, invcp, kappa;
+  double E, nu;  // Young's modulus and Poisson ratio (derived from K and G for EOS materials)
   // Mat::Mat, src/material.cpp:720-778
   explicit Mat(const om_material &m) : d(m), type(m.type) {
     if (type == MAT_EOS_STRENGTH) {
       rho0 = m.eos_p[0];
       K = m.eos_p[1];
       G = m.str_p[0];
+      E = 9 * K * G / (3 * K + G);
+      nu = (3 * K - 2 * G) / (2 * (3 * K + G));
       lambda = K - 2 * G / 3;
       signal_velocity = std::sqrt((lambda + 2 * G) / rho0);
       if (m.temp >= 0) {
@@ -363,7 +366,8 @@ struct Mat {
       }
     } else {
       rho0 = m.rho0;
-      double E = m.E, nu = m.nu;
+      E = m.E;
+      nu = m.nu;
       G = E / (2 * (1 + nu));
       lambda = E * nu / ((1 + nu) * (1 - 2 * nu));
       K = E / (3 * (1 - 2 * nu));
@@ -407,6 +411,14 @@ struct Fix {
   double c[3][4];  // velocity: v(t) = c0 + c1 t + c2 exp(c3 t); body force: c0
 };
 
+// contact fix between two solids (FixContactMinPenetration, FixContactHertz)
+enum { CONTACT_MIN_PENETRATION = 0, CONTACT_HERTZ = 1 };
+struct Contact {
+  int kind, s1, s2;
+  double mu;
+  double ftot[3] = {0, 0, 0};  // the fix's <id>_x, _y, _z
+};
+
 struct Sim {
   int method, scheme, basis, dim;
   double pic_flip;
@@ -424,6 +436,7 @@ struct Sim {
   std::vector<Grid> grids;
   std::vector<Solid> solids;
   std::vector<Fix> fixes;
+  std::vector<Contact> contacts;
   std::string err;
   double (*bf)(double, int) = bf_linear;
   double (*dbf)(double, int, double) = dbf_linear;
@@ -930,6 +943,92 @@ void update_heat_flux(Sim &s, Solid &S, bool doublemapping) {
 }
 
 // one time step, src/usl.cpp:43-92 and src/musl.cpp:43-93
+// Contact fixes, initial_integrate: every pair (ip1 of solid1, ip2 of
+// solid2) in the reference's loop order, so that each particle's mbp sums its
+// pairs in the same order (FixContactMinPenetration::initial_integrate,
+// src/fix_contact_min_penetration.cpp:83-235; FixContactHertz::initial_integrate,
+// src/fix_contact_hertz.cpp:82-197).  Only 2-D and 3-D runs take a contact.
+void contact_forces(Sim &s, Contact &C) {
+  Solid &A = s.solids[C.s1], &B = s.solids[C.s2];
+  const Mat &ma = s.mats[A.mat], &mb = s.mats[B.mat];
+  const double Estar = 1.0 / ((1 - ma.nu * ma.nu) / ma.E + (1 - mb.nu * mb.nu) / mb.E);
+  const double alpha = ma.kappa / (ma.kappa + mb.kappa);
+  const double cmax = std::max(s.grids[A.grid].cellsize, s.grids[B.grid].cellsize);
+  const bool hertz = C.kind == CONTACT_HERTZ;
+  // the reference's own constant for 4/3 in both fixes (#define four_thirds)
+  const double hertz_coef = s.dim == 3 ? 1.333333333 : 0.25 * M_PI;
+  const int dim = s.dim;
+  double ft[3] = {0, 0, 0};
+  auto radius = [&](double vol) {
+    if (dim == 3) return hertz ? 0.5 * std::pow(vol, 0.333333333) : 0.5 * std::cbrt(vol);
+    return 0.5 * std::sqrt(vol);
+  };
+  if (dim == 2 || dim == 3) {
+    for (int i = 0; i < A.np; i++) {
+      for (int j = 0; j < B.np; j++) {
+        double dx[3];
+        for (int d = 0; d < 3; d++) dx[d] = B.x[3 * j + d] - A.x[3 * i + d];
+        // per-axis screen on the larger cellsize (the 2-D min-penetration fix
+        // screens x and y only; z differences are zero in 2-D runs)
+        bool near = true;
+        const int ns = (dim == 2 && !hertz) ? 2 : 3;
+        for (int d = 0; d < ns; d++) near = near && dx[d] < cmax && dx[d] > -cmax;
+        if (!near) continue;
+        const double R1 = radius(A.vol[i]), R2 = radius(B.vol[j]), Rp = R1 + R2;
+        for (int d = 0; d < ns; d++) near = near && dx[d] < Rp && dx[d] > -Rp;
+        if (!near) continue;
+        const double r = std::sqrt(dx[0] * dx[0] + dx[1] * dx[1] + dx[2] * dx[2]);
+        if (!(r < Rp)) continue;
+        double f[3];
+        if (hertz) {
+          const double p = Rp - r;  // penetration
+          const double fmag = hertz_coef * Estar * std::sqrt(R1 * R2 / (R1 + R2) * p * p * p);
+          for (int d = 0; d < 3; d++) f[d] = fmag * dx[d] / r;
+          for (int d = 0; d < 3; d++) {
+            A.mbp[3 * i + d] -= f[d];
+            B.mbp[3 * j + d] += f[d];
+            ft[d] += f[d];
+          }
+          continue;
+        }
+        const double ir = 1.0 / r;
+        const double fmag = A.mass[i] * B.mass[j] / ((A.mass[i] + B.mass[j]) * s.dt * s.dt) * (1 - Rp * ir);
+        for (int d = 0; d < 3; d++) f[d] = fmag * dx[d];
+        if (C.mu != 0) {
+          double dv[3], vt[3];
+          for (int d = 0; d < 3; d++) dv[d] = B.v[3 * j + d] - A.v[3 * i + d];
+          const double dvn = (dv[0] * dx[0] + dv[1] * dx[1] + dv[2] * dx[2]) * ir * ir;
+          for (int d = 0; d < 3; d++) vt[d] = dv[d] - dvn * dx[d];
+          const double vtn = std::sqrt(vt[0] * vt[0] + vt[1] * vt[1] + vt[2] * vt[2]);
+          if (vtn != 0) {
+            const double ffric = C.mu * fmag * r;
+            for (int d = 0; d < 3; d++) f[d] -= ffric * (vt[d] / vtn);
+            if (s.thermal) {
+              // frictional heat: split alpha / (1 - alpha) in 2-D; in 3-D the
+              // reference gives both solids the share alpha
+              if (dim == 2) {
+                const double g = ffric * vtn * s.dt;
+                A.gamma[i] += alpha * A.vol0[i] * ma.invcp * g;
+                B.gamma[j] += (1.0 - alpha) * B.vol0[j] * mb.invcp * g;
+              } else {
+                const double g = alpha * ffric * vtn * s.dt;
+                A.gamma[i] += A.vol0[i] * ma.invcp * g;
+                B.gamma[j] += B.vol0[j] * mb.invcp * g;
+              }
+            }
+          }
+        }
+        for (int d = 0; d < 3; d++) {
+          A.mbp[3 * i + d] += f[d];
+          B.mbp[3 * j + d] -= f[d];
+          ft[d] += f[d];
+        }
+      }
+    }
+  }
+  for (int d = 0; d < 3; d++) C.ftot[d] = ft[d];
+}
+
 bool step(Sim &s) {
   bool TL = s.method == TLMPM;
   bool musl = s.scheme == MUSL;
@@ -944,6 +1043,8 @@ bool step(Sim &s) {
     S.dtCFL = 1.0e22;
     std::fill(S.mbp.begin(), S.mbp.end(), 0.0);
   }
+  // initial_integrate: the contact fixes (src/musl.cpp:49, src/usl.cpp:49, src/usf.cpp:49)
+  for (auto &C : s.contacts) contact_forces(s, C);
   // particles_to_grid (src/tlmpm.cpp:342-366, src/ulmpm.cpp:338-378), body
   // forces, update_grid_state and the velocity fixes
   auto p2g_grid = [&]() {
@@ -1267,6 +1368,18 @@ int om_add_fix(void *h, int kind, int grid, const uint8_t *mask, const int *set,
   }
   s->fixes.push_back(f);
   return (int)s->fixes.size() - 1;
+}
+// contact fix: kind 0 contact/minimize_penetration, 1 contact/hertz
+int om_add_contact(void *h, int kind, int s1, int s2, double mu) {
+  Sim *s = (Sim *)h;
+  Contact C;
+  C.kind = kind; C.s1 = s1; C.s2 = s2; C.mu = mu;
+  s->contacts.push_back(C);
+  return (int)s->contacts.size() - 1;
+}
+void om_contact_force(void *h, int k, double *out) {
+  Sim *s = (Sim *)h;
+  for (int d = 0; d < 3; d++) out[d] = s->contacts[k].ftot[d];
 }
 int om_set_threads(int n) {
 #ifdef _OPENMP

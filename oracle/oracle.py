@@ -66,6 +66,8 @@ def lib():
         L.om_poldec.argtypes = [dp, dp]
         L.om_eig_real.argtypes = [dp, dp]
         L.om_set_threads.argtypes = [i]
+        L.om_add_contact.argtypes = [p, i, i, i, d]
+        L.om_contact_force.argtypes = [p, i, dp]
         _lib = L
     return _lib
 
@@ -118,6 +120,8 @@ class OracleBackend:
             L.om_add_solid(self.h, sol.grid, sol.mat, sol.np, _dp(x0), _dp(v), _dp(m), _dp(vo), sol.T0)
         for f in s.fixes:
             self.add_fix(f)
+        for c in getattr(s, "contacts", []):
+            self.add_contact(c)
 
     def _solid_hi(self, sol):
         return self.s.grids[sol.grid].hi
@@ -144,6 +148,14 @@ class OracleBackend:
         st = (ctypes.c_int * 3)(*f.set)
         coef = np.ascontiguousarray(f.coef, float).ravel()
         self.L.om_add_fix(self.h, f.kind, f.grid, mask.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8)), st, _dp(coef))
+
+    def add_contact(self, c):
+        return self.L.om_add_contact(self.h, c.kind, c.solid1, c.solid2, c.mu)
+
+    def contact_force(self, k):
+        out = np.zeros(3)
+        self.L.om_contact_force(self.h, int(k), _dp(out))
+        return out
 
     def run(self, n):
         if self.L.om_run(self.h, int(n)) != 0:
