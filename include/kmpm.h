@@ -88,6 +88,14 @@ typedef struct {
                         APIC (and for ULMPM AFLIP, ASFLIP, MLS): affine transfers,
                         src/solid.cpp:392-426, 524-574, 1006-1153; cubic or quadratic spline,
                         mechanical runs; APIC and MLS set pic_flip = 0 */
+  int axisymmetric;  /* Domain::axisymmetric (src/domain.cpp:554-570): 2-D runs with x = r and
+                        y = z.  Adds the hoop terms: -vol0 PK1(2,2) w / x0_r (TL) or
+                        -vol sigma(2,2) w / x_r (UL) to the radial node force
+                        (src/solid.cpp:472-475, 513-519, 565-571) and v_r w / r to
+                        Fdot(2,2) / L(2,2) (src/solid.cpp:818-829, 900-913, 1046-1058,
+                        1120-1132).  The caller passes masses and volumes already
+                        multiplied by x0_r (Solid::populate, src/solid.cpp:2292-2295).
+                        Mechanical runs only (src/solid.cpp:2789-2792). */
 } kmpm_params;
 
 /* One material: Mat (src/material.h:45-68) with its EOS / Strength / Damage /

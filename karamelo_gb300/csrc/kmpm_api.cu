@@ -57,8 +57,10 @@ struct kmpm_ctx {
   std::vector<ContactDev> contacts;
   float *d_mbp = nullptr;             // external particle forces, 3 rows of ps floats
   bool contacts_dirty = false;
-  int smem_ext[2][2] = {{0}};         // dynamic shared memory of the scatters with mbp: [UL][thermal]
-  int smem_apic_ext[2] = {0, 0};      // [UL]
+  // the force scatter of this configuration (select_scatters) and the
+  // non-affine one of the USF scheme's second pass, with their shared memory
+  void *sc_force = nullptr, *sc_usf = nullptr;
+  int smem_force = 0, smem_usf = 0;
   // ---- device layout
   size_t ps = 0;
   int nblk_p = 0;
@@ -250,6 +252,7 @@ PartArgs part_args(kmpm_ctx *c) {
   a.track_strain = c->prm.track_strain;
   a.apic = c->apic() ? 1 : 0;
   a.asflip = (!c->TL() && c->prm.transfer == KMPM_TRANSFER_ASFLIP) ? 1 : 0;
+  a.axisym = c->prm.axisymmetric;
   a.dim = c->prm.dim;
   for (int d = 0; d < 3; d++) a.tile_t[d] = c->tdim[d];
   return a;
@@ -773,23 +776,7 @@ int setup_contacts(kmpm_ctx *c) {
   c->contacts_dirty = false;
   c->graph_valid = false;
   if (c->hcontacts.empty()) return KMPM_OK;
-  const int dim = c->prm.dim, basis = c->prm.basis;
-  if (dim >= 2) {
-    // the force scatters with external particle forces
-    void *fx[2][2] = {{c->K.p2g_tl_ext[0], c->K.p2g_tl_ext[1]}, {c->K.p2g_ul_ext[0], c->K.p2g_ul_ext[1]}};
-    for (int ul = 0; ul < 2; ul++)
-      for (int th = 0; th < 2; th++) {
-        c->smem_ext[ul][th] = p2g_smem_bytes(dim, basis, (ul ? P2G_UL : P2G_TL) | P2G_EXT, th == 1);
-        CK(cudaFuncSetAttribute(fx[ul][th], cudaFuncAttributeMaxDynamicSharedMemorySize, c->smem_ext[ul][th]));
-      }
-    if (c->apic()) {
-      void *fa[2] = {c->K.p2g_tl_apic_ext, c->K.p2g_ul_apic_ext};
-      for (int ul = 0; ul < 2; ul++) {
-        c->smem_apic_ext[ul] = p2g_smem_bytes(dim, basis, (ul ? P2G_UL_APIC : P2G_TL_APIC) | P2G_EXT, false);
-        CK(cudaFuncSetAttribute(fa[ul], cudaFuncAttributeMaxDynamicSharedMemorySize, c->smem_apic_ext[ul]));
-      }
-    }
-  }
+  const int dim = c->prm.dim;
   DALLOC(c->d_mbp, 3 * c->ps);
   CK(cudaMemsetAsync(c->d_mbp, 0, sizeof(float) * 3 * c->ps, c->st));
   for (const auto &h : c->hcontacts) {
@@ -840,9 +827,41 @@ int setup_contacts(kmpm_ctx *c) {
     DALLOC(d.ftot, 3);
     CK(cudaMemsetAsync(d.ftot, 0, 3 * sizeof(double), c->st));
     d.mbp = c->d_mbp;
+    d.axisym = c->prm.axisymmetric;
     c->contacts.push_back(d);
   }
   CK(cudaStreamSynchronize(c->st));
+  return KMPM_OK;
+}
+
+// The scatter kernel of one force mode: the mode's base (TL / UL), affine
+// transfers, external particle forces (contact fixes) and the axisymmetric
+// hoop term select the instantiation.
+void *force_scatter_fn(const kmpm_ctx *c, int mode, bool th) {
+  const StepKernels &K = c->K;
+  const bool ul = p2g_base(mode) == P2G_UL, ap = p2g_apic(mode), ex = p2g_ext(mode);
+  if (p2g_axi(mode)) return th ? nullptr : K.p2g_axi[ul][ap][ex];
+  if (ex) {
+    if (ap) return th ? nullptr : (ul ? K.p2g_ul_apic_ext : K.p2g_tl_apic_ext);
+    return ul ? K.p2g_ul_ext[th] : K.p2g_tl_ext[th];
+  }
+  if (ap) return th ? nullptr : (ul ? K.p2g_ul_apic : K.p2g_tl_apic);
+  return ul ? (th ? K.p2g_ul_th : K.p2g_ul) : (th ? K.p2g_tl_th : K.p2g_tl);
+}
+
+int select_scatters(kmpm_ctx *c) {
+  const bool TL = c->TL(), th = c->prm.thermal != 0;
+  const int flags = (!c->contacts.empty() && c->prm.dim >= 2 ? P2G_EXT : 0) | (c->prm.axisymmetric ? P2G_AXI : 0);
+  const int base = TL ? P2G_TL : P2G_UL;
+  const int mode = (c->apic() ? base + 3 : base) | flags;
+  const int mode_usf = base | flags;
+  c->sc_force = force_scatter_fn(c, mode, th);
+  c->sc_usf = force_scatter_fn(c, mode_usf, false);
+  if (!c->sc_force || !c->sc_usf) return fail(c, KMPM_ERR_ARG, "no scatter kernel for this combination");
+  c->smem_force = p2g_smem_bytes(c->prm.dim, c->prm.basis, mode, th);
+  c->smem_usf = p2g_smem_bytes(c->prm.dim, c->prm.basis, mode_usf, false);
+  CK(cudaFuncSetAttribute(c->sc_force, cudaFuncAttributeMaxDynamicSharedMemorySize, c->smem_force));
+  CK(cudaFuncSetAttribute(c->sc_usf, cudaFuncAttributeMaxDynamicSharedMemorySize, c->smem_usf));
   return KMPM_OK;
 }
 
@@ -887,13 +906,9 @@ int enqueue_step(kmpm_ctx *c) {
   const bool apic = c->apic();
   // particles_to_grid (APIC: compute_velocity_nodes_APIC with x_p = x0 (TL) or x (UL))
   p.apic_pos = TL ? -1 : PF_X;
-  if (ext) {
-    // the same scatters with w mbp added to the node forces
-    if (apic) LAUNCH(TL ? c->K.p2g_tl_apic_ext : c->K.p2g_ul_apic_ext, c->ntiles_launch, 256, c->smem_apic_ext[TL ? 0 : 1], p);
-    else LAUNCH(TL ? c->K.p2g_tl_ext[th] : c->K.p2g_ul_ext[th], c->ntiles_launch, 256, c->smem_ext[TL ? 0 : 1][th], p);
-  } else if (apic) LAUNCH(TL ? c->K.p2g_tl_apic : c->K.p2g_ul_apic, c->ntiles_launch, 256, c->smem_apic[TL ? 0 : 1], p);
-  else if (TL) LAUNCH(th ? c->K.p2g_tl_th : c->K.p2g_tl, c->ntiles_launch, 256, c->smem[1][th], p);
-  else LAUNCH(th ? c->K.p2g_ul_th : c->K.p2g_ul, c->ntiles_launch, 256, c->smem[2][th], p);
+  // (with w mbp added to the node forces when contacts exist, and the hoop
+  // term in axisymmetric runs: select_scatters)
+  LAUNCH(c->sc_force, c->ntiles_launch, 256, c->smem_force, p);
   MARK("p2g");
   // update_grid_state + fixes
   LAUNCH(c->K.grid_upd[TL][th][prec], c->nblk_g, 256, 0, g1);
@@ -906,9 +921,7 @@ int enqueue_step(kmpm_ctx *c) {
     ps.use_vu = 0;
     LAUNCH((th || prec) ? c->K.g2p2[TL][th][prec] : c->K.g2p2_v[TL][c->var_g2p2], c->nblk_p, 256, 0, ps);
     MARK("g2p_stress");
-    if (ext) LAUNCH(TL ? c->K.p2g_tl_ext[0] : c->K.p2g_ul_ext[0], c->ntiles_launch, 256, c->smem_ext[TL ? 0 : 1][0], p);
-    else if (TL) LAUNCH(c->K.p2g_tl, c->ntiles_launch, 256, c->smem[1][0], p);
-    else LAUNCH(c->K.p2g_ul, c->ntiles_launch, 256, c->smem[2][0], p);
+    LAUNCH(c->sc_usf, c->ntiles_launch, 256, c->smem_usf, p);
     MARK("p2g_forces");
     LAUNCH(c->K.grid_upd[TL][th][prec], c->nblk_g, 256, 0, g1);
     MARK("grid_update2");
@@ -1022,6 +1035,10 @@ int prepare(kmpm_ctx *c) {
     int r = setup_contacts(c);
     if (r != KMPM_OK) return r;
   }
+  if (!c->graph_valid) {
+    int r = select_scatters(c);
+    if (r != KMPM_OK) return r;
+  }
   return ensure_graph(c);
 }
 
@@ -1117,6 +1134,7 @@ int kmpm_create(const kmpm_params *params, kmpm_ctx **out) {
   if (p.independent && p.method != KMPM_TLMPM) return KMPM_ERR_ARG;  // ULMPM solids share one grid
   if (p.transfer < KMPM_TRANSFER_FLIP || p.transfer > KMPM_TRANSFER_MLS) return KMPM_ERR_ARG;
   if (p.transfer == KMPM_TRANSFER_MLS && p.method != KMPM_ULMPM) return KMPM_ERR_ARG;  // MLS is a ULMPM path
+  if (p.axisymmetric && (p.dim != 2 || p.thermal)) return KMPM_ERR_ARG;  // 2-D, mechanical
   {
     // affine transfers: the cubic or quadratic spline, mechanical runs
     const bool affine = p.transfer == KMPM_TRANSFER_APIC || (p.method == KMPM_ULMPM && p.transfer >= KMPM_TRANSFER_AFLIP);

@@ -58,7 +58,10 @@ __global__ void k_contact_prep(PartArgs a, ContactDev c) {
   const float vol = (1.f + jm1_of_H(H)) * P[PF_VOL0 * ps + p];
   // Rp = 0.5 vol^(1/3) (3-D; the Hertz fix writes pow(vol, 0.333333333), which
   // differs from the cube root by less than FP32 resolution) or 0.5 vol^(1/2)
-  const float Rp = c.dim == 3 ? 0.5f * cbrtf(vol) : 0.5f * sqrtf(vol);
+  // (the 2-D min-penetration fix takes vol / x_r in axisymmetric runs,
+  // src/fix_contact_min_penetration.cpp:119-125)
+  const float Rp = c.dim == 3 ? 0.5f * cbrtf(vol)
+                              : 0.5f * sqrtf((c.axisym && c.kind == KMPM_CONTACT_MIN_PENETRATION) ? vol / x[0] : vol);
   int cell[3] = {0, 0, 0};
   for (int d = 0; d < c.dim; d++) cell[d] = (int)floorf((x[d] - c.boxlo[d]) * c.inv_cmax);
   c.ra[i] = make_float4(x[0], x[1], x[2], Rp);

@@ -21,8 +21,13 @@ enum P2GMode : int {
   // f + mb of Grid::update_grid_velocities (src/grid.cpp:456), filled by
   // Solid::compute_external_forces_nodes (src/solid.cpp:428-449)
   P2G_EXT = 8,
+  // flag on the force modes of axisymmetric runs: the hoop term
+  // T_zz / r (1) joins the payload, and -w T_zz / r the radial force sums
+  // (src/solid.cpp:472-475, 513-519, 565-571)
+  P2G_AXI = 16,
 };
 __host__ __device__ constexpr int p2g_kind(int mode) { return mode & 7; }
+__host__ __device__ constexpr bool p2g_axi(int mode) { return (mode & P2G_AXI) != 0; }
 __host__ __device__ constexpr int p2g_base(int mode) { return p2g_kind(mode) >= P2G_TL_APIC ? p2g_kind(mode) - 3 : p2g_kind(mode); }
 __host__ __device__ constexpr bool p2g_apic(int mode) { return p2g_kind(mode) >= P2G_TL_APIC; }
 __host__ __device__ constexpr bool p2g_ext(int mode) { return (mode & P2G_EXT) != 0; }
@@ -39,7 +44,7 @@ __host__ __device__ constexpr int p2g_nin(int mode, bool th) {
           : p2g_base(mode) == P2G_TL ? (th ? 17 : 12)
           : p2g_base(mode) == P2G_UL ? (th ? 15 : 10)
                                      : (th ? 4 : 3)) +
-         (p2g_apic(mode) ? 12 : 0) + (p2g_ext(mode) ? 3 : 0);
+         (p2g_apic(mode) ? 12 : 0) + (p2g_ext(mode) ? 3 : 0) + (p2g_axi(mode) ? 1 : 0);
 }
 
 struct P2GArgs {
@@ -95,6 +100,7 @@ struct PartArgs {
   int tile_t[3];
   int apic;                  // APIC transfers: k_g2p2 forms grad v from moments and stores PF_C
   int asflip;                // ULMPM ASFLIP: positions move with the blended velocity
+  int axisym;                // 2-D axisymmetric: Fdot(2,2) / L(2,2) += v_r w / r
 };
 
 struct DtArgs {
@@ -119,6 +125,8 @@ struct StepKernels {
   void *p2g_tl_apic, *p2g_ul_apic, *p2g_vel_apic;  // cubic spline only (nullptr otherwise)
   // the force scatters with external particle forces (P2G_EXT): [thermal]
   void *p2g_tl_ext[2], *p2g_ul_ext[2], *p2g_tl_apic_ext, *p2g_ul_apic_ext;
+  // 2-D axisymmetric force scatters (P2G_AXI): [UL][APIC][EXT] (nullptr elsewhere)
+  void *p2g_axi[2][2][2];
   void *grid_mass[2], *grid_upd[2][2][2], *grid_vel[2][2][2];
   void *g2p1[2][2], *g2p2[2][2][2];
   // launch-shape candidates [TL][variant] of the gathers (FP32, no thermal):
@@ -155,6 +163,7 @@ struct ContactDev {
   int4 *rc;                  // per member: cell (3), tag (0 solid1, 1 solid2, -1 neither)
   double *blk, *ftot;        // per-block partial sums of the pair forces, their total
   float *mbp;                // 3 rows of ps floats: external particle forces
+  int axisym;                // 2-D axisymmetric: the min-penetration Rp uses vol / r
 };
 
 // kmpm_misc.cu
@@ -215,6 +224,11 @@ __device__ __forceinline__ void p2g_payload(const P2GArgs &a, const float *P, in
   if (p2g_ext(MODE_)) {
 #pragma unroll
     for (int d = 0; d < 3; d++) pay[o++] = a.mbp[d * ps + p];
+  }
+  if (p2g_axi(MODE_)) {
+    // T_zz / r: vol0 PK1(2,2) / x0_r (TL) or vol sigma(2,2) / x_r (UL)
+    const float r = P[PF_X0 * ps + p] + (a.pos_field == PF_X ? P[PF_X * ps + p] : 0.f);
+    pay[o++] = P[(PF_PK + (MODE == P2G_TL ? 8 : 2)) * ps + p] / r;
   }
 }
 

@@ -78,7 +78,9 @@ __device__ __forceinline__ void p2g_particle(float (&accr)[NSL][Q], const float 
         }
         t[r] = T0 * gxy0 + T1 * gxy1;
         // external particle force: f_r += s_z (wxy mbp_r)
-        if (p2g_ext(MODE)) t[r] = fmaf(-wxy, pay[p2g_nin(MODE & ~P2G_EXT, false) + r], t[r]);
+        if (p2g_ext(MODE)) t[r] = fmaf(-wxy, pay[p2g_nin(MODE & ~(P2G_EXT | P2G_AXI), false) + r], t[r]);
+        // axisymmetric hoop term (2-D, s_z = 1): f_0 -= w T_zz / r
+        if (p2g_axi(MODE) && r == 0) t[0] = fmaf(wxy, pay[p2g_nin(MODE & ~P2G_AXI, false)], t[0]);
         t2[r] = T2 * wxy;
       }
     }
@@ -650,6 +652,7 @@ __global__ void __launch_bounds__(256, MINB) k_g2p2(PartArgs a) {
     }
     float G[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
     float qg[3] = {0, 0, 0};
+    float vr = 0.f;
     // branch-free gather (clamped indices, see k_g2p1); a pair with a zero
     // weight is dropped as in the reference, so its slope is masked too
     int cx[S], cy[SY], cz[SZ];
@@ -694,12 +697,20 @@ __global__ void __launch_bounds__(256, MINB) k_g2p2(PartArgs a) {
           if (DIM >= 2) G[3 * r + 1] += gy * A[r];
           if (DIM == 3) G[3 * r + 2] += sxy * B[r];
         }
+        if (DIM == 2) vr += sxy * A[0];  // sum w v_r (axisymmetric hoop rate)
         if (THERMAL) {
           qg[0] -= gx * AT;
           qg[1] -= gy * AT;
           qg[2] -= sxy * BT;
         }
       }
+    }
+    if (DIM == 2 && a.axisym) {
+      // Fdot(2,2) / L(2,2) += sum w v_r / r, r = x0_r (TL) or the x_r of the
+      // rate (src/solid.cpp:818-829, 900-913; APIC 1046-1058, 1120-1132, where
+      // Di(2,2) = 1 in 2-D)
+      const float r = P[PF_X0 * ps + p] + (TL ? 0.f : P[(a.use_vu ? PF_X : PF_XN) * ps + p]);
+      G[8] += vr / r;
     }
     if ((BASIS == 1 || BASIS == 3) && a.apic)
 #pragma unroll
@@ -941,6 +952,19 @@ void fill_step_kernels(StepKernels &k) {
   } else {
     k.p2g_tl_apic = k.p2g_ul_apic = k.p2g_vel_apic = nullptr;
   }
+#define KMPM_AXI(ul, ap, ex, mode)                                                             \
+  k.p2g_axi[ul][ap][ex] = (void *)k_p2g<DIM, BASIS, (mode) | P2G_AXI | ((ex) ? P2G_EXT : 0), false>;
+  for (int u = 0; u < 2; u++)
+    for (int ap = 0; ap < 2; ap++)
+      for (int ex = 0; ex < 2; ex++) k.p2g_axi[u][ap][ex] = nullptr;
+  if constexpr (DIM == 2) {  // axisymmetric runs are 2-D
+    KMPM_AXI(0, 0, 0, P2G_TL) KMPM_AXI(0, 0, 1, P2G_TL) KMPM_AXI(1, 0, 0, P2G_UL) KMPM_AXI(1, 0, 1, P2G_UL)
+    if constexpr (BASIS == 1 || BASIS == 3) {
+      KMPM_AXI(0, 1, 0, P2G_TL_APIC) KMPM_AXI(0, 1, 1, P2G_TL_APIC)
+      KMPM_AXI(1, 1, 0, P2G_UL_APIC) KMPM_AXI(1, 1, 1, P2G_UL_APIC)
+    }
+  }
+#undef KMPM_AXI
   if constexpr (DIM >= 2) {  // contact fixes act in 2-D and 3-D runs
     k.p2g_tl_ext[0] = (void *)k_p2g<DIM, BASIS, P2G_TL | P2G_EXT, false>;
     k.p2g_tl_ext[1] = (void *)k_p2g<DIM, BASIS, P2G_TL | P2G_EXT, true>;

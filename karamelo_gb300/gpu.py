@@ -45,7 +45,7 @@ class KmpmParams(ctypes.Structure):
                 ("dt_factor", ctypes.c_double), ("dt_constant", ctypes.c_int), ("boxlo", ctypes.c_double * 3),
                 ("boxhi", ctypes.c_double * 3), ("precision", ctypes.c_int), ("sort_every", ctypes.c_int),
                 ("track_strain", ctypes.c_int), ("independent", ctypes.c_int), ("autotune", ctypes.c_int),
-                ("transfer", ctypes.c_int)]
+                ("transfer", ctypes.c_int), ("axisymmetric", ctypes.c_int)]
 
 
 class TrainOpts(ctypes.Structure):
@@ -152,6 +152,7 @@ class GpuBackend:
         prm.independent = int(independent)
         prm.autotune = int(autotune)
         prm.transfer = int(getattr(s, "transfer", 0))
+        prm.axisymmetric = int(getattr(s, "axisymmetric", False))
         h = ctypes.c_void_p()
         r = L.kmpm_create(ctypes.byref(prm), ctypes.byref(h))
         if r != KMPM_OK:

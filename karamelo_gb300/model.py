@@ -181,6 +181,18 @@ class MPM:
             self.s.grids.append(sc.grid_geometry(dim, self.s.basis, lo, hi, self.subhi, self.cellsize))
         self.dim_set = True
 
+    def axisymmetric(self, flag):
+        """``axisymmetric(true|false)``: Domain::set_axisymmetric,
+        src/domain.cpp:558-570.  Solids created afterwards get masses and
+        volumes multiplied by their radius x0_r (Solid::populate,
+        src/solid.cpp:2292-2295).  The GPU path takes it in 2-D mechanical runs."""
+        on = str(flag).lower() in ("true", "1")
+        if str(flag).lower() not in ("true", "false", "1", "0"):
+            raise KarameloError("axisymmetric(true) or axisymmetric(false)")
+        if on and (self.s.dim != 2 or self.s.thermal):
+            raise KarameloError("axisymmetric runs on the GPU path are 2-D and mechanical")
+        self.s.axisymmetric = on
+
     def region(self, name, kind, *args):
         """``region()``: Domain::add_region; block regions grow the box
         (src/region_block.cpp:45-120)."""
@@ -349,8 +361,14 @@ class MPM:
             raise KarameloError("Error: solid does not have any particles.")
         ptag = np.arange(1, n + 1, dtype=np.int64) + self.np_total
         self.np_total += n
+        masses, vols = np.full(n, mass), np.full(n, vol)
+        if self.s.axisymmetric:
+            # mass = mass_ x0_r, vol0 = mass / rho0 (src/solid.cpp:2292-2295)
+            rho0 = self.s.materials[self.material_ids[mat]].moduli()["rho0"]
+            masses = mass * x[:, 0]
+            vols = masses / rho0
         self.s.solids.append(sc.SolidSpec(name=name, grid=gid, mat=self.material_ids[mat], x0=x,
-                                          v=np.zeros((n, 3)), mass=np.full(n, mass), vol0=np.full(n, vol),
+                                          v=np.zeros((n, 3)), mass=masses, vol0=vols,
                                           T0=float(T0), ptag=ptag, mask=np.ones(n, np.int64)))
         self.solid_ids[name] = len(self.s.solids) - 1
 

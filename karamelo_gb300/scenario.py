@@ -154,6 +154,7 @@ class Scenario:
     dim: int = 3
     pic_flip: float = 0.99
     transfer: int = 0            # 0: PIC/FLIP blend, 1: APIC (kmpm_params.transfer)
+    axisymmetric: bool = False   # Domain::axisymmetric: 2-D, x = r, y = z
     thermal: bool = False
     dt: float = 1e-16            # Update::Update, src/update.cpp:38
     dt_factor: float = 0.9

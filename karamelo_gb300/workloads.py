@@ -250,3 +250,38 @@ def hertz_spheres(backend_factory=None, method="tlmpm/gpu", sub="FLIP", basis="c
         sim.fix("contact", contact, "sA", "sB", mu)
     sim.set_dt(dt)
     return sim
+
+
+def taylor_bar_axisymmetric(backend_factory=None, cellsize=0.2, R=3.2, L=32.4, ppc=2, v0=190.0,
+                            method="tlmpm/gpu", scheme="musl", basis="cubic-spline", pic_flip=0.99,
+                            dt_factor=0.1, sub="FLIP"):
+    """The copper Taylor bar as a 2-D axisymmetric run (x = r in [0, R], y = z;
+    units GPa, mm, ms): the bar of ``taylor_bar`` on its meridian plane, moving
+    along y towards the wall at y = L/2, with the axis nodes held at v_r = 0."""
+    p = dict(COPPER)
+    G = p["E"] / (2 * (1 + p["nu"]))
+    hL = L / 2
+    sim = MPM(backend_factory)
+    _method(sim, method, sub, basis, pic_flip)
+    sim.scheme(scheme)
+    sim.dimension(2, 0.0, 2.5 * R, -hL, hL, cellsize)
+    sim.axisymmetric("true")
+    sim.eos("eosl", "linear", p["rho"], p["K"])
+    sim.strength("jc", "johnson_cook", G, p["A"], p["B"], p["n"], p["epsdot0"], p["C"], p["m"], p["Tr"], p["Tm"])
+    sim.material("mat", "eos-strength", "eosl", "jc")
+    sim.region("bar", "block", 0.0, R, -hL, hL)
+    sim.solid("solid1", "region", "bar", ppc, "mat", cellsize, p["Tr"])
+    sim.region("wall", "block", "-INF", "INF", hL - 0.5 * cellsize, "INF")
+    sim.region("axis", "block", "-INF", 0.25 * cellsize, "-INF", "INF")
+    sim.group("gwall", "nodes", "region", "wall", "solid", "solid1")
+    sim.group("gaxis", "nodes", "region", "axis", "solid", "solid1")
+    sim.group("gbar", "particles", "region", "bar", "solid", "solid1")
+    sim.fix("v0", "initial_velocity_particles", "gbar", None, v0, None)
+    sim.fix("BC_axis", "velocity_nodes", "gaxis", 0, None)
+    sim.dt_factor(dt_factor)
+    return sim
+
+
+def taylor_bar_axisymmetric_wall(sim):
+    """The wall of the axisymmetric bar, added after the first step."""
+    sim.fix("BC_Wall", "velocity_nodes", "gwall", None, 0)

@@ -425,6 +425,7 @@ struct Sim {
   bool apic = false;  // affine transfers: APIC, and for ULMPM AFLIP / ASFLIP / MLS (src/ulmpm.cpp:79-85)
   bool asflip = false;  // ULMPM ASFLIP: positions move with the blended velocity (src/ulmpm.cpp:453-473)
   bool mls = false;     // ULMPM MLS: internal forces from moments (src/solid.cpp:524-574)
+  bool axisym = false;  // Domain::axisymmetric: 2-D with x = r, y = z (src/domain.cpp:554-570)
   bool thermal;
   double dt, dt_factor;
   bool dt_constant;
@@ -637,8 +638,9 @@ void compute_external_forces_nodes(Solid &S, Grid &g, bool reset) {
   }
 }
 
-// Solid::compute_internal_forces_nodes_TL, src/solid.cpp:452-480
-void compute_internal_forces_nodes_TL(Solid &S, Grid &g) {
+// Solid::compute_internal_forces_nodes_TL, src/solid.cpp:452-480 (axisymmetric:
+// the hoop term -vol0PK1(2,2) w / r, r = x0_r, in the same loop)
+void compute_internal_forces_nodes_TL(const Sim &s, Solid &S, Grid &g) {
 #pragma omp parallel for schedule(static)
   for (int in = 0; in < g.nn; in++) {
     double ft[3] = {0, 0, 0};
@@ -647,6 +649,7 @@ void compute_internal_forces_nodes_TL(Solid &S, Grid &g) {
       const M3 &P = S.vol0PK1[ip];
       const double *gw = &S.wfd_np[in][3 * j];
       for (int d = 0; d < 3; d++) ft[d] -= P(d, 0) * gw[0] + P(d, 1) * gw[1] + P(d, 2) * gw[2];
+      if (s.axisym) ft[0] -= P(2, 2) * S.wf_np[in][j] / S.x0[3 * ip];
     }
     for (int d = 0; d < 3; d++) g.f[3 * in + d] = ft[d];
   }
@@ -673,6 +676,13 @@ void compute_forces_nodes_UL(const Sim &s, Solid &S, Grid &g, bool reset) {
         g.mb[3 * in + d] += S.wf_np[in][j] * S.mbp[3 * ip + d];
       }
     }
+    // axisymmetric hoop term, in a second loop as the reference writes it
+    // (src/solid.cpp:513-519, 565-571): -vol sigma(2,2) w / r, r = x_r
+    if (s.axisym)
+      for (size_t j = 0; j < S.neigh_np[in].size(); j++) {
+        int ip = S.neigh_np[in][j];
+        g.f[3 * in] -= S.vol[ip] * (S.sigma[ip](2, 2) * S.wf_np[in][j] / S.x[3 * ip]);
+      }
   }
 }
 
@@ -959,8 +969,10 @@ void contact_forces(Sim &s, Contact &C) {
   const double hertz_coef = s.dim == 3 ? 1.333333333 : 0.25 * M_PI;
   const int dim = s.dim;
   double ft[3] = {0, 0, 0};
-  auto radius = [&](double vol) {
+  // Rp; the 2-D min-penetration fix divides the volume by r in axisymmetric runs
+  auto radius = [&](double vol, double r) {
     if (dim == 3) return hertz ? 0.5 * std::pow(vol, 0.333333333) : 0.5 * std::cbrt(vol);
+    if (s.axisym && !hertz) return 0.5 * std::sqrt(vol / r);
     return 0.5 * std::sqrt(vol);
   };
   if (dim == 2 || dim == 3) {
@@ -974,7 +986,7 @@ void contact_forces(Sim &s, Contact &C) {
         const int ns = (dim == 2 && !hertz) ? 2 : 3;
         for (int d = 0; d < ns; d++) near = near && dx[d] < cmax && dx[d] > -cmax;
         if (!near) continue;
-        const double R1 = radius(A.vol[i]), R2 = radius(B.vol[j]), Rp = R1 + R2;
+        const double R1 = radius(A.vol[i], A.x[3 * i]), R2 = radius(B.vol[j], B.x[3 * j]), Rp = R1 + R2;
         for (int d = 0; d < ns; d++) near = near && dx[d] < Rp && dx[d] > -Rp;
         if (!near) continue;
         const double r = std::sqrt(dx[0] * dx[0] + dx[1] * dx[1] + dx[2] * dx[2]);
@@ -1057,7 +1069,7 @@ bool step(Sim &s) {
       Grid &g = s.grids[S.grid];
       compute_velocity_nodes(s, S, g, true);
       compute_external_forces_nodes(S, g, true);
-      compute_internal_forces_nodes_TL(S, g);
+      compute_internal_forces_nodes_TL(s, S, g);
       if (s.thermal) {
         compute_temperature_nodes(S, g, true);
         compute_temperature_forces(S, g, true);
@@ -1127,6 +1139,8 @@ bool step(Sim &s) {
           const double w = S.wf_pn[ip][j];
           for (int a = 0; a < s.dim; a++)
             for (int b = 0; b < s.dim; b++) G(a, b) += vn[3 * in + a] * (g.x0[3 * in + b] - pos[3 * ip + b]) * w;
+          // axisymmetric: v_r w / r (src/solid.cpp:1046-1058, 1120-1132); Di(2,2) = 1 in 2-D
+          if (s.axisym) G(2, 2) += vn[3 * in] * w / pos[3 * ip];
         }
         for (int a = 0; a < 3; a++)
           for (int b = 0; b < 3; b++) G(a, b) *= S.Di[b];
@@ -1136,6 +1150,8 @@ bool step(Sim &s) {
           const double *gw = &S.wfd_pn[ip][3 * j];
           for (int a = 0; a < s.dim; a++)
             for (int b = 0; b < s.dim; b++) G(a, b) += vn[3 * in + a] * gw[b];
+          // axisymmetric: Fdot(2,2) / L(2,2) += v_r w / r (src/solid.cpp:818-829, 900-913)
+          if (s.axisym) G(2, 2) += vn[3 * in] * S.wf_pn[ip][j] / pos[3 * ip];
         }
       }
       if (TL) S.Fdot[ip] = G;  // src/solid.cpp:798-858
@@ -1303,6 +1319,14 @@ int om_set_transfer(void *h, int kind) {
   s->asflip = !TL && kind == 3;
   s->mls = !TL && kind == 4;
   if (kind == 1 || kind == 4) s->pic_flip = 0;
+  return 0;
+}
+// Domain::set_axisymmetric (src/domain.cpp:558-570): 2-D only; the reference
+// stops thermo-mechanical axisymmetric runs (src/solid.cpp:2789-2792)
+int om_set_axisymmetric(void *h, int on) {
+  Sim *s = (Sim *)h;
+  if (on && (s->dim != 2 || s->thermal)) { s->err = "axisymmetric runs are 2-D and mechanical"; return -1; }
+  s->axisym = on != 0;
   return 0;
 }
 const char *om_error(void *h) { return ((Sim *)h)->err.c_str(); }

@@ -67,6 +67,7 @@ def lib():
         L.om_eig_real.argtypes = [dp, dp]
         L.om_set_threads.argtypes = [i]
         L.om_add_contact.argtypes = [p, i, i, i, d]
+        L.om_set_axisymmetric.argtypes = [p, i]
         L.om_contact_force.argtypes = [p, i, dp]
         _lib = L
     return _lib
@@ -94,6 +95,8 @@ class OracleBackend:
                              int(s.dt_constant), _dp(lo), _dp(hi))
         self.L = L
         if getattr(s, "transfer", 0) != 0 and L.om_set_transfer(self.h, int(s.transfer)) != 0:
+            raise RuntimeError(L.om_error(self.h).decode())
+        if getattr(s, "axisymmetric", False) and L.om_set_axisymmetric(self.h, 1) != 0:
             raise RuntimeError(L.om_error(self.h).decode())
         for m in s.materials:
             L.om_add_material(self.h, ctypes.byref(m))
