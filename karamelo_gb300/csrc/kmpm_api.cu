@@ -36,8 +36,10 @@ struct kmpm_ctx {
   std::vector<HGrid> hgrids;
   struct HSolid {
     int grid, mat, n;
-    std::vector<double> x0, x, v, mass, vol0;
     double T0;
+    // the caller's arrays, copied to the device as given (FP64: x0, x, v as
+    // n*3, then mass, vol0); converted into the particle buffer at build
+    double *d_in = nullptr;
   };
   std::vector<HSolid> hsolids;
   struct HFix {
@@ -91,6 +93,11 @@ struct kmpm_ctx {
   int nscalars = 1;
   double *d_dtcfl = nullptr;
   ErrState *d_err = nullptr;
+  // host view of the error word: page-locked, mapped, written by a one-thread
+  // kernel at the end of every run, so that reading it needs no copy engine
+  // (a small copy would queue behind a dump's device-to-host copy)
+  ErrState *h_err = nullptr, *h_err_dev = nullptr;
+  double maxtime_dev = 1e300;  // StepScalars::maxtime as last written
   float *d_blk_c = nullptr, *d_blk_h = nullptr;
   double *d_eblk = nullptr, *d_eout = nullptr;
   int *d_keys = nullptr, *d_vals = nullptr;
@@ -517,6 +524,10 @@ int build(kmpm_ctx *c) {
   }
   DALLOC(c->d_dtcfl, c->ranges.size());
   DALLOC(c->d_err, 1);
+  CK(cudaHostAlloc((void **)&c->h_err, sizeof(ErrState), cudaHostAllocMapped));
+  CK(cudaHostGetDevicePointer((void **)&c->h_err_dev, c->h_err, 0));
+  std::memset((void *)c->h_err, 0, sizeof(ErrState));
+  c->maxtime_dev = 1e300;
   DALLOC(c->d_blk_c, c->nblk_p);
   DALLOC(c->d_blk_h, c->nblk_p);
   DALLOC(c->d_eblk, 2 * c->nblk_p);
@@ -527,62 +538,29 @@ int build(kmpm_ctx *c) {
   DALLOC(c->rtmp.v1, c->ps);
   DALLOC(c->rtmp.hist, 256 * ((c->ps + 2047) / 2048 + 1));
   DALLOC(c->rtmp.tot, 256);
-  // ---- particle upload (caller order within each solid), one field row at a time
+  // ---- particle upload: each solid's caller arrays (already on the device,
+  // kmpm_add_solid) converted into its slots; the other fields are zero
   c->T_ref = c->prm.thermal ? c->hsolids[0].T0 : 0.0;
-  {
-    // only the fields that are not zero at the start are copied: the buffer
-    // was zeroed on the context stream (H = F - I, sigma, eps_p, ... are 0)
-    std::vector<int> up;
-    for (int d = 0; d < 3; d++) up.push_back(PF_X0 + d);
-    for (int d = 0; d < 3; d++) up.push_back(PF_X + d);
-    if (!c->TL())
-      for (int d = 0; d < 3; d++) up.push_back(PF_XN + d);
-    for (int d = 0; d < 3; d++) up.push_back(PF_V + d);
-    up.insert(up.end(), {PF_MASS, PF_VOL0, PF_ORIG, PF_SID});
-    if (c->prm.thermal) up.push_back(PF_T);
-    std::vector<float> row(c->ps);
-    for (int f : up) {
-      std::fill(row.begin(), row.end(), 0.f);
-      bool nonzero = false;
-      for (size_t s = 0; s < c->hsolids.size(); s++) {
-        const auto &S = c->hsolids[s];
-        const RangeDev &r = c->ranges[c->TL() ? c->solid_range[s] : 0];
-        float *o = row.data() + (c->TL() ? r.start : r.start + c->solid_base[s]);
-        const int n = S.n;
-        if (f >= PF_X0 && f < PF_X0 + 3) {
-          const int d = f - PF_X0;
-          for (int i = 0; i < n; i++) o[i] = (float)S.x0[3 * i + d];
-        } else if ((f >= PF_X && f < PF_X + 3) || (f >= PF_XN && f < PF_XN + 3)) {
-          // positions are stored as the displacement from x0
-          const int d = (f >= PF_XN) ? f - PF_XN : f - PF_X;
-          for (int i = 0; i < n; i++) o[i] = (float)(S.x[3 * i + d] - S.x0[3 * i + d]);
-        } else if (f >= PF_V && f < PF_V + 3) {
-          const int d = f - PF_V;
-          for (int i = 0; i < n; i++) o[i] = (float)S.v[3 * i + d];
-        } else if (f == PF_MASS) {
-          for (int i = 0; i < n; i++) o[i] = (float)S.mass[i];
-        } else if (f == PF_VOL0) {
-          for (int i = 0; i < n; i++) o[i] = (float)S.vol0[i];
-        } else if (f == PF_T) {
-          // Solid::populate sets T = T0 only for thermo-mechanical runs; otherwise
-          // the vector is value-initialised (src/solid.cpp:2297-2306, 306-311)
-          const float t = (float)(S.T0 - c->T_ref);
-          for (int i = 0; i < n; i++) o[i] = t;
-        } else if (f == PF_ORIG) {
-          for (int i = 0; i < n; i++) { const int v = c->solid_base[s] + i; std::memcpy(o + i, &v, 4); }
-        } else if (f == PF_SID) {
-          const int v = (int)s;
-          for (int i = 0; i < n; i++) std::memcpy(o + i, &v, 4);
-        }
-      }
-      if (f == PF_ORIG || f == PF_SID) nonzero = true;  // integer bit patterns: always copied
-      for (size_t i = 0; i < row.size() && !nonzero; i++) nonzero = row[i] != 0.f;
-      if (!nonzero) continue;
-      CK(cudaMemcpyAsync(c->buf[0] + (size_t)f * c->ps, row.data(), sizeof(float) * c->ps, cudaMemcpyHostToDevice,
-                         c->st));
-      CK(cudaStreamSynchronize(c->st));
-    }
+  for (size_t s = 0; s < c->hsolids.size(); s++) {
+    auto &S = c->hsolids[s];
+    const RangeDev &r = c->ranges[c->TL() ? c->solid_range[s] : 0];
+    StageArgs sa{};
+    sa.in = S.d_in;
+    sa.n = S.n;
+    sa.slot0 = c->TL() ? r.start : r.start + c->solid_base[s];
+    sa.orig0 = c->solid_base[s];
+    sa.sid = (int)s;
+    sa.ul = c->TL() ? 0 : 1;
+    // Solid::populate sets T = T0 only for thermo-mechanical runs (src/solid.cpp:2297-2306)
+    sa.thermal = c->prm.thermal;
+    sa.T = (float)(S.T0 - c->T_ref);
+    sa.ps = c->ps;
+    sa.P = c->buf[0];
+    launch_stage_solid(sa, c->st);
   }
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(c->st));
+  for (auto &S : c->hsolids) dfree(S.d_in);
   // ---- kernel attributes
   const int modes[4] = {P2G_MASS, P2G_TL, P2G_UL, P2G_VEL};
   void *fns[4][2] = {{c->K.p2g_mass, c->K.p2g_mass}, {c->K.p2g_tl, c->K.p2g_tl_th}, {c->K.p2g_ul, c->K.p2g_ul_th},
@@ -1007,9 +985,11 @@ int ensure_graph(kmpm_ctx *c) {
 }
 
 int check_error(kmpm_ctx *c) {
-  ErrState e{};
-  CK(cudaMemcpyAsync(&e, c->d_err, sizeof(e), cudaMemcpyDeviceToHost, c->st));
+  launch_publish_err(c->d_err, c->h_err_dev, c->st);
+  CK(cudaGetLastError());
   CK(cudaStreamSynchronize(c->st));
+  ErrState e;
+  std::memcpy(&e, (const void *)c->h_err, sizeof(e));
   if (e.code == 0) return KMPM_OK;
   char buf[256];
   const char *what = e.code == ERR_J ? "J<=0" : e.code == ERR_LEFT ? "particle left the domain"
@@ -1055,6 +1035,7 @@ int autotune(kmpm_ctx *c) {
   const double big = 1e300;
   CK(cudaMemcpyAsync((char *)c->d_scalars + offsetof(StepScalars, maxtime), &big, sizeof(double),
                      cudaMemcpyHostToDevice, c->st));
+  c->maxtime_dev = big;
   float *pp[2] = {nullptr, nullptr};
   CK(cudaMemcpyAsync(pp, c->d_pp, sizeof(pp), cudaMemcpyDeviceToHost, c->st));
   CK(cudaStreamSynchronize(c->st));
@@ -1167,6 +1148,8 @@ int kmpm_destroy(kmpm_ctx *c) {
   dfree(c->d_fixes); dfree(c->d_fix_start); dfree(c->d_fix_count); dfree(c->d_scalars); dfree(c->d_dtcfl);
   dfree(c->d_dump);
   free_contacts(c);
+  for (auto &S : c->hsolids) dfree(S.d_in);
+  if (c->h_err) cudaFreeHost(c->h_err);
   if (c->cst) cudaStreamSynchronize(c->cst);
   for (auto &b : c->abufs) {
     dfree(b.buf);
@@ -1235,9 +1218,25 @@ int kmpm_add_solid(kmpm_ctx *c, int grid, int mat, int n, const double *x0, cons
       if (s.grid == grid) return fail(c, KMPM_ERR_ARG, "each TLMPM solid owns its grid");
   kmpm_ctx::HSolid s;
   s.grid = grid; s.mat = mat; s.n = n; s.T0 = T0;
-  s.x0.assign(x0, x0 + 3 * n); s.x.assign(x, x + 3 * n); s.v.assign(v, v + 3 * n);
-  s.mass.assign(mass, mass + n); s.vol0.assign(vol0, vol0 + n);
-  c->hsolids.push_back(std::move(s));
+  // straight to the device (no host copy or conversion); the caller's
+  // buffers are free again when this returns
+  const size_t nn = (size_t)n;
+  CK(cudaMalloc((void **)&s.d_in, sizeof(double) * 11 * nn));
+  const struct { const double *src; size_t off, cnt; } parts[5] = {
+      {x0, 0, 3 * nn}, {x, 3 * nn, 3 * nn}, {v, 6 * nn, 3 * nn}, {mass, 9 * nn, nn}, {vol0, 10 * nn, nn}};
+  for (const auto &q : parts) {
+    const cudaError_t e = cudaMemcpyAsync(s.d_in + q.off, q.src, sizeof(double) * q.cnt, cudaMemcpyHostToDevice, c->st);
+    if (e != cudaSuccess) {
+      cudaFree(s.d_in);
+      return fail(c, KMPM_ERR_CUDA, std::string("solid upload: ") + cudaGetErrorString(e));
+    }
+  }
+  const cudaError_t e = cudaStreamSynchronize(c->st);
+  if (e != cudaSuccess) {
+    cudaFree(s.d_in);
+    return fail(c, KMPM_ERR_CUDA, std::string("solid upload: ") + cudaGetErrorString(e));
+  }
+  c->hsolids.push_back(s);
   return (int)c->hsolids.size() - 1;
 }
 
@@ -1285,9 +1284,11 @@ int kmpm_contact_force(kmpm_ctx *c, int k, double out[3]) {
 }
 
 static int set_maxtime(kmpm_ctx *c, double maxtime) {
+  if (maxtime == c->maxtime_dev) return KMPM_OK;  // no copy between plain runs
   CK(cudaMemcpyAsync((char *)c->d_scalars + offsetof(StepScalars, maxtime), &maxtime, sizeof(double),
                      cudaMemcpyHostToDevice, c->st));
   CK(cudaStreamSynchronize(c->st));
+  c->maxtime_dev = maxtime;
   return KMPM_OK;
 }
 
@@ -1410,12 +1411,11 @@ int kmpm_download_particles(kmpm_ctx *c, int solid, int field, double *out) {
   if (!c || !out || solid < 0 || solid >= (int)c->hsolids.size()) return KMPM_ERR_ARG;
   const auto &S = c->hsolids[solid];
   if (!c->built) {
-    for (int i = 0; i < S.n; i++) {
-      if (field == KMPM_P_X) for (int d = 0; d < 3; d++) out[3 * i + d] = S.x[3 * i + d];
-      else if (field == KMPM_P_X0) for (int d = 0; d < 3; d++) out[3 * i + d] = S.x0[3 * i + d];
-      else if (field == KMPM_P_V) for (int d = 0; d < 3; d++) out[3 * i + d] = S.v[3 * i + d];
-      else return fail(c, KMPM_ERR_STATE, "field not available before the first run");
-    }
+    // the arrays as the caller gave them (x0, x, v at 0, 3n, 6n of the staging)
+    const size_t off = field == KMPM_P_X0 ? 0 : field == KMPM_P_X ? 3 : field == KMPM_P_V ? 6 : 99;
+    if (off == 99) return fail(c, KMPM_ERR_STATE, "field not available before the first run");
+    CK(cudaMemcpyAsync(out, S.d_in + off * S.n, sizeof(double) * 3 * S.n, cudaMemcpyDeviceToHost, c->st));
+    CK(cudaStreamSynchronize(c->st));
     return KMPM_OK;
   }
   if (field == KMPM_P_STRAIN_EL && !c->prm.track_strain)
@@ -1491,7 +1491,8 @@ int kmpm_upload_particles(kmpm_ctx *c, int solid, int field, const double *in) {
   if (field != KMPM_P_V) return fail(c, KMPM_ERR_ARG, "only velocities can be uploaded");
   auto &S = c->hsolids[solid];
   if (!c->built) {
-    for (int k = 0; k < 3 * S.n; k++) S.v[k] = in[k];
+    CK(cudaMemcpyAsync(S.d_in + 6 * (size_t)S.n, in, sizeof(double) * 3 * S.n, cudaMemcpyHostToDevice, c->st));
+    CK(cudaStreamSynchronize(c->st));
     return KMPM_OK;
   }
   const RangeDev &rg = c->ranges[c->TL() ? c->solid_range[solid] : 0];

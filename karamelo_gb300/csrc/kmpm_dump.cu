@@ -7,30 +7,6 @@
 
 namespace kmpm {
 
-// R of F = R U in FP64 (the scaled Newton iteration of the stress kernel's
-// polar_rotation, here to FP64 convergence; N. J. Higham, SIAM J. Sci. Stat.
-// Comput. 7, 1986)
-__device__ void polar_rotation_fp64(const double *F, double *R) {
-  double X[9];
-  for (int k = 0; k < 9; k++) X[k] = F[k];
-  for (int it = 0; it < 40; it++) {
-    double C[9];
-    C[0] = X[4] * X[8] - X[5] * X[7]; C[1] = X[5] * X[6] - X[3] * X[8]; C[2] = X[3] * X[7] - X[4] * X[6];
-    C[3] = X[2] * X[7] - X[1] * X[8]; C[4] = X[0] * X[8] - X[2] * X[6]; C[5] = X[1] * X[6] - X[0] * X[7];
-    C[6] = X[1] * X[5] - X[2] * X[4]; C[7] = X[2] * X[3] - X[0] * X[5]; C[8] = X[0] * X[4] - X[1] * X[3];
-    const double d = X[0] * C[0] + X[1] * C[1] + X[2] * C[2];
-    const double g = cbrt(1.0 / fabs(d)), gi = 1.0 / (g * d);
-    double diff = 0;
-    for (int k = 0; k < 9; k++) {
-      const double xn = 0.5 * (g * X[k] + gi * C[k]);
-      diff += (xn - X[k]) * (xn - X[k]);
-      X[k] = xn;
-    }
-    if (diff < 1e-30) break;
-  }
-  for (int k = 0; k < 9; k++) R[k] = X[k];
-}
-
 struct DumpArgs {
   int ri, solid, base, field, TL, rotate;
   double T_ref;
@@ -72,9 +48,16 @@ __global__ void k_dump(PartArgs a, DumpArgs d) {
         for (int k = 0; k < 9; k++) o[9 * i + k] = sg[k];
         break;
       }
-      double F[9], R[9], RS[9];
-      for (int k = 0; k < 9; k++) F[k] = f(PF_H + k) + (k % 4 == 0 ? 1.0 : 0.0);
-      polar_rotation_fp64(F, R);
+      // R of F = R U by the stress kernel's FP32 polar iteration (F itself is
+      // held in FP32, so an FP64 iteration would add digits the state does not
+      // have; FP64 runs at 1/60 of the FP32 rate here), the rotation in FP64
+      float Ff[9], Rf[9];
+      for (int k = 0; k < 9; k++) Ff[k] = P[(PF_H + k) * ps + p] + (k % 4 == 0 ? 1.f : 0.f);
+      double R[9], RS[9];
+      if (polar_rotation(Ff, Rf))
+        for (int k = 0; k < 9; k++) R[k] = (double)Rf[k];
+      else  // det F <= 0: the step has raised its error; the stress goes out unrotated
+        for (int k = 0; k < 9; k++) R[k] = (k % 4 == 0) ? 1.0 : 0.0;
       for (int r = 0; r < 3; r++)
         for (int c = 0; c < 3; c++) RS[3 * r + c] = R[3 * r] * sg[c] + R[3 * r + 1] * sg[3 + c] + R[3 * r + 2] * sg[6 + c];
       for (int r = 0; r < 3; r++)

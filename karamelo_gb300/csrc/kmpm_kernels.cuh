@@ -167,6 +167,18 @@ struct ContactDev {
 };
 
 // kmpm_misc.cu
+// one solid's caller arrays (device copy, FP64: x0, x, v as n*3, mass, vol0)
+// into its slots of the particle buffer
+struct StageArgs {
+  const double *in;
+  int n, slot0, orig0, sid, ul, thermal;
+  float T;
+  size_t ps;
+  float *P;
+};
+void launch_stage_solid(const StageArgs &a, cudaStream_t st);
+// the error word into mapped host memory (read after a stream synchronize)
+void launch_publish_err(const ErrState *d, ErrState *h_mapped, cudaStream_t st);
 void launch_cell_keys(const PartArgs &a, int nblk, int *keys, int use_x0, cudaStream_t st, int pad_last = 0);
 void launch_cell_ranges(const int *sorted_keys, int start, int n, int ncell_per_tile, int *cell_start, int *cell_end,
                         int *tile_start, int *tile_end, cudaStream_t st);

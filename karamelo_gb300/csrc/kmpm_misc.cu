@@ -46,6 +46,39 @@ void launch_cell_keys(const PartArgs &a, int nblk, int *keys, int use_x0, cudaSt
   k_cell_keys<<<nblk, 256, 0, st>>>(a, keys, use_x0, pad_last);
 }
 
+// Solid::populate's state into the buffer (src/solid.cpp:2284-2310): x0,
+// the displacement x - x0 (formed in FP64, so FP32 keeps it to its own
+// precision), v, mass, vol0, the caller index, the solid id and T - T_ref
+__global__ void k_stage_solid(StageArgs a) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.n) return;
+  const size_t n = (size_t)a.n, ps = a.ps, p = (size_t)a.slot0 + i;
+  const double *x0 = a.in, *x = a.in + 3 * n, *v = a.in + 6 * n, *m = a.in + 9 * n, *vol0 = a.in + 10 * n;
+  float *P = a.P;
+#pragma unroll
+  for (int d = 0; d < 3; d++) {
+    const double xd = x0[3 * i + d];
+    const float u = (float)(x[3 * i + d] - xd);
+    P[(PF_X0 + d) * ps + p] = (float)xd;
+    P[(PF_X + d) * ps + p] = u;
+    if (a.ul) P[(PF_XN + d) * ps + p] = u;
+    P[(PF_V + d) * ps + p] = (float)v[3 * i + d];
+  }
+  P[PF_MASS * ps + p] = (float)m[i];
+  P[PF_VOL0 * ps + p] = (float)vol0[i];
+  P[PF_ORIG * ps + p] = __int_as_float(a.orig0 + i);
+  P[PF_SID * ps + p] = __int_as_float(a.sid);
+  if (a.thermal) P[PF_T * ps + p] = a.T;
+}
+void launch_stage_solid(const StageArgs &a, cudaStream_t st) {
+  if (a.n > 0) k_stage_solid<<<(a.n + 255) / 256, 256, 0, st>>>(a);
+}
+
+__global__ void k_publish_err(const ErrState *d, ErrState *h) { *h = *d; }
+void launch_publish_err(const ErrState *d, ErrState *h_mapped, cudaStream_t st) {
+  k_publish_err<<<1, 1, 0, st>>>(d, h_mapped);
+}
+
 // first / last particle of every cell and tile in sorted keys (arrays zeroed before)
 __global__ void k_cell_ranges(const int *keys, int start, int n, int ncpt, int *cs, int *ce, int *ts, int *te) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
