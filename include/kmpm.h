@@ -140,6 +140,7 @@ typedef struct {
 #define KMPM_P_J 11
 #define KMPM_P_VOL 12
 #define KMPM_P_STRAIN_EL 13 /* n*9 (needs kmpm_params.track_strain) */
+#define KMPM_P_VOL0PK1 14 /* n*9, TLMPM: vol0 times the first Piola-Kirchhoff stress of the last stress update */
 #define KMPM_P_MASS 15
 
 /* grid fields for kmpm_download_grid */
@@ -168,6 +169,11 @@ int kmpm_add_grid(struct kmpm_ctx *ctx, const double lo[3], double cellsize, con
  * solids each own one grid; ULMPM solids share grid 0.  Returns the id. */
 int kmpm_add_solid(struct kmpm_ctx *ctx, int grid, int mat, int n, const double *x0, const double *x,
                    const double *v, const double *mass, const double *vol0, double T0);
+
+/* Solid::np_per_cell, the particles per cell per direction the solid was
+ * populated with (src/solid.cpp:2027).  Needed only by APIC with the linear
+ * basis, whose inertia tensor depends on it (1 or 2, src/solid.cpp:1447-1462). */
+int kmpm_set_np_per_cell(struct kmpm_ctx *ctx, int solid, int np_per_cell);
 
 /* A fix on the nodes of one grid.  coef[4*d..4*d+3] = (c0,c1,c2,c3) give the
  * value of axis d as c0 + c1*time + c2*exp(c3*time) (velocity_nodes) or the
@@ -215,10 +221,38 @@ int kmpm_solid_scalars(struct kmpm_ctx *ctx, int solid, double *time, double *dt
 /* Download / upload one particle field of one solid in the caller's
  * particle order (the download before Output::write, src/output.cpp:128-200). */
 int kmpm_download_particles(struct kmpm_ctx *ctx, int solid, int field, double *out);
+
+/* Upload one particle field of one solid (caller order, the layout of
+ * kmpm_download_particles).  Before the first run: KMPM_P_X, KMPM_P_X0 and
+ * KMPM_P_V (the arrays kmpm_add_solid took).  After it (kmpm_run(ctx, 0)
+ * builds the context): KMPM_P_X, KMPM_P_V, KMPM_P_SIGMA (as stored: the
+ * corotational frame for TLMPM), KMPM_P_F, KMPM_P_EPS_P, KMPM_P_EPSDOT_P,
+ * KMPM_P_DAMAGE, KMPM_P_DAMAGE_INIT, KMPM_P_T, KMPM_P_STRAIN_EL and, for
+ * TLMPM, KMPM_P_VOL0PK1 -- the particle state Solid::read_restart restores
+ * (src/solid.cpp:2894-2957); L, Fdot and the APIC matrix restart at zero, as
+ * there.  The device keeps positions as x0 + u and F as I + H (FP32 u, H):
+ * x and F pass through FP64 sums, exact unless u or H is more than 2^29
+ * times smaller than x0 or 1, where their last bits go (kmpm_save_state
+ * keeps them). */
 int kmpm_upload_particles(struct kmpm_ctx *ctx, int solid, int field, const double *in);
 
-/* Asynchronous download (no counterpart in the reference; the dump path of
- * SURVEY's next rows): the field is gathered on the context's stream in
+/* Update::atime, Update::dt and Update::ntimestep as a restart sets them
+ * (Update::read_restart, src/update.cpp:303-338); every solid of an
+ * independent batch gets the same values. */
+int kmpm_set_scalars(struct kmpm_ctx *ctx, double time, double dt, long long ntimestep);
+
+/* Device snapshot (no counterpart in the reference, which restarts from the
+ * host state above): the particle buffer in its binned slot order, the step
+ * scalars and the node arrays, copied raw.  kmpm_load_state on a context made
+ * by the same setup calls restores the state bit for bit, so that the run
+ * continues exactly as if it had not stopped.  kmpm_state_size gives the
+ * bytes kmpm_save_state writes. */
+int kmpm_state_size(struct kmpm_ctx *ctx, unsigned long long *bytes);
+int kmpm_save_state(struct kmpm_ctx *ctx, void *out, unsigned long long bytes);
+int kmpm_load_state(struct kmpm_ctx *ctx, const void *in, unsigned long long bytes);
+
+/* Asynchronous download (no counterpart in the reference, whose dumps stop
+ * the run while they write): the field is gathered on the context's stream in
  * order with the steps, then copied to `out` on a second stream while later
  * kmpm_run calls proceed.  `out` must be page-locked host memory
  * (cudaHostAlloc / cudaHostRegister) of n*width doubles and stays owned by

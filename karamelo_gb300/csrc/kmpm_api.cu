@@ -36,6 +36,7 @@ struct kmpm_ctx {
   std::vector<HGrid> hgrids;
   struct HSolid {
     int grid, mat, n;
+    int np_per_cell = 0;  // Solid::np_per_cell (particles per cell per direction; linear APIC)
     double T0;
     // the caller's arrays, copied to the device as given (FP64: x0, x, v as
     // n*3, then mass, vol0); converted into the particle buffer at build
@@ -401,6 +402,7 @@ int build(kmpm_ctx *c) {
     }
     g.cellsize = (float)h.cellsize;
     g.inv_cellsize = (float)(1.0 / h.cellsize);
+    g.apic_di = 0.f;
     g.node_off = node_off;
     g.tile_off = tile_off;
     g.cell_off = tile_off * c->NCELL;
@@ -454,6 +456,19 @@ int build(kmpm_ctx *c) {
   c->nblk_p = (int)blk_range.size();
   if (c->TL())  // per-grid clock of independent solids: the range of the solid owning the grid
     for (size_t s = 0; s < c->hsolids.size(); s++) c->grids[c->hsolids[s].grid].solid0 = c->solid_range[s];
+  if (c->apic() && basis == KMPM_BASIS_LINEAR) {
+    // Solid::compute_inertia_tensor (src/solid.cpp:1447-1462): Di = 16/4 (one
+    // particle per cell per direction) or 16/3 (two) over cellsize^2
+    for (size_t s = 0; s < c->hsolids.size(); s++) {
+      const int npc = c->hsolids[s].np_per_cell;
+      if (npc != 1 && npc != 2)
+        return fail(c, KMPM_ERR_ARG,
+                    "Number of particle per cell not supported with linear shape functions and APIC "
+                    "(kmpm_set_np_per_cell: 1 or 2)");
+      const double cs = c->hgrids[c->hsolids[s].grid].cellsize;
+      c->grids[c->hsolids[s].grid].apic_di = (float)((npc == 1 ? 16.0 / 4.0 : 16.0 / 3.0) / (cs * cs));
+    }
+  }
   // ---- device allocations
   DALLOC(c->buf[0], c->ps * PF_COUNT);
   DALLOC(c->buf[1], c->ps * PF_COUNT);
@@ -574,6 +589,7 @@ int build(kmpm_ctx *c) {
     const int am[3] = {P2G_TL_APIC, P2G_UL_APIC, P2G_VEL_APIC};
     void *af[3] = {c->K.p2g_tl_apic, c->K.p2g_ul_apic, c->K.p2g_vel_apic};
     for (int m = 0; m < 3; m++) {
+      if (!af[m]) continue;  // linear basis: TLMPM modes only
       c->smem_apic[m] = p2g_smem_bytes(dim, basis, am[m], false);
       CK(cudaFuncSetAttribute(af[m], cudaFuncAttributeMaxDynamicSharedMemorySize, c->smem_apic[m]));
     }
@@ -1117,9 +1133,12 @@ int kmpm_create(const kmpm_params *params, kmpm_ctx **out) {
   if (p.transfer == KMPM_TRANSFER_MLS && p.method != KMPM_ULMPM) return KMPM_ERR_ARG;  // MLS is a ULMPM path
   if (p.axisymmetric && (p.dim != 2 || p.thermal)) return KMPM_ERR_ARG;  // 2-D, mechanical
   {
-    // affine transfers: the cubic or quadratic spline, mechanical runs
+    // affine transfers: the cubic or quadratic spline, or the linear basis for
+    // TLMPM (src/solid.cpp:1447-1473); mechanical runs
     const bool affine = p.transfer == KMPM_TRANSFER_APIC || (p.method == KMPM_ULMPM && p.transfer >= KMPM_TRANSFER_AFLIP);
-    if (affine && ((p.basis != KMPM_BASIS_CUBIC && p.basis != KMPM_BASIS_QUADRATIC) || p.thermal)) return KMPM_ERR_ARG;
+    const bool basis_ok = p.basis == KMPM_BASIS_CUBIC || p.basis == KMPM_BASIS_QUADRATIC ||
+                          (p.basis == KMPM_BASIS_LINEAR && p.method == KMPM_TLMPM);
+    if (affine && (!basis_ok || p.thermal)) return KMPM_ERR_ARG;
   }
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return KMPM_ERR_CUDA;
@@ -1238,6 +1257,13 @@ int kmpm_add_solid(kmpm_ctx *c, int grid, int mat, int n, const double *x0, cons
   }
   c->hsolids.push_back(s);
   return (int)c->hsolids.size() - 1;
+}
+
+int kmpm_set_np_per_cell(kmpm_ctx *c, int solid, int np_per_cell) {
+  if (!c || solid < 0 || solid >= (int)c->hsolids.size() || np_per_cell < 1) return KMPM_ERR_ARG;
+  if (c->built) return fail(c, KMPM_ERR_STATE, "set before the first run");
+  c->hsolids[solid].np_per_cell = np_per_cell;
+  return KMPM_OK;
 }
 
 int kmpm_add_fix(kmpm_ctx *c, int kind, int grid, const unsigned char *node_mask, const int set[3], const double coef[12]) {
@@ -1488,32 +1514,161 @@ int kmpm_sync_downloads(kmpm_ctx *c) {
 
 int kmpm_upload_particles(kmpm_ctx *c, int solid, int field, const double *in) {
   if (!c || !in || solid < 0 || solid >= (int)c->hsolids.size()) return KMPM_ERR_ARG;
-  if (field != KMPM_P_V) return fail(c, KMPM_ERR_ARG, "only velocities can be uploaded");
   auto &S = c->hsolids[solid];
   if (!c->built) {
-    CK(cudaMemcpyAsync(S.d_in + 6 * (size_t)S.n, in, sizeof(double) * 3 * S.n, cudaMemcpyHostToDevice, c->st));
+    // into the arrays kmpm_add_solid took (x0, x, v at 0, 3n, 6n)
+    const size_t off = field == KMPM_P_X0 ? 0 : field == KMPM_P_X ? 3 : field == KMPM_P_V ? 6 : 99;
+    if (off == 99) return fail(c, KMPM_ERR_STATE, "only x0, x and v can be uploaded before the first run");
+    CK(cudaMemcpyAsync(S.d_in + off * S.n, in, sizeof(double) * 3 * S.n, cudaMemcpyHostToDevice, c->st));
     CK(cudaStreamSynchronize(c->st));
     return KMPM_OK;
   }
-  const RangeDev &rg = c->ranges[c->TL() ? c->solid_range[solid] : 0];
-  std::vector<int> orig, sid;
-  int r = slot_map(c, rg, orig, sid);
-  if (r != KMPM_OK) return r;
-  std::vector<std::vector<float>> H;
-  r = fetch_rows(c, {PF_V, PF_V + 1, PF_V + 2}, rg.start, rg.count, H);
-  if (r != KMPM_OK) return r;
-  for (int q = 0; q < rg.count; q++) {
-    if (sid[q] != solid) continue;
-    const int i = orig[q] - c->solid_base[solid];
-    for (int d = 0; d < 3; d++) H[PF_V + d][q] = (float)in[3 * i + d];
+  switch (field) {
+    case KMPM_P_X: case KMPM_P_V: case KMPM_P_SIGMA: case KMPM_P_F: case KMPM_P_EPS_P: case KMPM_P_EPSDOT_P:
+    case KMPM_P_DAMAGE: case KMPM_P_DAMAGE_INIT: case KMPM_P_T: case KMPM_P_STRAIN_EL:
+      break;
+    case KMPM_P_VOL0PK1:
+      if (!c->TL()) return fail(c, KMPM_ERR_ARG, "vol0PK1 is TLMPM state");
+      break;
+    case KMPM_P_X0:
+      return fail(c, KMPM_ERR_STATE, "x0 is fixed once the context is built (TLMPM bins by it)");
+    default:
+      return fail(c, KMPM_ERR_ARG, "this field cannot be uploaded");
   }
+  if (field == KMPM_P_T && !c->prm.thermal) return fail(c, KMPM_ERR_STATE, "temperature needs a thermo-mechanical run");
+  if (field == KMPM_P_STRAIN_EL && !c->prm.track_strain)
+    return fail(c, KMPM_ERR_STATE, "strain_el is tracked only with track_strain");
+  const size_t need = (size_t)S.n * dump_width(field);
+  if (need > c->dump_cap) {
+    dfree(c->d_dump);
+    DALLOC(c->d_dump, need);
+    c->dump_cap = need;
+  }
+  CK(cudaMemcpyAsync(c->d_dump, in, sizeof(double) * need, cudaMemcpyHostToDevice, c->st));
+  const int ri = c->TL() ? c->solid_range[solid] : 0;
+  launch_load(part_args(c), ri, c->ranges[ri].count, solid, c->solid_base[solid], field, c->TL() ? 1 : 0, c->T_ref,
+              c->d_dump, c->st);
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(c->st));
+  return KMPM_OK;
+}
+
+int kmpm_set_scalars(kmpm_ctx *c, double time, double dt, long long ntimestep) {
+  if (!c) return KMPM_ERR_ARG;
+  int r = prepare(c);
+  if (r != KMPM_OK) return r;
+  std::vector<StepScalars> sv(c->nscalars);
+  CK(cudaMemcpyAsync(sv.data(), c->d_scalars, sizeof(StepScalars) * sv.size(), cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  for (auto &x : sv) {
+    x.time = time;
+    x.dt = dt;
+    x.ntimestep = ntimestep;
+  }
+  CK(cudaMemcpyAsync(c->d_scalars, sv.data(), sizeof(StepScalars) * sv.size(), cudaMemcpyHostToDevice, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  return KMPM_OK;
+}
+
+// ---- device snapshot: header, field ids, scalars, particle rows, node arrays
+struct SnapHeader {
+  char magic[8];
+  int version, method, dim, basis, nfields, nscalars, nnodes_pad, nsolids;
+  unsigned long long ps;
+};
+static const char SNAP_MAGIC[8] = {'K', 'M', 'P', 'M', 'S', 'N', 'P', '1'};
+
+static unsigned long long snap_bytes(kmpm_ctx *c, const std::vector<int> &fl) {
+  return sizeof(SnapHeader) + sizeof(int) * fl.size() + sizeof(StepScalars) * c->nscalars +
+         sizeof(float) * c->ps * fl.size() + 3 * sizeof(float4) * (unsigned long long)c->nnodes_pad +
+         sizeof(float) * (unsigned long long)c->nnodes_pad;
+}
+
+static int current_buffer(kmpm_ctx *c, float **cur) {
+  CK(cudaMemcpyAsync(cur, c->d_pp, sizeof(float *), cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  return KMPM_OK;
+}
+
+int kmpm_state_size(kmpm_ctx *c, unsigned long long *bytes) {
+  if (!c || !bytes) return KMPM_ERR_ARG;
+  int r = prepare(c);
+  if (r != KMPM_OK) return r;
+  *bytes = snap_bytes(c, active_fields(c));
+  return KMPM_OK;
+}
+
+int kmpm_save_state(kmpm_ctx *c, void *out, unsigned long long bytes) {
+  if (!c || !out) return KMPM_ERR_ARG;
+  int r = prepare(c);
+  if (r != KMPM_OK) return r;
+  const std::vector<int> fl = active_fields(c);
+  if (bytes < snap_bytes(c, fl)) return fail(c, KMPM_ERR_ARG, "snapshot buffer too small (kmpm_state_size)");
+  char *o = (char *)out;
+  SnapHeader h{};
+  std::memcpy(h.magic, SNAP_MAGIC, 8);
+  h.version = 1; h.method = c->prm.method; h.dim = c->prm.dim; h.basis = c->prm.basis;
+  h.nfields = (int)fl.size(); h.nscalars = c->nscalars; h.nnodes_pad = c->nnodes_pad;
+  h.nsolids = (int)c->hsolids.size(); h.ps = c->ps;
+  std::memcpy(o, &h, sizeof(h)); o += sizeof(h);
+  std::memcpy(o, fl.data(), sizeof(int) * fl.size()); o += sizeof(int) * fl.size();
+  CK(cudaMemcpyAsync(o, c->d_scalars, sizeof(StepScalars) * c->nscalars, cudaMemcpyDeviceToHost, c->st));
+  o += sizeof(StepScalars) * c->nscalars;
   float *cur = nullptr;
-  CK(cudaMemcpyAsync(&cur, c->d_pp, sizeof(float *), cudaMemcpyDeviceToHost, c->st));
+  r = current_buffer(c, &cur);
+  if (r != KMPM_OK) return r;
+  for (int f : fl) {
+    CK(cudaMemcpyAsync(o, cur + (size_t)f * c->ps, sizeof(float) * c->ps, cudaMemcpyDeviceToHost, c->st));
+    o += sizeof(float) * c->ps;
+  }
+  for (float4 *a : {c->nodeA, c->nodeB, c->nodeX}) {
+    CK(cudaMemcpyAsync(o, a, sizeof(float4) * c->nnodes_pad, cudaMemcpyDeviceToHost, c->st));
+    o += sizeof(float4) * c->nnodes_pad;
+  }
+  CK(cudaMemcpyAsync(o, c->nodeT, sizeof(float) * c->nnodes_pad, cudaMemcpyDeviceToHost, c->st));
   CK(cudaStreamSynchronize(c->st));
-  for (int d = 0; d < 3; d++)
-    CK(cudaMemcpyAsync(cur + (size_t)(PF_V + d) * c->ps + rg.start, H[PF_V + d].data(), sizeof(float) * rg.count,
-                       cudaMemcpyHostToDevice, c->st));
+  return KMPM_OK;
+}
+
+int kmpm_load_state(kmpm_ctx *c, const void *in, unsigned long long bytes) {
+  if (!c || !in) return KMPM_ERR_ARG;
+  int r = prepare(c);
+  if (r != KMPM_OK) return r;
+  const std::vector<int> fl = active_fields(c);
+  if (bytes < sizeof(SnapHeader)) return fail(c, KMPM_ERR_ARG, "not a snapshot");
+  const char *o = (const char *)in;
+  SnapHeader h;
+  std::memcpy(&h, o, sizeof(h));
+  o += sizeof(h);
+  if (std::memcmp(h.magic, SNAP_MAGIC, 8) != 0 || h.version != 1) return fail(c, KMPM_ERR_ARG, "not a snapshot");
+  if (h.method != c->prm.method || h.dim != c->prm.dim || h.basis != c->prm.basis || h.nfields != (int)fl.size() ||
+      h.nscalars != c->nscalars || h.nnodes_pad != c->nnodes_pad || h.nsolids != (int)c->hsolids.size() ||
+      h.ps != c->ps || bytes < snap_bytes(c, fl))
+    return fail(c, KMPM_ERR_ARG, "snapshot of a different setup");
+  if (std::memcmp(o, fl.data(), sizeof(int) * fl.size()) != 0) return fail(c, KMPM_ERR_ARG, "snapshot fields differ");
+  o += sizeof(int) * fl.size();
+  CK(cudaMemcpyAsync(c->d_scalars, o, sizeof(StepScalars) * c->nscalars, cudaMemcpyHostToDevice, c->st));
+  o += sizeof(StepScalars) * c->nscalars;
+  float *cur = nullptr;
+  r = current_buffer(c, &cur);
+  if (r != KMPM_OK) return r;
+  for (int f : fl) {
+    CK(cudaMemcpyAsync(cur + (size_t)f * c->ps, o, sizeof(float) * c->ps, cudaMemcpyHostToDevice, c->st));
+    o += sizeof(float) * c->ps;
+  }
+  for (float4 *a : {c->nodeA, c->nodeB, c->nodeX}) {
+    CK(cudaMemcpyAsync(a, o, sizeof(float4) * c->nnodes_pad, cudaMemcpyHostToDevice, c->st));
+    o += sizeof(float4) * c->nnodes_pad;
+  }
+  CK(cudaMemcpyAsync(c->nodeT, o, sizeof(float) * c->nnodes_pad, cudaMemcpyHostToDevice, c->st));
   CK(cudaStreamSynchronize(c->st));
+  // the slot maps of the host caches follow the restored order; maxtime
+  // as written with the scalars
+  c->orig_cache.clear();
+  c->sid_cache.clear();
+  StepScalars s0{};
+  std::memcpy(&s0, (const char *)in + sizeof(SnapHeader) + sizeof(int) * fl.size(), sizeof(s0));
+  c->maxtime_dev = s0.maxtime;
   return KMPM_OK;
 }
 

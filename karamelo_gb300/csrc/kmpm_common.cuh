@@ -64,6 +64,7 @@ struct GridDev {
   float lo[3];       // lower bound of the lattice
   float inv_cellsize;
   float cellsize;
+  float apic_di;     // linear-basis APIC: Di of the grid's solid (16/4 or 16/3 over cellsize^2)
 };
 
 // A contiguous particle range that shares one grid: one per solid for TLMPM,

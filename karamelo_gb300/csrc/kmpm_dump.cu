@@ -68,6 +68,9 @@ __global__ void k_dump(PartArgs a, DumpArgs d) {
     case KMPM_P_F:
       for (int k = 0; k < 9; k++) o[9 * i + k] = f(PF_H + k) + (k % 4 == 0 ? 1.0 : 0.0);
       break;
+    case KMPM_P_VOL0PK1:
+      for (int k = 0; k < 9; k++) o[9 * i + k] = d.TL ? f(PF_PK + k) : 0.0;
+      break;
     case KMPM_P_J:
     case KMPM_P_VOL: {
       double H[9];
@@ -88,10 +91,80 @@ __global__ void k_dump(PartArgs a, DumpArgs d) {
   }
 }
 
+// Uploads for a restart (Solid::read_restart, src/solid.cpp:2894-2957): the
+// inverse of k_dump, one field of one solid from caller order into its slots.
+// Positions go in as the displacement from the stored x0, formed in FP64, so
+// a download followed by an upload is exact.
+struct LoadArgs {
+  int ri, solid, base, field, TL;
+  double T_ref;
+  const double *in;
+};
+
+__global__ void k_load(PartArgs a, LoadArgs d) {
+  const RangeDev rd = a.ranges[d.ri];
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= rd.count) return;
+  const int p = rd.start + q;
+  float *P = *a.Pp;
+  const size_t ps = a.ps;
+  if (__float_as_int(P[PF_SID * ps + p]) != d.solid) return;
+  const size_t i = (size_t)(__float_as_int(P[PF_ORIG * ps + p]) - d.base);
+  const double *in = d.in;
+  auto put = [&](int fld, double v) { P[fld * ps + p] = (float)v; };
+  // upper triangle of a row-major 3x3 into the symmetric order xx yy zz xy xz yz
+  const int up[6] = {0, 4, 8, 1, 2, 5};
+  bool ul_pk = false;
+  switch (d.field) {
+    case KMPM_P_X:
+      for (int k = 0; k < 3; k++) {
+        const double u = in[3 * i + k] - (double)P[(PF_X0 + k) * ps + p];
+        put(PF_X + k, u);
+        if (!d.TL) put(PF_XN + k, u);
+      }
+      break;
+    case KMPM_P_V:
+      for (int k = 0; k < 3; k++) put(PF_V + k, in[3 * i + k]);
+      break;
+    case KMPM_P_SIGMA:
+      for (int k = 0; k < 6; k++) put(PF_SIG + k, in[9 * i + up[k]]);
+      ul_pk = !d.TL;
+      break;
+    case KMPM_P_STRAIN_EL:
+      for (int k = 0; k < 6; k++) put(PF_STRAIN + k, in[9 * i + up[k]]);
+      break;
+    case KMPM_P_F:
+      for (int k = 0; k < 9; k++) put(PF_H + k, in[9 * i + k] - (k % 4 == 0 ? 1.0 : 0.0));
+      ul_pk = !d.TL;
+      break;
+    case KMPM_P_VOL0PK1:
+      for (int k = 0; k < 9; k++) put(PF_PK + k, in[9 * i + k]);
+      break;
+    case KMPM_P_EPS_P: put(PF_EPSP, in[i]); break;
+    case KMPM_P_EPSDOT_P: put(PF_EPSDOT, in[i]); break;
+    case KMPM_P_DAMAGE: put(PF_DMG, in[i]); break;
+    case KMPM_P_DAMAGE_INIT: put(PF_DMGI, in[i]); break;
+    case KMPM_P_T: put(PF_T, in[i] - d.T_ref); break;
+  }
+  if (ul_pk) {
+    // ULMPM scatters vol sigma with vol = J vol0, as the stress kernel stores it
+    float H[9];
+    for (int k = 0; k < 9; k++) H[k] = P[(PF_H + k) * ps + p];
+    const float vol = (1.f + jm1_of_H(H)) * P[PF_VOL0 * ps + p];
+    for (int k = 0; k < 6; k++) P[(PF_PK + k) * ps + p] = vol * P[(PF_SIG + k) * ps + p];
+  }
+}
+
+void launch_load(const PartArgs &a, int ri, int count, int solid, int base, int field, int TL, double T_ref,
+                 const double *in, cudaStream_t st) {
+  LoadArgs d{ri, solid, base, field, TL, T_ref, in};
+  if (count > 0) k_load<<<(count + 255) / 256, 256, 0, st>>>(a, d);
+}
+
 int dump_width(int field) {
   switch (field) {
     case KMPM_P_X: case KMPM_P_X0: case KMPM_P_V: return 3;
-    case KMPM_P_SIGMA: case KMPM_P_SIGMA_ROT: case KMPM_P_F: case KMPM_P_STRAIN_EL: return 9;
+    case KMPM_P_SIGMA: case KMPM_P_SIGMA_ROT: case KMPM_P_F: case KMPM_P_STRAIN_EL: case KMPM_P_VOL0PK1: return 9;
     case KMPM_P_EPS_P: case KMPM_P_EPSDOT_P: case KMPM_P_DAMAGE: case KMPM_P_DAMAGE_INIT: case KMPM_P_T:
     case KMPM_P_J: case KMPM_P_VOL: case KMPM_P_MASS: return 1;
     default: return 0;

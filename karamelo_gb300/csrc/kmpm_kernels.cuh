@@ -143,6 +143,9 @@ void get_step_kernels(int dim, int basis, StepKernels &k);
 int dump_width(int field);
 void launch_dump(const PartArgs &a, int ri, int count, int solid, int base, int field, int TL, int rotate,
                  double T_ref, double *out, cudaStream_t st);
+// the inverse: one field of one solid from caller order (FP64, device) into its slots
+void launch_load(const PartArgs &a, int ri, int count, int solid, int base, int field, int TL, double T_ref,
+                 const double *in, cudaStream_t st);
 int p2g_smem_bytes(int dim, int basis, int mode, bool thermal);
 
 // kmpm_contact.cu: one contact fix between two solids (device form)

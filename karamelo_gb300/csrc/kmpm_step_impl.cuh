@@ -631,7 +631,7 @@ __global__ void __launch_bounds__(256, MINB) k_g2p2(PartArgs a) {
     ax.eval(g, xp);
     constexpr int S = Stencil<BASIS>::S;
     constexpr int SY = DIM >= 2 ? S : 1, SZ = DIM == 3 ? S : 1;
-    if ((BASIS == 1 || BASIS == 3) && a.apic) {
+    if ((BASIS == 0 || BASIS == 1 || BASIS == 3) && a.apic) {
       // APIC (compute_rate_deformation_gradient_{TL,UL}_APIC,
       // src/solid.cpp:1006-1153): grad v = sum w v_node (x_node - x_p)^T Di with
       // Di = 3 / cellsize^2 (cubic) or 4 / cellsize^2 (quadratic)
@@ -641,7 +641,8 @@ __global__ void __launch_bounds__(256, MINB) k_g2p2(PartArgs a) {
       // point: before the move (USL) or after it (MUSL)
       // x_node - x_p = h o_k + (x_w - x_p): o_k from the weights (Axis::eval)
       // and, for ULMPM MUSL, the move x_w - x_p = u - u_moved of this step
-      const float Di = (BASIS == 3 ? 4.f : 3.f) * g.inv_cellsize * g.inv_cellsize;
+      // (linear TLMPM: 16/4 or 16/3 over cellsize^2 by particles per cell, src/solid.cpp:1448-1462)
+      const float Di = BASIS == 0 ? g.apic_di : (BASIS == 3 ? 4.f : 3.f) * g.inv_cellsize * g.inv_cellsize;
 #pragma unroll
       for (int d = 0; d < DIM; d++) {
         const float dw = (TL || a.use_vu) ? 0.f : P[(PF_X + d) * ps + p] - P[(PF_XN + d) * ps + p];
@@ -712,7 +713,7 @@ __global__ void __launch_bounds__(256, MINB) k_g2p2(PartArgs a) {
       const float r = P[PF_X0 * ps + p] + (TL ? 0.f : P[(a.use_vu ? PF_X : PF_XN) * ps + p]);
       G[8] += vr / r;
     }
-    if ((BASIS == 1 || BASIS == 3) && a.apic)
+    if ((BASIS == 0 || BASIS == 1 || BASIS == 3) && a.apic)
 #pragma unroll
       for (int k = 0; k < 9; k++) P[(PF_C + k) * ps + p] = G[k];  // C of the next transfers
     // ---- deformation gradient (src/solid.cpp:1155-1244), stored as H = F - I
@@ -945,10 +946,16 @@ void fill_step_kernels(StepKernels &k) {
   k.p2g_ul_th = (void *)k_p2g<DIM, BASIS, P2G_UL, true>;
   k.p2g_vel = (void *)k_p2g<DIM, BASIS, P2G_VEL, false>;
   k.p2g_vel_th = (void *)k_p2g<DIM, BASIS, P2G_VEL, true>;
-  if constexpr (BASIS == 1 || BASIS == 3) {  // APIC runs with the cubic and quadratic splines
+  // APIC runs with the cubic and quadratic splines, and for TLMPM with the
+  // linear basis (src/solid.cpp:1447-1473)
+  if constexpr (BASIS == 1 || BASIS == 3) {
     k.p2g_tl_apic = (void *)k_p2g<DIM, BASIS, P2G_TL_APIC, false>;
     k.p2g_ul_apic = (void *)k_p2g<DIM, BASIS, P2G_UL_APIC, false>;
     k.p2g_vel_apic = (void *)k_p2g<DIM, BASIS, P2G_VEL_APIC, false>;
+  } else if constexpr (BASIS == 0) {
+    k.p2g_tl_apic = (void *)k_p2g<DIM, BASIS, P2G_TL_APIC, false>;
+    k.p2g_vel_apic = (void *)k_p2g<DIM, BASIS, P2G_VEL_APIC, false>;
+    k.p2g_ul_apic = nullptr;
   } else {
     k.p2g_tl_apic = k.p2g_ul_apic = k.p2g_vel_apic = nullptr;
   }
@@ -959,8 +966,10 @@ void fill_step_kernels(StepKernels &k) {
       for (int ex = 0; ex < 2; ex++) k.p2g_axi[u][ap][ex] = nullptr;
   if constexpr (DIM == 2) {  // axisymmetric runs are 2-D
     KMPM_AXI(0, 0, 0, P2G_TL) KMPM_AXI(0, 0, 1, P2G_TL) KMPM_AXI(1, 0, 0, P2G_UL) KMPM_AXI(1, 0, 1, P2G_UL)
-    if constexpr (BASIS == 1 || BASIS == 3) {
+    if constexpr (BASIS == 0 || BASIS == 1 || BASIS == 3) {
       KMPM_AXI(0, 1, 0, P2G_TL_APIC) KMPM_AXI(0, 1, 1, P2G_TL_APIC)
+    }
+    if constexpr (BASIS == 1 || BASIS == 3) {
       KMPM_AXI(1, 1, 0, P2G_UL_APIC) KMPM_AXI(1, 1, 1, P2G_UL_APIC)
     }
   }
@@ -973,6 +982,9 @@ void fill_step_kernels(StepKernels &k) {
     if constexpr (BASIS == 1 || BASIS == 3) {
       k.p2g_tl_apic_ext = (void *)k_p2g<DIM, BASIS, P2G_TL_APIC | P2G_EXT, false>;
       k.p2g_ul_apic_ext = (void *)k_p2g<DIM, BASIS, P2G_UL_APIC | P2G_EXT, false>;
+    } else if constexpr (BASIS == 0) {
+      k.p2g_tl_apic_ext = (void *)k_p2g<DIM, BASIS, P2G_TL_APIC | P2G_EXT, false>;
+      k.p2g_ul_apic_ext = nullptr;
     } else {
       k.p2g_tl_apic_ext = k.p2g_ul_apic_ext = nullptr;
     }

@@ -22,7 +22,11 @@ ERRORS = {-1: "KMPM_ERR_ARG", -2: "KMPM_ERR_CUDA", -3: "KMPM_ERR_STATE", -10: "K
 
 PARTICLE_FIELDS = {"x": (0, 3), "x0": (1, 3), "v": (2, 3), "sigma_raw": (3, 9), "sigma": (4, 9), "F": (5, 9),
                    "eps_p": (6, 1), "epsdot_p": (7, 1), "damage": (8, 1), "damage_init": (9, 1), "T": (10, 1),
-                   "J": (11, 1), "vol": (12, 1), "strain_el": (13, 9), "mass": (15, 1)}
+                   "J": (11, 1), "vol": (12, 1), "strain_el": (13, 9), "vol0PK1": (14, 9), "mass": (15, 1)}
+# the particle state Solid::read_restart restores (src/solid.cpp:2894-2957)
+RESTART_FIELDS_TL = ("x", "v", "sigma_raw", "strain_el", "vol0PK1", "F", "eps_p", "epsdot_p", "damage",
+                     "damage_init")
+RESTART_FIELDS_UL = ("x", "v", "sigma_raw", "strain_el", "F", "eps_p", "epsdot_p", "damage", "damage_init")
 GRID_FIELDS = {"mass": (0, 1), "v": (1, 3), "v_update": (2, 3), "x": (3, 3), "T": (6, 1)}
 
 EXPORTED = ["kmpm_create", "kmpm_destroy", "kmpm_last_error", "kmpm_add_material", "kmpm_add_grid",
@@ -34,7 +38,8 @@ EXPORTED = ["kmpm_create", "kmpm_destroy", "kmpm_last_error", "kmpm_add_material
             "kmpm_mlp_get_params", "kmpm_mlp_set_norm", "kmpm_mlp_get_norm", "kmpm_mlp_loss_grad", "kmpm_mlp_train",
             "kmpm_mlp_predict", "kmpm_mlp_predict_tc", "kmpm_log_start", "kmpm_log_stop", "kmpm_log_data",
             "kmpm_jc_label", "kmpm_set_surrogate", "kmpm_surrogate_stats", "kmpm_tuning",
-            "kmpm_download_particles_async", "kmpm_sync_downloads", "kmpm_add_contact", "kmpm_contact_force"]
+            "kmpm_download_particles_async", "kmpm_sync_downloads", "kmpm_add_contact", "kmpm_contact_force",
+            "kmpm_set_scalars", "kmpm_state_size", "kmpm_save_state", "kmpm_load_state", "kmpm_set_np_per_cell"]
 
 MLP_NIN, MLP_NOUT, MLP_NPARAMS, MLP_NNORM = 15, 7, 35975, 74
 
@@ -125,6 +130,11 @@ def load(path: str = LIB_PATH):
     L.kmpm_tuning.restype = ctypes.c_char_p
     L.kmpm_add_contact.argtypes = [p, i, i, i, d]
     L.kmpm_contact_force.argtypes = [p, i, dp]
+    L.kmpm_set_scalars.argtypes = [p, d, d, ll]
+    L.kmpm_set_np_per_cell.argtypes = [p, i, i]
+    L.kmpm_state_size.argtypes = [p, ctypes.POINTER(ull)]
+    L.kmpm_save_state.argtypes = [p, ctypes.c_void_p, ull]
+    L.kmpm_load_state.argtypes = [p, ctypes.c_void_p, ull]
     _lib = L
     return L
 
@@ -170,8 +180,10 @@ class GpuBackend:
             v = np.ascontiguousarray(sol.v, float)
             m = np.ascontiguousarray(sol.mass, float)
             vo = np.ascontiguousarray(sol.vol0, float)
-            self._ck(L.kmpm_add_solid(h, sol.grid, sol.mat, sol.np, _dp(x0), _dp(x0), _dp(v), _dp(m), _dp(vo),
-                                      sol.T0), allow_id=True)
+            si = self._ck(L.kmpm_add_solid(h, sol.grid, sol.mat, sol.np, _dp(x0), _dp(x0), _dp(v), _dp(m), _dp(vo),
+                                           sol.T0), allow_id=True)
+            if getattr(sol, "ppc", 0):
+                self._ck(L.kmpm_set_np_per_cell(h, si, int(sol.ppc)))
         for f in s.fixes:
             self.add_fix(f)
         for c in s.contacts:
@@ -245,6 +257,46 @@ class GpuBackend:
     def upload_velocity(self, si: int, v):
         v = np.ascontiguousarray(v, float)
         self._ck(self.L.kmpm_upload_particles(self.h, si, 2, _dp(v)))
+
+    def upload(self, si: int, field: str, values):
+        """Upload one particle field (the layout ``particles`` returns)."""
+        code, w = PARTICLE_FIELDS[field]
+        a = np.ascontiguousarray(values, float).reshape(-1)
+        assert a.size == self.s.solids[si].np * w
+        self._ck(self.L.kmpm_upload_particles(self.h, si, code, _dp(a)))
+
+    def set_scalars(self, time: float, dt: float, ntimestep: int):
+        self._ck(self.L.kmpm_set_scalars(self.h, float(time), float(dt), int(ntimestep)))
+
+    # ---- restart (Solid::write_restart / read_restart, src/solid.cpp:2841-2957)
+    def restart_state(self):
+        """The per-particle state a restart file carries, as FP64 arrays per
+        solid, with the clock (time, dt, ntimestep)."""
+        names = RESTART_FIELDS_TL if self.s.method == sc.TLMPM else RESTART_FIELDS_UL
+        extra = ("T",) if self.s.thermal else ()
+        return {"scalars": self.scalars(),
+                "solids": [{f: self.particles(si, f) for f in names + extra} for si in range(len(self.s.solids))]}
+
+    def restore_state(self, st):
+        """Restore ``restart_state`` into a context made by the same setup."""
+        self.run(0)  # builds the context
+        for si, fields in enumerate(st["solids"]):
+            for f, a in fields.items():
+                self.upload(si, f, a)
+        t, dt, n = st["scalars"]
+        self.set_scalars(t, dt, n)
+
+    # ---- device snapshot (bit-exact checkpoint of the whole device state)
+    def save_state(self) -> bytes:
+        n = ctypes.c_ulonglong()
+        self._ck(self.L.kmpm_state_size(self.h, ctypes.byref(n)))
+        buf = ctypes.create_string_buffer(n.value)
+        self._ck(self.L.kmpm_save_state(self.h, buf, n.value))
+        return buf.raw
+
+    def load_state(self, blob: bytes):
+        buf = ctypes.create_string_buffer(blob, len(blob))
+        self._ck(self.L.kmpm_load_state(self.h, buf, len(blob)))
 
     def grid(self, gi: int, field: str):
         code, w = GRID_FIELDS[field]

@@ -121,8 +121,10 @@ class MPM:
         if self.s.basis == sc.BERNSTEIN and self.s.method == sc.ULMPM:
             raise KarameloError("Bernstein-quadratic shape functions are only supported with TLMPM")
         affine = self.s.transfer == 1 or (self.s.method == sc.ULMPM and self.s.transfer >= 2)
-        if affine and self.s.basis not in (sc.CUBIC, sc.QUADRATIC):
-            raise KarameloError(f"{sub} on the GPU path runs with the cubic or quadratic spline")
+        linear_tl = self.s.basis == sc.LINEAR and self.s.method == sc.TLMPM
+        if affine and self.s.basis not in (sc.CUBIC, sc.QUADRATIC) and not linear_tl:
+            # Solid::compute_inertia_tensor, src/solid.cpp:1447-1473
+            raise KarameloError(f"{sub} runs with the cubic or quadratic spline (and, for tlmpm, linear)")
         rest = list(rest)
         if sub in ("FLIP", "AFLIP", "ASFLIP"):
             self.s.pic_flip = float(rest.pop(0))
@@ -369,7 +371,7 @@ class MPM:
             vols = masses / rho0
         self.s.solids.append(sc.SolidSpec(name=name, grid=gid, mat=self.material_ids[mat], x0=x,
                                           v=np.zeros((n, 3)), mass=masses, vol0=vols,
-                                          T0=float(T0), ptag=ptag, mask=np.ones(n, np.int64)))
+                                          T0=float(T0), ptag=ptag, mask=np.ones(n, np.int64), ppc=ppc))
         self.solid_ids[name] = len(self.s.solids) - 1
 
     # ------------------------------------------------------------ groups/fixes

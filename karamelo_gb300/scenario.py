@@ -111,6 +111,7 @@ class SolidSpec:
     T0: float
     ptag: np.ndarray          # (n,) int64, 1-based global tags
     mask: np.ndarray = None   # (n,) group bitmask
+    ppc: int = 0              # Solid::np_per_cell: particles per cell per direction
 
     @property
     def np(self) -> int:

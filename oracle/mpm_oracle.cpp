@@ -401,6 +401,7 @@ struct Solid {
   std::vector<std::vector<double>> wfd_pn, wfd_np;  // 3 per entry
   double dtCFL;
   double Di[3] = {1, 1, 1};  // APIC inertia tensor inverse (diagonal), Solid::compute_inertia_tensor
+  int np_per_cell = 0;       // Solid::np_per_cell (src/solid.cpp:2027)
 };
 
 enum { FIX_VEL_NODES = 0, FIX_BODY_FORCE = 1 };
@@ -514,7 +515,8 @@ void grid_init(Sim &s, Grid &g, const double *boundlo, const double *boundhi, do
 // (cubic) or 4 / cellsize^2 (quadratic) on the active dimensions, 1 on the others
 void compute_inertia_tensor(const Sim &s, Solid &S) {
   const double c = s.grids[S.grid].cellsize;
-  const double k = s.basis == QUADRATIC ? 4.0 : 3.0;
+  // linear: 16/4 (one particle per cell per direction) or 16/3 (two), src/solid.cpp:1447-1462
+  const double k = s.basis == QUADRATIC ? 4.0 : s.basis == LINEAR ? (S.np_per_cell == 1 ? 16.0 / 4.0 : 16.0 / 3.0) : 3.0;
   for (int d = 0; d < 3; d++) S.Di[d] = d < s.dim ? k / (c * c) : 1.0;
 }
 
@@ -1311,8 +1313,8 @@ int om_set_transfer(void *h, int kind) {
   const bool TL = s->method == TLMPM;
   if (kind < 0 || kind > 4 || (kind == 4 && TL)) { s->err = "unsupported sub-method"; return -1; }
   const bool affine = kind == 1 || (!TL && kind >= 2);
-  if (affine && s->basis != CUBIC && s->basis != QUADRATIC) {
-    s->err = "affine transfers are restated for the cubic and quadratic splines";
+  if (affine && s->basis != CUBIC && s->basis != QUADRATIC && !(s->basis == LINEAR && TL)) {
+    s->err = "affine transfers are restated for the cubic and quadratic splines, and the linear basis in TLMPM";
     return -1;
   }
   s->apic = affine;
@@ -1392,6 +1394,16 @@ int om_add_fix(void *h, int kind, int grid, const uint8_t *mask, const int *set,
   }
   s->fixes.push_back(f);
   return (int)s->fixes.size() - 1;
+}
+// Solid::np_per_cell; linear APIC accepts 1 or 2 (src/solid.cpp:1453-1462)
+int om_set_np_per_cell(void *h, int si, int n) {
+  Sim *s = (Sim *)h;
+  if (s->apic && s->basis == LINEAR && n != 1 && n != 2) {
+    s->err = "Number of particle per cell not supported with linear shape functions and APIC";
+    return -1;
+  }
+  s->solids[si].np_per_cell = n;
+  return 0;
 }
 // contact fix: kind 0 contact/minimize_penetration, 1 contact/hertz
 int om_add_contact(void *h, int kind, int s1, int s2, double mu) {

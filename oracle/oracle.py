@@ -68,6 +68,7 @@ def lib():
         L.om_set_threads.argtypes = [i]
         L.om_add_contact.argtypes = [p, i, i, i, d]
         L.om_set_axisymmetric.argtypes = [p, i]
+        L.om_set_np_per_cell.argtypes = [p, i, i]
         L.om_contact_force.argtypes = [p, i, dp]
         _lib = L
     return _lib
@@ -120,7 +121,9 @@ class OracleBackend:
             v = np.ascontiguousarray(sol.v, float)
             m = np.ascontiguousarray(sol.mass, float)
             vo = np.ascontiguousarray(sol.vol0, float)
-            L.om_add_solid(self.h, sol.grid, sol.mat, sol.np, _dp(x0), _dp(v), _dp(m), _dp(vo), sol.T0)
+            si = L.om_add_solid(self.h, sol.grid, sol.mat, sol.np, _dp(x0), _dp(v), _dp(m), _dp(vo), sol.T0)
+            if getattr(sol, "ppc", 0) and L.om_set_np_per_cell(self.h, si, int(sol.ppc)) != 0:
+                raise RuntimeError(L.om_error(self.h).decode())
         for f in s.fixes:
             self.add_fix(f)
         for c in getattr(s, "contacts", []):

@@ -31,7 +31,7 @@ def pair(oracle_mod, build, steps, **kw):
 
 def _cpu(build):
     return {W.taylor_bar: "tlmpm", W.two_disks: "ulmpm", W.dam_break: "ulmpm", W.tensile_bar_2d: "tlmpm",
-            W.spinning_disk: "ulmpm"}[build]
+            W.spinning_disk: "ulmpm", W.bouncing_balls: "tlmpm"}[build]
 
 
 def check(g, o, tol, solid=0):
@@ -243,7 +243,7 @@ def test_hyperelastic_and_linear_materials(gpu_lib, oracle_mod, kind):
     check(g, o, {"x": 1e-6, "v": 1e-3, "sigma": 1e-3})
 
 
-# ---------------------------------------------------------------- APIC (§8(f) next row 1)
+# ---------------------------------------------------------------- APIC
 @pytest.mark.parametrize("scheme", ["musl", "usl"])
 def test_taylor_bar_apic(gpu_lib, oracle_mod, scheme):
     """TLMPM with APIC transfers (compute_velocity_nodes_APIC and
@@ -294,7 +294,7 @@ def test_async_downloads_match_sync(gpu_lib):
     assert not np.array_equal(be.particles(0, "x"), ref["x"])
 
 
-# ---------------------------------------------------------------- USF (§8(f) next row 4)
+# ---------------------------------------------------------------- USF
 @pytest.mark.parametrize("basis", ["cubic-spline", "linear"])
 def test_taylor_bar_usf(gpu_lib, oracle_mod, basis):
     """USF::run (src/usf.cpp:34-95): stress from the first scatter's grid
@@ -319,7 +319,7 @@ def test_tensile_bar_usf(gpu_lib, oracle_mod):
     check(g, o, {"x": 1e-6, "v": 1e-3, "sigma": 1e-3})
 
 
-# ---------------------------------------------------------------- quadratic spline (§8(f) next row 4)
+# ---------------------------------------------------------------- quadratic spline
 def test_dam_break_quadratic(gpu_lib, oracle_mod):
     """ULMPM dam break with the quadratic B-spline (src/basis_functions.h:140-241)."""
     g, o = pair(oracle_mod, W.dam_break, [60], cellsize=0.05, method="ulmpm/gpu", basis="quadratic-spline")
@@ -333,7 +333,7 @@ def test_spinning_disk_apic_quadratic(gpu_lib, oracle_mod):
     assert abs(W.angular_momentum(g) / W.angular_momentum(o) - 1) < 1e-4
 
 
-# ---------------------------------------------------------------- AFLIP / ASFLIP / MLS (§8(f) next row 1)
+# ---------------------------------------------------------------- AFLIP / ASFLIP / MLS
 @pytest.mark.parametrize("sub", ["AFLIP", "ASFLIP", "MLS"])
 def test_dam_break_affine_submethods(gpu_lib, oracle_mod, sub):
     """ULMPM dam break with the other affine sub-methods: AFLIP and ASFLIP
@@ -349,3 +349,22 @@ def test_spinning_disk_affine_submethods(gpu_lib, oracle_mod, sub):
     g, o = pair(oracle_mod, W.spinning_disk, [1, 150], method="ulmpm/gpu", scheme="musl", sub=sub)
     check(g, o, {"x": 1e-6, "v": 1e-4, "sigma": 3e-3})
     assert abs(W.angular_momentum(g) / W.angular_momentum(o) - 1) < 1e-4
+
+
+# ---------------------------------------------------------------- APIC, linear basis (TLMPM)
+@pytest.mark.parametrize("ppc", [1, 2])
+def test_bouncing_balls_apic_linear(gpu_lib, oracle_mod, ppc):
+    """The reference's bouncing-balls example in its APIC form (TLMPM, linear
+    basis, examples/Bouncing_balls/TLMPM/APIC/bouncing_balls2.mpm): Di = 16/4
+    or 16/3 over cellsize^2 by the particles per cell (src/solid.cpp:1447-1462),
+    through the contact fix."""
+    g, o = pair(oracle_mod, W.bouncing_balls, [300], method="tlmpm/gpu", sub="APIC", basis="linear",
+                centre=0.16, ppc=ppc)
+    for s in (0, 1):
+        check(g, o, {"x": 3e-5, "v": 5e-4, "sigma": 5e-3}, solid=s)
+
+
+def test_taylor_bar_apic_linear(gpu_lib, oracle_mod):
+    g, o = pair(oracle_mod, W.taylor_bar, [1, W.taylor_bar_wall, 50], cellsize=0.8, method="tlmpm/gpu",
+                sub="APIC", basis="linear")
+    check(g, o, {"x": 1e-6, "v": 1e-4, "sigma": 1e-4, "F": 1e-6})
