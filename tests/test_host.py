@@ -57,7 +57,9 @@ def test_unsupported_inputs_raise():
     with pytest.raises(KarameloError):
         sim.method("ulmpm/gpu", "FLIP", "Bernstein-quadratic", 0.99)
     with pytest.raises(KarameloError):
-        sim.method("tlmpm/gpu", "APIC", "linear")
+        sim.method("ulmpm/gpu", "APIC", "linear")   # src/solid.cpp:1452: linear APIC is TLMPM only
+    with pytest.raises(KarameloError):
+        sim.method("tlmpm/gpu", "APIC", "Bernstein-quadratic")
     sim.dimension(2, 0, 1, 0, 1, 0.1)
     with pytest.raises(KarameloError):
         sim.material("r", "rigid", 1000)
