@@ -493,8 +493,9 @@ int build(kmpm_ctx *c) {
   CK(cudaMemcpyAsync(c->d_grid_blk0, grid_blk0.data(), sizeof(int) * grid_blk0.size(), cudaMemcpyHostToDevice, c->st));
   DALLOC(c->d_mats, c->mats.size());
   CK(cudaMemcpyAsync(c->d_mats, c->mats.data(), sizeof(MatDev) * c->mats.size(), cudaMemcpyHostToDevice, c->st));
-  DALLOC(c->nodeA, c->nnodes_pad);
-  DALLOC(c->nodeB, c->nnodes_pad);
+  // v and v_update interleaved: nodeB is the odd float4s of the same array
+  DALLOC(c->nodeA, (size_t)NODE_STRIDE * c->nnodes_pad);
+  c->nodeB = c->nodeA + 1;
   DALLOC(c->nodeX, c->nnodes_pad);
   DALLOC(c->nodeT, c->nnodes_pad);
   {
@@ -1162,7 +1163,8 @@ int kmpm_destroy(kmpm_ctx *c) {
   for (auto e : c->prof_ev) cudaEventDestroy(e);
   dfree(c->buf[0]); dfree(c->buf[1]); dfree(c->d_pp); dfree(c->d_ranges); dfree(c->d_blk_range);
   dfree(c->d_solid_mat); dfree(c->d_grids); dfree(c->d_blk_grid); dfree(c->d_grid_blk0); dfree(c->d_mats);
-  dfree(c->nodeA); dfree(c->nodeB); dfree(c->nodeX); dfree(c->nodeT); dfree(c->d_tiles);
+  c->nodeB = nullptr;  // inside nodeA's allocation
+  dfree(c->nodeA); dfree(c->nodeX); dfree(c->nodeT); dfree(c->d_tiles);
   dfree(c->d_cs); dfree(c->d_ce); dfree(c->d_ts); dfree(c->d_te); dfree(c->partial);
   dfree(c->d_fixes); dfree(c->d_fix_start); dfree(c->d_fix_count); dfree(c->d_scalars); dfree(c->d_dtcfl);
   dfree(c->d_dump);
@@ -1580,7 +1582,7 @@ static const char SNAP_MAGIC[8] = {'K', 'M', 'P', 'M', 'S', 'N', 'P', '1'};
 
 static unsigned long long snap_bytes(kmpm_ctx *c, const std::vector<int> &fl) {
   return sizeof(SnapHeader) + sizeof(int) * fl.size() + sizeof(StepScalars) * c->nscalars +
-         sizeof(float) * c->ps * fl.size() + 3 * sizeof(float4) * (unsigned long long)c->nnodes_pad +
+         sizeof(float) * c->ps * fl.size() + (NODE_STRIDE + 1) * sizeof(float4) * (unsigned long long)c->nnodes_pad +
          sizeof(float) * (unsigned long long)c->nnodes_pad;
 }
 
@@ -1621,10 +1623,11 @@ int kmpm_save_state(kmpm_ctx *c, void *out, unsigned long long bytes) {
     CK(cudaMemcpyAsync(o, cur + (size_t)f * c->ps, sizeof(float) * c->ps, cudaMemcpyDeviceToHost, c->st));
     o += sizeof(float) * c->ps;
   }
-  for (float4 *a : {c->nodeA, c->nodeB, c->nodeX}) {
-    CK(cudaMemcpyAsync(o, a, sizeof(float4) * c->nnodes_pad, cudaMemcpyDeviceToHost, c->st));
-    o += sizeof(float4) * c->nnodes_pad;
-  }
+  // v / v_update (interleaved) and x of the nodes
+  CK(cudaMemcpyAsync(o, c->nodeA, sizeof(float4) * NODE_STRIDE * c->nnodes_pad, cudaMemcpyDeviceToHost, c->st));
+  o += sizeof(float4) * NODE_STRIDE * c->nnodes_pad;
+  CK(cudaMemcpyAsync(o, c->nodeX, sizeof(float4) * c->nnodes_pad, cudaMemcpyDeviceToHost, c->st));
+  o += sizeof(float4) * c->nnodes_pad;
   CK(cudaMemcpyAsync(o, c->nodeT, sizeof(float) * c->nnodes_pad, cudaMemcpyDeviceToHost, c->st));
   CK(cudaStreamSynchronize(c->st));
   return KMPM_OK;
@@ -1656,10 +1659,10 @@ int kmpm_load_state(kmpm_ctx *c, const void *in, unsigned long long bytes) {
     CK(cudaMemcpyAsync(cur + (size_t)f * c->ps, o, sizeof(float) * c->ps, cudaMemcpyHostToDevice, c->st));
     o += sizeof(float) * c->ps;
   }
-  for (float4 *a : {c->nodeA, c->nodeB, c->nodeX}) {
-    CK(cudaMemcpyAsync(a, o, sizeof(float4) * c->nnodes_pad, cudaMemcpyHostToDevice, c->st));
-    o += sizeof(float4) * c->nnodes_pad;
-  }
+  CK(cudaMemcpyAsync(c->nodeA, o, sizeof(float4) * NODE_STRIDE * c->nnodes_pad, cudaMemcpyHostToDevice, c->st));
+  o += sizeof(float4) * NODE_STRIDE * c->nnodes_pad;
+  CK(cudaMemcpyAsync(c->nodeX, o, sizeof(float4) * c->nnodes_pad, cudaMemcpyHostToDevice, c->st));
+  o += sizeof(float4) * c->nnodes_pad;
   CK(cudaMemcpyAsync(c->nodeT, o, sizeof(float) * c->nnodes_pad, cudaMemcpyHostToDevice, c->st));
   CK(cudaStreamSynchronize(c->st));
   // the slot maps of the host caches follow the restored order; maxtime
@@ -1680,10 +1683,11 @@ int kmpm_download_grid(kmpm_ctx *c, int grid, int field, double *out) {
   const int nn = g.n[0] * g.n[1] * g.n[2];
   std::vector<float4> A(nn), B(nn);
   std::vector<float> Tn(nn);
-  if (field == KMPM_G_MASS || field == KMPM_G_V)
-    CK(cudaMemcpyAsync(A.data(), c->nodeA + g.node_off, sizeof(float4) * nn, cudaMemcpyDeviceToHost, c->st));
-  else if (field == KMPM_G_V_UPDATE)
-    CK(cudaMemcpyAsync(A.data(), c->nodeB + g.node_off, sizeof(float4) * nn, cudaMemcpyDeviceToHost, c->st));
+  if (field == KMPM_G_MASS || field == KMPM_G_V || field == KMPM_G_V_UPDATE) {
+    const float4 *src = (field == KMPM_G_V_UPDATE ? c->nodeB : c->nodeA) + (size_t)NODE_STRIDE * g.node_off;
+    CK(cudaMemcpy2DAsync(A.data(), sizeof(float4), src, NODE_STRIDE * sizeof(float4), sizeof(float4), nn,
+                         cudaMemcpyDeviceToHost, c->st));
+  }
   else if (field == KMPM_G_X)
     CK(cudaMemcpyAsync(A.data(), c->nodeX + g.node_off, sizeof(float4) * nn, cudaMemcpyDeviceToHost, c->st));
   else if (field == KMPM_G_T)

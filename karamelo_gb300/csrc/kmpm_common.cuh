@@ -7,7 +7,8 @@
 //              position, and padded to a multiple of 256 so that every
 //              256-thread block of a particle kernel belongs to one solid;
 //   nodes:     float4 A = (v, mass) and float4 B = (v_update, T_update) per
-//              node, grids concatenated and padded to multiples of 256;
+//              node, interleaved (A B A B ..., 32 bytes per node), grids
+//              concatenated and padded to multiples of 256;
 //   tiles:     a grid's cells are grouped in tiles of T^dim cells; the
 //              scatter kernel writes each tile's footprint (the nodes its
 //              particles touch) to its own slice of a partial buffer, and the
@@ -96,6 +97,15 @@ template <> struct MatP<double> {
   __device__ static const double *str(const MatDev &m) { return m.str_p; }
   __device__ static const double *dam(const MatDev &m) { return m.dam_p; }
 };
+
+// Node vectors: v (A) and v_update (B) of node i interleaved at float4 2i and
+// 2i + 1, 32 bytes per node, so that one 256-bit load reads both.
+constexpr int NODE_STRIDE = 2;
+__device__ __forceinline__ void ld_node_pair(const float4 *p, float4 &A, float4 &B) {
+  asm("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+      : "=f"(A.x), "=f"(A.y), "=f"(A.z), "=f"(A.w), "=f"(B.x), "=f"(B.y), "=f"(B.z), "=f"(B.w)
+      : "l"(p));
+}
 
 // Per-solid time-step scalars kept on the device so a captured step replays.
 struct StepScalars {
@@ -432,9 +442,14 @@ __device__ inline float min_abs_eig_real(const float *H) {
     float arg = r > 0.f ? (-q / 2.f) / (r * r * r) : 0.f;
     arg = fminf(1.f, fmaxf(-1.f, arg));
     float phi = acosf(arg);
-    float e0 = 1.f + sh + 2.f * r * cosf(phi / 3.f);
-    float e1 = 1.f + sh + 2.f * r * cosf((phi + 2.f * 3.14159265358979f) / 3.f);
-    float e2 = 1.f + sh + 2.f * r * cosf((phi + 4.f * 3.14159265358979f) / 3.f);
+    // cos(phi/3 + 2 pi k/3) for k = 0, 1, 2 from one sine and cosine:
+    // cos(a + 2pi/3) = -c/2 - (sqrt 3/2) s, cos(a + 4pi/3) = -c/2 + (sqrt 3/2) s
+    float sn, cs;
+    sincosf(phi / 3.f, &sn, &cs);
+    const float h3 = 0.866025403784439f * sn;
+    float e0 = 1.f + sh + 2.f * r * cs;
+    float e1 = 1.f + sh + 2.f * r * (-0.5f * cs - h3);
+    float e2 = 1.f + sh + 2.f * r * (-0.5f * cs + h3);
     m = fminf(fabsf(e0), fminf(fabsf(e1), fabsf(e2)));
   } else {
     float sd = sqrtf(disc);

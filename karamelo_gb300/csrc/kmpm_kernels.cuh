@@ -71,7 +71,7 @@ struct GridArgs {
   const float *partial;
   size_t pstride_tile;
   const int *tile_start, *tile_end;
-  float4 *nodeA, *nodeB, *nodeX;
+  float4 *nodeA, *nodeB, *nodeX;  // nodeA / nodeB: one array, stride NODE_STRIDE
   float *nodeT;
   const FixDev *fixes;
   const int *fix_start, *fix_count;
@@ -88,7 +88,7 @@ struct PartArgs {
   const int *solid_mat;      // solid id -> material id (ULMPM per-particle lookup)
   const GridDev *grids;
   const MatDev *mats;
-  const float4 *nodeA, *nodeB;
+  const float4 *nodeA, *nodeB;  // one array, stride NODE_STRIDE
   const float *nodeT;
   StepScalars *scalars;
   ErrState *err;

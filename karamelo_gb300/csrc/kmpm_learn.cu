@@ -93,7 +93,7 @@ __global__ void __launch_bounds__(MODE == MODE_SUR ? 512 : 256, MODE == MODE_SUR
     for (int k = 0; k < SY; k++) cy[k] = min(max(ax.ax[1].i0 + k, 0), g.n[1] - 1);
 #pragma unroll
     for (int k = 0; k < SZ; k++) cz[k] = min(max(ax.ax[2].i0 + k, 0), g.n[2] - 1);
-    const float4 *__restrict__ NV = (a.use_vu ? a.nodeB : a.nodeA) + g.node_off;
+    const float4 *__restrict__ NV = (a.use_vu ? a.nodeB : a.nodeA) + NODE_STRIDE * g.node_off;
     // the gather of k_g2p2 (sum factorisation over the z slots)
 #pragma unroll
     for (int i = 0; i < S; i++) {
@@ -106,7 +106,7 @@ __global__ void __launch_bounds__(MODE == MODE_SUR ? 512 : 256, MODE == MODE_SUR
 #pragma unroll
         for (int k = 0; k < SZ; k++) {
           const float sz = ax.ax[2].s[k], dsz = ax.ax[2].ds[k];
-          const float4 V = __ldg(NV + row + cz[k]);
+          const float4 V = __ldg(NV + NODE_STRIDE * (row + cz[k]));
           const float vn[3] = {V.x, V.y, V.z};
 #pragma unroll
           for (int r = 0; r < DIM; r++) {

@@ -419,9 +419,9 @@ __global__ void __launch_bounds__(256) k_grid(GridArgs a) {
   if (GMODE == GM_MASS) {
     R s[1];
     gather_partials<DIM, BASIS, 1, R>(a, g, li, ix, s);
-    float4 A = a.nodeA[node];
+    float4 A = a.nodeA[NODE_STRIDE * node];
     A.w = (float)s[0];
-    a.nodeA[node] = A;
+    a.nodeA[NODE_STRIDE * node] = A;
     return;
   }
   if (GMODE == GM_UPDATE) {
@@ -430,7 +430,7 @@ __global__ void __launch_bounds__(256) k_grid(GridArgs a) {
     R s[Q];
     gather_partials<DIM, BASIS, Q, R>(a, g, li, ix, s);
     const int o = TL ? 0 : 1;
-    float4 A = a.nodeA[node];
+    float4 A = a.nodeA[NODE_STRIDE * node];
     const R m = TL ? (R)A.w : s[0];
     R v[3], f[3], mb[3] = {0, 0, 0}, vu[3];
     // Solid::compute_velocity_nodes: v = p/m only where m > 0 (src/solid.cpp:357)
@@ -462,13 +462,13 @@ __global__ void __launch_bounds__(256) k_grid(GridArgs a) {
       for (int d = 0; d < 3; d++)
         if (fx.set[d]) { vu[d] = (R)fix_value(fx, d, time); v[d] = (R)fix_value(fx, d, time - sc.dt); }
     }
-    a.nodeA[node] = make_float4((float)v[0], (float)v[1], (float)v[2], (float)m);
-    a.nodeB[node] = make_float4((float)vu[0], (float)vu[1], (float)vu[2], (float)Tu);
+    a.nodeA[NODE_STRIDE * node] = make_float4((float)v[0], (float)v[1], (float)v[2], (float)m);
+    a.nodeB[NODE_STRIDE * node] = make_float4((float)vu[0], (float)vu[1], (float)vu[2], (float)Tu);
     if (THERMAL) a.nodeT[node] = (float)T;
     return;
   }
   // GM_VEL: MUSL velocities_to_grid (+ BCs on v) and TL grid positions
-  float4 A = a.nodeA[node];
+  float4 A = a.nodeA[NODE_STRIDE * node];
   R v[3] = {A.x, A.y, A.z};
   if (a.remap) {
     constexpr int Q = THERMAL ? 4 : 3;
@@ -486,7 +486,7 @@ __global__ void __launch_bounds__(256) k_grid(GridArgs a) {
       for (int d = 0; d < 3; d++)
         if (fx.set[d]) v[d] = (R)fix_value(fx, d, time);
     }
-    a.nodeA[node] = make_float4((float)v[0], (float)v[1], (float)v[2], A.w);
+    a.nodeA[NODE_STRIDE * node] = make_float4((float)v[0], (float)v[1], (float)v[2], A.w);
   }
   if (TL) {  // Grid::update_grid_positions (src/grid.cpp:468-474): x += dt v
     float4 X = a.nodeX[node];
@@ -558,8 +558,7 @@ __global__ void __launch_bounds__(256, MINB) k_g2p1(PartArgs a) {
   for (int k = 0; k < SY; k++) cy[k] = min(max(ax.ax[1].i0 + k, 0), g.n[1] - 1);
 #pragma unroll
   for (int k = 0; k < SZ; k++) cz[k] = min(max(ax.ax[2].i0 + k, 0), g.n[2] - 1);
-  const float4 *__restrict__ NA = a.nodeA + g.node_off;
-  const float4 *__restrict__ NB = a.nodeB + g.node_off;
+  const float4 *__restrict__ NA = a.nodeA + NODE_STRIDE * g.node_off;  // v, v_update interleaved
   float vu[3] = {0, 0, 0}, dv[3] = {0, 0, 0}, Tp = 0.f;
 #pragma unroll
   for (int i = 0; i < S; i++) {
@@ -570,8 +569,8 @@ __global__ void __launch_bounds__(256, MINB) k_g2p1(PartArgs a) {
 #pragma unroll
       for (int k = 0; k < SZ; k++) {
         const float w = sxy * ax.ax[2].s[k];
-        const float4 A = __ldg(NA + row + cz[k]);
-        const float4 B = __ldg(NB + row + cz[k]);
+        float4 A, B;
+        ld_node_pair(NA + NODE_STRIDE * (row + cz[k]), A, B);
         vu[0] += w * B.x; vu[1] += w * B.y; vu[2] += w * B.z;
         dv[0] += w * (B.x - A.x); dv[1] += w * (B.y - A.y); dv[2] += w * (B.z - A.z);
         if (THERMAL) Tp += w * B.w;
@@ -663,7 +662,7 @@ __global__ void __launch_bounds__(256, MINB) k_g2p2(PartArgs a) {
     for (int k = 0; k < SY; k++) cy[k] = min(max(ax.ax[1].i0 + k, 0), g.n[1] - 1);
 #pragma unroll
     for (int k = 0; k < SZ; k++) cz[k] = min(max(ax.ax[2].i0 + k, 0), g.n[2] - 1);
-    const float4 *__restrict__ NV = (a.use_vu ? a.nodeB : a.nodeA) + g.node_off;
+    const float4 *__restrict__ NV = (a.use_vu ? a.nodeB : a.nodeA) + NODE_STRIDE * g.node_off;
     // sum factorisation over the z slots: for every (i, j), A = sum_k s_z V
     // and B = sum_k ds_z V, then grad v += (ds_x s_y A, s_x ds_y A, s_x s_y B)
     // (dropped pairs add 0: see Axis::eval)
@@ -678,7 +677,7 @@ __global__ void __launch_bounds__(256, MINB) k_g2p2(PartArgs a) {
 #pragma unroll
         for (int k = 0; k < SZ; k++) {
           const float sz = ax.ax[2].s[k], dsz = ax.ax[2].ds[k];
-          const float4 V = __ldg(NV + row + cz[k]);
+          const float4 V = __ldg(NV + NODE_STRIDE * (row + cz[k]));
           const float vn[3] = {V.x, V.y, V.z};
 #pragma unroll
           for (int r = 0; r < DIM; r++) {
