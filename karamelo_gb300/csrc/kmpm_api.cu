@@ -132,6 +132,7 @@ struct kmpm_ctx {
   LearnKernels LK{};
   // autotuner: chosen launch-shape variant of each gather kernel, its record
   int var_g2p1 = 0, var_g2p2 = 0;
+  bool law_jc = false;  // every material is linear EOS + Johnson-Cook: the specialised stress kernels
   bool tuned = false;
   long long runs = 0;
   std::string tuning = "{}";
@@ -382,6 +383,12 @@ int build(kmpm_ctx *c) {
   const int dim = c->prm.dim, basis = c->prm.basis;
   if (c->hsolids.empty()) return fail(c, KMPM_ERR_STATE, "no solid was added");
   get_step_kernels(dim, basis, c->K);
+  // the specialised stress kernels: every material linear EOS + Johnson-Cook,
+  // no damage, no temperature law
+  c->law_jc = !c->prm.thermal && !c->mats.empty();
+  for (const auto &m : c->mats)
+    c->law_jc = c->law_jc && m.type == KMPM_MAT_EOS_STRENGTH && m.eos == 0 && m.strength == 2 && m.damage < 0 &&
+                m.temp < 0 && m.cp == 0.0;
   tile_dims(dim, basis, c->tdim);
   c->NCELL = c->tdim[0] * c->tdim[1] * c->tdim[2];
   // ---- grids
@@ -844,6 +851,14 @@ void *force_scatter_fn(const kmpm_ctx *c, int mode, bool th) {
   return ul ? (th ? K.p2g_ul_th : K.p2g_ul) : (th ? K.p2g_tl_th : K.p2g_tl);
 }
 
+// launch shape v of the FP32 mechanical stress kernel, specialised to the
+// materials where that applies
+void *g2p2_variant(const kmpm_ctx *c, int v) {
+  const bool TL = c->TL();
+  if (c->law_jc && c->K.g2p2_jc[TL][v]) return c->K.g2p2_jc[TL][v];
+  return c->K.g2p2_v[TL][v];
+}
+
 int select_scatters(kmpm_ctx *c) {
   const bool TL = c->TL(), th = c->prm.thermal != 0;
   const int flags = (!c->contacts.empty() && c->prm.dim >= 2 ? P2G_EXT : 0) | (c->prm.axisymmetric ? P2G_AXI : 0);
@@ -914,7 +929,7 @@ int enqueue_step(kmpm_ctx *c) {
     // forces of the new stress, the grid update and the particle update
     PartArgs ps = pa;
     ps.use_vu = 0;
-    LAUNCH((th || prec) ? c->K.g2p2[TL][th][prec] : c->K.g2p2_v[TL][c->var_g2p2], c->nblk_p, 256, 0, ps);
+    LAUNCH((th || prec) ? c->K.g2p2[TL][th][prec] : g2p2_variant(c, c->var_g2p2), c->nblk_p, 256, 0, ps);
     MARK("g2p_stress");
     LAUNCH(c->sc_usf, c->ntiles_launch, 256, c->smem_usf, p);
     MARK("p2g_forces");
@@ -956,7 +971,7 @@ int enqueue_step(kmpm_ctx *c) {
   }
   // compute_rate_deformation_gradient + update_deformation_gradient + update_stress
   if (c->learn_mode == MODE_PLAIN) {
-    LAUNCH((th || prec) ? c->K.g2p2[TL][th][prec] : c->K.g2p2_v[TL][c->var_g2p2], c->nblk_p, 256, 0, pa);
+    LAUNCH((th || prec) ? c->K.g2p2[TL][th][prec] : g2p2_variant(c, c->var_g2p2), c->nblk_p, 256, 0, pa);
   } else {
     LearnArgs la{};
     la.blob = c->d_blob;
@@ -1067,7 +1082,7 @@ int autotune(kmpm_ctx *c) {
   for (int rep = 0; rep < 4; rep++)
     for (int k = 0; k < 2; k++)
       for (int v = 0; v < G2P_NVAR; v++) {
-        void *fn = k == 0 ? c->K.g2p1_v[TL][v] : c->K.g2p2_v[TL][v];
+        void *fn = k == 0 ? c->K.g2p1_v[TL][v] : g2p2_variant(c, v);
         CK(cudaEventRecord(e0, c->st));
         int r = launch(c, fn, dim3(c->nblk_p), dim3(256), 0, &pa);
         if (r != KMPM_OK) return r;

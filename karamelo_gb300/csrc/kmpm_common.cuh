@@ -484,15 +484,22 @@ struct ConstitutiveIn {
   float J, Jm1, rho, cellsize;
 };
 
+// Constitutive laws the stress kernel is compiled for: LAW_ANY dispatches on
+// the material at run time; LAW_EOS_LINEAR_JC fixes linear EOS +
+// Johnson-Cook strength without damage or temperature (the copper bar), so
+// that the other laws' code leaves the kernel.
+enum : int { LAW_ANY = 0, LAW_EOS_LINEAR_JC = 1 };
+
 // EOS::compute_pressure (src/eos_linear.cpp:71-74, src/eos_shock.cpp:99-133,
 // src/eos_fluid.cpp:68-73); T is the particle temperature or 0.
-template <typename R>
+template <typename R, int LAW = LAW_ANY>
 __device__ inline R eos_pressure(const MatDev &m, R J, R Jm1, R rho, R damage, R trD, R cellsize, R T) {
   const auto *ep = MatP<R>::eos(m);
-  if (m.eos == 0) return -R(ep[1]) * Jm1 * (R(1) - damage);
+  const int eos = LAW == LAW_EOS_LINEAR_JC ? 0 : m.eos;
+  if (eos == 0) return -R(ep[1]) * Jm1 * (R(1) - damage);
   // rho/rho0 = 1/J; the compressions below are written in J - 1 so that FP32
   // keeps them accurate when J is close to 1 (no 1/J - 1 cancellation)
-  if (m.eos == 2) {  // K ((rho/rho0)^gamma - 1) = K expm1(-gamma log1p(J-1))
+  if (eos == 2) {  // K ((rho/rho0)^gamma - 1) = K expm1(-gamma log1p(J-1))
     return R(ep[1]) * expm1(-R(ep[2]) * log1p(Jm1));
   }
   R rho0 = ep[0], c0 = ep[2], S = ep[3], Gamma = ep[4], cv = ep[5], Tr = ep[6];
@@ -530,13 +537,14 @@ __device__ __forceinline__ R jc_flow_stress(const R *p, R epsp, R epsdot, R T) {
   return ys;
 }
 
-template <typename R>
+template <typename R, int LAW = LAW_ANY>
 __device__ inline Sym<R> strength_update(const MatDev &m, R dt, const Sym<R> &sig, const Sym<R> &D, R &dep, R epsp,
                                          R epsdot, R damage, R T) {
   Sym<R> out;
   dep = R(0);
   const auto *p = MatP<R>::str(m);
-  if (m.strength == 0) {  // linear: dev(sigma) + dt 2G(1-D) dev(D)
+  const int strength = LAW == LAW_EOS_LINEAR_JC ? 2 : m.strength;
+  if (strength == 0) {  // linear: dev(sigma) + dt 2G(1-D) dev(D)
     Sym<R> s = sig, d = D;
     s.dev(); d.dev();
     R f = dt * R(2) * R(p[0]) * (R(1) - damage);
@@ -544,14 +552,14 @@ __device__ inline Sym<R> strength_update(const MatDev &m, R dt, const Sym<R> &si
     for (int k = 0; k < 6; k++) out.a[k] = s.a[k] + f * d.a[k];
     return out;
   }
-  if (m.strength == 4) {  // fluid: 2 mu dev(D)
+  if (strength == 4) {  // fluid: 2 mu dev(D)
     Sym<R> d = D;
     d.dev();
 #pragma unroll
     for (int k = 0; k < 6; k++) out.a[k] = R(2) * R(p[0]) * d.a[k];
     return out;
   }
-  if (m.strength == 1) {  // perfect plasticity
+  if (strength == 1) {  // perfect plasticity
     R Gd = R(p[0]) * (R(1) - damage), syD = R(p[1]) * (R(1) - damage);
     Sym<R> s = sig, d = D;
     s.dev(); d.dev();
@@ -572,7 +580,7 @@ __device__ inline Sym<R> strength_update(const MatDev &m, R dt, const Sym<R> &si
     return out;
   }
   R G = p[0], ys;
-  if (m.strength == 2) {
+  if (strength == 2) {
     ys = jc_flow_stress<R>(p, epsp, epsdot, T);
   } else {
     R A = p[1], B = p[2], C = p[3], n = p[4];

@@ -132,6 +132,9 @@ struct StepKernels {
   // launch-shape candidates [TL][variant] of the gathers (FP32, no thermal):
   // __launch_bounds__(256, G2P1_MINB[v] / G2P2_MINB[v]); variant 0 is the default
   void *g2p1_v[2][3], *g2p2_v[2][3];
+  // the same stress-kernel shapes compiled for linear EOS + Johnson-Cook only
+  // (LAW_EOS_LINEAR_JC; 3-D, nullptr elsewhere)
+  void *g2p2_jc[2][3];
 };
 constexpr int G2P_NVAR = 3;
 constexpr int G2P1_MINB[G2P_NVAR] = {4, 3, 6};

@@ -608,7 +608,7 @@ __global__ void __launch_bounds__(256, MINB) k_g2p1(PartArgs a) {
 
 // rate of deformation + deformation gradient + stress + wave speed
 // (src/solid.cpp:798-936, 1155-1438)
-template <int DIM, int BASIS, bool TL, bool THERMAL, int PREC, int MINB = 3>
+template <int DIM, int BASIS, bool TL, bool THERMAL, int PREC, int MINB = 3, int LAW = LAW_ANY>
 __global__ void __launch_bounds__(256, MINB) k_g2p2(PartArgs a) {
   __shared__ float red_c[256], red_h[256];
   if (run_finished(a.scalars)) return;
@@ -759,7 +759,7 @@ __global__ void __launch_bounds__(256, MINB) k_g2p2(PartArgs a) {
     Sym<float> D;
 #pragma unroll
     for (int k = 0; k < 6; k++) D.a[k] = 0.f;
-    const bool nh = m.type == 1;
+    const bool nh = LAW == LAW_ANY && m.type == 1;
     if (!nh) {
       if (TL) {
         if (!polar_rotation(F, R)) {
@@ -791,7 +791,7 @@ __global__ void __launch_bounds__(256, MINB) k_g2p2(PartArgs a) {
     for (int k = 0; k < 6; k++) sig.a[k] = P[(PF_SIG + k) * ps + p];
     float PK1[9];
     bool have_pk1 = false;
-    if (m.type == 0) {  // LINEAR
+    if (LAW == LAW_ANY && m.type == 0) {  // LINEAR
       const float G2 = 2.f * m.f_G, lam = m.f_lambda;
       const float trinc = dt * D.tr();
 #pragma unroll
@@ -828,7 +828,7 @@ __global__ void __launch_bounds__(256, MINB) k_g2p2(PartArgs a) {
         P[(PF_STRAIN + 5) * ps + p] = 0.5f * FtF[5];
       }
     } else {  // EOS + strength (+ damage + temperature)
-      const bool hasT = m.f_cp != 0.f;
+      const bool hasT = LAW == LAW_ANY && m.f_cp != 0.f;
       float T = hasT ? a.T_ref + P[PF_T * ps + p] : 0.f;  // PF_T holds T - T_ref
       float epsp = P[PF_EPSP * ps + p], epsdot = P[PF_EPSDOT * ps + p];
       float dinit = m.damage >= 0 ? P[PF_DMGI * ps + p] : 0.f;
@@ -848,16 +848,16 @@ __global__ void __launch_bounds__(256, MINB) k_g2p2(PartArgs a) {
 #pragma unroll
         for (int k = 0; k < 6; k++) sdev.a[k] = (float)sdd.a[k];
       } else {
-        pH = eos_pressure<float>(m, J, Jm1, rho, dmg, D.tr(), g.cellsize, T);
+        pH = eos_pressure<float, LAW>(m, J, Jm1, rho, dmg, D.tr(), g.cellsize, T);
         if (hasT) pH += m.f_temp_p[3] * (m.f_temp_p[4] - T);
-        sdev = strength_update<float>(m, dt, sig, D, dep, epsp, epsdot, dmg, T);
+        sdev = strength_update<float, LAW>(m, dt, sig, D, dep, epsp, epsdot, dmg, T);
       }
       epsp += dep;
       const float tav = 1000.f * g.cellsize / m.f_signal_velocity;
       epsdot -= epsdot * dt / tav;
       epsdot += dep / tav;
       epsdot = fmaxf(0.f, epsdot);
-      if (m.damage >= 0) {
+      if (LAW == LAW_ANY && m.damage >= 0) {
         float Tdm = a.thermal ? a.T_ref + P[PF_T * ps + p] : 0.f;
         damage_update<float>(m, dinit, dmg, pH, sdev, epsdot, dep, Tdm);
         P[PF_DMGI * ps + p] = dinit;
@@ -1026,6 +1026,17 @@ void fill_step_kernels(StepKernels &k) {
   KMPM_VAR_SET(false)
   KMPM_VAR_SET(true)
 #undef KMPM_VAR_SET
+  for (int t = 0; t < 2; t++)
+    for (int v = 0; v < G2P_NVAR; v++) k.g2p2_jc[t][v] = nullptr;
+  if constexpr (DIM == 3) {  // the benchmark's material: linear EOS + Johnson-Cook
+#define KMPM_JC_SET(tl)                                                                               \
+  k.g2p2_jc[tl][0] = (void *)k_g2p2<DIM, BASIS, tl, false, 0, G2P2_MINB[0], LAW_EOS_LINEAR_JC>;        \
+  k.g2p2_jc[tl][1] = (void *)k_g2p2<DIM, BASIS, tl, false, 0, G2P2_MINB[1], LAW_EOS_LINEAR_JC>;        \
+  k.g2p2_jc[tl][2] = (void *)k_g2p2<DIM, BASIS, tl, false, 0, G2P2_MINB[2], LAW_EOS_LINEAR_JC>;
+    KMPM_JC_SET(false)
+    KMPM_JC_SET(true)
+#undef KMPM_JC_SET
+  }
 }
 
 }  // namespace kmpm
