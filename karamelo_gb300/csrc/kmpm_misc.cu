@@ -438,7 +438,7 @@ int p2g_smem_bytes(int dim, int basis, int mode, bool thermal) {
   const int Q = p2g_nq(mode, thermal), QINP = (p2g_nin(mode, thermal) + 3) & ~3;
   const int slab = (Q * NF + 3) & ~3;
   // affine modes also stage the per-slot offsets (x_node - x_p) / h
-  return 4 * 8 * (slab + 32 * 4 + 32 * QINP + 32 * dim * S * (p2g_apic(mode) ? 3 : 2));
+  return 4 * 8 * (slab + 32 * QINP + 32 * dim * S * (p2g_apic(mode) ? 3 : 2));
 }
 
 }  // namespace kmpm

@@ -113,8 +113,14 @@ __device__ __forceinline__ void p2g_particle(float (&accr)[NSL][Q], const float 
   }
 }
 
+// Resident blocks per SM the register budget is set for: three for the plain
+// 3-D mechanical scatters (their shared memory leaves room for three), one
+// (no bound) for the others, whose larger payloads would spill.
+template <int DIM, int MODE, bool THERMAL>
+constexpr int p2g_min_blocks() { return (DIM == 3 && !THERMAL && p2g_kind(MODE) == MODE && !p2g_apic(MODE)) ? 3 : 1; }
+
 template <int DIM, int BASIS, int MODE, bool THERMAL>
-__global__ void __launch_bounds__(256) k_p2g(P2GArgs a) {
+__global__ void __launch_bounds__(256, (p2g_min_blocks<DIM, MODE, THERMAL>())) k_p2g(P2GArgs a) {
   using TS = TileShape<DIM, BASIS>;
   constexpr int S = TS::S, SC = TS::SC, LO = Stencil<BASIS>::LO;
   constexpr int TX = TS::TX, TY = TS::TY, TZ = TS::TZ, L = TS::L;
@@ -131,13 +137,12 @@ __global__ void __launch_bounds__(256) k_p2g(P2GArgs a) {
   constexpr int NG = 32 / GS;
   constexpr int SLAB = (Q * NF + 3) & ~3;
   constexpr bool AP = p2g_apic(MODE);
-  constexpr int STAGE = 32 * 4 + 32 * QINP + 32 * DIM * S * (AP ? 3 : 2);
+  constexpr int STAGE = 32 * QINP + 32 * DIM * S * (AP ? 3 : 2);
 
   extern __shared__ __align__(16) float smem[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   float *slab = smem + warp * SLAB;                                // Q * NF
-  float4 *spos = reinterpret_cast<float4 *>(smem + TS::NWARP * SLAB + warp * STAGE);  // 32
-  float *spay = reinterpret_cast<float *>(spos + 32);                                 // 32 * QINP
+  float *spay = smem + TS::NWARP * SLAB + warp * STAGE;                                // 32 * QINP
   float2 *sbas = reinterpret_cast<float2 *>(spay + 32 * QINP);                        // 32 * DIM * S
   float *sofs = reinterpret_cast<float *>(sbas + 32 * DIM * S);  // affine modes: 32 * DIM * S offsets
 
@@ -216,8 +221,10 @@ __global__ void __launch_bounds__(256) k_p2g(P2GArgs a) {
       const int cnt = min(32, ccount - c0);
       if (c0 > 0 && lane < cnt) KMPM_LOAD_PARTICLE(cstart + c0 + lane);  // cells with more than 32 particles
       // ---- stage (lane = particle)
+      // this cell's positions stay in registers (the prefetch below reuses
+      // ppos); the basis loop takes particle j's from lane j by shuffles
+      const float cp0 = ppos[0], cp1 = DIM >= 2 ? ppos[DIM >= 2 ? 1 : 0] : 0.f, cp2 = DIM == 3 ? ppos[DIM == 3 ? 2 : 0] : 0.f;
       if (lane < cnt) {
-        spos[lane] = make_float4(ppos[0], DIM >= 2 ? ppos[DIM >= 2 ? 1 : 0] : 0.f, DIM == 3 ? ppos[DIM == 3 ? 2 : 0] : 0.f, 0.f);
 #pragma unroll
         for (int v = 0; v < QINP / 4; v++)
           reinterpret_cast<float4 *>(spay + lane * QINP)[v] =
@@ -236,12 +243,15 @@ __global__ void __launch_bounds__(256) k_p2g(P2GArgs a) {
         if (DIM == 3) interior = interior && cubic_interior(i0[2], gn2, gng2);
       }
       if (interior) {
-        for (int it = lane; it < cnt * DIM; it += 32) {
-          const int j = it / DIM, d = it % DIM;
+        for (int base = 0; base < cnt * DIM; base += 32) {
+          const int it = base + lane;
+          const int j = it < cnt * DIM ? it / DIM : 0, d = it % DIM;
+          const float px = __shfl_sync(0xffffffffu, cp0, j), py = __shfl_sync(0xffffffffu, cp1, j),
+                      pz = __shfl_sync(0xffffffffu, cp2, j);
+          if (it >= cnt * DIM) continue;
           const int i0d = d == 0 ? i0[0] : (d == 1 ? i0[1] : i0[2]);
           const float lod = d == 0 ? glo0 : (d == 1 ? glo1 : glo2);
-          const float4 pj = spos[j];
-          const float t = ((d == 0 ? pj.x : (d == 1 ? pj.y : pj.z)) - lod) * ih;
+          const float t = ((d == 0 ? px : (d == 1 ? py : pz)) - lod) * ih;
           float sv[4], dsv[4];
           const float f = t - (float)(i0d + 1);
           cubic_weights(f, ih, sv, dsv);
@@ -259,8 +269,12 @@ __global__ void __launch_bounds__(256) k_p2g(P2GArgs a) {
           for (int kk = 0; kk < 4; kk++) sbas[it * S + kk] = make_float2(sv[kk], dsv[kk]);
         }
       } else
-      for (int it = lane; it < cnt * DIM * S; it += 32) {
-        const int j = it / (DIM * S), d = (it / S) % DIM, kk = it % S;
+      for (int base = 0; base < cnt * DIM * S; base += 32) {
+        const int it = base + lane;
+        const int j = it < cnt * DIM * S ? it / (DIM * S) : 0, d = (it / S) % DIM, kk = it % S;
+        const float px = __shfl_sync(0xffffffffu, cp0, j), py = __shfl_sync(0xffffffffu, cp1, j),
+                    pz = __shfl_sync(0xffffffffu, cp2, j);
+        if (it >= cnt * DIM * S) continue;
         // per-axis constants selected without indexing local arrays
         const int i = (d == 0 ? i0[0] : (d == 1 ? i0[1] : i0[2])) + kk;
         const int nd = d == 0 ? gn0 : (d == 1 ? gn1 : gn2);
@@ -269,8 +283,7 @@ __global__ void __launch_bounds__(256) k_p2g(P2GArgs a) {
         float sv = 0.f, dsv = 0.f, ov = 0.f;
         if (i >= 0 && i < nd) {
           const float xn = lod + (float)i * h;
-          const float4 pj = spos[j];
-          const float r = ((d == 0 ? pj.x : (d == 1 ? pj.y : pj.z)) - xn) * ih;
+          const float r = ((d == 0 ? px : (d == 1 ? py : pz)) - xn) * ih;
           basis<BASIS>(r, node_type<BASIS>(i, ngd), ih, sv, dsv);
           dsv = sv != 0.f ? dsv : 0.f;  // as Axis::eval
           ov = -r;
@@ -278,6 +291,7 @@ __global__ void __launch_bounds__(256) k_p2g(P2GArgs a) {
           // src/solid.cpp:524-574): w Di (x_node - x_p) in place of grad w
           if (AP && a.mls) dsv = sv * (ov * h) * a.mls_di;
         }
+        (void)px; (void)py; (void)pz;
         sbas[it] = make_float2(sv, dsv);
         if (AP) sofs[it] = ov;
       }
