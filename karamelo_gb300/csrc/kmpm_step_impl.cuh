@@ -113,11 +113,15 @@ __device__ __forceinline__ void p2g_particle(float (&accr)[NSL][Q], const float 
   }
 }
 
-// Resident blocks per SM the register budget is set for: three for the plain
-// 3-D mechanical scatters (their shared memory leaves room for three), one
-// (no bound) for the others, whose larger payloads would spill.
+// Resident blocks per SM the register budget is set for: for the plain 3-D
+// mechanical scatters as many as their shared memory allows (four for the
+// mass and velocity sums, three for the force scatters), one (no bound) for
+// the others, whose larger payloads would spill.
 template <int DIM, int MODE, bool THERMAL>
-constexpr int p2g_min_blocks() { return (DIM == 3 && !THERMAL && p2g_kind(MODE) == MODE && !p2g_apic(MODE)) ? 3 : 1; }
+constexpr int p2g_min_blocks() {
+  return (DIM == 3 && !THERMAL && p2g_kind(MODE) == MODE && !p2g_apic(MODE))
+             ? ((MODE == P2G_VEL || MODE == P2G_MASS) ? 4 : 3) : 1;
+}
 
 template <int DIM, int BASIS, int MODE, bool THERMAL>
 __global__ void __launch_bounds__(256, (p2g_min_blocks<DIM, MODE, THERMAL>())) k_p2g(P2GArgs a) {
