@@ -119,7 +119,7 @@ __device__ __forceinline__ void p2g_particle(float (&accr)[NSL][Q], const float 
 // the others, whose larger payloads would spill.
 template <int DIM, int MODE, bool THERMAL>
 constexpr int p2g_min_blocks() {
-  return (DIM == 3 && !THERMAL && p2g_kind(MODE) == MODE && !p2g_apic(MODE))
+  return (DIM >= 2 && !THERMAL && p2g_kind(MODE) == MODE && !p2g_apic(MODE))
              ? ((MODE == P2G_VEL || MODE == P2G_MASS) ? 4 : 3) : 1;
 }
 
