@@ -133,6 +133,9 @@ struct kmpm_ctx {
   // autotuner: chosen launch-shape variant of each gather kernel, its record
   int var_g2p1 = 0, var_g2p2 = 0;
   bool law_jc = false;  // every material is linear EOS + Johnson-Cook: the specialised stress kernels
+  // plastic strain or damage was uploaded (a restart): those rows may be
+  // non-zero whatever the laws, and are permuted with the others
+  bool restored_state = false;
   bool tuned = false;
   long long runs = 0;
   std::string tuning = "{}";
@@ -364,11 +367,21 @@ int mark(kmpm_ctx *c, const char *name) {
   } while (0)
 
 // particle fields that live in the device buffer for this configuration
+// (rows that stay zero for the whole run are left out: both buffers start
+// zeroed, and the kernels only ever write zeros into them)
 std::vector<int> active_fields(kmpm_ctx *c) {
   std::vector<int> f;
   auto add = [&](int base, int n) { for (int i = 0; i < n; i++) f.push_back(base + i); };
+  bool plastic = false, damage = false;
+  for (const auto &m : c->mats) {
+    plastic = plastic || (m.type == KMPM_MAT_EOS_STRENGTH && m.strength >= 1 && m.strength <= 3);
+    damage = damage || (m.type == KMPM_MAT_EOS_STRENGTH && m.damage >= 0);
+  }
   add(PF_X0, 3); add(PF_X, 3); add(PF_V, 3); add(PF_MASS, 1); add(PF_VOL0, 1); add(PF_H, 9); add(PF_SIG, 6);
-  add(PF_EPSP, 2); add(PF_DMG, 2); add(PF_PK, 9); add(PF_ORIG, 1); add(PF_SID, 1);
+  if (plastic || c->learn_mode != MODE_PLAIN || c->restored_state) add(PF_EPSP, 2);
+  if (damage || c->restored_state) add(PF_DMG, 2);
+  add(PF_PK, c->TL() ? 9 : 6);  // ULMPM scatters vol sigma (6)
+  add(PF_ORIG, 1); add(PF_SID, 1);
   bool thermal = c->prm.thermal;
   for (auto &m : c->mats) if (m.cp != 0) thermal = true;
   if (thermal) { add(PF_T, 2); add(PF_Q, 3); }
@@ -376,6 +389,16 @@ std::vector<int> active_fields(kmpm_ctx *c) {
   if (!c->TL()) add(PF_XN, 3);
   if (c->apic()) add(PF_C, 9);
   return f;
+}
+
+// the fields ULMPM's re-binning permutes (destination << 8 | source): the
+// moved displacement becomes the binned one
+void set_ul_fields(kmpm_ctx *c) {
+  c->ul_fields.clear();
+  for (int f : active_fields(c)) {
+    int src = (f >= PF_X && f < PF_X + 3) ? PF_XN + (f - PF_X) : f;
+    c->ul_fields.push_back((f << 8) | src);
+  }
 }
 
 // ---------------------------------------------------------------- build
@@ -602,11 +625,7 @@ int build(kmpm_ctx *c) {
       CK(cudaFuncSetAttribute(af[m], cudaFuncAttributeMaxDynamicSharedMemorySize, c->smem_apic[m]));
     }
   }
-  c->ul_fields.clear();
-  for (int f : active_fields(c)) {
-    int src = (f >= PF_X && f < PF_X + 3) ? PF_XN + (f - PF_X) : f;
-    c->ul_fields.push_back((f << 8) | src);
-  }
+  set_ul_fields(c);
   // ---- TLMPM: bin once by x0 (static connectivity, src/tlmpm.cpp:339) and compute the nodal mass
   if (c->TL()) {
     PartArgs pa = part_args(c);
@@ -1553,6 +1572,12 @@ int kmpm_upload_particles(kmpm_ctx *c, int solid, int field, const double *in) {
       return fail(c, KMPM_ERR_ARG, "this field cannot be uploaded");
   }
   if (field == KMPM_P_T && !c->prm.thermal) return fail(c, KMPM_ERR_STATE, "temperature needs a thermo-mechanical run");
+  if ((field == KMPM_P_EPS_P || field == KMPM_P_EPSDOT_P || field == KMPM_P_DAMAGE || field == KMPM_P_DAMAGE_INIT) &&
+      !c->restored_state) {
+    c->restored_state = true;  // keep these rows through the re-binning from now on
+    set_ul_fields(c);
+    c->graph_valid = false;
+  }
   if (field == KMPM_P_STRAIN_EL && !c->prm.track_strain)
     return fail(c, KMPM_ERR_STATE, "strain_el is tracked only with track_strain");
   const size_t need = (size_t)S.n * dump_width(field);
@@ -1652,13 +1677,25 @@ int kmpm_load_state(kmpm_ctx *c, const void *in, unsigned long long bytes) {
   if (!c || !in) return KMPM_ERR_ARG;
   int r = prepare(c);
   if (r != KMPM_OK) return r;
-  const std::vector<int> fl = active_fields(c);
   if (bytes < sizeof(SnapHeader)) return fail(c, KMPM_ERR_ARG, "not a snapshot");
   const char *o = (const char *)in;
   SnapHeader h;
   std::memcpy(&h, o, sizeof(h));
   o += sizeof(h);
   if (std::memcmp(h.magic, SNAP_MAGIC, 8) != 0 || h.version != 1) return fail(c, KMPM_ERR_ARG, "not a snapshot");
+  std::vector<int> fl = active_fields(c);
+  if (h.nfields != (int)fl.size() && !c->restored_state) {
+    // a snapshot of a context that had uploaded plastic strain or damage
+    c->restored_state = true;
+    std::vector<int> wide = active_fields(c);
+    if (h.nfields == (int)wide.size()) {
+      set_ul_fields(c);
+      c->graph_valid = false;
+      fl = wide;
+    } else {
+      c->restored_state = false;
+    }
+  }
   if (h.method != c->prm.method || h.dim != c->prm.dim || h.basis != c->prm.basis || h.nfields != (int)fl.size() ||
       h.nscalars != c->nscalars || h.nnodes_pad != c->nnodes_pad || h.nsolids != (int)c->hsolids.size() ||
       h.ps != c->ps || bytes < snap_bytes(c, fl))

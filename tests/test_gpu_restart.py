@@ -110,3 +110,29 @@ def test_snapshot_of_another_setup_is_refused(gpu_lib):
         b.backend.load_state(blob)
     with pytest.raises(KmpmError):
         b.backend.load_state(b"not a snapshot" * 10)
+
+
+def test_uploaded_history_follows_rebinning(gpu_lib):
+    """The dam break's water has no plastic or damage law, so its runs leave
+    ε_p and damage at zero and the re-binning does not move them.  A restart
+    can still bring non-zero values (its file is the reference's, whatever
+    the laws): once uploaded they must follow their particles through the
+    re-binning, and a snapshot of that state loads into a fresh context."""
+    a = _dam(5)
+    rng = np.random.default_rng(7)
+    n = a.s.solids[0].np
+    ep = rng.uniform(0.0, 0.5, n)
+    dm = rng.uniform(0.0, 0.01, n)
+    a.backend.upload(0, "eps_p", ep)
+    a.backend.upload(0, "damage", dm)
+    a.run(20)
+    assert np.array_equal(a.particles(0, "eps_p"), ep.astype(np.float32).astype(float))
+    assert np.array_equal(a.particles(0, "damage"), dm.astype(np.float32).astype(float))
+    blob = a.backend.save_state()
+    b = _dam_fresh()
+    b.backend.run(0)
+    b.backend.load_state(blob)
+    for sim in (a, b):
+        sim.run(10)
+    for f in FIELDS + ("damage",):
+        assert np.array_equal(a.particles(0, f), b.particles(0, f)), f
