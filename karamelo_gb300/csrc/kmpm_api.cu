@@ -102,6 +102,13 @@ struct kmpm_ctx {
   float *d_blk_c = nullptr, *d_blk_h = nullptr;
   double *d_eblk = nullptr, *d_eout = nullptr;
   int *d_keys = nullptr, *d_vals = nullptr;
+  // ULMPM re-binning as an update of the last binning (launch_rebin); the
+  // full radix sort of every key each step with KMPM_FULL_REBIN=1
+  bool full_rebin = false;
+  int ncell_pad = 0;
+  int *d_knew = nullptr, *d_cin = nullptr, *d_cout = nullptr, *d_mpre = nullptr, *d_bsum = nullptr;
+  int *d_blkm = nullptr, *d_brun = nullptr, *d_bsort = nullptr;
+  unsigned *d_mflag = nullptr;
   RadixTemp rtmp{};
   int key_bits = 0;
   std::vector<int> ul_fields;
@@ -544,8 +551,11 @@ int build(kmpm_ctx *c) {
     CK(cudaStreamSynchronize(c->st));
   }
   const int ncells = c->ntiles_total * c->NCELL;
-  DALLOC(c->d_cs, ncells);
-  DALLOC(c->d_ce, ncells);
+  // padded to whole chunks of the re-binning's cell kernels, with one cell
+  // past the end (the total of the movers' prefix)
+  c->ncell_pad = (ncells + RB_CHUNK) / RB_CHUNK * RB_CHUNK;
+  DALLOC(c->d_cs, c->ncell_pad);
+  DALLOC(c->d_ce, c->ncell_pad);
   DALLOC(c->d_ts, c->ntiles_total);
   DALLOC(c->d_te, c->ntiles_total);
   {
@@ -584,6 +594,24 @@ int build(kmpm_ctx *c) {
   DALLOC(c->rtmp.v1, c->ps);
   DALLOC(c->rtmp.hist, 256 * ((c->ps + 2047) / 2048 + 1));
   DALLOC(c->rtmp.tot, 256);
+  if (!c->TL()) {
+    if (const char *ev = std::getenv("KMPM_FULL_REBIN"); ev && ev[0] == '1') c->full_rebin = true;
+    const int n = c->ranges[0].count, nblk = (n + 255) / 256;
+    DALLOC(c->d_knew, n);
+    DALLOC(c->d_mflag, (size_t)nblk * 8);
+    DALLOC(c->d_cin, c->ncell_pad);
+    DALLOC(c->d_cout, c->ncell_pad);
+    DALLOC(c->d_mpre, c->ncell_pad);
+    DALLOC(c->d_bsum, 2 * (c->ncell_pad / RB_CHUNK));
+    DALLOC(c->d_blkm, nblk);
+    DALLOC(c->d_brun, n);
+    DALLOC(c->d_bsort, n);
+    // the binning the first step updates: every slot in cell 0 (keys are
+    // zero), which the ranges say
+    const int cs0 = c->ranges[0].start, ce0 = c->ranges[0].start + n;
+    CK(cudaMemcpy(c->d_cs, &cs0, sizeof(int), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(c->d_ce, &ce0, sizeof(int), cudaMemcpyHostToDevice));
+  }
   // ---- particle upload: each solid's caller arrays (already on the device,
   // kmpm_add_solid) converted into its slots; the other fields are zero
   c->T_ref = c->prm.thermal ? c->hsolids[0].T0 : 0.0;
@@ -908,18 +936,32 @@ int enqueue_step(kmpm_ctx *c) {
     // compute_grid_weight_functions_and_gradients (src/ulmpm.cpp:88-337):
     // re-bin all particles by the cell of their current position
     const RangeDev &r = c->ranges[0];
-    launch_cell_keys(pa, c->nblk_p, c->d_keys, 0, c->st);
-    launch_iota(c->d_vals, r.count, c->st);
-    radix_sort(c->d_keys, c->d_vals, r.count, c->key_bits, c->rtmp, c->st);
+    if (c->full_rebin) {
+      launch_cell_keys(pa, c->nblk_p, c->d_keys, 0, c->st);
+      launch_iota(c->d_vals, r.count, c->st);
+      radix_sort(c->d_keys, c->d_vals, r.count, c->key_bits, c->rtmp, c->st);
+      CK(cudaMemsetAsync(c->d_cs, 0, sizeof(int) * (size_t)c->ncell_pad, c->st));
+      CK(cudaMemsetAsync(c->d_ce, 0, sizeof(int) * (size_t)c->ncell_pad, c->st));
+      CK(cudaMemsetAsync(c->d_ts, 0, sizeof(int) * c->ntiles_total, c->st));
+      CK(cudaMemsetAsync(c->d_te, 0, sizeof(int) * c->ntiles_total, c->st));
+      launch_cell_ranges(c->d_keys, r.start, r.count, c->NCELL, c->d_cs, c->d_ce, c->d_ts, c->d_te, c->st);
+      nl += 3 + 3 * ((c->key_bits + 7) / 8);
+    } else {
+      RebinArgs rb{};
+      rb.pa = pa;
+      rb.grid = r.grid; rb.start = r.start; rb.n = r.count;
+      rb.ncell = c->ntiles_total * c->NCELL; rb.ncell_pad = c->ncell_pad; rb.ncpt = c->NCELL;
+      rb.keys = c->d_keys; rb.knew = c->d_knew; rb.mflag = c->d_mflag;
+      rb.cin = c->d_cin; rb.cout = c->d_cout; rb.mpre = c->d_mpre; rb.bsum = c->d_bsum; rb.blkm = c->d_blkm;
+      rb.brun = c->d_brun; rb.bsort = c->d_bsort;
+      rb.cell_start = c->d_cs; rb.cell_end = c->d_ce; rb.tile_start = c->d_ts; rb.tile_end = c->d_te;
+      rb.perm = c->d_vals;
+      nl += launch_rebin(rb, c->st);
+    }
     launch_permute(c->d_pp, c->d_pp + 1, c->ps, c->d_vals, r.start, r.count, c->ul_fields.data(),
                    (int)c->ul_fields.size(), c->st);
     launch_swap_ptrs(c->d_pp, c->st);
-    CK(cudaMemsetAsync(c->d_cs, 0, sizeof(int) * (size_t)c->ntiles_total * c->NCELL, c->st));
-    CK(cudaMemsetAsync(c->d_ce, 0, sizeof(int) * (size_t)c->ntiles_total * c->NCELL, c->st));
-    CK(cudaMemsetAsync(c->d_ts, 0, sizeof(int) * c->ntiles_total, c->st));
-    CK(cudaMemsetAsync(c->d_te, 0, sizeof(int) * c->ntiles_total, c->st));
-    launch_cell_ranges(c->d_keys, r.start, r.count, c->NCELL, c->d_cs, c->d_ce, c->d_ts, c->d_te, c->st);
-    nl += 5 + 3 * ((c->key_bits + 7) / 8);
+    nl += 2;
     MARK("bin_sort");
   }
   // reset() + initial_integrate: the contact fixes fill mbp from the current
@@ -1214,6 +1256,8 @@ int kmpm_destroy(kmpm_ctx *c) {
   if (c->cst) cudaStreamDestroy(c->cst);
   dfree(c->d_blob); dfree(c->d_lstats); dfree(c->d_log_count); dfree(c->d_log);
   dfree(c->d_err); dfree(c->d_blk_c); dfree(c->d_blk_h); dfree(c->d_eblk); dfree(c->d_eout);
+  dfree(c->d_knew); dfree(c->d_mflag); dfree(c->d_cin); dfree(c->d_cout); dfree(c->d_mpre); dfree(c->d_bsum);
+  dfree(c->d_blkm); dfree(c->d_brun); dfree(c->d_bsort);
   dfree(c->d_keys); dfree(c->d_vals); dfree(c->rtmp.k1); dfree(c->rtmp.v1); dfree(c->rtmp.hist); dfree(c->rtmp.tot);
   if (c->st) cudaStreamDestroy(c->st);
   delete c;

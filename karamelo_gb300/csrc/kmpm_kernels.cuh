@@ -199,6 +199,42 @@ void radix_sort(int *keys, int *vals, int n, int key_bits, RadixTemp &tmp, cudaS
 // kmpm_contact.cu: launches one contact's kernels on st; returns the number of launches
 int launch_contact(const PartArgs &a, const ContactDev &c, RadixTemp &rt, cudaStream_t st);
 void launch_iota(int *v, int n, cudaStream_t st);
+
+// cell key of a position: global tile * cells per tile + cell within the
+// tile (tile-major order), cells clamped to the lattice
+__device__ __forceinline__ int cell_key(const GridDev &g, int T0, int T1, int T2, const float x[3], int dim) {
+  int c[3] = {0, 0, 0};
+#pragma unroll
+  for (int d = 0; d < 3; d++)
+    if (d < dim) c[d] = max(0, min((int)((x[d] - g.lo[d]) * g.inv_cellsize), g.ncell[d] - 1));
+  const int tl = ((c[0] / T0) * g.ntile[1] + c[1] / T1) * g.ntile[2] + c[2] / T2;
+  const int lc = ((c[0] % T0) * T1 + c[1] % T1) * T2 + c[2] % T2;
+  return (g.tile_off + tl) * (T0 * T1 * T2) + lc;
+}
+
+// ULMPM re-binning as an update of the previous binning (kmpm_rebin.cu).
+// keys / cell_start / cell_end hold a consistent binning of the current slot
+// order on entry (sorted keys, and the ranges of those keys) and the binning
+// by the new positions on exit; perm gets the stable-sort permutation.
+constexpr int RB_CELLS_PER_THREAD = 16;
+constexpr int RB_CHUNK = 256 * RB_CELLS_PER_THREAD;  // cells per block of the count / range kernels
+struct RebinArgs {
+  PartArgs pa;
+  int grid, start, n;     // the particle range [start, start + n) on grid `grid`
+  int ncell, ncell_pad;   // cells of all tiles; allocated (multiple of RB_CHUNK, > ncell)
+  int ncpt;               // cells per tile
+  int *keys;              // [n] cell of every slot, sorted
+  int *knew;              // [n] cell of the new position
+  unsigned *mflag;        // [nblk * 8] bit per slot: the cell changed
+  int *cin, *cout;        // [ncell_pad] movers into / out of every cell (zero between steps)
+  int *mpre;              // [ncell_pad] exclusive prefix of cin
+  int *bsum;              // [2 * nchunk] per-chunk sums of the new counts and of cin
+  int *blkm;              // [nblk] movers per 256 slots
+  int *brun, *bsort;      // [n] movers grouped by destination cell; then sorted by slot in each group
+  int *cell_start, *cell_end, *tile_start, *tile_end;
+  int *perm;              // [n] source slot (relative to start) of every destination slot
+};
+int launch_rebin(const RebinArgs &r, cudaStream_t st);  // returns the number of launches
 void launch_permute(float *const *src_pp, float *const *dst_pp, size_t ps, const int *perm, int start, int n,
                     const int *fields, int nfields, cudaStream_t st);
 void launch_swap_ptrs(float **pp, cudaStream_t st);

@@ -18,28 +18,21 @@ __global__ void k_cell_keys(PartArgs a, int *keys, int use_x0, int pad_last) {
   const int ri = a.blk_range[blockIdx.x];
   const RangeDev rd = a.ranges[ri];
   const int p = rd.start + (blockIdx.x - rd.blk0) * 256 + threadIdx.x;
-  const GridDev g = a.grids[rd.grid];
-  const int *T = a.tile_t;
+  const GridDev &g = a.grids[rd.grid];  // by reference: a copy lands on the stack
+  const int T0 = a.tile_t[0], T1 = a.tile_t[1], T2 = a.tile_t[2];
   if (p >= rd.start + rd.count) {
     // padding slot: the last key of its grid, so that a stable sort of all
     // slots keeps every range's particles first and its padding last
     if (pad_last)
-      keys[p] = (g.tile_off + g.ntile[0] * g.ntile[1] * g.ntile[2]) * (T[0] * T[1] * T[2]) - 1;
+      keys[p] = (g.tile_off + g.ntile[0] * g.ntile[1] * g.ntile[2]) * (T0 * T1 * T2) - 1;
     return;
   }
   const float *P = *a.Pp;
-  int c[3] = {0, 0, 0};
-  for (int d = 0; d < a.dim; d++) {
-    const float xp = P[(PF_X0 + d) * a.ps + p] + (use_x0 ? 0.f : P[(PF_XN + d) * a.ps + p]);
-    int cd = (int)((xp - g.lo[d]) * g.inv_cellsize);
-    c[d] = max(0, min(cd, g.ncell[d] - 1));
-  }
-  const int t[3] = {c[0] / T[0], c[1] / T[1], c[2] / T[2]};
-  const int l[3] = {c[0] % T[0], c[1] % T[1], c[2] % T[2]};
-  const int tl = (t[0] * g.ntile[1] + t[1]) * g.ntile[2] + t[2];
-  const int lc = (l[0] * T[1] + l[1]) * T[2] + l[2];
-  const int ncpt = T[0] * T[1] * T[2];
-  keys[p] = (g.tile_off + tl) * ncpt + lc;
+  float x[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+  for (int d = 0; d < 3; d++)
+    if (d < a.dim) x[d] = P[(PF_X0 + d) * a.ps + p] + (use_x0 ? 0.f : P[(PF_XN + d) * a.ps + p]);
+  keys[p] = cell_key(g, T0, T1, T2, x, a.dim);
 }
 
 void launch_cell_keys(const PartArgs &a, int nblk, int *keys, int use_x0, cudaStream_t st, int pad_last) {
@@ -229,9 +222,17 @@ __global__ void k_permute(float *const *src_pp, float *const *dst_pp, size_t ps,
   const float *src = *src_pp;
   float *dst = *dst_pp;
   const int j = start + perm[i];
-  for (int k = 0; k < nf; k++) {
-    const int df = fl.f[k] >> 8, sf = fl.f[k] & 255;
-    dst[df * ps + start + i] = src[sf * ps + j];
+  // eight independent loads in flight before their stores: the gather is
+  // latency-bound with one
+  constexpr int B = 8;
+  for (int k0 = 0; k0 < nf; k0 += B) {
+    float v[B];
+#pragma unroll
+    for (int b = 0; b < B; b++)
+      if (k0 + b < nf) v[b] = __ldg(src + (size_t)(fl.f[k0 + b] & 255) * ps + j);
+#pragma unroll
+    for (int b = 0; b < B; b++)
+      if (k0 + b < nf) dst[(size_t)(fl.f[k0 + b] >> 8) * ps + start + i] = v[b];
   }
 }
 void launch_permute(float *const *src_pp, float *const *dst_pp, size_t ps, const int *perm, int start, int n,
