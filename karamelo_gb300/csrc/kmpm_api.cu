@@ -139,6 +139,13 @@ struct kmpm_ctx {
   LearnKernels LK{};
   // autotuner: chosen launch-shape variant of each gather kernel, its record
   int var_g2p1 = 0, var_g2p2 = 0;
+  // learned return map on linear EOS + Johnson-Cook: the plain stress kernel
+  // queues the plastic steps and k_learn_queue runs the network over them
+  // (KMPM_SUR_FUSED=1: the fused k_g2p2_learn instead)
+  float *d_lq_f = nullptr;
+  int *d_lq_i = nullptr, *d_lq_count = nullptr;
+  long long lq_cap = 0;
+  int nsm = 0;
   bool law_jc = false;  // every material is linear EOS + Johnson-Cook: the specialised stress kernels
   // plastic strain or damage was uploaded (a restart): those rows may be
   // non-zero whatever the laws, and are permuted with the others
@@ -274,6 +281,11 @@ PartArgs part_args(kmpm_ctx *c) {
   a.axisym = c->prm.axisymmetric;
   a.dim = c->prm.dim;
   for (int d = 0; d < 3; d++) a.tile_t[d] = c->tdim[d];
+  a.lq_f = c->d_lq_f;
+  a.lq_i = c->d_lq_i;
+  a.lq_count = c->d_lq_count;
+  a.lq_stats = c->d_lstats;
+  a.lq_cap = c->lq_cap;
   return a;
 }
 
@@ -900,6 +912,13 @@ void *force_scatter_fn(const kmpm_ctx *c, int mode, bool th) {
 
 // launch shape v of the FP32 mechanical stress kernel, specialised to the
 // materials where that applies
+// the learned return map through the queue (plain stress kernel + k_learn_queue)
+bool sur_queued(const kmpm_ctx *c) {
+  if (c->learn_mode != MODE_SUR || !c->law_jc || !c->K.g2p2_jcq[0] || !c->LK.queue) return false;
+  const char *ev = std::getenv("KMPM_SUR_FUSED");
+  return !(ev && ev[0] == '1');
+}
+
 void *g2p2_variant(const kmpm_ctx *c, int v) {
   const bool TL = c->TL();
   if (c->law_jc && c->K.g2p2_jc[TL][v]) return c->K.g2p2_jc[TL][v];
@@ -1045,10 +1064,15 @@ int enqueue_step(kmpm_ctx *c) {
     la.log_thresh = c->log_thresh;
     la.nblk = c->nblk_p;
     void *args[] = {&pa, &la};
-    if (c->learn_mode == MODE_SUR)
+    if (sur_queued(c)) {
+      CK(cudaMemsetAsync(c->d_lq_count, 0, sizeof(int), c->st));
+      LAUNCH(c->K.g2p2_jcq[c->var_g2p2], c->nblk_p, 256, 0, pa);
+      CK(cudaLaunchKernel(c->LK.queue, dim3(c->nsm), dim3(512), args, c->LK.sur_smem, c->st));
+    } else if (c->learn_mode == MODE_SUR) {
       CK(cudaLaunchKernel(c->LK.sur, dim3((c->nblk_p + 1) / 2), dim3(512), args, c->LK.sur_smem, c->st));
-    else
+    } else {
       CK(cudaLaunchKernel(c->LK.log, dim3(c->nblk_p), dim3(256), args, 0, c->st));
+    }
     nl++;
   }
   MARK("g2p_stress");
@@ -1111,6 +1135,16 @@ int prepare(kmpm_ctx *c) {
   if (!c->graph_valid) {
     int r = select_scatters(c);
     if (r != KMPM_OK) return r;
+  }
+  if (sur_queued(c) && !c->d_lq_f) {  // room for every particle: the queue cannot overflow
+    c->lq_cap = (long long)c->ps;
+    DALLOC(c->d_lq_f, (size_t)LQ_NF * c->lq_cap);
+    DALLOC(c->d_lq_i, (size_t)LQ_NI * c->lq_cap);
+    DALLOC(c->d_lq_count, 1);
+    int dev = 0;
+    CK(cudaGetDevice(&dev));
+    CK(cudaDeviceGetAttribute(&c->nsm, cudaDevAttrMultiProcessorCount, dev));
+    CK(cudaStreamSynchronize(c->st));
   }
   return ensure_graph(c);
 }
@@ -1256,6 +1290,7 @@ int kmpm_destroy(kmpm_ctx *c) {
   if (c->cst) cudaStreamDestroy(c->cst);
   dfree(c->d_blob); dfree(c->d_lstats); dfree(c->d_log_count); dfree(c->d_log);
   dfree(c->d_err); dfree(c->d_blk_c); dfree(c->d_blk_h); dfree(c->d_eblk); dfree(c->d_eout);
+  dfree(c->d_lq_f); dfree(c->d_lq_i); dfree(c->d_lq_count);
   dfree(c->d_knew); dfree(c->d_mflag); dfree(c->d_cin); dfree(c->d_cout); dfree(c->d_mpre); dfree(c->d_bsum);
   dfree(c->d_blkm); dfree(c->d_brun); dfree(c->d_bsort);
   dfree(c->d_keys); dfree(c->d_vals); dfree(c->rtmp.k1); dfree(c->rtmp.v1); dfree(c->rtmp.hist); dfree(c->rtmp.tot);
@@ -1934,6 +1969,7 @@ int kmpm_set_surrogate(kmpm_ctx *c, kmpm_mlp *m, double tol) {
   CK(cudaMemsetAsync(c->d_lstats, 0, 4 * sizeof(unsigned long long), c->st));
   CK(cudaStreamSynchronize(c->st));
   CK(cudaFuncSetAttribute(c->LK.sur, cudaFuncAttributeMaxDynamicSharedMemorySize, c->LK.sur_smem));
+  CK(cudaFuncSetAttribute(c->LK.queue, cudaFuncAttributeMaxDynamicSharedMemorySize, c->LK.sur_smem));
   c->sur_tol = (float)tol;
   c->learn_mode = MODE_SUR;
   c->graph_valid = false;

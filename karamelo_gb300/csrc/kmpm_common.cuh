@@ -539,7 +539,7 @@ __device__ __forceinline__ R jc_flow_stress(const R *p, R epsp, R epsdot, R T) {
 
 template <typename R, int LAW = LAW_ANY>
 __device__ inline Sym<R> strength_update(const MatDev &m, R dt, const Sym<R> &sig, const Sym<R> &D, R &dep, R epsp,
-                                         R epsdot, R damage, R T) {
+                                         R epsdot, R damage, R T, bool *returned = nullptr) {
   Sym<R> out;
   dep = R(0);
   const auto *p = MatP<R>::str(m);
@@ -594,6 +594,7 @@ __device__ inline Sym<R> strength_update(const MatDev &m, R dt, const Sym<R> &si
   out.dev();
   R J2 = R(KMPM_SQRT_3_OVER_2) * out.norm();
   if (J2 < ys) return out;
+  if (returned) *returned = true;  // the trial state reached the yield surface
   dep = (J2 - ys) / (R(3) * Gd);
   R sc = ys / J2;
 #pragma unroll

@@ -101,7 +101,20 @@ struct PartArgs {
   int apic;                  // APIC transfers: k_g2p2 forms grad v from moments and stores PF_C
   int asflip;                // ULMPM ASFLIP: positions move with the blended velocity
   int axisym;                // 2-D axisymmetric: Fdot(2,2) / L(2,2) += v_r w / r
+  // queue of the plastic particle-steps for the learned return map (the
+  // stress kernel's QUEUE variant writes it, k_learn_queue reads it):
+  // LQ_NF float rows and LQ_NI int rows of lq_cap entries each
+  float *lq_f;
+  int *lq_i;
+  int *lq_count;
+  unsigned long long *lq_stats;
+  long long lq_cap;
 };
+// queue rows: slot, material; dt, tav, D (6), sigma before the step (6),
+// eps_p, eps_p rate, pressure, trace of strain_el, R (9), cof F (9)
+enum { LQ_P = 0, LQ_MAT = 1, LQ_NI = 2 };
+enum { LQ_DT = 0, LQ_TAV = 1, LQ_D = 2, LQ_SIG = 8, LQ_EPSP = 14, LQ_EPSDOT = 15, LQ_PH = 16, LQ_TRE = 17,
+       LQ_R = 18, LQ_COF = 27, LQ_NF = 36 };
 
 struct DtArgs {
   const RangeDev *ranges;
@@ -135,6 +148,7 @@ struct StepKernels {
   // the same stress-kernel shapes compiled for linear EOS + Johnson-Cook only
   // (LAW_EOS_LINEAR_JC; 3-D, nullptr elsewhere)
   void *g2p2_jc[2][3];
+  void *g2p2_jcq[3];  // 3-D cubic TLMPM, linear EOS + Johnson-Cook, queueing plastic steps
 };
 constexpr int G2P_NVAR = 3;
 constexpr int G2P1_MINB[G2P_NVAR] = {4, 3, 6};

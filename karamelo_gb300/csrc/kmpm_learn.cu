@@ -10,7 +10,12 @@
 //             answer (its stress correction kept along the trial deviator)
 //             misses the yield-function or flow-rule residual tolerance
 //
-// Both cover TLMPM with materials of type eos-strength whose strength is
+//   queue     the network over the plastic steps that the plain stress
+//             kernel (k_g2p2 with QUEUE, linear EOS + Johnson-Cook) queued
+//             after its closed-form update: where the network's answer
+//             passes the same tests it replaces that update
+//
+// All cover TLMPM with materials of type eos-strength whose strength is
 // Johnson-Cook (the host checks this), FP32, no nodal temperature field.
 // Everything else is the arithmetic of k_g2p2: rate of deformation,
 // deformation gradient, polar decomposition, EOS, damage, plastic-work heat,
@@ -341,6 +346,132 @@ __global__ void __launch_bounds__(MODE == MODE_SUR ? 512 : 256, MODE == MODE_SUR
   }
 }
 
+// The network over the queue of plastic particle-steps.  The plain kernel
+// has already written the closed-form update of every queued step; where the
+// network's answer passes the residual tests of k_g2p2_learn (MODE_SUR), this
+// kernel writes the update again from that answer: eps_p, its rate, sigma,
+// strain_el and the PK1 operand (the material has linear EOS + Johnson-Cook,
+// no damage and no temperature, so nothing else depends on the return).
+// One 512-thread CTA per SM walks the queue in 512-row chunks (four 128-row
+// M-tiles per forward pass).
+__global__ void __launch_bounds__(512, 1) k_learn_queue(PartArgs a, LearnArgs l) {
+  extern __shared__ __align__(1024) unsigned char lsmem[];
+  if (run_finished(a.scalars)) return;
+  mlp::TileCtx tcx;
+  bool wready = false;
+  mlp::tile_begin<4>(tcx, lsmem, l.blob);
+  mlp::tile_weights_ready(tcx, wready);
+  const long long cap = a.lq_cap;
+  const int n = (int)min((long long)*a.lq_count, cap);
+  const int nch = (n + 511) / 512;
+  float *P = *a.Pp;
+  const size_t ps = a.ps;
+  const float *q = a.lq_f;
+  for (int ch = blockIdx.x; ch < nch && tcx.ok; ch += gridDim.x) {
+    const long long j = (long long)ch * 512 + threadIdx.x;
+    const bool valid = j < n;
+    int p = 0, mi = 0;
+    float dt = 0.f, epsp = 0.f, epsdot = 0.f;
+    Sym<float> D, sig;
+    float feat[mlp::NIN];
+    if (valid) {
+      p = a.lq_i[LQ_P * cap + j];
+      mi = a.lq_i[LQ_MAT * cap + j];
+      dt = q[LQ_DT * cap + j];
+#pragma unroll
+      for (int k = 0; k < 6; k++) {
+        D.a[k] = q[(LQ_D + k) * cap + j];
+        sig.a[k] = q[(LQ_SIG + k) * cap + j];
+      }
+      epsp = q[LQ_EPSP * cap + j];
+      epsdot = q[LQ_EPSDOT * cap + j];
+      learn_features(D, dt, sig, epsp, 0.f, epsdot, a.mats[mi].f_str_p[4], feat);
+    } else {
+#pragma unroll
+      for (int k = 0; k < mlp::NIN; k++) feat[k] = 0.f;
+    }
+    const bool inside = mlp::tile_put_features(tcx, feat, valid);
+    float y[mlp::NOUT];
+    if (!mlp::tile_forward<4>(tcx, y)) {
+      if (threadIdx.x == 0) raise_error(a.err, ERR_TIMEOUT, -1, a.scalars[0].ntimestep);
+      break;
+    }
+    bool use_net = false;
+    if (valid && inside) {
+      const MatDev &m = a.mats[mi];
+      const float *sp = m.f_str_p;
+      // the trial state and flow stress of the closed form (dmg = 0, T = 0)
+      const float ys = jc_flow_stress<float>(sp, epsp, epsdot, 0.f);
+      const float Gd = sp[0], f = dt * 2.f * Gd;
+      Sym<float> str;
+#pragma unroll
+      for (int k = 0; k < 6; k++) str.a[k] = sig.a[k] + f * D.a[k];
+      str.dev();
+      const float J2tr = (float)KMPM_SQRT_3_OVER_2 * str.norm();
+      float dsn = 0.f, ss = 0.f;
+#pragma unroll
+      for (int k = 0; k < 6; k++) {
+        const float wk = k < 3 ? 1.f : 2.f;
+        dsn += wk * y[k] * str.a[k];
+        ss += wk * str.a[k] * str.a[k];
+      }
+      const float f1 = 1.f + dsn / ss;
+      const float J2n = J2tr * fabsf(f1);
+      const float dep = y[6];
+      const float iys = 1.f / ys;
+      const float r_yield = fabsf(J2n - ys) * iys;
+      const float r_flow = fabsf(J2tr - J2n - 3.f * Gd * dep) * iys;
+      if (dep >= 0.f && f1 > 0.f && r_yield <= l.tol && r_flow <= l.tol) {
+        use_net = true;
+        Sym<float> sdev;
+#pragma unroll
+        for (int k = 0; k < 6; k++) sdev.a[k] = f1 * str.a[k];
+        // the tail of k_g2p2's eos-strength update with this return
+        const float tav = q[LQ_TAV * cap + j];
+        float ed = epsdot;
+        ed -= ed * dt / tav;
+        ed += dep / tav;
+        ed = fmaxf(0.f, ed);
+        P[PF_EPSP * ps + p] = epsp + dep;
+        P[PF_EPSDOT * ps + p] = ed;
+        const float pf = q[LQ_PH * cap + j];
+        if (a.track_strain) {
+          const float tr3 = (dt * D.tr() + q[LQ_TRE * cap + j]) / 3.f;
+          const float iG = 1.f / m.f_G;
+#pragma unroll
+          for (int k = 0; k < 6; k++) P[(PF_STRAIN + k) * ps + p] = sdev.a[k] * iG + (k < 3 ? tr3 : 0.f);
+        }
+        Sym<float> sn = sdev;
+        sn.a[0] -= pf; sn.a[1] -= pf; sn.a[2] -= pf;
+#pragma unroll
+        for (int k = 0; k < 6; k++) P[(PF_SIG + k) * ps + p] = sn.a[k];
+        float R[9], cofF[9];
+#pragma unroll
+        for (int k = 0; k < 9; k++) {
+          R[k] = q[(LQ_R + k) * cap + j];
+          cofF[k] = q[(LQ_COF + k) * cap + j];
+        }
+        float Sm[9] = {sn.a[0], sn.a[3], sn.a[4], sn.a[3], sn.a[1], sn.a[5], sn.a[4], sn.a[5], sn.a[2]};
+        float RS[9], RSR[9], PK1[9];
+        matmul3(R, Sm, RS);
+        matmulT3(RS, R, RSR);
+        matmul3(RSR, cofF, PK1);
+        const float vol0 = P[PF_VOL0 * ps + p];
+#pragma unroll
+        for (int k = 0; k < 9; k++) P[(PF_PK + k) * ps + p] = PK1[k] * vol0;
+      }
+    }
+    const unsigned b_net = __ballot_sync(0xffffffffu, use_net), b_out = __ballot_sync(0xffffffffu, valid && !inside),
+                   b_res = __ballot_sync(0xffffffffu, valid && inside && !use_net);
+    if ((threadIdx.x & 31) == 0 && (b_net | b_out | b_res)) {
+      atomicAdd(&a.lq_stats[1], (unsigned long long)__popc(b_net));
+      atomicAdd(&a.lq_stats[2], (unsigned long long)__popc(b_out));
+      atomicAdd(&a.lq_stats[3], (unsigned long long)__popc(b_res));
+    }
+  }
+  mlp::tile_end<4>(tcx);
+}
+
 // Closed-form return map of material `mat` on logged inputs (labels for the
 // training set): Y = (s_new - s_trial (6), dep, plastic flag).
 __global__ void k_jc_label(const MatDev *mats, int mat, const float *__restrict__ X, long long n, float *__restrict__ Y) {
@@ -373,6 +504,7 @@ void get_learn_kernels(LearnKernels &k) {
   k.log = (void *)k_g2p2_learn<3, 1, MODE_LOG>;
   k.sur = (void *)k_g2p2_learn<3, 1, MODE_SUR>;
   k.label = (void *)k_jc_label;
+  k.queue = (void *)k_learn_queue;
   k.sur_smem = mlp::Smem<4>::BYTES;
 }
 

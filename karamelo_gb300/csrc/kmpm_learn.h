@@ -22,7 +22,7 @@ struct LearnArgs {
 };
 
 struct LearnKernels {
-  void *log, *sur, *label;
+  void *log, *sur, *label, *queue;
   int sur_smem;
 };
 void get_learn_kernels(LearnKernels &k);

@@ -626,7 +626,9 @@ __global__ void __launch_bounds__(256, MINB) k_g2p1(PartArgs a) {
 
 // rate of deformation + deformation gradient + stress + wave speed
 // (src/solid.cpp:798-936, 1155-1438)
-template <int DIM, int BASIS, bool TL, bool THERMAL, int PREC, int MINB = 3, int LAW = LAW_ANY>
+// QUEUE: also append every plastic step (undamaged particle) to the learned
+// return map's queue with what k_learn_queue needs to redo its update
+template <int DIM, int BASIS, bool TL, bool THERMAL, int PREC, int MINB = 3, int LAW = LAW_ANY, bool QUEUE = false>
 __global__ void __launch_bounds__(256, MINB) k_g2p2(PartArgs a) {
   __shared__ float red_c[256], red_h[256];
   if (run_finished(a.scalars)) return;
@@ -868,7 +870,48 @@ __global__ void __launch_bounds__(256, MINB) k_g2p2(PartArgs a) {
       } else {
         pH = eos_pressure<float, LAW>(m, J, Jm1, rho, dmg, D.tr(), g.cellsize, T);
         if (hasT) pH += m.f_temp_p[3] * (m.f_temp_p[4] - T);
-        sdev = strength_update<float, LAW>(m, dt, sig, D, dep, epsp, epsdot, dmg, T);
+        bool returned = false;
+        sdev = strength_update<float, LAW>(m, dt, sig, D, dep, epsp, epsdot, dmg, T, &returned);
+        if constexpr (QUEUE) {
+          const bool enq = returned && dmg == 0.f;
+          const unsigned act = __activemask();
+          const unsigned want = __ballot_sync(act, enq);
+          if (want) {
+            const int lane = threadIdx.x & 31, leader = __ffs(want) - 1;
+            int base = 0;
+            if (lane == leader) {
+              base = atomicAdd(a.lq_count, __popc(want));
+              atomicAdd(&a.lq_stats[0], (unsigned long long)__popc(want));
+            }
+            base = __shfl_sync(act, base, leader);
+            if (enq) {
+              const long long j = base + __popc(want & ((1u << lane) - 1u)), cap = a.lq_cap;
+              float *q = a.lq_f;
+              a.lq_i[LQ_P * cap + j] = p;
+              a.lq_i[LQ_MAT * cap + j] = mi;
+              q[LQ_DT * cap + j] = dt;
+              q[LQ_TAV * cap + j] = 1000.f * g.cellsize / m.f_signal_velocity;
+#pragma unroll
+              for (int k = 0; k < 6; k++) {
+                q[(LQ_D + k) * cap + j] = D.a[k];
+                q[(LQ_SIG + k) * cap + j] = sig.a[k];
+              }
+              q[LQ_EPSP * cap + j] = epsp;
+              q[LQ_EPSDOT * cap + j] = epsdot;
+              q[LQ_PH * cap + j] = pH;
+              float tre = 0.f;
+              if (a.track_strain)
+#pragma unroll
+                for (int k = 0; k < 3; k++) tre += P[(PF_STRAIN + k) * ps + p];
+              q[LQ_TRE * cap + j] = tre;
+#pragma unroll
+              for (int k = 0; k < 9; k++) {
+                q[(LQ_R + k) * cap + j] = R[k];
+                q[(LQ_COF + k) * cap + j] = cofF[k];
+              }
+            }
+          }
+        }
       }
       epsp += dep;
       const float tav = 1000.f * g.cellsize / m.f_signal_velocity;
@@ -1054,6 +1097,12 @@ void fill_step_kernels(StepKernels &k) {
     KMPM_JC_SET(false)
     KMPM_JC_SET(true)
 #undef KMPM_JC_SET
+  }
+  for (int v = 0; v < G2P_NVAR; v++) k.g2p2_jcq[v] = nullptr;
+  if constexpr (DIM == 3 && BASIS == 1) {  // the learned return map's path
+    k.g2p2_jcq[0] = (void *)k_g2p2<DIM, BASIS, true, false, 0, G2P2_MINB[0], LAW_EOS_LINEAR_JC, true>;
+    k.g2p2_jcq[1] = (void *)k_g2p2<DIM, BASIS, true, false, 0, G2P2_MINB[1], LAW_EOS_LINEAR_JC, true>;
+    k.g2p2_jcq[2] = (void *)k_g2p2<DIM, BASIS, true, false, 0, G2P2_MINB[2], LAW_EOS_LINEAR_JC, true>;
   }
 }
 

@@ -232,3 +232,26 @@ def test_trained_network_gain(trained):
     assert share(a) > 0.1, (a, stats)
     assert share(b) < 0.005, b
     assert share(a) > 20 * share(b)
+
+
+def test_queued_network_matches_fused_kernel(trained):
+    """Two schedules of the learned return map: the plain stress kernel
+    queueing the plastic steps for a separate network kernel (the default for
+    linear EOS + Johnson-Cook), and the network fused into the stress kernel
+    (KMPM_SUR_FUSED=1).  Both apply the same tests to the same answers, so
+    they serve about the same steps and end at the same state."""
+    import os
+    mlp, _, _, _ = trained
+    steps = 800
+    a = _learned_bar(mlp, steps)
+    os.environ["KMPM_SUR_FUSED"] = "1"
+    try:
+        b = _learned_bar(mlp, steps)
+    finally:
+        del os.environ["KMPM_SUR_FUSED"]
+    sa, sb = a.backend.surrogate_stats(), b.backend.surrogate_stats()
+    assert sa["network"] > 0 and sb["network"] > 0, (sa, sb)
+    assert abs(sa["plastic"] - sb["plastic"]) <= 0.01 * sb["plastic"], (sa, sb)
+    assert abs(sa["network"] - sb["network"]) <= 0.02 * sb["network"], (sa, sb)
+    for f, tol in (("sigma", 1e-4), ("x", 1e-6), ("eps_p", 1e-4)):
+        assert _rel(a.particles(0, f), b.particles(0, f)) <= tol, f
