@@ -42,27 +42,21 @@ __global__ void k_dump(PartArgs a, DumpArgs d) {
       for (int k = 0; k < 9; k++) o[9 * i + k] = f(PF_STRAIN + sm[k]);
       break;
     case KMPM_P_SIGMA_ROT: {
-      double sg[9];
-      for (int k = 0; k < 9; k++) sg[k] = f(PF_SIG + sm[k]);
       if (!d.rotate) {
-        for (int k = 0; k < 9; k++) o[9 * i + k] = sg[k];
+        for (int k = 0; k < 9; k++) o[9 * i + k] = f(PF_SIG + sm[k]);
         break;
       }
-      // R of F = R U by the stress kernel's FP32 polar iteration (F itself is
-      // held in FP32, so an FP64 iteration would add digits the state does not
-      // have; FP64 runs at 1/60 of the FP32 rate here), the rotation in FP64
-      float Ff[9], Rf[9];
+      // R of F = R U by the stress kernel's FP32 polar iteration, and R sigma
+      // R^T in FP32 as the stress kernel forms its PK1 operand: sigma, F and R
+      // are FP32 state, and FP64 runs at 1/60 of the FP32 rate here
+      float Ff[9], R[9], Sm[9], RS[9], RSR[9];
       for (int k = 0; k < 9; k++) Ff[k] = P[(PF_H + k) * ps + p] + (k % 4 == 0 ? 1.f : 0.f);
-      double R[9], RS[9];
-      if (polar_rotation(Ff, Rf))
-        for (int k = 0; k < 9; k++) R[k] = (double)Rf[k];
-      else  // det F <= 0: the step has raised its error; the stress goes out unrotated
-        for (int k = 0; k < 9; k++) R[k] = (k % 4 == 0) ? 1.0 : 0.0;
-      for (int r = 0; r < 3; r++)
-        for (int c = 0; c < 3; c++) RS[3 * r + c] = R[3 * r] * sg[c] + R[3 * r + 1] * sg[3 + c] + R[3 * r + 2] * sg[6 + c];
-      for (int r = 0; r < 3; r++)
-        for (int c = 0; c < 3; c++)
-          o[9 * i + 3 * r + c] = RS[3 * r] * R[3 * c] + RS[3 * r + 1] * R[3 * c + 1] + RS[3 * r + 2] * R[3 * c + 2];
+      if (!polar_rotation(Ff, R))  // det F <= 0: the step has raised its error; the stress goes out unrotated
+        for (int k = 0; k < 9; k++) R[k] = (k % 4 == 0) ? 1.f : 0.f;
+      for (int k = 0; k < 9; k++) Sm[k] = P[(PF_SIG + sm[k]) * ps + p];
+      matmul3(R, Sm, RS);
+      matmulT3(RS, R, RSR);
+      for (int k = 0; k < 9; k++) o[9 * i + k] = (double)RSR[k];
       break;
     }
     case KMPM_P_F:

@@ -153,18 +153,31 @@ __global__ void __launch_bounds__(256) k_rebin_count(RebinArgs r) {
 }
 
 // exclusive scan in place of a[0], a[stride], ... (n entries) by one block
-// of 1024 threads, each owning a contiguous segment
+// of 1024 threads, each owning a contiguous segment read 16 entries at a time
+// (independent loads in flight: one block has no other warps to hide them)
 __device__ void scan_segments(int *a, int n, int stride, int *sw) {
+  constexpr int U = 16;
   const int seg = (n + 1023) / 1024;
   const int b = threadIdx.x * seg, e = min(n, b + seg);
   int s = 0;
-  for (int k = b; k < e; k++) s += a[(size_t)k * stride];
+  for (int k0 = b; k0 < e; k0 += U) {
+    int v[U];
+#pragma unroll
+    for (int u = 0; u < U; u++) v[u] = k0 + u < e ? a[(size_t)(k0 + u) * stride] : 0;
+#pragma unroll
+    for (int u = 0; u < U; u++) s += v[u];
+  }
   int tot;
   int run = block_excl_scan<1024>(s, sw, tot);
-  for (int k = b; k < e; k++) {
-    const int v = a[(size_t)k * stride];
-    a[(size_t)k * stride] = run;
-    run += v;
+  for (int k0 = b; k0 < e; k0 += U) {
+    int v[U];
+#pragma unroll
+    for (int u = 0; u < U; u++) v[u] = k0 + u < e ? a[(size_t)(k0 + u) * stride] : 0;
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      if (k0 + u < e) a[(size_t)(k0 + u) * stride] = run;
+      run += v[u];
+    }
   }
 }
 
