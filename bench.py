@@ -24,6 +24,7 @@ implementation of the step (the oracle port) on the host cores.
 from __future__ import annotations
 
 import argparse
+import gc
 import json
 import os
 import statistics
@@ -221,6 +222,10 @@ def bench_ours(args):
     for s in pinned:  # the caller's dump buffers, in use before (first touch of page-locked pages)
         for t in s.values():
             t.zero_()
+    # no collector pass inside the timed region: freeing a context there
+    # (cudaFree) would synchronise the device in the middle of the steps
+    gc.collect()
+    gc.disable()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     sim2.backend = GpuBackend(sim2.s, precision=args.precision, track_strain=False)
@@ -240,6 +245,7 @@ def bench_ours(args):
     be2.sync_downloads()
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - t0
+    gc.enable()
     e2e = n * (done + 1) / e2e_s
     h2d = n * (3 + 3 + 3 + 1 + 1) * 8  # x0, x, v, mass, vol0 as FP64 from the caller
     d2h = dumps * n * (3 + 3 + 9) * 8
@@ -321,6 +327,7 @@ def bench_learned(args, plain_backend, plain_sigma, plain_x, n, plain_ms):
     ms = e0.elapsed_time(e1)
     st = be.surrogate_stats()
     sig, x = sim.particles(0, "sigma"), sim.particles(0, "x")
+    be.close()
     length = lambda a: float(a[:, 0].max() - a[:, 0].min())
     value = n * args.steps / (ms / 1000.0)
     return {"value": value, "unit": UNIT, "ms_per_step": ms / args.steps, "plain_ms_per_step": plain_ms / args.steps,

@@ -643,6 +643,20 @@ __global__ void __launch_bounds__(256, MINB) k_g2p2(PartArgs a) {
     const MatDev &m = a.mats[mi];
     const StepScalars &sc = a.scalars[a.indep ? a.blk_range[blockIdx.x] : 0];
     const float dt = (float)sc.dt;
+    // the state rows read after the node gather: start their DRAM reads now,
+    // into L2, so that they overlap the gather (a hint: no registers held)
+    if (LAW == LAW_EOS_LINEAR_JC) {
+      const int rows[] = {PF_H, PF_H + 1, PF_H + 2, PF_H + 3, PF_H + 4, PF_H + 5, PF_H + 6, PF_H + 7, PF_H + 8,
+                          PF_SIG, PF_SIG + 1, PF_SIG + 2, PF_SIG + 3, PF_SIG + 4, PF_SIG + 5,
+                          PF_EPSP, PF_EPSDOT, PF_DMG, PF_VOL0, PF_V, PF_V + 1, PF_V + 2};
+      // each address is formed inside the asm block: the compiler must not keep
+      // these 22 addresses live across the gather for the later loads
+      const unsigned long long base = (unsigned long long)(P + p), row_bytes = 4ull * ps;
+#pragma unroll
+      for (int r : rows)
+        asm volatile("{ .reg .u64 ad; mad.lo.u64 ad, %1, %2, %0; prefetch.global.L2 [ad]; }" ::"l"(base),
+                     "l"(row_bytes), "l"((unsigned long long)r));
+    }
     float xp[3];
 #pragma unroll
     for (int d = 0; d < 3; d++) xp[d] = P[(PF_X0 + d) * ps + p] + (TL ? 0.f : P[(PF_X + d) * ps + p]);

@@ -194,11 +194,16 @@ class GpuBackend:
             raise KmpmError(r, self.L.kmpm_last_error(self.h).decode())
         return r
 
+    def close(self):
+        """Free the context and its device memory now (kmpm_destroy), not
+        whenever the garbage collector reaches this object."""
+        if getattr(self, "h", None):
+            self.L.kmpm_destroy(self.h)
+            self.h = None
+
     def __del__(self):
         try:
-            if getattr(self, "h", None):
-                self.L.kmpm_destroy(self.h)
-                self.h = None
+            self.close()
         except Exception:
             pass
 
