@@ -20,6 +20,8 @@ using namespace kmpm;
 
 namespace kmpm {
 void launch_step_begin(StepScalars *s, int n, cudaStream_t st);
+void launch_fix_values(FixDev *fixes, int nfix, const GridDev *grids, const StepScalars *scalars, int indep,
+                       cudaStream_t st);
 }
 
 struct kmpm_ctx {
@@ -88,6 +90,7 @@ struct kmpm_ctx {
   float *partial = nullptr;
   size_t pstride_tile = 0;
   FixDev *d_fixes = nullptr;
+  int nfix_dev = 0;
   int *d_fix_start = nullptr, *d_fix_count = nullptr;
   std::vector<uint8_t *> d_masks;
   StepScalars *d_scalars = nullptr;
@@ -809,6 +812,7 @@ int upload_fixes(kmpm_ctx *c) {
     count[gi] = (int)fx.size() - start[gi];
   }
   DALLOC(c->d_fixes, fx.size());
+  c->nfix_dev = (int)fx.size();
   if (!fx.empty())
     CK(cudaMemcpyAsync(c->d_fixes, fx.data(), sizeof(FixDev) * fx.size(), cudaMemcpyHostToDevice, c->st));
   DALLOC(c->d_fix_start, start.size());
@@ -950,6 +954,10 @@ int enqueue_step(kmpm_ctx *c) {
   PartArgs pa = part_args(c);
   MARK("begin");
   launch_step_begin(c->d_scalars, c->nscalars, c->st);
+  if (c->nfix_dev > 0) {
+    launch_fix_values(c->d_fixes, c->nfix_dev, c->d_grids, c->d_scalars, c->indep(), c->st);
+    nl++;
+  }
   nl++;
   if (!TL) {
     // compute_grid_weight_functions_and_gradients (src/ulmpm.cpp:88-337):

@@ -124,6 +124,10 @@ struct FixDev {
   int kind, grid, set[3];
   double c[3][4];
   const uint8_t *mask;  // node mask of that grid (local node index)
+  // velocity fixes: c0 + c1 t + c2 exp(c3 t) at this step's time and at the
+  // time one dt earlier, evaluated once per step (k_fix_values) rather than
+  // per masked node (an FP64 exp)
+  double now[3], prev[3];
 };
 
 enum ErrCode : int {

@@ -334,6 +334,26 @@ void launch_dt(const DtArgs &a, cudaStream_t st) {
 
 void launch_step_begin(StepScalars *s, int n, cudaStream_t st) { k_step_begin<<<1, 256, 0, st>>>(s, n); }
 
+// FixVelocityNodes' values at this step's time and one dt earlier
+// (src/fix_velocity_nodes.cpp:130-271): time and dt do not change between
+// the start of a step and its time update, so once per step serves every
+// masked node
+__global__ void k_fix_values(FixDev *fixes, int nfix, const GridDev *grids, const StepScalars *scalars, int indep) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nfix) return;
+  FixDev &f = fixes[k];
+  const StepScalars &sc = scalars[indep ? grids[f.grid].solid0 : 0];
+  const double t = sc.time, tp = sc.time - sc.dt;
+  for (int d = 0; d < 3; d++) {
+    f.now[d] = f.c[d][0] + f.c[d][1] * t + f.c[d][2] * exp(f.c[d][3] * t);
+    f.prev[d] = f.c[d][0] + f.c[d][1] * tp + f.c[d][2] * exp(f.c[d][3] * tp);
+  }
+}
+void launch_fix_values(FixDev *fixes, int nfix, const GridDev *grids, const StepScalars *scalars, int indep,
+                       cudaStream_t st) {
+  if (nfix > 0) k_fix_values<<<(nfix + 127) / 128, 128, 0, st>>>(fixes, nfix, grids, scalars, indep);
+}
+
 // ------------------------------------------------------------------ energy
 // 1/2 m |v|^2 and 1/2 vol sigma:strain_el in FP64 block partials, then a
 // fixed-order sum (deterministic)

@@ -410,10 +410,6 @@ __device__ __forceinline__ void gather_partials(const GridArgs &a, const GridDev
   (void)li;
 }
 
-__device__ __forceinline__ double fix_value(const FixDev &f, int d, double t) {
-  return f.c[d][0] + f.c[d][1] * t + f.c[d][2] * exp(f.c[d][3] * t);
-}
-
 // GM_MASS: nodal mass only (TL once).  GM_UPDATE: after the first scatter.
 // GM_VEL: after the MUSL re-map (or USL: positions only).  R is the
 // arithmetic of the nodal sums and of v = p/m (double for the FP64 islands).
@@ -432,7 +428,6 @@ __global__ void __launch_bounds__(256) k_grid(GridArgs a) {
   const int node = g.node_off + li;
   const StepScalars &sc = a.scalars[a.indep ? g.solid0 : 0];
   const R dt = (R)sc.dt;
-  const double time = sc.time;
 
   if (GMODE == GM_MASS) {
     R s[1];
@@ -478,7 +473,7 @@ __global__ void __launch_bounds__(256) k_grid(GridArgs a) {
       const FixDev &fx = a.fixes[k];
       if (fx.kind != 0 || !fx.mask[li]) continue;
       for (int d = 0; d < 3; d++)
-        if (fx.set[d]) { vu[d] = (R)fix_value(fx, d, time); v[d] = (R)fix_value(fx, d, time - sc.dt); }
+        if (fx.set[d]) { vu[d] = (R)fx.now[d]; v[d] = (R)fx.prev[d]; }
     }
     a.nodeA[NODE_STRIDE * node] = make_float4((float)v[0], (float)v[1], (float)v[2], (float)m);
     a.nodeB[NODE_STRIDE * node] = make_float4((float)vu[0], (float)vu[1], (float)vu[2], (float)Tu);
@@ -502,7 +497,7 @@ __global__ void __launch_bounds__(256) k_grid(GridArgs a) {
       const FixDev &fx = a.fixes[k];
       if (fx.kind != 0 || !fx.mask[li]) continue;
       for (int d = 0; d < 3; d++)
-        if (fx.set[d]) v[d] = (R)fix_value(fx, d, time);
+        if (fx.set[d]) v[d] = (R)fx.now[d];
     }
     a.nodeA[NODE_STRIDE * node] = make_float4((float)v[0], (float)v[1], (float)v[2], A.w);
   }
