@@ -237,8 +237,9 @@ def bench_ours(args):
         k = min(10, args.steps - done)
         sim2.run(k)
         done += k
-        if dumps >= 2:
-            be2.sync_downloads()  # the set about to be reused has landed
+        if dumps >= 2:  # the set about to be reused has landed (the other may still be in flight)
+            for t in pinned[dumps % 2].values():
+                be2.wait_download(t)
         for f in widths:
             be2.particles_async(0, f, pinned[dumps % 2][f])
         dumps += 1

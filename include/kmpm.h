@@ -256,9 +256,12 @@ int kmpm_load_state(struct kmpm_ctx *ctx, const void *in, unsigned long long byt
  * order with the steps, then copied to `out` on a second stream while later
  * kmpm_run calls proceed.  `out` must be page-locked host memory
  * (cudaHostAlloc / cudaHostRegister) of n*width doubles and stays owned by
- * the caller; its content is valid after kmpm_sync_downloads. */
+ * the caller; its content is valid after kmpm_sync_downloads (every queued
+ * download) or kmpm_wait_download(ctx, out) (the last one queued into `out`,
+ * leaving later downloads in flight; KMPM_OK at once if none is). */
 int kmpm_download_particles_async(struct kmpm_ctx *ctx, int solid, int field, double *out);
 int kmpm_sync_downloads(struct kmpm_ctx *ctx);
+int kmpm_wait_download(struct kmpm_ctx *ctx, const double *out);
 
 /* Download one grid field (n*1 or n*3 doubles, reference node order). */
 int kmpm_download_grid(struct kmpm_ctx *ctx, int grid, int field, double *out);

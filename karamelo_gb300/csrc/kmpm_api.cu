@@ -167,6 +167,7 @@ struct kmpm_ctx {
     size_t cap = 0;
     cudaEvent_t gathered = nullptr, copied = nullptr;
     bool busy = false;
+    const double *dst = nullptr;  // the caller's buffer of the last copy
   };
   std::vector<AsyncBuf> abufs;
   bool indep() const { return prm.independent != 0; }
@@ -1625,6 +1626,20 @@ int kmpm_download_particles_async(kmpm_ctx *c, int solid, int field, double *out
   CK(cudaMemcpyAsync(out, b->buf, sizeof(double) * need, cudaMemcpyDeviceToHost, c->cst));
   CK(cudaEventRecord(b->copied, c->cst));
   b->busy = true;
+  for (auto &x : c->abufs)  // a buffer has one pending copy at a time
+    if (&x != b && x.dst == out) x.dst = nullptr;
+  b->dst = out;
+  return KMPM_OK;
+}
+
+int kmpm_wait_download(kmpm_ctx *c, const double *out) {
+  if (!c || !out) return KMPM_ERR_ARG;
+  for (auto &b : c->abufs)
+    if (b.dst == out) {
+      if (b.busy) CK(cudaEventSynchronize(b.copied));
+      b.busy = false;
+      b.dst = nullptr;
+    }
   return KMPM_OK;
 }
 

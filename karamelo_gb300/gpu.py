@@ -38,7 +38,7 @@ EXPORTED = ["kmpm_create", "kmpm_destroy", "kmpm_last_error", "kmpm_add_material
             "kmpm_mlp_get_params", "kmpm_mlp_set_norm", "kmpm_mlp_get_norm", "kmpm_mlp_loss_grad", "kmpm_mlp_train",
             "kmpm_mlp_predict", "kmpm_mlp_predict_tc", "kmpm_log_start", "kmpm_log_stop", "kmpm_log_data",
             "kmpm_jc_label", "kmpm_set_surrogate", "kmpm_surrogate_stats", "kmpm_tuning",
-            "kmpm_download_particles_async", "kmpm_sync_downloads", "kmpm_add_contact", "kmpm_contact_force",
+            "kmpm_download_particles_async", "kmpm_sync_downloads", "kmpm_wait_download", "kmpm_add_contact", "kmpm_contact_force",
             "kmpm_set_scalars", "kmpm_state_size", "kmpm_save_state", "kmpm_load_state", "kmpm_set_np_per_cell"]
 
 MLP_NIN, MLP_NOUT, MLP_NPARAMS, MLP_NNORM = 15, 7, 35975, 74
@@ -127,6 +127,7 @@ def load(path: str = LIB_PATH):
     L.kmpm_tuning.argtypes = [p]
     L.kmpm_download_particles_async.argtypes = [p, i, i, fp]
     L.kmpm_sync_downloads.argtypes = [p]
+    L.kmpm_wait_download.argtypes = [p, ctypes.c_void_p]
     L.kmpm_tuning.restype = ctypes.c_char_p
     L.kmpm_add_contact.argtypes = [p, i, i, i, d]
     L.kmpm_contact_force.argtypes = [p, i, dp]
@@ -258,6 +259,10 @@ class GpuBackend:
 
     def sync_downloads(self):
         self._ck(self.L.kmpm_sync_downloads(self.h))
+
+    def wait_download(self, out):
+        """Wait for the last download queued into ``out`` only."""
+        self._ck(self.L.kmpm_wait_download(self.h, out.data_ptr()))
 
     def upload_velocity(self, si: int, v):
         v = np.ascontiguousarray(v, float)

@@ -294,6 +294,35 @@ def test_async_downloads_match_sync(gpu_lib):
     assert not np.array_equal(be.particles(0, "x"), ref["x"])
 
 
+def test_wait_download_of_one_buffer(gpu_lib):
+    """kmpm_wait_download: waiting for one buffer's copy leaves the others
+    queued; each buffer holds the state of the step its download was queued
+    at, and a second download into a buffer replaces the first."""
+    torch = pytest.importorskip("torch")
+    g = W.taylor_bar(None, cellsize=0.8)
+    g.backend = GpuBackend(g.s, autotune=False)
+    be = g.backend
+    g.run(1)
+    W.taylor_bar_wall(g)
+    n = g.s.solids[0].np
+    bufs = [torch.empty(n * 3, dtype=torch.float64, pin_memory=True) for _ in range(3)]
+    refs = []
+    for k in range(3):
+        g.run(10)
+        refs.append(be.particles(0, "x"))
+        be.particles_async(0, "x", bufs[k])
+    be.wait_download(bufs[0])
+    assert np.array_equal(bufs[0].numpy().reshape(-1, 3), refs[0])
+    g.run(10)
+    refs[0] = be.particles(0, "x")
+    be.particles_async(0, "x", bufs[0])  # the buffer again: its new content
+    for k in (2, 0, 1):
+        be.wait_download(bufs[k])
+        assert np.array_equal(bufs[k].numpy().reshape(-1, 3), refs[k]), k
+    be.wait_download(bufs[1])  # nothing in flight for it: returns at once
+    be.sync_downloads()
+
+
 # ---------------------------------------------------------------- USF
 @pytest.mark.parametrize("basis", ["cubic-spline", "linear"])
 def test_taylor_bar_usf(gpu_lib, oracle_mod, basis):
