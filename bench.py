@@ -229,24 +229,33 @@ def bench_ours(args):
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     sim2.backend = GpuBackend(sim2.s, precision=args.precision, track_strain=False)
+    t_create = time.perf_counter()
     sim2.run(1)
     W.taylor_bar_wall(sim2)
     be2 = sim2.backend
-    done, dumps = 0, 0
+    t_first = time.perf_counter()
+    done, dumps, t_runs, t_waits, t_queue = 0, 0, 0.0, 0.0, 0.0
     while done < args.steps:
         k = min(10, args.steps - done)
+        a0 = time.perf_counter()
         sim2.run(k)
+        a1 = time.perf_counter()
         done += k
         if dumps >= 2:  # the set about to be reused has landed (the other may still be in flight)
             for t in pinned[dumps % 2].values():
                 be2.wait_download(t)
+        a2 = time.perf_counter()
         for f in widths:
             be2.particles_async(0, f, pinned[dumps % 2][f])
         dumps += 1
+        t_runs, t_waits, t_queue = t_runs + (a1 - a0), t_waits + (a2 - a1), t_queue + (time.perf_counter() - a2)
+    t_loop = time.perf_counter()
     be2.sync_downloads()
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - t0
     gc.enable()
+    e2e_parts = {"create": t_create - t0, "first_step_and_wall": t_first - t_create, "runs": t_runs,
+                 "download_waits": t_waits, "download_queueing": t_queue, "final_sync": e2e_s - (t_loop - t0)}
     e2e = n * (done + 1) / e2e_s
     h2d = n * (3 + 3 + 3 + 1 + 1) * 8  # x0, x, v, mass, vol0 as FP64 from the caller
     d2h = dumps * n * (3 + 3 + 9) * 8
@@ -276,7 +285,8 @@ def bench_ours(args):
                 "d2h_bytes_per_step": d2h // (done + 1),
                 "note": "C ABI from host FP64 arrays: upload + binning + steps + an asynchronous dump "
                         "(x, v, rotated sigma, FP64, into two alternating sets of page-locked buffers, "
-                        "first touched before the timed region) every 10 steps"},
+                        "first touched before the timed region) every 10 steps",
+                "seconds": {k: round(v, 4) for k, v in e2e_parts.items()}},
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,
                      "alg_bytes_per_launch": alg},
