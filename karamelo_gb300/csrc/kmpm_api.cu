@@ -618,8 +618,9 @@ int build(kmpm_ctx *c) {
     DALLOC(c->d_cin, c->ncell_pad);
     DALLOC(c->d_cout, c->ncell_pad);
     DALLOC(c->d_mpre, c->ncell_pad);
-    DALLOC(c->d_bsum, 2 * (c->ncell_pad / RB_CHUNK));
-    DALLOC(c->d_blkm, nblk);
+    // the single-block scans read whole 4096-int tiles
+    DALLOC(c->d_bsum, (2 * (c->ncell_pad / RB_CHUNK) + 4095) / 4096 * 4096);
+    DALLOC(c->d_blkm, (nblk + 4095) / 4096 * 4096);
     DALLOC(c->d_brun, n);
     DALLOC(c->d_bsort, n);
     // the binning the first step updates: every slot in cell 0 (keys are

@@ -242,8 +242,8 @@ struct RebinArgs {
   unsigned *mflag;        // [nblk * 8] bit per slot: the cell changed
   int *cin, *cout;        // [ncell_pad] movers into / out of every cell (zero between steps)
   int *mpre;              // [ncell_pad] exclusive prefix of cin
-  int *bsum;              // [2 * nchunk] per-chunk sums of the new counts and of cin
-  int *blkm;              // [nblk] movers per 256 slots
+  int *bsum;              // [2 * nchunk] per-chunk sums of the new counts and of cin (padded to 4096 ints)
+  int *blkm;              // [nblk] movers per 256 slots (padded to 4096 ints)
   int *brun, *bsort;      // [n] movers grouped by destination cell; then sorted by slot in each group
   int *cell_start, *cell_end, *tile_start, *tile_end;
   int *perm;              // [n] source slot (relative to start) of every destination slot

@@ -152,43 +152,39 @@ __global__ void __launch_bounds__(256) k_rebin_count(RebinArgs r) {
   }
 }
 
-// exclusive scan in place of a[0], a[stride], ... (n entries) by one block
-// of 1024 threads, each owning a contiguous segment read 16 entries at a time
-// (independent loads in flight: one block has no other warps to hide them)
-__device__ void scan_segments(int *a, int n, int stride, int *sw) {
-  constexpr int U = 16;
-  const int seg = (n + 1023) / 1024;
-  const int b = threadIdx.x * seg, e = min(n, b + seg);
-  int s = 0;
-  for (int k0 = b; k0 < e; k0 += U) {
-    int v[U];
-#pragma unroll
-    for (int u = 0; u < U; u++) v[u] = k0 + u < e ? a[(size_t)(k0 + u) * stride] : 0;
-#pragma unroll
-    for (int u = 0; u < U; u++) s += v[u];
+// exclusive scans in place by one block of 1024 threads, one int4 per thread
+// per 4096-int tile (coalesced), with the running total carried across tiles.
+// The arrays are padded to whole tiles; entries past the valid range only
+// follow it, so whatever they hold does not change its prefixes.
+__device__ void scan_ints(int *a, int n, int *sw) {
+  int carry = 0;
+  for (int base = 0; base < n; base += 4096) {
+    const int4 v = ld4(a + base + 4 * threadIdx.x);
+    int tot;
+    const int e = block_excl_scan<1024>(v.x + v.y + v.z + v.w, sw, tot) + carry;
+    st4(a + base + 4 * threadIdx.x, make_int4(e, e + v.x, e + v.x + v.y, e + v.x + v.y + v.z));
+    carry += tot;
   }
-  int tot;
-  int run = block_excl_scan<1024>(s, sw, tot);
-  for (int k0 = b; k0 < e; k0 += U) {
-    int v[U];
-#pragma unroll
-    for (int u = 0; u < U; u++) v[u] = k0 + u < e ? a[(size_t)(k0 + u) * stride] : 0;
-#pragma unroll
-    for (int u = 0; u < U; u++) {
-      if (k0 + u < e) a[(size_t)(k0 + u) * stride] = run;
-      run += v[u];
-    }
+}
+// the same over pairs (a[2k], a[2k+1]), scanned as two sequences
+__device__ void scan_pairs(int *a, int npairs, int *sw) {
+  int c0 = 0, c1 = 0;
+  for (int base = 0; base < npairs; base += 2048) {
+    const int4 v = ld4(a + 2 * base + 4 * threadIdx.x);  // pairs base + 2t and base + 2t + 1
+    int t0, t1;
+    const int e0 = block_excl_scan<1024>(v.x + v.z, sw, t0) + c0;
+    const int e1 = block_excl_scan<1024>(v.y + v.w, sw, t1) + c1;
+    st4(a + 2 * base + 4 * threadIdx.x, make_int4(e0, e1, e0 + v.x, e1 + v.y));
+    c0 += t0;
+    c1 += t1;
   }
 }
 
 __global__ void __launch_bounds__(1024) k_rebin_scan(RebinArgs r, int nchunk, int nblk) {
   if (run_finished(r.pa.scalars)) return;
   __shared__ int sw[33];
-  scan_segments(r.bsum, nchunk, 2, sw);
-  __syncthreads();
-  scan_segments(r.bsum + 1, nchunk, 2, sw);
-  __syncthreads();
-  scan_segments(r.blkm, nblk, 1, sw);
+  scan_pairs(r.bsum, nchunk, sw);
+  scan_ints(r.blkm, nblk, sw);
 }
 
 __global__ void __launch_bounds__(256) k_rebin_ranges(RebinArgs r) {
