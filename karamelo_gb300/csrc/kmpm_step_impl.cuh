@@ -638,9 +638,10 @@ __global__ void __launch_bounds__(256, MINB) k_g2p2(PartArgs a) {
     const MatDev &m = a.mats[mi];
     const StepScalars &sc = a.scalars[a.indep ? a.blk_range[blockIdx.x] : 0];
     const float dt = (float)sc.dt;
-    // the state rows read after the node gather: start their DRAM reads now,
-    // into L2, so that they overlap the gather (a hint: no registers held)
-    if (LAW == LAW_EOS_LINEAR_JC) {
+    // the state rows the EOS + strength update reads after the node gather
+    // (material type 2): start their DRAM reads now, into L2, so that they
+    // overlap the gather (a hint: no registers held)
+    if (LAW == LAW_EOS_LINEAR_JC || (PREC == 0 && m.type == 2)) {
       const int rows[] = {PF_H, PF_H + 1, PF_H + 2, PF_H + 3, PF_H + 4, PF_H + 5, PF_H + 6, PF_H + 7, PF_H + 8,
                           PF_SIG, PF_SIG + 1, PF_SIG + 2, PF_SIG + 3, PF_SIG + 4, PF_SIG + 5,
                           PF_EPSP, PF_EPSDOT, PF_DMG, PF_VOL0, PF_V, PF_V + 1, PF_V + 2};
