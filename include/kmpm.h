@@ -301,9 +301,10 @@ const char *kmpm_profile_phase(struct kmpm_ctx *ctx, int i);
  *           corotational frame), Cauchy stress before the step (6), equivalent
  *           plastic strain, temperature, log(1 + epsdot_p / epsdot0)
  *   outputs (KMPM_MLP_NOUT): s_new - s_trial (6), plastic strain increment
- * It is trained on the GPU in FP32 (kmpm_mlp_train) and evaluated inside the
- * G2P stress kernel as BF16 tensor-core MMAs with FP32 accumulation
- * (kmpm_set_surrogate).  Parameters are one flat FP32 vector of
+ * It is trained on the GPU in FP32 (kmpm_mlp_train) and evaluated as BF16
+ * tensor-core MMAs with FP32 accumulation (kmpm_set_surrogate): over the
+ * plastic steps the G2P stress kernel queues when every material is linear
+ * EOS + Johnson-Cook, else inside that kernel.  Parameters are one flat FP32 vector of
  * KMPM_MLP_NPARAMS values: W1[128x15] b1[128] W2[128x128] b2 W3[128x128] b3
  * W4[7x128] b4[7] (row-major, out x in).  The normalisation vector holds
  * in_mean[15] in_std[15] out_mean[7] out_scale[7] env_lo[15] env_hi[15];
