@@ -285,3 +285,44 @@ def taylor_bar_axisymmetric(backend_factory=None, cellsize=0.2, R=3.2, L=32.4, p
 def taylor_bar_axisymmetric_wall(sim):
     """The wall of the axisymmetric bar, added after the first step."""
     sim.fix("BC_Wall", "velocity_nodes", "gwall", None, 0)
+
+
+def vertical_bar(backend_factory=None, N=10, ppc=1, method="tlmpm/gpu", sub="FLIP", basis="cubic-spline",
+                 pic_flip=0.99, scheme="musl"):
+    """A neo-Hookean bar (1 m long, 1 m x 1 m section; E = 1e6 Pa, nu = 0.3,
+    rho = 1050 kg/m^3) hanging from its top face under 1000 m/s^2 of gravity
+    (examples/Vertical_bar/Cubic_spline/N_20/FLIP/vertical_bar.mpm): the nodes
+    at y >= -cellsize/4 hold v_y = 0, dt_factor 0.2, N cells along the bar.
+    The reference logs dy_tip, the vertical displacement of the centre of
+    mass of the particles in the bottom corner cell (``vertical_bar_tip``)."""
+    L = 1.0
+    hL = 0.5 * L
+    h = L / N
+    sim = MPM(backend_factory)
+    _method(sim, method, sub, basis, pic_flip)
+    sim.scheme(scheme)
+    sim.dimension(3, -hL, hL, -L, 0.0, -hL, hL, h)
+    sim.region("box", "block", -hL, hL, -L, 0.0, -hL, hL)
+    sim.material("mat1", "neo-hookean", 1050.0, 1e6, 0.3)
+    sim.solid("solid1", "region", "box", ppc, "mat1", h, 0)
+    sim.region("rBCLX", "block", "INF", "INF", -h / 4, "INF", "INF", "INF")
+    sim.group("gBCLX", "nodes", "region", "rBCLX", "solid", "solid1")
+    sim.fix("fBCLX", "velocity_nodes", "gBCLX", None, 0, None)
+    sim.fix("fbody", "body_force", "all", 0, -1e3, 0)
+    sim.dt_factor(0.2)
+    return sim
+
+
+def vertical_bar_tip(sim, x=None):
+    """Mass-weighted centre of the particles in the region
+    block(INF, -hL + h/2, INF, -L + 3h/4, INF, -hL + h/2) of the script
+    (its group gTip), from positions x (default: the initial lattice)."""
+    import numpy as np
+    s = sim.s.solids[0]
+    x0 = s.x0
+    h = sim.cellsize
+    sel = (x0[:, 0] <= -0.5 + h / 2 + 1e-12) & (x0[:, 1] <= -1.0 + 3 * h / 4 + 1e-12) & \
+          (x0[:, 2] <= -0.5 + h / 2 + 1e-12)
+    xs = x0 if x is None else x
+    m = s.mass[sel]
+    return (m[:, None] * xs[sel]).sum(0) / m.sum()

@@ -1448,6 +1448,12 @@ void om_scalars(void *h, double *out) {
   Sim *s = (Sim *)h;
   out[0] = s->time; out[1] = s->dt; out[2] = (double)s->ntimestep;
 }
+// the clock, as a restart sets it (Update::read_restart, src/update.cpp:363-393):
+// the next step runs with this dt, and adjust_dt sets the one after
+void om_set_scalars(void *h, double time, double dt) {
+  Sim *s = (Sim *)h;
+  s->time = time; s->dt = dt;
+}
 // Particle fields: 0 x, 1 x0, 2 v, 3 sigma (as stored), 4 sigma rotated (R sigma R^T for TL dumps,
 // src/dump_particle.cpp:98-102), 5 F, 6 eps_p, 7 epsdot_p, 8 damage, 9 damage_init, 10 T, 11 J, 12 vol,
 // 13 strain_el, 14 vol0PK1, 15 mass

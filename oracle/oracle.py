@@ -57,6 +57,7 @@ def lib():
         L.om_run.argtypes = [p, i]
         L.om_run_time.argtypes = [p, d]
         L.om_scalars.argtypes = [p, dp]
+        L.om_set_scalars.argtypes = [p, ctypes.c_double, ctypes.c_double]
         L.om_get_particles.argtypes = [p, i, i, dp]
         L.om_get_grid.argtypes = [p, i, i, dp]
         L.om_energy.argtypes = [p, dp]
@@ -177,6 +178,11 @@ class OracleBackend:
         out = np.zeros(3)
         self.L.om_scalars(self.h, _dp(out))
         return out[0], out[1], int(out[2])
+
+    def set_scalars(self, time, dt, ntimestep=None):
+        """Set the clock (the next step runs with this dt); the signature of
+        GpuBackend.set_scalars, whose step counter the oracle keeps itself."""
+        self.L.om_set_scalars(self.h, float(time), float(dt))
 
     def particles(self, si, field):
         code, w = PARTICLE_FIELDS[field]

@@ -1,0 +1,73 @@
+"""Parity with the reference's own published runs: the vertical bar
+(examples/Vertical_bar: a 3-D TLMPM, MUSL, FLIP 0.99, cubic-spline
+neo-Hookean bar, 1 m long, hanging under 1000 m/s^2 from nodes held at
+v_y = 0), whose logs record dt and the tip displacement dy_tip every step.
+tests/golden/vertical_bar_golden.npz holds their first 121 lines
+(tests/golden/make_vertical_bar_golden.py).
+
+The logs come from an older Karamelo whose adjust_dt leaves out the particle
+speed, so each step here runs with the logged dt (set through the clock, as
+a restart does).  The logged dy_tip carries the constant offset its step-0
+line shows (the script's y0_tip is evaluated before the run); it is
+subtracted.  The oracle then follows the N = 20 run (two particles per cell,
+64,000 particles) to 8e-6 relative through step 100, about the precision of
+the log's six printed digits, and the N = 10 run (one particle per cell) to
+4e-6 through step 10 and 3e-4 through step 50.  After that the coarse bar,
+by then stretched to almost twice its length, leaves the older run.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from karamelo_gb300 import workloads as W
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden", "vertical_bar_golden.npz")
+
+
+def _follow(sim, be, key, nsteps):
+    """Run nsteps with the logged dt; relative error of dy_tip per step."""
+    g = np.load(GOLDEN)
+    dt, dyr = g[key + "_dt"], g[key + "_dy_tip"]
+    dyr = dyr - dyr[0]
+    y0 = W.vertical_bar_tip(sim)[1]
+    rel = np.zeros(nsteps + 1)
+    for s in range(1, nsteps + 1):
+        if s >= 2:
+            t, _, n = be.scalars()
+            be.set_scalars(t, dt[s], n)
+        sim.run(1)
+        dy = W.vertical_bar_tip(sim, sim.particles(0, "x"))[1] - y0
+        rel[s] = abs(dy - dyr[s]) / abs(dyr[s]) if s >= 2 else 0.0
+    return rel
+
+
+def test_body_force_total(oracle_mod):
+    g = np.load(GOLDEN)
+    for key, N, ppc in (("n10_ppc1", 10, 1), ("n20_ppc2", 20, 2)):
+        sim = W.vertical_bar(oracle_mod.OracleBackend, N=N, ppc=ppc, method="tlmpm")
+        assert sim.s.solids[0].np == N ** 3 * ppc ** 3
+        assert abs(sim.s.solids[0].mass.sum() * -1e3 / g[key + "_fbody_y"][1] - 1) < 1e-12
+
+
+def test_oracle_follows_reference_run_n20(oracle_mod):
+    sim = W.vertical_bar(oracle_mod.OracleBackend, N=20, ppc=2, method="tlmpm")
+    rel = _follow(sim, sim._ensure_backend(), "n20_ppc2", 100)
+    assert rel[2:].max() < 2e-5, rel.max()
+
+
+def test_oracle_follows_reference_run_n10(oracle_mod):
+    sim = W.vertical_bar(oracle_mod.OracleBackend, N=10, ppc=1, method="tlmpm")
+    rel = _follow(sim, sim._ensure_backend(), "n10_ppc1", 50)
+    assert rel[2:11].max() < 2e-5, rel[2:11].max()
+    assert rel[2:].max() < 5e-4, rel.max()
+
+
+@pytest.mark.gpu
+def test_gpu_follows_reference_run_n20(gpu_lib):
+    """The CUDA path (FP32) on the same run."""
+    from karamelo_gb300.gpu import GpuBackend
+    sim = W.vertical_bar(None, N=20, ppc=2)
+    sim.backend = GpuBackend(sim.s, autotune=False)
+    rel = _follow(sim, sim.backend, "n20_ppc2", 100)
+    assert rel[2:].max() < 1e-3, rel.max()
