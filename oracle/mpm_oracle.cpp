@@ -8,11 +8,12 @@
 //   - The 1-D basis functions below are checked against the reference's own
 //     header (src/basis_functions.h, compiled by oracle/Makefile into
 //     oracle/_ref/ and stored as golden vectors in tests/golden/).
-//   - The whole TLMPM MUSL FLIP cubic-spline step with a neo-Hookean
-//     material, a body force and a velocity fix follows the reference's
-//     published runs of examples/Vertical_bar (their logged tip
-//     displacement, tests/golden/vertical_bar_golden.npz) to 8e-6 relative
-//     over 100 steps.
+//   - The whole TLMPM MUSL step with a neo-Hookean material, a body force
+//     and a velocity fix follows the reference's published runs of
+//     examples/Vertical_bar (their logged tip displacement,
+//     tests/golden/vertical_bar_golden.npz): FLIP with the cubic spline to
+//     8e-6 relative over 100 steps; FLIP with the linear basis and APIC with
+//     either basis to 4e-6 over 50 steps.
 //   - The reference itself cannot be built here (it needs Eigen 3 and MPI),
 //     so the other laws and transfers rest on this line-by-line restatement
 //     of the cited reference functions: double precision, with the

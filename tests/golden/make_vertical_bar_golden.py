@@ -3,7 +3,9 @@ published runs of its vertical-bar example (examples/Vertical_bar/*.data in
 the Karamelo tree: the logs of a 3-D TLMPM, MUSL, FLIP 0.99, cubic-spline
 neo-Hookean bar hanging under 1000 m/s^2, one line per step with columns
 Step, dt, Time, fbody_x, fbody_y, fbody_z, dy_tip).  The first 121 lines of
-two logs are kept: N = 10 with one particle per cell, and N = 20 with two.
+five logs are kept: FLIP with the cubic spline at N = 10 (one particle per
+cell) and N = 20 (two), FLIP with the linear basis at N = 20 (one), and APIC
+with the cubic spline and with the linear basis at N = 20 (two).
 Run where the Karamelo tree is available:
 
     python tests/golden/make_vertical_bar_golden.py [path/to/Karamelo]
@@ -15,7 +17,10 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LOGS = {"n10_ppc1": "FLIP_99_cubic-spline_N-10_1_particle_per_cell.data",
-        "n20_ppc2": "FLIP_99_cubic-spline_N-20_2_particle_per_cell.data"}
+        "n20_ppc2": "FLIP_99_cubic-spline_N-20_2_particle_per_cell.data",
+        "linear_n20_ppc1": "FLIP_99_linear_N-20_1_particle_per_cell.data",
+        "apic_n20_ppc2": "APIC_cubic-spline_N-20_2_particle_per_cell.data",
+        "apic_linear_n20_ppc2": "APIC_linear_N-20_2_particle_per_cell.data"}
 
 
 def main():

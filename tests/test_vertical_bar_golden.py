@@ -13,7 +13,9 @@ subtracted.  The oracle then follows the N = 20 run (two particles per cell,
 64,000 particles) to 8e-6 relative through step 100, about the precision of
 the log's six printed digits, and the N = 10 run (one particle per cell) to
 4e-6 through step 10 and 3e-4 through step 50.  After that the coarse bar,
-by then stretched to almost twice its length, leaves the older run.
+by then stretched to almost twice its length, leaves the older run.  The
+linear-basis FLIP run and the APIC runs (cubic and linear) at N = 20 agree
+to 4e-6 through step 50.
 """
 import os
 
@@ -53,6 +55,19 @@ def test_body_force_total(oracle_mod):
 def test_oracle_follows_reference_run_n20(oracle_mod):
     sim = W.vertical_bar(oracle_mod.OracleBackend, N=20, ppc=2, method="tlmpm")
     rel = _follow(sim, sim._ensure_backend(), "n20_ppc2", 100)
+    assert rel[2:].max() < 2e-5, rel.max()
+
+
+@pytest.mark.parametrize("key,ppc,sub,basis", [
+    ("linear_n20_ppc1", 1, "FLIP", "linear"),
+    ("apic_n20_ppc2", 2, "APIC", "cubic-spline"),
+    ("apic_linear_n20_ppc2", 2, "APIC", "linear"),   # Di from the particles per cell
+])
+def test_oracle_follows_reference_run_basis_and_transfer(oracle_mod, key, ppc, sub, basis):
+    """The linear basis and the APIC transfer, at N = 20: measured 3e-6 to
+    4e-6 relative through step 50."""
+    sim = W.vertical_bar(oracle_mod.OracleBackend, N=20, ppc=ppc, sub=sub, basis=basis, method="tlmpm")
+    rel = _follow(sim, sim._ensure_backend(), key, 50)
     assert rel[2:].max() < 2e-5, rel.max()
 
 
