@@ -1019,13 +1019,13 @@ int enqueue_step(kmpm_ctx *c) {
     // forces of the new stress, the grid update and the particle update
     PartArgs ps = pa;
     ps.use_vu = 0;
-    LAUNCH((th || prec) ? c->K.g2p2[TL][th][prec] : g2p2_variant(c, c->var_g2p2), c->nblk_p, 256, 0, ps);
+    LAUNCH((th || prec) ? c->K.g2p2[TL][th][prec] : g2p2_variant(c, c->var_g2p2), c->nblk_p, 256, G2P2_SMEM, ps);
     MARK("g2p_stress");
     LAUNCH(c->sc_usf, c->ntiles_launch, 256, c->smem_usf, p);
     MARK("p2g_forces");
     LAUNCH(c->K.grid_upd[TL][th][prec], c->nblk_g, 256, 0, g1);
     MARK("grid_update2");
-    LAUNCH(c->K.g2p1_v[TL][c->var_g2p1], c->nblk_p, 256, 0, pa);
+    LAUNCH(c->K.g2p1_v[TL][c->var_g2p1], c->nblk_p, 256, G2P1_SMEM, pa);
     MARK("g2p_advance");
     if (TL) {
       GridArgs g2 = grid_args(c, 0);
@@ -1041,7 +1041,7 @@ int enqueue_step(kmpm_ctx *c) {
     return KMPM_OK;
   }
   // grid_to_points + advance_particles
-  LAUNCH(th ? c->K.g2p1[TL][th] : c->K.g2p1_v[TL][c->var_g2p1], c->nblk_p, 256, 0, pa);
+  LAUNCH(th ? c->K.g2p1[TL][th] : c->K.g2p1_v[TL][c->var_g2p1], c->nblk_p, 256, G2P1_SMEM, pa);
   MARK("g2p_advance");
   if (musl) {
     // velocities_to_grid + post_velocities_to_grid (+ TL grid positions)
@@ -1061,7 +1061,7 @@ int enqueue_step(kmpm_ctx *c) {
   }
   // compute_rate_deformation_gradient + update_deformation_gradient + update_stress
   if (c->learn_mode == MODE_PLAIN) {
-    LAUNCH((th || prec) ? c->K.g2p2[TL][th][prec] : g2p2_variant(c, c->var_g2p2), c->nblk_p, 256, 0, pa);
+    LAUNCH((th || prec) ? c->K.g2p2[TL][th][prec] : g2p2_variant(c, c->var_g2p2), c->nblk_p, 256, G2P2_SMEM, pa);
   } else {
     LearnArgs la{};
     la.blob = c->d_blob;
@@ -1076,7 +1076,7 @@ int enqueue_step(kmpm_ctx *c) {
     void *args[] = {&pa, &la};
     if (sur_queued(c)) {
       CK(cudaMemsetAsync(c->d_lq_count, 0, sizeof(int), c->st));
-      LAUNCH(c->K.g2p2_jcq[c->var_g2p2], c->nblk_p, 256, 0, pa);
+      LAUNCH(c->K.g2p2_jcq[c->var_g2p2], c->nblk_p, 256, G2P2_SMEM, pa);
       CK(cudaLaunchKernel(c->LK.queue, dim3(c->nsm), dim3(512), args, c->LK.sur_smem, c->st));
     } else if (c->learn_mode == MODE_SUR) {
       CK(cudaLaunchKernel(c->LK.sur, dim3((c->nblk_p + 1) / 2), dim3(512), args, c->LK.sur_smem, c->st));
@@ -1189,7 +1189,7 @@ int autotune(kmpm_ctx *c) {
       for (int v = 0; v < G2P_NVAR; v++) {
         void *fn = k == 0 ? c->K.g2p1_v[TL][v] : g2p2_variant(c, v);
         CK(cudaEventRecord(e0, c->st));
-        int r = launch(c, fn, dim3(c->nblk_p), dim3(256), 0, &pa);
+        int r = launch(c, fn, dim3(c->nblk_p), dim3(256), k == 0 ? G2P1_SMEM : G2P2_SMEM, &pa);
         if (r != KMPM_OK) return r;
         CK(cudaEventRecord(e1, c->st));
         CK(cudaEventSynchronize(e1));

@@ -151,6 +151,12 @@ struct StepKernels {
   void *g2p2_jcq[3];  // 3-D cubic TLMPM, linear EOS + Johnson-Cook, queueing plastic steps
 };
 constexpr int G2P_NVAR = 3;
+// node staging of the gathers (k_g2p1, k_g2p2): nodes of a block's stencil
+// bounding box copied into shared memory, and the dynamic shared memory of
+// the two kernels (v and v_update pairs; one (v, T) vector)
+constexpr int G2P_STAGE_NODES = 1024;
+constexpr int G2P1_SMEM = G2P_STAGE_NODES * 32;
+constexpr int G2P2_SMEM = G2P_STAGE_NODES * 16;
 constexpr int G2P1_MINB[G2P_NVAR] = {4, 3, 6};
 constexpr int G2P2_MINB[G2P_NVAR] = {3, 2, 4};
 

@@ -538,55 +538,153 @@ __device__ __forceinline__ int range_particle(const PartArgs &a, RangeDev &rd) {
   return p < rd.start + rd.count ? p : -1;
 }
 
+// ---- node staging of the gathers
+// Every 256-particle block of a gather kernel copies the nodes of the
+// bounding box of its particles' stencils from HBM into shared memory once
+// (zeros where the box leaves the grid), and each particle then reads its
+// stencil nodes there, at compile-time offsets from one base.  Particles are
+// sorted by (tile, cell), so a block's box is small (a block of a full 3-D
+// tile spans two cell layers: 5 x 7 x 7 nodes); a block whose box holds more
+// than G2P_STAGE_NODES nodes (it spans tiles far apart in the tile order)
+// gathers from global memory instead.  The 8 particles of one cell read the
+// same shared-memory words (broadcast), where the same loads through L1 had
+// been bound by its wavefront rate.
+// Block-wide bounding box [lo, lo + nb) of the stencil origins i0 of the
+// block's particles, widened by the stencil width S; false if the block has
+// no particle or the box holds more than cap nodes.  Every thread of the
+// block must call it (it synchronises the block).
+template <int DIM, int S>
+__device__ __forceinline__ bool stage_box(bool valid, const int (&i0)[3], int cap, int (&lo)[3], int (&nb)[3],
+                                          int &vol) {
+  __shared__ int red[8][6];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  int v[6];
+#pragma unroll
+  for (int d = 0; d < 3; d++) {
+    v[d] = valid ? i0[d] : INT_MAX;
+    v[3 + d] = valid ? -i0[d] : INT_MAX;  // min of -i0 = -max
+  }
+#pragma unroll
+  for (int k = 0; k < 6; k++) v[k] = __reduce_min_sync(0xffffffffu, v[k]);
+  if (lane == 0)
+#pragma unroll
+    for (int k = 0; k < 6; k++) red[warp][k] = v[k];
+  __syncthreads();
+#pragma unroll
+  for (int k = 0; k < 6; k++) {
+    int m = red[0][k];
+#pragma unroll
+    for (int w = 1; w < 8; w++) m = min(m, red[w][k]);
+    v[k] = m;
+  }
+  if (v[0] == INT_MAX) return false;
+  long long vv = 1;
+#pragma unroll
+  for (int d = 0; d < 3; d++) {
+    lo[d] = d < DIM ? v[d] : 0;
+    nb[d] = d < DIM ? -v[3 + d] - v[d] + S : 1;
+    vv *= nb[d];
+  }
+  vol = (int)min(vv, (long long)INT_MAX);
+  return vv <= cap;
+}
+
+// Box element e -> grid node (local index), or -1 outside the grid.
+__device__ __forceinline__ int stage_node(const GridDev &g, const int (&lo)[3], const int (&nb)[3], int e) {
+  const int c = e % nb[2], b = (e / nb[2]) % nb[1], a = e / (nb[1] * nb[2]);
+  const int ix = lo[0] + a, iy = lo[1] + b, iz = lo[2] + c;
+  if (ix < 0 || ix >= g.n[0] || iy < 0 || iy >= g.n[1] || iz < 0 || iz >= g.n[2]) return -1;
+  return (ix * g.n[1] + iy) * g.n[2] + iz;
+}
+
 // grid_to_points + advance_particles (src/solid.cpp:576-635, 786-790)
 // MINB: resident blocks per SM the register budget is set for (launch shape
-// picked per run by the autotuner, kmpm_api.cu)
+// picked per run by the autotuner, kmpm_api.cu).  Dynamic shared memory:
+// G2P_STAGE_NODES * 32 bytes (the staged v, v_update pairs).
 template <int DIM, int BASIS, bool TL, bool THERMAL, int MINB = 4>
 __global__ void __launch_bounds__(256, MINB) k_g2p1(PartArgs a) {
+  extern __shared__ __align__(16) float4 g2p_stage[];
   if (run_finished(a.scalars)) return;
   RangeDev rd;
   const int p = range_particle(a, rd);
-  if (p < 0) return;
+  const bool valid = p >= 0;
   float *P = *a.Pp;
   const GridDev g = a.grids[rd.grid];
   const StepScalars &sc = a.scalars[a.indep ? a.blk_range[blockIdx.x] : 0];
   const float dt = (float)sc.dt;
   const size_t ps = a.ps;
+  const int pl = valid ? p : rd.start;  // a thread without a particle evaluates a stand-in (never written)
   float xp[3], up[3];
 #pragma unroll
   for (int d = 0; d < 3; d++) {
-    up[d] = P[(PF_X + d) * ps + p];
-    xp[d] = P[(PF_X0 + d) * ps + p] + (TL ? 0.f : up[d]);
+    up[d] = P[(PF_X + d) * ps + pl];
+    xp[d] = P[(PF_X0 + d) * ps + pl] + (TL ? 0.f : up[d]);
   }
   PAxes<DIM, BASIS> ax;
   ax.eval(g, xp);
   constexpr int S = Stencil<BASIS>::S;
   constexpr int SY = DIM >= 2 ? S : 1, SZ = DIM == 3 ? S : 1;
-  // branch-free gather: per-axis node indices clamped into the grid (a node
-  // outside it has a zero value, so its clamped stand-in contributes nothing)
-  int cx[S], cy[SY], cz[SZ];
-#pragma unroll
-  for (int k = 0; k < S; k++) cx[k] = min(max(ax.ax[0].i0 + k, 0), g.n[0] - 1);
-#pragma unroll
-  for (int k = 0; k < SY; k++) cy[k] = min(max(ax.ax[1].i0 + k, 0), g.n[1] - 1);
-#pragma unroll
-  for (int k = 0; k < SZ; k++) cz[k] = min(max(ax.ax[2].i0 + k, 0), g.n[2] - 1);
   const float4 *__restrict__ NA = a.nodeA + NODE_STRIDE * g.node_off;  // v, v_update interleaved
-  float vu[3] = {0, 0, 0}, dv[3] = {0, 0, 0}, Tp = 0.f;
+  const int i0[3] = {ax.ax[0].i0, ax.ax[1].i0, ax.ax[2].i0};
+  int lo[3], nb[3], vol;
+  const bool staged = stage_box<DIM, S>(valid, i0, G2P_STAGE_NODES, lo, nb, vol);
+  if (staged) {
+    for (int e = threadIdx.x; e < vol; e += blockDim.x) {
+      const int n = stage_node(g, lo, nb, e);
+      float4 A = make_float4(0.f, 0.f, 0.f, 0.f), B = A;
+      if (n >= 0) ld_node_pair(NA + NODE_STRIDE * n, A, B);
+      g2p_stage[2 * e] = A;
+      g2p_stage[2 * e + 1] = B;
+    }
+    __syncthreads();
+  }
+  if (!valid) return;
+  float vu[3] = {0, 0, 0}, va[3] = {0, 0, 0}, Tp = 0.f;
+  if (staged) {
+    // stencil node (i, j, k) is box element base + (i nb1 + j) nb2 + k
+    const int base = ((i0[0] - lo[0]) * nb[1] + (i0[1] - lo[1])) * nb[2] + (i0[2] - lo[2]);
 #pragma unroll
-  for (int i = 0; i < S; i++) {
+    for (int i = 0; i < S; i++) {
 #pragma unroll
-    for (int j = 0; j < SY; j++) {
-      const float sxy = ax.ax[0].s[i] * ax.ax[1].s[j];
-      const int row = (cx[i] * g.n[1] + cy[j]) * g.n[2];
+      for (int j = 0; j < SY; j++) {
+        const float sxy = ax.ax[0].s[i] * ax.ax[1].s[j];
+        const float4 *row = g2p_stage + 2 * (base + (i * nb[1] + j) * nb[2]);
 #pragma unroll
-      for (int k = 0; k < SZ; k++) {
-        const float w = sxy * ax.ax[2].s[k];
-        float4 A, B;
-        ld_node_pair(NA + NODE_STRIDE * (row + cz[k]), A, B);
-        vu[0] += w * B.x; vu[1] += w * B.y; vu[2] += w * B.z;
-        dv[0] += w * (B.x - A.x); dv[1] += w * (B.y - A.y); dv[2] += w * (B.z - A.z);
-        if (THERMAL) Tp += w * B.w;
+        for (int k = 0; k < SZ; k++) {
+          const float w = sxy * ax.ax[2].s[k];
+          const float4 A = row[2 * k], B = row[2 * k + 1];
+          vu[0] = fmaf(w, B.x, vu[0]); vu[1] = fmaf(w, B.y, vu[1]); vu[2] = fmaf(w, B.z, vu[2]);
+          va[0] = fmaf(w, A.x, va[0]); va[1] = fmaf(w, A.y, va[1]); va[2] = fmaf(w, A.z, va[2]);
+          if (THERMAL) Tp = fmaf(w, B.w, Tp);
+        }
+      }
+    }
+  } else {
+    // branch-free gather from global memory: per-axis node indices clamped
+    // into the grid (a node outside it has a zero value, so its clamped
+    // stand-in contributes nothing)
+    int cx[S], cy[SY], cz[SZ];
+#pragma unroll
+    for (int k = 0; k < S; k++) cx[k] = min(max(i0[0] + k, 0), g.n[0] - 1);
+#pragma unroll
+    for (int k = 0; k < SY; k++) cy[k] = min(max(i0[1] + k, 0), g.n[1] - 1);
+#pragma unroll
+    for (int k = 0; k < SZ; k++) cz[k] = min(max(i0[2] + k, 0), g.n[2] - 1);
+#pragma unroll
+    for (int i = 0; i < S; i++) {
+#pragma unroll
+      for (int j = 0; j < SY; j++) {
+        const float sxy = ax.ax[0].s[i] * ax.ax[1].s[j];
+        const int row = (cx[i] * g.n[1] + cy[j]) * g.n[2];
+#pragma unroll
+        for (int k = 0; k < SZ; k++) {
+          const float w = sxy * ax.ax[2].s[k];
+          float4 A, B;
+          ld_node_pair(NA + NODE_STRIDE * (row + cz[k]), A, B);
+          vu[0] = fmaf(w, B.x, vu[0]); vu[1] = fmaf(w, B.y, vu[1]); vu[2] = fmaf(w, B.z, vu[2]);
+          va[0] = fmaf(w, A.x, va[0]); va[1] = fmaf(w, A.y, va[1]); va[2] = fmaf(w, A.z, va[2]);
+          if (THERMAL) Tp = fmaf(w, B.w, Tp);
+        }
       }
     }
   }
@@ -599,7 +697,9 @@ __global__ void __launch_bounds__(256, MINB) k_g2p1(PartArgs a) {
     // writes the moved displacement to PF_XN: this step's weights keep PF_X.
     const float v = P[(PF_V + d) * ps + p];
     // v = (1-alpha) v_update + alpha (v + dt a), with dt a = sum w (v_update - v)
-    const float vnew = (1.f - alpha) * vu[d] + alpha * (v + dv[d]);
+    // = sum w v_update - sum w v
+    const float dv = vu[d] - va[d];
+    const float vnew = (1.f - alpha) * vu[d] + alpha * (v + dv);
     if (TL) P[(PF_X + d) * ps + p] = up[d] + dt * vu[d];
     else {
       // ASFLIP moves the particle with the blended velocity
@@ -619,6 +719,77 @@ __global__ void __launch_bounds__(256, MINB) k_g2p1(PartArgs a) {
   }
 }
 
+// Node sources of the velocity-gradient gather: (v, T) of stencil node
+// (i, j, k) from the staged box in shared memory or from global memory
+// (clamped indices).
+struct GradFetchStage {
+  const float4 *st;
+  int base, nb1, nb2;
+  __device__ __forceinline__ int row(int i, int j, int) const { return base + (i * nb1 + j) * nb2; }
+  __device__ __forceinline__ float4 at(int row, int k) const { return st[row + k]; }
+};
+template <int S, bool THERMAL> struct GradFetchGlobal {
+  const float4 *NV;   // v (or v_update) of the grid's nodes, stride NODE_STRIDE
+  const float *NT;    // nodal T of the grid (thermal, not use_vu)
+  int cx[S], cy[S], cz[S], n1, n2;
+  bool use_vu;
+  __device__ __forceinline__ int row(int i, int j, int) const { return (cx[i] * n1 + cy[j]) * n2; }
+  __device__ __forceinline__ float4 at(int row, int k) const {
+    float4 V = __ldg(NV + NODE_STRIDE * (row + cz[k]));
+    if (THERMAL && !use_vu) V.w = NT[row + cz[k]];
+    return V;
+  }
+};
+
+// Sum-factorised gradient gather over the z slots: for every (i, j),
+// A = sum_k s_z V and B = sum_k ds_z V, then grad v += (ds_x s_y A,
+// s_x ds_y A, s_x s_y B) (dropped pairs add 0: see Axis::eval).  Also the
+// thermal gradient (qg -= grad T) and, in 2-D, sum w v_r.
+template <int DIM, int BASIS, bool THERMAL, typename F>
+__device__ __forceinline__ void grad_gather(const PAxes<DIM, BASIS> &ax, const F &f, float (&G)[9], float (&qg)[3],
+                                            float &vr) {
+  constexpr int S = Stencil<BASIS>::S;
+  constexpr int SY = DIM >= 2 ? S : 1, SZ = DIM == 3 ? S : 1;
+#pragma unroll
+  for (int i = 0; i < S; i++) {
+    const float sx = ax.ax[0].s[i], dsx = ax.ax[0].ds[i];
+#pragma unroll
+    for (int j = 0; j < SY; j++) {
+      const float sy = ax.ax[1].s[j], dsy = ax.ax[1].ds[j];
+      const int row = f.row(i, j, 0);
+      float A[3] = {0.f, 0.f, 0.f}, B[3] = {0.f, 0.f, 0.f}, AT = 0.f, BT = 0.f;
+#pragma unroll
+      for (int k = 0; k < SZ; k++) {
+        const float sz = ax.ax[2].s[k], dsz = ax.ax[2].ds[k];
+        const float4 V = f.at(row, k);
+        const float vn[3] = {V.x, V.y, V.z};
+#pragma unroll
+        for (int r = 0; r < DIM; r++) {
+          A[r] += sz * vn[r];
+          if (DIM == 3) B[r] += dsz * vn[r];
+        }
+        if (THERMAL) {
+          AT += sz * V.w;
+          if (DIM == 3) BT += dsz * V.w;
+        }
+      }
+      const float sxy = sx * sy, gx = dsx * sy, gy = sx * dsy;
+#pragma unroll
+      for (int r = 0; r < DIM; r++) {
+        G[3 * r] += gx * A[r];
+        if (DIM >= 2) G[3 * r + 1] += gy * A[r];
+        if (DIM == 3) G[3 * r + 2] += sxy * B[r];
+      }
+      if (DIM == 2) vr += sxy * A[0];  // sum w v_r (axisymmetric hoop rate)
+      if (THERMAL) {
+        qg[0] -= gx * AT;
+        qg[1] -= gy * AT;
+        qg[2] -= sxy * BT;
+      }
+    }
+  }
+}
+
 // rate of deformation + deformation gradient + stress + wave speed
 // (src/solid.cpp:798-936, 1155-1438)
 // QUEUE: also append every plastic step (undamaged particle) to the learned
@@ -626,14 +797,40 @@ __global__ void __launch_bounds__(256, MINB) k_g2p1(PartArgs a) {
 template <int DIM, int BASIS, bool TL, bool THERMAL, int PREC, int MINB = 3, int LAW = LAW_ANY, bool QUEUE = false>
 __global__ void __launch_bounds__(256, MINB) k_g2p2(PartArgs a) {
   __shared__ float red_c[256], red_h[256];
+  extern __shared__ __align__(16) float4 g2p_stage[];  // G2P_STAGE_NODES (v, T) of the staged box
   if (run_finished(a.scalars)) return;
   RangeDev rd;
-  const int p = range_particle(a, rd);
+  const int p0 = range_particle(a, rd);
+  const bool valid = p0 >= 0;
+  const int p = valid ? p0 : rd.start;  // a thread without a particle evaluates a stand-in (never written)
   float my_c = 0.f, my_h = 1.f;
-  if (p >= 0) {
-    float *P = *a.Pp;
-    const size_t ps = a.ps;
-    const GridDev g = a.grids[rd.grid];
+  float *P = *a.Pp;
+  const size_t ps = a.ps;
+  const GridDev g = a.grids[rd.grid];
+  float xp[3];
+#pragma unroll
+  for (int d = 0; d < 3; d++) xp[d] = P[(PF_X0 + d) * ps + p] + (TL ? 0.f : P[(PF_X + d) * ps + p]);
+  PAxes<DIM, BASIS> ax;
+  ax.eval(g, xp);
+  constexpr int S = Stencil<BASIS>::S;
+  constexpr int SY = DIM >= 2 ? S : 1, SZ = DIM == 3 ? S : 1;
+  const int i0[3] = {ax.ax[0].i0, ax.ax[1].i0, ax.ax[2].i0};
+  int lo[3], nb[3], vol;
+  const bool staged = stage_box<DIM, S>(valid, i0, G2P_STAGE_NODES, lo, nb, vol);
+  const float4 *__restrict__ NV = (a.use_vu ? a.nodeB : a.nodeA) + NODE_STRIDE * g.node_off;
+  if (staged) {
+    for (int e = threadIdx.x; e < vol; e += blockDim.x) {
+      const int n = stage_node(g, lo, nb, e);
+      float4 V = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (n >= 0) {
+        V = __ldg(NV + NODE_STRIDE * n);
+        if (THERMAL && !a.use_vu) V.w = a.nodeT[g.node_off + n];
+      }
+      g2p_stage[e] = V;
+    }
+    __syncthreads();
+  }
+  if (valid) {
     const int mi = rd.mat >= 0 ? rd.mat : a.solid_mat[__float_as_int(P[PF_SID * ps + p])];
     const MatDev &m = a.mats[mi];
     const StepScalars &sc = a.scalars[a.indep ? a.blk_range[blockIdx.x] : 0];
@@ -653,13 +850,6 @@ __global__ void __launch_bounds__(256, MINB) k_g2p2(PartArgs a) {
         asm volatile("{ .reg .u64 ad; mad.lo.u64 ad, %1, %2, %0; prefetch.global.L2 [ad]; }" ::"l"(base),
                      "l"(row_bytes), "l"((unsigned long long)r));
     }
-    float xp[3];
-#pragma unroll
-    for (int d = 0; d < 3; d++) xp[d] = P[(PF_X0 + d) * ps + p] + (TL ? 0.f : P[(PF_X + d) * ps + p]);
-    PAxes<DIM, BASIS> ax;
-    ax.eval(g, xp);
-    constexpr int S = Stencil<BASIS>::S;
-    constexpr int SY = DIM >= 2 ? S : 1, SZ = DIM == 3 ? S : 1;
     if ((BASIS == 0 || BASIS == 1 || BASIS == 3) && a.apic) {
       // APIC (compute_rate_deformation_gradient_{TL,UL}_APIC,
       // src/solid.cpp:1006-1153): grad v = sum w v_node (x_node - x_p)^T Di with
@@ -683,57 +873,27 @@ __global__ void __launch_bounds__(256, MINB) k_g2p2(PartArgs a) {
     float G[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
     float qg[3] = {0, 0, 0};
     float vr = 0.f;
-    // branch-free gather (clamped indices, see k_g2p1); a pair with a zero
-    // weight is dropped as in the reference, so its slope is masked too
-    int cx[S], cy[SY], cz[SZ];
+    // the staged box in shared memory, or global memory with clamped indices
+    // (see k_g2p1); a pair with a zero weight is dropped as in the
+    // reference, so its slope is masked too
+    if (staged) {
+      GradFetchStage f{g2p_stage, ((i0[0] - lo[0]) * nb[1] + (i0[1] - lo[1])) * nb[2] + (i0[2] - lo[2]), nb[1],
+                       nb[2]};
+      grad_gather<DIM, BASIS, THERMAL>(ax, f, G, qg, vr);
+    } else {
+      GradFetchGlobal<S, THERMAL> f;
+      f.NV = NV;
+      f.NT = a.nodeT + g.node_off;
+      f.n1 = g.n[1];
+      f.n2 = g.n[2];
+      f.use_vu = a.use_vu != 0;
 #pragma unroll
-    for (int k = 0; k < S; k++) cx[k] = min(max(ax.ax[0].i0 + k, 0), g.n[0] - 1);
-#pragma unroll
-    for (int k = 0; k < SY; k++) cy[k] = min(max(ax.ax[1].i0 + k, 0), g.n[1] - 1);
-#pragma unroll
-    for (int k = 0; k < SZ; k++) cz[k] = min(max(ax.ax[2].i0 + k, 0), g.n[2] - 1);
-    const float4 *__restrict__ NV = (a.use_vu ? a.nodeB : a.nodeA) + NODE_STRIDE * g.node_off;
-    // sum factorisation over the z slots: for every (i, j), A = sum_k s_z V
-    // and B = sum_k ds_z V, then grad v += (ds_x s_y A, s_x ds_y A, s_x s_y B)
-    // (dropped pairs add 0: see Axis::eval)
-#pragma unroll
-    for (int i = 0; i < S; i++) {
-      const float sx = ax.ax[0].s[i], dsx = ax.ax[0].ds[i];
-#pragma unroll
-      for (int j = 0; j < SY; j++) {
-        const float sy = ax.ax[1].s[j], dsy = ax.ax[1].ds[j];
-        const int row = (cx[i] * g.n[1] + cy[j]) * g.n[2];
-        float A[3] = {0.f, 0.f, 0.f}, B[3] = {0.f, 0.f, 0.f}, AT = 0.f, BT = 0.f;
-#pragma unroll
-        for (int k = 0; k < SZ; k++) {
-          const float sz = ax.ax[2].s[k], dsz = ax.ax[2].ds[k];
-          const float4 V = __ldg(NV + NODE_STRIDE * (row + cz[k]));
-          const float vn[3] = {V.x, V.y, V.z};
-#pragma unroll
-          for (int r = 0; r < DIM; r++) {
-            A[r] += sz * vn[r];
-            if (DIM == 3) B[r] += dsz * vn[r];
-          }
-          if (THERMAL) {
-            const float Tn = a.use_vu ? V.w : a.nodeT[g.node_off + row + cz[k]];
-            AT += sz * Tn;
-            if (DIM == 3) BT += dsz * Tn;
-          }
-        }
-        const float sxy = sx * sy, gx = dsx * sy, gy = sx * dsy;
-#pragma unroll
-        for (int r = 0; r < DIM; r++) {
-          G[3 * r] += gx * A[r];
-          if (DIM >= 2) G[3 * r + 1] += gy * A[r];
-          if (DIM == 3) G[3 * r + 2] += sxy * B[r];
-        }
-        if (DIM == 2) vr += sxy * A[0];  // sum w v_r (axisymmetric hoop rate)
-        if (THERMAL) {
-          qg[0] -= gx * AT;
-          qg[1] -= gy * AT;
-          qg[2] -= sxy * BT;
-        }
+      for (int k = 0; k < S; k++) {
+        f.cx[k] = min(max(i0[0] + k, 0), g.n[0] - 1);
+        f.cy[k] = SY > 1 ? min(max(i0[1] + k, 0), g.n[1] - 1) : 0;
+        f.cz[k] = SZ > 1 ? min(max(i0[2] + k, 0), g.n[2] - 1) : 0;
       }
+      grad_gather<DIM, BASIS, THERMAL>(ax, f, G, qg, vr);
     }
     if (DIM == 2 && a.axisym) {
       // Fdot(2,2) / L(2,2) += sum w v_r / r, r = x0_r (TL) or the x_r of the
