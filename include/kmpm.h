@@ -370,24 +370,27 @@ int kmpm_surrogate_stats(struct kmpm_ctx *ctx, long long out[4]);
 
 /* Nodal mass without device allocation.  No counterpart in the reference.
  *
- * For callers that may not allocate device memory at the point where they
- * need nodal masses: code running while a CUDA graph is being captured
- * (cudaMalloc is not permitted during capture), or an application whose
- * device memory belongs entirely to its own pool and budget.  The caller
+ * For host applications that own all of their GPU memory through their own
+ * pool allocator and budget: they reserve the device memory up front and may
+ * not call cudaMalloc behind the pool's back (the call could fail once the
+ * pool holds the memory, and it would escape their accounting).  The caller
  * passes device buffers: x (n*3 floats, x y z per particle), mass (n floats)
  * and node_mass (one float per node of the grid described by lo, cellsize,
- * nnodes and nglobal, as in kmpm_add_grid); the result is what
- * Solid::compute_mass_nodes (src/solid.cpp:317-335) computes, by the same
- * deterministic scatter that kmpm_run uses.  Nothing is allocated: every
- * intermediate array lives in one fixed-size device array of
- * KMPM_NOALLOC_SCRATCH_BYTES that every GPU loading this library holds until
- * the process exits.  Limits: at most KMPM_NOALLOC_MAX_PARTICLES particles and
- * KMPM_NOALLOC_MAX_CELLS binning cells (larger problems return KMPM_ERR_ARG
- * with a message in err).  The first call on a device looks up that array's
- * device address: make it outside any stream capture.  Calls share the array;
- * two calls that overlap on the GPU race on it.  Work is queued on `stream`
- * (a cudaStream_t, may be 0); err (errlen bytes, may be NULL) receives the
- * message of a failure. */
+ * nnodes and nglobal, as in kmpm_add_grid; basis 0-3 as KMPM_BASIS_*); the
+ * result is what Solid::compute_mass_nodes (src/solid.cpp:317-335) computes,
+ * by the same deterministic scatter that kmpm_run uses, bit for bit.  Nothing
+ * is allocated: every intermediate array lives in one fixed-size device array
+ * of KMPM_NOALLOC_SCRATCH_BYTES that every GPU loading this library holds
+ * until the process exits.  Limits: at most KMPM_NOALLOC_MAX_PARTICLES
+ * particles and KMPM_NOALLOC_MAX_CELLS binning cells (larger problems return
+ * KMPM_ERR_ARG with a message in err).  A particle outside the grid's cells
+ * (or with a non-finite coordinate) makes the call return
+ * KMPM_ERR_LEFT_DOMAIN, and node_mass is then not meaningful.  Work is queued
+ * on `stream` (a cudaStream_t, may be 0), and the call returns once that work
+ * has finished, because the status depends on it.  The first call on a device
+ * looks up that array's device address: make it before any stream capture.
+ * Calls share the array; two calls that overlap on the GPU race on it.  err
+ * (errlen bytes, may be NULL) receives the message of a failure. */
 #define KMPM_NOALLOC_MAX_PARTICLES 131072
 #define KMPM_NOALLOC_MAX_CELLS 262144
 #define KMPM_NOALLOC_SCRATCH_BYTES (24u << 20)

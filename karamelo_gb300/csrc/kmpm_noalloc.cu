@@ -2,20 +2,21 @@
 // (Solid::compute_mass_nodes, src/solid.cpp:317-335) for callers that cannot
 // allocate device memory.
 //
-// Some hosts may not call cudaMalloc at the point where they need nodal
-// masses: code that runs while a CUDA graph is being captured (allocation is
-// not allowed during capture), or an embedding application whose device
-// memory is entirely owned by its own pool and budget.  This entry point takes
-// the caller's input and output buffers and keeps every intermediate array
-// (binning keys, sort buffers, cell and tile ranges, the scatter's tile
-// partials) in one file-scope device array of fixed size instead.
+// Some host applications own all of their GPU memory through their own pool
+// allocator and budget: they reserve the device memory up front and may not
+// call cudaMalloc behind the pool's back (the call could fail once the pool
+// holds the memory, and it would escape their accounting).  This entry point
+// takes the caller's input and output buffers and keeps every intermediate
+// array (binning keys, sort buffers, cell and tile ranges, the scatter's tile
+// partials, an error counter) in one file-scope device array of fixed size
+// instead.
 //
 // Properties of that array:
 //   - it has a fixed size (KMPM_NOALLOC_SCRATCH_BYTES) and exists on every
 //     GPU that loads this library until the process exits;
 //   - its device address is looked up once per device, with that device
 //     current, by the first call made on that device: make that first call
-//     outside any stream capture;
+//     before any stream capture;
 //   - all calls share it and it keeps the last call's contents, so this code
 //     clears whatever must start at zero; two calls whose work overlaps on the
 //     GPU (different streams, no ordering between them) race on it.
@@ -49,18 +50,24 @@ struct Carve {
   }
 };
 
-// keys of the caller's particles (caller order); x is n*3 floats (x,y,z per particle)
-__global__ void k_na_keys(const float *x, int n, const GridDev *gp, int dim, int t0, int t1, int t2, int *keys,
-                          int *vals) {
+// keys of the caller's particles (caller order); x is n*3 floats (x,y,z per
+// particle).  A particle outside the grid's cells (or with a non-finite
+// coordinate) is counted in *bad: its cell index is clamped only so that every
+// access stays in bounds, and the call reports the count as an error.
+__global__ void k_na_keys(const float *x, int n, const GridDev g, int dim, int t0, int t1, int t2, int *keys,
+                          int *vals, int *bad) {
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= n) return;
-  const GridDev g = *gp;
   const int T[3] = {t0, t1, t2};
   int c[3] = {0, 0, 0};
+  bool inside = true;
   for (int d = 0; d < dim; d++) {
-    int cd = (int)((x[3 * p + d] - g.lo[d]) * g.inv_cellsize);
+    const float t = (x[3 * p + d] - g.lo[d]) * g.inv_cellsize;
+    inside = inside && t >= 0.f && t < (float)g.ncell[d];
+    const int cd = (int)fminf(fmaxf(t, 0.f), (float)(g.ncell[d] - 1));
     c[d] = max(0, min(cd, g.ncell[d] - 1));
   }
+  if (!inside) atomicAdd(bad, 1);
   const int tl = ((c[0] / T[0]) * g.ntile[1] + c[1] / T[1]) * g.ntile[2] + c[2] / T[2];
   const int lc = ((c[0] % T[0]) * T[1] + c[1] % T[1]) * T[2] + c[2] % T[2];
   keys[p] = tl * (T[0] * T[1] * T[2]) + lc;
@@ -81,7 +88,11 @@ __global__ void k_na_tiles(int2 *tiles, int ntiles) {
   if (t < ntiles) tiles[t] = make_int2(0, t);
 }
 
-__global__ void k_na_init(float **pp, float *P, StepScalars *sc) {
+// The grid description arrives by value (a kernel argument), so no host
+// memory is read once the call has returned.
+__global__ void k_na_init(GridDev gv, GridDev *gd, float **pp, float *P, StepScalars *sc, int *bad) {
+  *gd = gv;
+  *bad = 0;
   pp[0] = P;
   pp[1] = P;
   sc->dt = 0;
@@ -113,7 +124,7 @@ template <int DIM, int BASIS> struct NaKernels {
 };
 
 void na_kernels(int dim, int basis, void **p2g, void **grid) {
-  switch (dim * 3 + basis) {
+  switch (basis == 3 ? 100 + dim : dim * 3 + basis) {
     case 3: *p2g = NaKernels<1, 0>::p2g(); *grid = NaKernels<1, 0>::grid(); break;
     case 4: *p2g = NaKernels<1, 1>::p2g(); *grid = NaKernels<1, 1>::grid(); break;
     case 5: *p2g = NaKernels<1, 2>::p2g(); *grid = NaKernels<1, 2>::grid(); break;
@@ -122,7 +133,11 @@ void na_kernels(int dim, int basis, void **p2g, void **grid) {
     case 8: *p2g = NaKernels<2, 2>::p2g(); *grid = NaKernels<2, 2>::grid(); break;
     case 9: *p2g = NaKernels<3, 0>::p2g(); *grid = NaKernels<3, 0>::grid(); break;
     case 10: *p2g = NaKernels<3, 1>::p2g(); *grid = NaKernels<3, 1>::grid(); break;
-    default: *p2g = NaKernels<3, 2>::p2g(); *grid = NaKernels<3, 2>::grid(); break;
+    case 11: *p2g = NaKernels<3, 2>::p2g(); *grid = NaKernels<3, 2>::grid(); break;
+    // quadratic B-spline (basis 3): dim 1, 2, 3
+    case 101: *p2g = NaKernels<1, 3>::p2g(); *grid = NaKernels<1, 3>::grid(); break;
+    case 102: *p2g = NaKernels<2, 3>::p2g(); *grid = NaKernels<2, 3>::grid(); break;
+    default: *p2g = NaKernels<3, 3>::p2g(); *grid = NaKernels<3, 3>::grid(); break;
   }
 }
 
@@ -143,7 +158,7 @@ extern "C" int kmpm_p2g_mass_noalloc(const float *x, const float *mass, int n, i
                                      double cellsize, const int nnodes[3], const int nglobal[3], float *node_mass,
                                      void *stream, char *err, int errlen) {
   if (!x || !mass || !node_mass || !lo || !nnodes || !nglobal || n < 0 || dim < 1 || dim > 3 || basis < 0 ||
-      basis > 2 || !(cellsize > 0))
+      basis > 3 || !(cellsize > 0))
     return set_err(err, errlen, KMPM_ERR_ARG, "kmpm_p2g_mass_noalloc: bad argument");
   if (n > KMPM_NOALLOC_MAX_PARTICLES)
     return set_err(err, errlen, KMPM_ERR_ARG, "kmpm_p2g_mass_noalloc: more particles than KMPM_NOALLOC_MAX_PARTICLES");
@@ -195,6 +210,7 @@ extern "C" int kmpm_p2g_mass_noalloc(const float *x, const float *mass, int n, i
   float **pp = cv.take<float *>(base, 2);
   StepScalars *sc = cv.take<StepScalars>(base, 1);
   GridDev *gd = cv.take<GridDev>(base, 1);
+  int *bad = cv.take<int>(base, 1);
   float *P = cv.take<float>(base, ps * (PF_MASS + 1));
   int *keys = cv.take<int>(base, n + 1), *vals = cv.take<int>(base, n + 1);
   RadixTemp rt{};
@@ -214,15 +230,14 @@ extern "C" int kmpm_p2g_mass_noalloc(const float *x, const float *mass, int n, i
     cudaError_t e_ = (call);                                                        \
     if (e_ != cudaSuccess) return set_err(err, errlen, KMPM_ERR_CUDA, cudaGetErrorString(e_)); \
   } while (0)
-  NA_CK(cudaMemcpyAsync(gd, &g, sizeof(GridDev), cudaMemcpyHostToDevice, st));
-  k_na_init<<<1, 1, 0, st>>>(pp, P, sc);
+  k_na_init<<<1, 1, 0, st>>>(g, gd, pp, P, sc, bad);
   // the previous call's cell and tile ranges must not leak into this one
   NA_CK(cudaMemsetAsync(cs, 0, sizeof(int) * ncells, st));
   NA_CK(cudaMemsetAsync(ce, 0, sizeof(int) * ncells, st));
   NA_CK(cudaMemsetAsync(ts, 0, sizeof(int) * ntiles, st));
   NA_CK(cudaMemsetAsync(te, 0, sizeof(int) * ntiles, st));
   if (n > 0) {
-    k_na_keys<<<(n + 255) / 256, 256, 0, st>>>(x, n, gd, dim, t[0], t[1], t[2], keys, vals);
+    k_na_keys<<<(n + 255) / 256, 256, 0, st>>>(x, n, g, dim, t[0], t[1], t[2], keys, vals, bad);
     int key_bits = 1;
     while ((1LL << key_bits) < ncells) key_bits++;
     radix_sort(keys, vals, n, key_bits, rt, st);
@@ -263,6 +278,16 @@ extern "C" int kmpm_p2g_mass_noalloc(const float *x, const float *mass, int n, i
     NA_CK(cudaLaunchKernel(kgrid, dim3((unsigned)((nn + 255) / 256)), dim3(256), args, 0, st));
   }
   NA_CK(cudaGetLastError());
+  // the count of particles outside the grid decides the status: wait for the
+  // work and read it back (a four-byte copy into this stack frame)
+  int nbad = 0;
+  NA_CK(cudaMemcpyAsync(&nbad, bad, sizeof(int), cudaMemcpyDeviceToHost, st));
+  NA_CK(cudaStreamSynchronize(st));
 #undef NA_CK
+  if (nbad > 0) {
+    char msg[160];
+    std::snprintf(msg, sizeof msg, "kmpm_p2g_mass_noalloc: %d particle(s) outside the grid's cells", nbad);
+    return set_err(err, errlen, KMPM_ERR_LEFT_DOMAIN, msg);
+  }
   return KMPM_OK;
 }
