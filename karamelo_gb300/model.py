@@ -28,7 +28,10 @@ counterpart of the reference's ``error->all`` / ``error->one``.
 """
 from __future__ import annotations
 
-from typing import Callable, Dict, Optional
+import functools
+import inspect
+import math
+from typing import Callable, Dict, List, Optional
 
 import numpy as np
 
@@ -61,6 +64,92 @@ def _coef(value) -> np.ndarray:
     return np.array([float(value), 0.0, 0.0, 0.0])
 
 
+def exact_literal(x: float) -> str:
+    """``x`` written in Karamelo's input language so that its parser yields
+    exactly this double.  The parser reads each numeric literal with ``stof``
+    (single precision, src/input.cpp:405-411) and then evaluates in double,
+    so a literal such as 0.8 would arrive as 0.800000011920929.  Here x =
+    M 2^E with an integer M < 2^53 is written as a sum of 24-bit pieces of M
+    scaled by powers of two; every literal is exact in single precision and
+    every operation is exact in double."""
+    x = float(x)
+    if not math.isfinite(x):
+        raise ValueError(f"non-finite script literal {x}")
+    if x == 0.0:
+        return "0"
+    if x == int(x) and abs(x) < 2 ** 24:
+        return str(int(x)) if x > 0 else f"(0-{int(-x)})"
+    m, e = math.frexp(abs(x))
+    M, E = int(m * 2 ** 53), e - 53
+    while M % 2 == 0:
+        M //= 2
+        E += 1
+    a, rem = divmod(M, 2 ** 48)
+    b, c = divmod(rem, 2 ** 24)
+    terms = []
+    if a:
+        terms.append(f"{a}*{2 ** 48}")
+    if b:
+        terms.append(f"{b}*{2 ** 24}")
+    if c:
+        terms.append(str(c))
+    body = "(" + "+".join(terms) + ")"
+    # scale by 2^E in factors of at most 2^100 (each a power of two, exact in single precision)
+    while E < 0:
+        k = min(-E, 100)
+        body = f"({body}/{2 ** k})"
+        E += k
+    while E > 0:
+        k = min(E, 100)
+        body = f"({body}*{2 ** k})"
+        E -= k
+    return body if x > 0 else f"(0-{body})"
+
+
+def script_arg(v) -> str:
+    """One command argument in Karamelo's input language."""
+    if v is None:
+        return "NULL"
+    if isinstance(v, TimeFn):
+        c0, c1, c2, c3 = (float(t) for t in v.c)
+        return (f"{exact_literal(c0)}+{exact_literal(c1)}*time+"
+                f"{exact_literal(c2)}*exp({exact_literal(c3)}*time)")
+    if isinstance(v, (bool, np.bool_)):
+        return "true" if v else "false"
+    if isinstance(v, (int, np.integer, float, np.floating)):
+        return exact_literal(float(v))
+    if v in ("-INF", "+INF"):
+        # the reference's block region takes INF for every bound (a lower
+        # bound reads it as -BIG) but rejects -INF for zlo (src/region_block.cpp:102)
+        return "INF"
+    return str(v)
+
+
+def _command(fn):
+    """Marks a script command: besides running it, the call is recorded as a
+    line of Karamelo's input language (``MPM.script``), so that the reference
+    itself can run the same sequence of commands."""
+    sig = inspect.signature(fn)
+
+    @functools.wraps(fn)
+    def wrapper(self, *args):
+        bound = sig.bind(self, *args)
+        vals = []
+        for name, par in list(sig.parameters.items())[1:]:
+            if par.kind == inspect.Parameter.VAR_POSITIONAL:
+                vals.extend(bound.arguments.get(name, ()))
+            elif name in bound.arguments:
+                vals.append(bound.arguments[name])
+            elif fn.__name__ == "solid" and name == "T0":
+                vals.append(par.default)  # the reference's solid() takes T0 explicitly
+        if fn.__name__ == "method" and vals and isinstance(vals[0], str) and vals[0].endswith("/gpu"):
+            vals[0] = vals[0][:-4]
+        self.script.append(f"{fn.__name__}({', '.join(script_arg(v) for v in vals)})")
+        return fn(self, *args)
+
+    return wrapper
+
+
 _SUPPORTED_FIXES = ("velocity_nodes", "body_force", "initial_velocity_particles", "kinetic_energy", "strain_energy")
 
 
@@ -85,8 +174,11 @@ class MPM:
         self.method_set = False
         self.dim_set = False
         self.ntimestep = 0
+        # the commands so far, in Karamelo's input language (see _command)
+        self.script: List[str] = []
 
     # ------------------------------------------------------------ method/scheme
+    @_command
     def method(self, style: str, sub: str, basis: str = "linear", *rest):
         """``method()``: Update::create_method, src/update.cpp:108-196."""
         base = style[:-4] if style.endswith("/gpu") else style
@@ -140,6 +232,7 @@ class MPM:
             raise KarameloError("Illegal method command: too many arguments")
         self.method_set = True
 
+    @_command
     def scheme(self, style: str):
         """``scheme()``: Update::create_scheme, src/update.cpp:83-102 (default MUSL)."""
         base = style[:-4] if style.endswith("/gpu") else style
@@ -152,16 +245,19 @@ class MPM:
         else:
             raise KarameloError(f"Illegal scheme style {style}: usl, musl or usf")
 
+    @_command
     def set_dt(self, dt):
         """Update::set_dt, src/update.cpp:58-65."""
         self.s.dt = float(dt)
         self.s.dt_constant = True
 
+    @_command
     def dt_factor(self, f):
         """Update::set_dt_factor, src/update.cpp:51-56."""
         self.s.dt_factor = float(f)
 
     # ------------------------------------------------------------ domain/regions
+    @_command
     def dimension(self, dim, *args):
         """Domain::set_dimension, src/domain.cpp:496-551."""
         if not self.method_set:
@@ -183,6 +279,7 @@ class MPM:
             self.s.grids.append(sc.grid_geometry(dim, self.s.basis, lo, hi, self.subhi, self.cellsize))
         self.dim_set = True
 
+    @_command
     def axisymmetric(self, flag):
         """``axisymmetric(true|false)``: Domain::set_axisymmetric,
         src/domain.cpp:558-570.  Solids created afterwards get masses and
@@ -195,6 +292,7 @@ class MPM:
             raise KarameloError("axisymmetric runs on the GPU path are 2-D and mechanical")
         self.s.axisymmetric = on
 
+    @_command
     def region(self, name, kind, *args):
         """``region()``: Domain::add_region; block regions grow the box
         (src/region_block.cpp:45-120)."""
@@ -203,6 +301,7 @@ class MPM:
         self.regions[name] = make_region(kind, args, self.s.dim, self.s.boxlo, self.s.boxhi, len(self.regions))
 
     # ------------------------------------------------------------ materials
+    @_command
     def eos(self, name, kind, *p):
         """``eos()``: src/eos_linear.cpp, src/eos_shock.cpp, src/eos_fluid.cpp."""
         n = {"linear": 2, "shock": 9, "fluid": 3}
@@ -213,6 +312,7 @@ class MPM:
         self.eoses[name] = ({"linear": sc.EOS_LINEAR, "shock": sc.EOS_SHOCK, "fluid": sc.EOS_FLUID}[kind],
                             [float(x) for x in p[: n[kind]]])
 
+    @_command
     def strength(self, name, kind, *p):
         """``strength()``: src/strength_*.cpp."""
         n = {"linear": 1, "plastic": 2, "johnson_cook": 9, "swift": 5, "fluid": 1}
@@ -227,6 +327,7 @@ class MPM:
             raise KarameloError("Error: reference temperature Tr equals melting temperature Tm")
         self.strengths[name] = (code[kind], vals)
 
+    @_command
     def damage(self, name, kind, *p):
         """``damage()``: src/damage_jc.cpp:32-89."""
         if kind != "damage_johnson_cook":
@@ -235,6 +336,7 @@ class MPM:
             raise KarameloError("damage_johnson_cook: too few arguments")
         self.damages[name] = (sc.DAMAGE_JC, [float(x) for x in p[:8]])
 
+    @_command
     def temperature(self, name, kind, *p):
         """``temperature()``: src/temperature_plastic_work.cpp:20-57."""
         if kind != "plastic_work":
@@ -243,6 +345,7 @@ class MPM:
             raise KarameloError("plastic_work: wrong number of arguments")
         self.temperatures[name] = (sc.TEMP_PLASTIC_WORK, [float(x) for x in p])
 
+    @_command
     def material(self, name, kind, *p):
         """Material::add_material, src/material.cpp:249-380."""
         if name in self.material_ids:
@@ -285,6 +388,7 @@ class MPM:
         self.material_ids[name] = len(self.s.materials) - 1
 
     # ------------------------------------------------------------ solids
+    @_command
     def solid(self, name, kind, region, ppc, mat, cellsize, T0=0.0):
         """``solid(id, region, region_id, ppc1d, mat, cellsize, T0)``:
         Solid::Solid + Solid::populate, src/solid.cpp:59-163, 1810-2336."""
@@ -375,6 +479,7 @@ class MPM:
         self.solid_ids[name] = len(self.s.solids) - 1
 
     # ------------------------------------------------------------ groups/fixes
+    @_command
     def group(self, name, pon, kind, region, sel="all", *solids):
         """Group::assign, src/group.cpp:65-238 (region match on x0)."""
         if pon not in ("particles", "nodes"):
@@ -394,6 +499,7 @@ class MPM:
                 masks[si] = reg.match(g.node_positions(self.s.dim))
         self.groups[name] = dict(pon=pon, solid=-1 if sel == "all" else targets[-1], masks=masks)
 
+    @_command
     def fix(self, name, kind, group, *vals):
         """Modify::add_fix for the fixes the GPU method lowers; any other fix is an error
         (the GPU path has no CPU fallback)."""
@@ -474,12 +580,14 @@ class MPM:
                 self.backend = GpuBackend(self.s)
         return self.backend
 
+    @_command
     def run(self, n):
         """Run::command, src/run.cpp:32-57."""
         b = self._ensure_backend()
         b.run(int(n))
         self.ntimestep += int(n)
 
+    @_command
     def run_time(self, t):
         """RunTime::command, src/run_time.cpp:30-60."""
         b = self._ensure_backend()

@@ -326,3 +326,39 @@ def vertical_bar_tip(sim, x=None):
     xs = x0 if x is None else x
     m = s.mass[sel]
     return (m[:, None] * xs[sel]).sum(0) / m.sum()
+
+
+def block_bar(f, method, strength, eos="linear", thermal=False, damage=None, basis="cubic-spline",
+               scheme="musl", v0=100.0, mat_kind="eos-strength"):
+    """Small 3-D bar (2 x 1.2 x 1.2 mm, cellsize 0.4) hitting a wall, with the
+    given strength / EOS / temperature laws (units GPa, mm, ms)."""
+    sim = MPM(f)
+    extra = ["thermo-mechanical"] if thermal else []
+    sim.method(method, "FLIP", basis, 0.99, *extra)
+    sim.scheme(scheme)
+    sim.dimension(3, -4, 1.2, -1.2, 1.2, -1.2, 1.2, 0.4)
+    E, nu, rho = 115.0, 0.31, 8.94e-6
+    K, G = E / (3 * (1 - 2 * nu)), E / (2 * (1 + nu))
+    if mat_kind == "eos-strength":
+        if eos == "linear":
+            sim.eos("e", "linear", rho, K)
+        else:
+            sim.eos("e", "shock", rho, K, 3940.0, 1.49, 2.0, 3.8e-7, 25.0, 1.0, 0.1)
+        args = {"johnson_cook": (G, 0.09, 0.292, 0.31, 1e-3, 0.025, 1.09, 25.0, 1356.0),
+                "plastic": (G, 0.2), "swift": (G, 0.09, 0.3, 0.01, 0.4), "linear": (G,)}[strength]
+        sim.strength("s", strength, *args)
+        laws = ["e", "s"]
+        if thermal:
+            sim.temperature("t", "plastic_work", 0.9, 385.0, 4e-4, 1e-5, 25.0, 1356.0)
+            laws.append("t")
+        sim.material("m", "eos-strength", *laws)
+    else:
+        sim.material("m", mat_kind, rho, E, nu)
+    sim.region("bar", "block", -2, 0.8, -0.8, 0.8, -0.8, 0.8)
+    sim.solid("s1", "region", "bar", 2, "m", 0.4, 25.0)
+    sim.region("wall", "block", 0.6, "INF", "-INF", "INF", "-INF", "INF")
+    sim.group("gw", "nodes", "region", "wall", "solid", "s1")
+    sim.group("gp", "particles", "region", "bar", "solid", "s1")
+    sim.fix("v0", "initial_velocity_particles", "gp", v0, None, None)
+    sim.dt_factor(0.2)
+    return sim
