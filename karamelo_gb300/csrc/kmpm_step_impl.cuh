@@ -370,6 +370,224 @@ __global__ void __launch_bounds__(256, (p2g_min_blocks<DIM, MODE, THERMAL>())) k
   }
 }
 
+// ============================================================== P2G by cell rows
+// The scatter of the 3-D four-wide stencils (cubic and quadratic B-splines)
+// for the plain modes (TL and UL forces, the MUSL velocity re-map, without
+// thermal, affine, contact or axisymmetric terms).  Same tiles, warps and
+// slab footprints as k_p2g; the cells of warp w's x-layer are visited a z-row
+// (4 cells, contiguous in the sorted order) at a time:
+//   - stage (lane = particle): up to 32 particles of the row at once, each
+//     lane its own particle's payload and the per-axis basis values of its
+//     three axes, relative to its cell;
+//   - accumulate (lane = (a, b, c) with a, b the stencil's x and y slots and
+//     c in {0, 1}): the particles of the row's cells in sorted order, the
+//     lane adding into z slots c and c + 2 of each.  Over the row those are
+//     the nodes z = c .. c + 5 of the row's footprint, held in six register
+//     accumulators: the cell lz adds to accumulators lz and lz + 2, a
+//     compile-time index once the four cells are unrolled;
+//   - flush once per row: lanes c = 1 hand their z = 1..5 sums to lanes c = 0
+//     (a fixed shuffle), which add them into the warp's slab with their own.
+// Every sum runs in a fixed order: the result is bit-reproducible.
+template <int MODE, int Q>
+__device__ __forceinline__ void p2g_row_particle(float (&A0)[Q], float (&A2)[Q], const float *pay, float2 bx,
+                                                 float2 by, float2 bz0, float2 bz2) {
+  constexpr int OM = MODE == P2G_UL ? 1 : 0;  // UL sums start with the mass
+  constexpr bool FORCE = MODE != P2G_VEL;
+  const float wxy = bx.x * by.x;
+  float q[3 + OM];
+#pragma unroll
+  for (int d = 0; d < 3 + OM; d++) q[d] = wxy * pay[d];
+  float t[3], t2[3];
+  if (FORCE) {
+    const float gxy0 = bx.y * by.x, gxy1 = bx.x * by.y;
+#pragma unroll
+    for (int r = 0; r < 3; r++) {
+      float T0, T1, T2;
+      if (MODE == P2G_TL) {  // vol0 PK1, row-major
+        T0 = pay[3 + 3 * r]; T1 = pay[4 + 3 * r]; T2 = pay[5 + 3 * r];
+      } else {  // vol sigma, symmetric xx yy zz xy xz yz
+        const float *sg = pay + 4;
+        T0 = r == 0 ? sg[0] : (r == 1 ? sg[3] : sg[4]);
+        T1 = r == 0 ? sg[3] : (r == 1 ? sg[1] : sg[5]);
+        T2 = r == 0 ? sg[4] : (r == 1 ? sg[5] : sg[2]);
+      }
+      t[r] = T0 * gxy0 + T1 * gxy1;
+      t2[r] = T2 * wxy;
+    }
+  }
+#pragma unroll
+  for (int d = 0; d < 3 + OM; d++) {
+    A0[d] = fmaf(bz0.x, q[d], A0[d]);
+    A2[d] = fmaf(bz2.x, q[d], A2[d]);
+  }
+  if (FORCE)
+#pragma unroll
+    for (int r = 0; r < 3; r++) {
+      A0[3 + OM + r] = fmaf(-bz0.x, t[r], fmaf(-bz0.y, t2[r], A0[3 + OM + r]));
+      A2[3 + OM + r] = fmaf(-bz2.x, t[r], fmaf(-bz2.y, t2[r], A2[3 + OM + r]));
+    }
+}
+
+template <int BASIS, int MODE>
+__global__ void __launch_bounds__(256, (MODE == P2G_VEL ? 4 : 3)) k_p2g_row(P2GArgs a) {
+  static_assert(Stencil<BASIS>::S == 4 && Stencil<BASIS>::SC == 1, "four-wide stencils");
+  using TS = TileShape<3, BASIS>;
+  constexpr int S = 4, LO = Stencil<BASIS>::LO;
+  constexpr int TX = TS::TX, TY = TS::TY, TZ = TS::TZ;
+  constexpr int WY = TS::WY, WZ = TS::WZ, NW = TS::NW, NF = TS::NF, FX = TS::FX;
+  static_assert(TS::L == 1 && TZ == 4 && FX == 4, "one x-layer of 4 x 4 cells per warp");
+  constexpr int Q = p2g_nq(MODE, false);
+  constexpr int QIN = p2g_nin(MODE, false);
+  constexpr int QINP = (QIN + 3) & ~3;
+  constexpr int SLAB = (Q * NF + 3) & ~3;
+  constexpr int STAGE = 32 * QINP + 32 * 3 * S * 2;
+
+  extern __shared__ __align__(16) float smem[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  float *slab = smem + warp * SLAB;
+  float *spay = smem + TS::NWARP * SLAB + warp * STAGE;                  // [32][QINP]
+  float2 *sbas = reinterpret_cast<float2 *>(spay + 32 * QINP);          // [axis][slot][32]
+
+  const int2 td = a.tiles[blockIdx.x];
+  const GridDev g = a.grids[td.x];
+  const int tlin = td.y;
+  const int tile_global = g.tile_off + tlin;
+  if (a.tile_end[tile_global] == a.tile_start[tile_global] || run_finished(a.scalars)) return;
+  const int tc2 = tlin % g.ntile[2], tc1 = (tlin / g.ntile[2]) % g.ntile[1], tc0 = tlin / (g.ntile[1] * g.ntile[2]);
+  const float h = g.cellsize, ih = g.inv_cellsize;
+  const float *P = *a.Pp;
+  const size_t ps = a.ps;
+  const bool use_u = a.pos_field == PF_X;
+
+  for (int k = lane; k < Q * NF; k += 32) slab[k] = 0.f;
+
+  // this lane's stencil slots in the accumulate phase
+  const int sa = lane >> 3, sb = (lane >> 1) & 3, sc = lane & 1;
+  const float2 *px = sbas + (0 * S + sa) * 32, *py = sbas + (1 * S + sb) * 32;
+  const float2 *pz0 = sbas + (2 * S + sc) * 32, *pz2 = sbas + (2 * S + sc + 2) * 32;
+  const int i0x = (tc0 * TX + warp) - LO;
+
+  for (int ly = 0; ly < TY; ly++) {
+    // the row's four cells (local index (lx TY + ly) TZ + lz) and their
+    // particle ranges [st, en); the non-empty ones are contiguous in the
+    // sorted order (an empty cell's range is st == en, of any value)
+    const int cbase = tile_global * TS::NCELL + (warp * TY + ly) * TZ;
+    const int cv = lane < 8 ? (lane < 4 ? a.cell_start[cbase + lane] : a.cell_end[cbase + lane - 4]) : 0;
+    int st[4], en[4], lo4[4];
+    int rs = INT_MAX, re = INT_MIN;
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      st[k] = __shfl_sync(0xffffffffu, cv, k);
+      en[k] = __shfl_sync(0xffffffffu, cv, 4 + k);
+      const bool full = en[k] > st[k];
+      lo4[k] = full ? st[k] : INT_MAX;
+      rs = full ? min(rs, st[k]) : rs;
+      re = full ? max(re, en[k]) : re;
+    }
+    if (rs == INT_MAX) continue;
+    const int i0y = (tc1 * TY + ly) - LO;
+    float acc[6][Q];
+#pragma unroll
+    for (int m = 0; m < 6; m++)
+#pragma unroll
+      for (int qq = 0; qq < Q; qq++) acc[m][qq] = 0.f;
+
+    for (int c0 = rs; c0 < re; c0 += 32) {
+      const int cnt = min(32, re - c0);
+      // ---- stage (lane = particle)
+      if (lane < cnt) {
+        const int p = c0 + lane;
+        int lz = 0;  // the non-empty cell holding p: the last one starting at or before it
+#pragma unroll
+        for (int k = 1; k < 4; k++) lz = lo4[k] <= p ? k : lz;
+        float pay[QIN];
+        p2g_payload<MODE, false>(a, P, p, pay);
+#pragma unroll
+        for (int v = 0; v < QINP / 4; v++)
+          reinterpret_cast<float4 *>(spay + lane * QINP)[v] =
+              make_float4(pay[4 * v], 4 * v + 1 < QIN ? pay[min(4 * v + 1, QIN - 1)] : 0.f,
+                          4 * v + 2 < QIN ? pay[min(4 * v + 2, QIN - 1)] : 0.f,
+                          4 * v + 3 < QIN ? pay[min(4 * v + 3, QIN - 1)] : 0.f);
+        const int i0[3] = {i0x, i0y, (tc2 * TZ + lz) - LO};
+#pragma unroll
+        for (int d = 0; d < 3; d++) {
+          const float xp = P[(PF_X0 + d) * ps + p] + (use_u ? P[(PF_X + d) * ps + p] : 0.f);
+          const float lod = d == 0 ? g.lo[0] : (d == 1 ? g.lo[1] : g.lo[2]);
+          const int nd = d == 0 ? g.n[0] : (d == 1 ? g.n[1] : g.n[2]);
+          const int ngd = d == 0 ? g.ng[0] : (d == 1 ? g.ng[1] : g.ng[2]);
+          float sv[S], dsv[S];
+          if (BASIS == 1 && cubic_interior(i0[d], nd, ngd)) {
+            cubic_weights((xp - lod) * ih - (float)(i0[d] + 1), ih, sv, dsv);
+          } else {
+#pragma unroll
+            for (int kk = 0; kk < S; kk++) {
+              const int i = i0[d] + kk;
+              sv[kk] = 0.f;
+              dsv[kk] = 0.f;
+              if (i >= 0 && i < nd) {
+                const float r = (xp - (lod + (float)i * h)) * ih;
+                basis<BASIS>(r, node_type<BASIS>(i, ngd), ih, sv[kk], dsv[kk]);
+                dsv[kk] = sv[kk] != 0.f ? dsv[kk] : 0.f;  // as Axis::eval
+              }
+            }
+          }
+#pragma unroll
+          for (int kk = 0; kk < S; kk++) sbas[(d * S + kk) * 32 + lane] = make_float2(sv[kk], dsv[kk]);
+        }
+      }
+      __syncwarp();
+      // ---- accumulate (lane = node): cell after cell, particles in sorted order
+#pragma unroll
+      for (int lz = 0; lz < 4; lz++) {
+        const int jlo = max(st[lz] - c0, 0), jhi = min(en[lz] - c0, cnt);
+        for (int j = jlo; j < jhi; j++) {
+          float pay[QINP];
+#pragma unroll
+          for (int v = 0; v < QINP / 4; v++) {
+            const float4 t4 = reinterpret_cast<const float4 *>(spay + j * QINP)[v];
+            pay[4 * v] = t4.x; pay[4 * v + 1] = t4.y; pay[4 * v + 2] = t4.z; pay[4 * v + 3] = t4.w;
+          }
+          p2g_row_particle<MODE, Q>(acc[lz], acc[lz + 2], pay, px[j], py[j], pz0[j], pz2[j]);
+        }
+      }
+      __syncwarp();
+    }
+    // ---- flush: lanes c = 1 hold z = 1..6 as accumulators 0..5; their z = 1..5
+    // join the c = 0 lanes' accumulators 1..5 (a fixed order)
+#pragma unroll
+    for (int m = 0; m < 5; m++)
+#pragma unroll
+      for (int qq = 0; qq < Q; qq++) {
+        const float o = __shfl_xor_sync(0xffffffffu, acc[m][qq], 1);
+        if (sc == 0) acc[m + 1][qq] += o;
+      }
+    const int fy = ly + sb;
+#pragma unroll
+    for (int m = 0; m < 6; m++) {
+      if (sc == 1 && m < 5) continue;
+      const int fz = m + sc;
+      const int fi = (sa * WY + fy) * WZ + fz;
+#pragma unroll
+      for (int qq = 0; qq < Q; qq++) slab[qq * NF + fi] += acc[m][qq];
+    }
+    __syncwarp();
+  }
+  __syncthreads();
+  // ---- sum the slabs in warp order into the tile footprint
+  float *out = a.partial + (size_t)tile_global * a.pstride_tile;
+  for (int k = threadIdx.x; k < Q * NW; k += blockDim.x) {
+    const int qq = k / NW, fi = k % NW;
+    const int fx = fi / (WY * WZ), fyz = fi % (WY * WZ);
+    float sum = 0.f;
+#pragma unroll
+    for (int w = 0; w < TS::NWARP; w++) {
+      const int x = fx - w;
+      if (x >= 0 && x < FX) sum += smem[w * SLAB + qq * NF + x * WY * WZ + fyz];
+    }
+    out[k] = sum;
+  }
+}
+
 // ============================================================== grid
 // Sum of the tile partials covering one node, in a fixed tile order.
 template <int DIM, int BASIS, int Q, typename ACC>
@@ -1176,6 +1394,13 @@ void fill_step_kernels(StepKernels &k) {
   k.p2g_ul_th = (void *)k_p2g<DIM, BASIS, P2G_UL, true>;
   k.p2g_vel = (void *)k_p2g<DIM, BASIS, P2G_VEL, false>;
   k.p2g_vel_th = (void *)k_p2g<DIM, BASIS, P2G_VEL, true>;
+  if constexpr (DIM == 3 && (BASIS == 1 || BASIS == 3)) {
+    k.p2g_row[0] = (void *)k_p2g_row<BASIS, P2G_TL>;
+    k.p2g_row[1] = (void *)k_p2g_row<BASIS, P2G_UL>;
+    k.p2g_row[2] = (void *)k_p2g_row<BASIS, P2G_VEL>;
+  } else {
+    k.p2g_row[0] = k.p2g_row[1] = k.p2g_row[2] = nullptr;
+  }
   // APIC runs with the cubic and quadratic splines, and for TLMPM with the
   // linear basis (src/solid.cpp:1447-1473)
   if constexpr (BASIS == 1 || BASIS == 3) {

@@ -1495,6 +1495,19 @@ int om_get_particles(void *h, int si, int field, double *out) {
   }
   return S.np;
 }
+// Rounds every particle state field to single precision in place: the
+// sensitivity-floor protocol of the parity tests runs the oracle with this
+// applied after each step, to bound how far an FP32 computation of the same
+// run may legitimately stray from the FP64 one.
+void om_round_state_f32(void *h) {
+  Sim *s = (Sim *)h;
+  auto rv = [](std::vector<double> &A) { for (double &x : A) x = (double)(float)x; };
+  auto rm = [](std::vector<M3> &A) { for (M3 &m : A) for (double &x : m.a) x = (double)(float)x; };
+  for (auto &S : s->solids) {
+    rv(S.x); rv(S.v); rv(S.epsp); rv(S.epsdot); rv(S.damage); rv(S.damage_init); rv(S.T); rv(S.J); rv(S.vol);
+    rm(S.sigma); rm(S.F); rm(S.strain_el); rm(S.vol0PK1);
+  }
+}
 // Grid fields: 0 mass, 1 v, 2 v_update, 3 x, 4 f, 5 mb, 6 T
 int om_get_grid(void *h, int gi, int field, double *out) {
   Grid &g = ((Sim *)h)->grids[gi];

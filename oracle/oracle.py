@@ -61,6 +61,7 @@ def lib():
         L.om_get_particles.argtypes = [p, i, i, dp]
         L.om_get_grid.argtypes = [p, i, i, dp]
         L.om_energy.argtypes = [p, dp]
+        L.om_round_state_f32.argtypes = [p]
         L.om_basis.restype = d
         L.om_basis.argtypes = [i, i, d, i, d]
         L.om_constitutive.argtypes = [p, i, dp, dp, dp, dp]
@@ -196,6 +197,10 @@ class OracleBackend:
         out = np.zeros(self.grid_nn[gi] * w)
         self.L.om_get_grid(self.h, gi, code, _dp(out))
         return out.reshape(-1, 3) if w == 3 else out
+
+    def round_state_f32(self):
+        """Particle state rounded to single precision (sensitivity-floor runs)."""
+        self.L.om_round_state_f32(self.h)
 
     def energies(self):
         out = np.zeros(2)
