@@ -205,6 +205,7 @@ def bench_ours(args):
     clk = clocks.stop()
     plain_sigma, plain_x = sim.particles(0, "sigma"), sim.particles(0, "x")
     learned = None if args.no_learned else bench_learned(args, be, plain_sigma, plain_x, n, ms)
+    islands = None if (args.no_islands or args.precision) else bench_islands(args, plain_sigma, plain_x, n, ms)
     ms, units = aggregate_replicas(ms, n * args.steps, "cuda")
     value = units / (ms / 1000.0)
     launches = be.launches_per_step() * args.steps
@@ -298,6 +299,8 @@ def bench_ours(args):
     }
     if learned is not None:
         line["learned"] = learned
+    if islands is not None:
+        line["fp64_islands"] = islands
     if world == 1 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
         v, npart, done_c, dtc = run_cpu_sample(args.cpu_cellsize, args.cpu_steps, args.ref_budget, threads)
@@ -305,6 +308,42 @@ def bench_ours(args):
                                 "sample": f"{done_c} oracle steps of the same bar at cellsize {args.cpu_cellsize} mm "
                                           f"({npart} particles) after its untimed first step"}
     print(json.dumps(line), flush=True)
+
+
+def bench_islands(args, plain_sigma, plain_x, n, plain_ms):
+    """The same bar and steps with the FP64 islands (KMPM_PREC_FP64_ISLANDS:
+    nodal sums and v = p/m, det and inverse of F, and the EOS and strength
+    update in FP64; the rest FP32): throughput against the plain FP32 path
+    and the final state's distance from it."""
+    import numpy as np
+    import torch
+    from karamelo_gb300 import workloads as W
+    from karamelo_gb300.gpu import GpuBackend
+    sim = W.taylor_bar(None, cellsize=args.cellsize)
+    sim.backend = GpuBackend(sim.s, precision=1, track_strain=False)
+    sim.run(1)
+    W.taylor_bar_wall(sim)
+    be = sim.backend
+    be.run(args.warmup)
+    phases = be.profile(args.profile_steps)  # as the plain arm: same step count before the timed steps
+    stream = torch.cuda.ExternalStream(be.stream())
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    be.run(args.steps)
+    e1.record(stream)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1)
+
+    def rel(a, b):
+        return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+    out = {"value": n * args.steps / (ms / 1000.0), "unit": UNIT, "ms_per_step": ms / args.steps,
+           "over_plain": plain_ms / ms,
+           "rel_l2_sigma_vs_plain": rel(sim.particles(0, "sigma"), plain_sigma),
+           "rel_l2_x_vs_plain": rel(sim.particles(0, "x"), plain_x),
+           "phases_ms": phases}
+    be.close()
+    return out
 
 
 def bench_learned(args, plain_backend, plain_sigma, plain_x, n, plain_ms):
@@ -449,6 +488,7 @@ def main():
     ap.add_argument("--instances", type=int, default=1024)
     ap.add_argument("--tol", type=float, default=1e-3)
     ap.add_argument("--no-learned", action="store_true")
+    ap.add_argument("--no-islands", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
