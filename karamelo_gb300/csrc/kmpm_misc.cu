@@ -458,8 +458,9 @@ int p2g_smem_bytes(int dim, int basis, int mode, bool thermal) {
   const int NF = ((L - 1) * SC + S) * WY * WZ;
   const int Q = p2g_nq(mode, thermal), QINP = (p2g_nin(mode, thermal) + 3) & ~3;
   const int slab = (Q * NF + 3) & ~3;
-  // affine modes also stage the per-slot offsets (x_node - x_p) / h
-  return 4 * 8 * (slab + 32 * QINP + 32 * dim * S * (p2g_apic(mode) ? 3 : 2));
+  // affine modes also stage the per-slot offsets (x_node - x_p) / h; the
+  // row scatter (k_p2g_row) pads each of its dim * S basis rows by one float2
+  return 4 * 8 * (slab + 32 * QINP + 32 * dim * S * (p2g_apic(mode) ? 3 : 2) + dim * S * 2);
 }
 
 }  // namespace kmpm

@@ -440,13 +440,16 @@ __global__ void __launch_bounds__(256, (MODE == P2G_VEL ? 4 : 3)) k_p2g_row(P2GA
   constexpr int QIN = p2g_nin(MODE, false);
   constexpr int QINP = (QIN + 3) & ~3;
   constexpr int SLAB = (Q * NF + 3) & ~3;
-  constexpr int STAGE = 32 * QINP + 32 * 3 * S * 2;
+  // basis rows of SROW float2 (one per staged particle, padded so that the
+  // four slots of one particle fall in different banks)
+  constexpr int SROW = 33;
+  constexpr int STAGE = 32 * QINP + SROW * 3 * S * 2;
 
   extern __shared__ __align__(16) float smem[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   float *slab = smem + warp * SLAB;
   float *spay = smem + TS::NWARP * SLAB + warp * STAGE;                  // [32][QINP]
-  float2 *sbas = reinterpret_cast<float2 *>(spay + 32 * QINP);          // [axis][slot][32]
+  float2 *sbas = reinterpret_cast<float2 *>(spay + 32 * QINP);          // [axis][slot][SROW]
 
   const int2 td = a.tiles[blockIdx.x];
   const GridDev g = a.grids[td.x];
@@ -463,8 +466,8 @@ __global__ void __launch_bounds__(256, (MODE == P2G_VEL ? 4 : 3)) k_p2g_row(P2GA
 
   // this lane's stencil slots in the accumulate phase
   const int sa = lane >> 3, sb = (lane >> 1) & 3, sc = lane & 1;
-  const float2 *px = sbas + (0 * S + sa) * 32, *py = sbas + (1 * S + sb) * 32;
-  const float2 *pz0 = sbas + (2 * S + sc) * 32, *pz2 = sbas + (2 * S + sc + 2) * 32;
+  const float2 *px = sbas + (0 * S + sa) * SROW, *py = sbas + (1 * S + sb) * SROW;
+  const float2 *pz0 = sbas + (2 * S + sc) * SROW, *pz2 = sbas + (2 * S + sc + 2) * SROW;
   const int i0x = (tc0 * TX + warp) - LO;
 
   for (int ly = 0; ly < TY; ly++) {
@@ -532,7 +535,7 @@ __global__ void __launch_bounds__(256, (MODE == P2G_VEL ? 4 : 3)) k_p2g_row(P2GA
             }
           }
 #pragma unroll
-          for (int kk = 0; kk < S; kk++) sbas[(d * S + kk) * 32 + lane] = make_float2(sv[kk], dsv[kk]);
+          for (int kk = 0; kk < S; kk++) sbas[(d * S + kk) * SROW + lane] = make_float2(sv[kk], dsv[kk]);
         }
       }
       __syncwarp();
