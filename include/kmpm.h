@@ -212,6 +212,12 @@ int kmpm_run(struct kmpm_ctx *ctx, int nsteps);
 /* RunTime::command (src/run_time.cpp:30-60): steps until time >= maxtime. */
 int kmpm_run_time(struct kmpm_ctx *ctx, double maxtime, int *nsteps_done);
 
+/* At most nsteps steps of a RunTime::command (src/run_time.cpp:30-60): stops
+ * once time >= maxtime, so that a caller can end a run_time at its output
+ * steps (Output::next) as the reference's scheme loop does
+ * (src/musl.cpp:82-91).  nsteps_done (may be NULL) receives the steps run. */
+int kmpm_run_until(struct kmpm_ctx *ctx, int nsteps, double maxtime, int *nsteps_done);
+
 /* Update::atime, Update::dt, Update::ntimestep. */
 int kmpm_scalars(struct kmpm_ctx *ctx, double *time, double *dt, long long *ntimestep);
 

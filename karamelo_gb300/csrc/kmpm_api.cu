@@ -1495,6 +1495,35 @@ int kmpm_run_time(kmpm_ctx *c, double maxtime, int *nsteps_done) {
   return KMPM_OK;
 }
 
+int kmpm_run_until(kmpm_ctx *c, int nsteps, double maxtime, int *nsteps_done) {
+  if (!c || nsteps < 0) return KMPM_ERR_ARG;
+  if (c->indep()) return fail(c, KMPM_ERR_ARG, "run_until needs one clock: not available for independent solids");
+  int r = prepare(c);
+  if (r != KMPM_OK) return r;
+  r = maybe_tune(c);
+  if (r != KMPM_OK) return r;
+  StepScalars s{};
+  r = read_scalars(c, s);
+  if (r != KMPM_OK) return r;
+  const long long n0 = s.ntimestep;
+  // at most nsteps steps of a RunTime::command (src/run_time.cpp:30-60): the
+  // steps check the time bound on the device, so a batch never overshoots it
+  r = set_maxtime(c, maxtime);
+  if (r != KMPM_OK) return r;
+  while (s.time < maxtime && s.ntimestep - n0 < nsteps) {
+    const int k = (int)std::min<long long>(64, nsteps - (s.ntimestep - n0));
+    for (int i = 0; i < k; i++) CK(cudaGraphLaunch(c->gexec, c->st));
+    r = check_error(c);
+    if (r != KMPM_OK) return r;
+    r = read_scalars(c, s);
+    if (r != KMPM_OK) return r;
+  }
+  r = set_maxtime(c, 1e300);
+  if (r != KMPM_OK) return r;
+  if (nsteps_done) *nsteps_done = (int)(s.ntimestep - n0);
+  return KMPM_OK;
+}
+
 int kmpm_scalars(kmpm_ctx *c, double *time, double *dt, long long *ntimestep) {
   if (!c) return KMPM_ERR_ARG;
   StepScalars s{};
