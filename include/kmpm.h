@@ -76,7 +76,6 @@ typedef struct {
   double boxlo[3];   /* Domain::boxlo / boxhi */
   double boxhi[3];
   int precision;     /* KMPM_PREC_* */
-  int sort_every;    /* ULMPM: particles are re-binned by cell every step; kept for ABI growth */
   int track_strain;  /* keep Solid::strain_el (needed by the strain-energy output) */
   int independent;   /* TLMPM only: every solid is an independent simulation with its own
                         dt and time (a batch of runs in one launch per phase); 0 = one

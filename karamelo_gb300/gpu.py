@@ -48,7 +48,7 @@ class KmpmParams(ctypes.Structure):
     _fields_ = [("method", ctypes.c_int), ("scheme", ctypes.c_int), ("basis", ctypes.c_int), ("dim", ctypes.c_int),
                 ("pic_flip", ctypes.c_double), ("thermal", ctypes.c_int), ("dt", ctypes.c_double),
                 ("dt_factor", ctypes.c_double), ("dt_constant", ctypes.c_int), ("boxlo", ctypes.c_double * 3),
-                ("boxhi", ctypes.c_double * 3), ("precision", ctypes.c_int), ("sort_every", ctypes.c_int),
+                ("boxhi", ctypes.c_double * 3), ("precision", ctypes.c_int),
                 ("track_strain", ctypes.c_int), ("independent", ctypes.c_int), ("autotune", ctypes.c_int),
                 ("transfer", ctypes.c_int), ("axisymmetric", ctypes.c_int)]
 
@@ -159,7 +159,6 @@ class GpuBackend:
         for k in range(3):
             prm.boxlo[k], prm.boxhi[k] = float(s.boxlo[k]), float(s.boxhi[k])
         prm.precision = precision
-        prm.sort_every = 1
         prm.track_strain = int(track_strain)
         prm.independent = int(independent)
         prm.autotune = int(autotune)

@@ -363,3 +363,32 @@ def test_taylor_bar_apic_linear(gpu_lib, oracle_mod):
     g, o = pair(oracle_mod, W.taylor_bar, [1, W.taylor_bar_wall, 50], cellsize=0.8, method="tlmpm/gpu",
                 sub="APIC", basis="linear")
     check(g, o, {"x": 1e-6, "v": 1e-4, "sigma": 1e-4, "F": 1e-6})
+
+
+def test_run_until_batches_match_run_time(gpu_lib):
+    """kmpm_run_until (a run_time that ends at the output steps, as the GPU
+    scheme's loop does) in batches of 7 steps reaches the same state as one
+    kmpm_run_time to the same end time, bit for bit."""
+    import ctypes
+    out = []
+    for batched in (False, True):
+        sim = W.taylor_bar(None, cellsize=0.8)
+        sim.run(1)
+        W.taylor_bar_wall(sim)
+        be = sim.backend
+        t_end = sim.time + 1e-3
+        if batched:
+            done, total = ctypes.c_int(0), 0
+            while True:
+                assert be.L.kmpm_run_until(be.h, 7, t_end, ctypes.byref(done)) == 0
+                total += done.value
+                assert done.value <= 7
+                if done.value < 7 or sim.time >= t_end:
+                    break
+            assert total > 7
+        else:
+            sim.run_time(1e-3)
+        out.append((sim.time, sim.particles(0, "x"), sim.particles(0, "sigma")))
+    assert out[0][0] == out[1][0]
+    for a, b in zip(out[0][1:], out[1][1:]):
+        assert np.array_equal(a, b)
