@@ -8,7 +8,7 @@ cell) and N = 20 (two), FLIP with the linear basis at N = 20 (one), and APIC
 with the cubic spline and with the linear basis at N = 20 (two).
 Run where the Karamelo tree is available:
 
-    python tests/golden/make_vertical_bar_golden.py [path/to/Karamelo]
+    python tests/golden/make_vertical_bar_golden.py path/to/Karamelo
 """
 import os
 import sys
@@ -24,7 +24,9 @@ LOGS = {"n10_ppc1": "FLIP_99_cubic-spline_N-10_1_particle_per_cell.data",
 
 
 def main():
-    root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    if len(sys.argv) != 2:
+        sys.exit("usage: make_vertical_bar_golden.py <root of the Karamelo tree>")
+    root = sys.argv[1]
     out = {}
     for key, name in LOGS.items():
         a = np.genfromtxt(os.path.join(root, "examples", "Vertical_bar", name), skip_header=1)[:121]
