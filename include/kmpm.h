@@ -141,6 +141,8 @@ typedef struct {
 #define KMPM_P_STRAIN_EL 13 /* n*9 (needs kmpm_params.track_strain) */
 #define KMPM_P_VOL0PK1 14 /* n*9, TLMPM: vol0 times the first Piola-Kirchhoff stress of the last stress update */
 #define KMPM_P_MASS 15
+#define KMPM_P_SIGMA_ROT6 16 /* n*6: the rotated stress as the reference dump writes it,
+                                s11 s22 s33 s12 s13 s23 (src/dump_particle.cpp:116-121); download only */
 
 /* grid fields for kmpm_download_grid */
 #define KMPM_G_MASS 0

@@ -3,6 +3,9 @@
 // the host<->device conversions between the caller's FP64 arrays and the
 // device's FP32 structure of arrays.
 #include <algorithm>
+#include <map>
+#include <mutex>
+#include <tuple>
 #include <cstddef>
 #include <cmath>
 #include <cstdio>
@@ -1229,12 +1232,50 @@ int autotune(kmpm_ctx *c) {
 }
 
 // tune once, at the first run after at least one step (a state with motion)
+// Launch shapes already chosen in this process, by problem signature
+// (method, dim, basis, law specialisation, particle count to a factor of 2):
+// a later context of the same problem takes the choice without its trial
+// launches.
+struct TuneKey {
+  int tl, dim, basis, law_jc, transfer, log2n;
+  bool operator<(const TuneKey &o) const {
+    return std::tie(tl, dim, basis, law_jc, transfer, log2n) <
+           std::tie(o.tl, o.dim, o.basis, o.law_jc, o.transfer, o.log2n);
+  }
+};
+std::mutex g_tune_mutex;
+std::map<TuneKey, std::pair<std::pair<int, int>, std::string>> g_tune_cache;
+
+TuneKey tune_key(const kmpm_ctx *c) {
+  long long n = 0;
+  for (const auto &r : c->ranges) n += r.count;
+  int l = 0;
+  while ((1LL << (l + 1)) <= std::max(n, 1LL)) l++;
+  return TuneKey{c->TL() ? 1 : 0, c->prm.dim, c->prm.basis, c->law_jc ? 1 : 0, c->prm.transfer, l};
+}
+
 int maybe_tune(kmpm_ctx *c) {
   const bool due = c->prm.autotune && !c->tuned && c->runs > 0;
   c->runs++;
   if (!due) return KMPM_OK;
+  if (!c->prm.thermal && c->prm.precision == KMPM_PREC_FP32) {
+    std::lock_guard<std::mutex> lock(g_tune_mutex);
+    auto it = g_tune_cache.find(tune_key(c));
+    if (it != g_tune_cache.end()) {
+      c->tuned = true;
+      c->var_g2p1 = it->second.first.first;
+      c->var_g2p2 = it->second.first.second;
+      c->tuning = "{\"cached\": true, \"from\": " + it->second.second + "}";
+      c->graph_valid = false;
+      return ensure_graph(c);
+    }
+  }
   int r = autotune(c);
   if (r != KMPM_OK) return r;
+  if (!c->prm.thermal && c->prm.precision == KMPM_PREC_FP32) {
+    std::lock_guard<std::mutex> lock(g_tune_mutex);
+    g_tune_cache[tune_key(c)] = {{c->var_g2p1, c->var_g2p2}, c->tuning};
+  }
   return ensure_graph(c);
 }
 

@@ -41,9 +41,17 @@ __global__ void k_dump(PartArgs a, DumpArgs d) {
     case KMPM_P_STRAIN_EL:
       for (int k = 0; k < 9; k++) o[9 * i + k] = f(PF_STRAIN + sm[k]);
       break;
-    case KMPM_P_SIGMA_ROT: {
+    case KMPM_P_SIGMA_ROT:
+    case KMPM_P_SIGMA_ROT6: {
+      // the six components s11 s22 s33 s12 s13 s23 the reference dump writes
+      // (src/dump_particle.cpp:116-121), or the full 3x3
+      const bool six = d.field == KMPM_P_SIGMA_ROT6;
+      const int up[6] = {0, 4, 8, 1, 2, 5};
       if (!d.rotate) {
-        for (int k = 0; k < 9; k++) o[9 * i + k] = f(PF_SIG + sm[k]);
+        if (six)
+          for (int k = 0; k < 6; k++) o[6 * i + k] = f(PF_SIG + k);
+        else
+          for (int k = 0; k < 9; k++) o[9 * i + k] = f(PF_SIG + sm[k]);
         break;
       }
       // R of F = R U by the stress kernel's FP32 polar iteration, and R sigma
@@ -56,7 +64,10 @@ __global__ void k_dump(PartArgs a, DumpArgs d) {
       for (int k = 0; k < 9; k++) Sm[k] = P[(PF_SIG + sm[k]) * ps + p];
       matmul3(R, Sm, RS);
       matmulT3(RS, R, RSR);
-      for (int k = 0; k < 9; k++) o[9 * i + k] = (double)RSR[k];
+      if (six)
+        for (int k = 0; k < 6; k++) o[6 * i + k] = (double)RSR[up[k]];
+      else
+        for (int k = 0; k < 9; k++) o[9 * i + k] = (double)RSR[k];
       break;
     }
     case KMPM_P_F:
@@ -159,6 +170,7 @@ int dump_width(int field) {
   switch (field) {
     case KMPM_P_X: case KMPM_P_X0: case KMPM_P_V: return 3;
     case KMPM_P_SIGMA: case KMPM_P_SIGMA_ROT: case KMPM_P_F: case KMPM_P_STRAIN_EL: case KMPM_P_VOL0PK1: return 9;
+    case KMPM_P_SIGMA_ROT6: return 6;
     case KMPM_P_EPS_P: case KMPM_P_EPSDOT_P: case KMPM_P_DAMAGE: case KMPM_P_DAMAGE_INIT: case KMPM_P_T:
     case KMPM_P_J: case KMPM_P_VOL: case KMPM_P_MASS: return 1;
     default: return 0;

@@ -22,7 +22,8 @@ ERRORS = {-1: "KMPM_ERR_ARG", -2: "KMPM_ERR_CUDA", -3: "KMPM_ERR_STATE", -10: "K
 
 PARTICLE_FIELDS = {"x": (0, 3), "x0": (1, 3), "v": (2, 3), "sigma_raw": (3, 9), "sigma": (4, 9), "F": (5, 9),
                    "eps_p": (6, 1), "epsdot_p": (7, 1), "damage": (8, 1), "damage_init": (9, 1), "T": (10, 1),
-                   "J": (11, 1), "vol": (12, 1), "strain_el": (13, 9), "vol0PK1": (14, 9), "mass": (15, 1)}
+                   "J": (11, 1), "vol": (12, 1), "strain_el": (13, 9), "vol0PK1": (14, 9), "mass": (15, 1),
+                   "sigma6": (16, 6)}
 # the particle state Solid::read_restart restores (src/solid.cpp:2894-2957)
 RESTART_FIELDS_TL = ("x", "v", "sigma_raw", "strain_el", "vol0PK1", "F", "eps_p", "epsdot_p", "damage",
                      "damage_init")
@@ -246,7 +247,7 @@ class GpuBackend:
         n = self.s.solids[si].np
         out = np.zeros(n * w)
         self._ck(self.L.kmpm_download_particles(self.h, si, code, _dp(out)))
-        return out.reshape(n, 3, 3) if w == 9 else (out.reshape(n, 3) if w == 3 else out)
+        return out.reshape(n, 3, 3) if w == 9 else (out.reshape(n, w) if w in (3, 6) else out)
 
     def particles_async(self, si: int, field: str, out):
         """Queue the download of one field into ``out``, a page-locked float64

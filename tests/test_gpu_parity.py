@@ -392,3 +392,16 @@ def test_run_until_batches_match_run_time(gpu_lib):
     assert out[0][0] == out[1][0]
     for a, b in zip(out[0][1:], out[1][1:]):
         assert np.array_equal(a, b)
+
+
+def test_sigma6_download_is_the_dumped_components(gpu_lib):
+    """KMPM_P_SIGMA_ROT6: s11 s22 s33 s12 s13 s23 of the rotated stress, as
+    the reference's particle dump writes them, equal to the 3x3 download."""
+    sim = W.taylor_bar(None, cellsize=0.8)
+    sim.run(1)
+    W.taylor_bar_wall(sim)
+    sim.run(20)
+    s9, s6 = sim.particles(0, "sigma"), sim.particles(0, "sigma6")
+    assert s6.shape == (s9.shape[0], 6)
+    for k, (a, b) in enumerate(((0, 0), (1, 1), (2, 2), (0, 1), (0, 2), (1, 2))):
+        assert np.array_equal(s6[:, k], s9[:, a, b])
