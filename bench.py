@@ -50,6 +50,9 @@ PHASE_BYTES = {
     "grid_update": (0, 52),     # m, p, f -> v, v_update (+ fixes)
     "g2p_advance": (60, 24),    # x0, u, v -> u, v ; gathers v, v_update
     "p2g_velocity": (28, 12),   # x0, m, v -> nodal p
+    # the two above in one pass (MUSL, k_g2p1_remap_row): x0, u, v, m -> u, v;
+    # gathers v, v_update and writes nodal p
+    "g2p_advance_remap": (64, 36),
     "grid_velocity": (0, 52),   # m, p -> v (+ BC), x += dt v
     "g2p_stress": (200, 12),    # x0, v, F, sigma, eps_p, epsdot, vol0 -> F, sigma, eps_p, epsdot, vol0*PK1
 }

@@ -173,6 +173,7 @@ struct kmpm_ctx {
     const double *dst = nullptr;  // the caller's buffer of the last copy
   };
   std::vector<AsyncBuf> abufs;
+  bool fuse_remap = false;  // MUSL gather + re-map in one kernel (k_g2p1_remap_row)
   bool indep() const { return prm.independent != 0; }
   // affine transfers: APIC, and for ULMPM also AFLIP / ASFLIP / MLS
   // (src/ulmpm.cpp:79-85; TLMPM takes the affine path for APIC only, src/tlmpm.cpp:354)
@@ -313,6 +314,14 @@ P2GArgs p2g_args(kmpm_ctx *c) {
   a.apic_pos = -1;
   a.mls = (!c->TL() && c->prm.transfer == KMPM_TRANSFER_MLS) ? 1 : 0;
   a.mbp = c->d_mbp;
+  a.nodeA = c->nodeA;
+  a.pic_flip = (float)c->prm.pic_flip;
+  for (int d = 0; d < 3; d++) {
+    a.boxlo[d] = (float)c->prm.boxlo[d];
+    a.boxhi[d] = (float)c->prm.boxhi[d];
+  }
+  a.err = c->d_err;
+  a.indep = c->indep();
   {
     const double cs = c->hgrids.empty() ? 1.0 : c->hgrids[0].cellsize;
     a.mls_di = (float)((c->prm.basis == KMPM_BASIS_QUADRATIC ? 4.0 : 3.0) / (cs * cs));
@@ -440,6 +449,14 @@ int build(kmpm_ctx *c) {
       c->K.p2g_ul = c->K.p2g_row[1];
       c->K.p2g_vel = c->K.p2g_row[2];
     }
+  }
+  // MUSL with FLIP/PIC transfers on mechanical 3-D runs: the gather and the
+  // re-map scatter in one pass (KMPM_SPLIT_MUSL=1 or KMPM_CELL_SCATTER=1:
+  // the two kernels)
+  {
+    const char *es = std::getenv("KMPM_SPLIT_MUSL"), *ec = std::getenv("KMPM_CELL_SCATTER");
+    c->fuse_remap = c->K.g2p1_remap[0] && c->musl() && !c->prm.thermal && !c->apic() && !(es && es[0] == '1') &&
+                    !(ec && ec[0] == '1');
   }
   // the specialised stress kernels: every material linear EOS + Johnson-Cook,
   // no damage, no temperature law
@@ -673,6 +690,9 @@ int build(kmpm_ctx *c) {
       c->smem[m][t] = p2g_smem_bytes(dim, basis, modes[m], t == 1);
       CK(cudaFuncSetAttribute(fns[m][t], cudaFuncAttributeMaxDynamicSharedMemorySize, c->smem[m][t]));
     }
+  if (c->fuse_remap)
+    CK(cudaFuncSetAttribute(c->K.g2p1_remap[c->TL() ? 1 : 0], cudaFuncAttributeMaxDynamicSharedMemorySize,
+                            c->K.g2p1_remap_smem));
   if (c->apic()) {
     const int am[3] = {P2G_TL_APIC, P2G_UL_APIC, P2G_VEL_APIC};
     void *af[3] = {c->K.p2g_tl_apic, c->K.p2g_ul_apic, c->K.p2g_vel_apic};
@@ -1052,24 +1072,34 @@ int enqueue_step(kmpm_ctx *c) {
     c->launches_per_step = nl;
     return KMPM_OK;
   }
-  // grid_to_points + advance_particles
-  LAUNCH(th ? c->K.g2p1[TL][th] : c->K.g2p1_v[TL][c->var_g2p1], c->nblk_p, 256, G2P1_SMEM, pa);
-  MARK("g2p_advance");
-  if (musl) {
-    // velocities_to_grid + post_velocities_to_grid (+ TL grid positions)
-    // APIC re-map: ULMPM takes x_p after the move, with this step's weights
-    P2GArgs pv = p;
-    pv.apic_pos = TL ? -1 : PF_XN;
-    if (apic) LAUNCH(c->K.p2g_vel_apic, c->ntiles_launch, 256, c->smem_apic[2], pv);
-    else LAUNCH(th ? c->K.p2g_vel_th : c->K.p2g_vel, c->ntiles_launch, 256, c->smem[3][th], pv);
-    MARK("p2g_velocity");
+  if (c->fuse_remap) {
+    // grid_to_points + advance_particles + velocities_to_grid in one pass
+    // over the tiles, then post_velocities_to_grid (+ TL grid positions)
+    LAUNCH(c->K.g2p1_remap[TL], c->ntiles_launch, 256, c->K.g2p1_remap_smem, p);
+    MARK("g2p_advance_remap");
     GridArgs g2 = grid_args(c, 1);
     LAUNCH(c->K.grid_vel[TL][th][prec], c->nblk_g, 256, 0, g2);
     MARK("grid_velocity");
-  } else if (TL) {
-    GridArgs g2 = grid_args(c, 0);
-    LAUNCH(c->K.grid_vel[TL][th][prec], c->nblk_g, 256, 0, g2);
-    MARK("grid_positions");
+  } else {
+    // grid_to_points + advance_particles
+    LAUNCH(th ? c->K.g2p1[TL][th] : c->K.g2p1_v[TL][c->var_g2p1], c->nblk_p, 256, G2P1_SMEM, pa);
+    MARK("g2p_advance");
+    if (musl) {
+      // velocities_to_grid + post_velocities_to_grid (+ TL grid positions)
+      // APIC re-map: ULMPM takes x_p after the move, with this step's weights
+      P2GArgs pv = p;
+      pv.apic_pos = TL ? -1 : PF_XN;
+      if (apic) LAUNCH(c->K.p2g_vel_apic, c->ntiles_launch, 256, c->smem_apic[2], pv);
+      else LAUNCH(th ? c->K.p2g_vel_th : c->K.p2g_vel, c->ntiles_launch, 256, c->smem[3][th], pv);
+      MARK("p2g_velocity");
+      GridArgs g2 = grid_args(c, 1);
+      LAUNCH(c->K.grid_vel[TL][th][prec], c->nblk_g, 256, 0, g2);
+      MARK("grid_velocity");
+    } else if (TL) {
+      GridArgs g2 = grid_args(c, 0);
+      LAUNCH(c->K.grid_vel[TL][th][prec], c->nblk_g, 256, 0, g2);
+      MARK("grid_positions");
+    }
   }
   // compute_rate_deformation_gradient + update_deformation_gradient + update_stress
   if (c->learn_mode == MODE_PLAIN) {
@@ -1196,8 +1226,9 @@ int autotune(kmpm_ctx *c) {
   CK(cudaEventCreate(&e0));
   CK(cudaEventCreate(&e1));
   double t[2][G2P_NVAR] = {{0}};
+  const int k0 = c->fuse_remap ? 1 : 0;  // no separate gather kernel to tune
   for (int rep = 0; rep < 4; rep++)
-    for (int k = 0; k < 2; k++)
+    for (int k = k0; k < 2; k++)
       for (int v = 0; v < G2P_NVAR; v++) {
         void *fn = k == 0 ? c->K.g2p1_v[TL][v] : g2p2_variant(c, v);
         CK(cudaEventRecord(e0, c->st));
@@ -1221,11 +1252,16 @@ int autotune(kmpm_ctx *c) {
   c->var_g2p1 = best[0];
   c->var_g2p2 = best[1];
   char buf[512];
+  char adv[160];
+  if (c->fuse_remap)
+    std::snprintf(adv, sizeof(adv), "{\"fused_with_remap\": true}");
+  else
+    std::snprintf(adv, sizeof(adv), "{\"min_blocks\": [%d, %d, %d], \"ms\": [%.4f, %.4f, %.4f], \"chosen\": %d}",
+                  G2P1_MINB[0], G2P1_MINB[1], G2P1_MINB[2], t[0][0], t[0][1], t[0][2], G2P1_MINB[best[0]]);
   std::snprintf(buf, sizeof(buf),
-                "{\"g2p_advance\": {\"min_blocks\": [%d, %d, %d], \"ms\": [%.4f, %.4f, %.4f], \"chosen\": %d}, "
+                "{\"g2p_advance\": %s, "
                 "\"g2p_stress\": {\"min_blocks\": [%d, %d, %d], \"ms\": [%.4f, %.4f, %.4f], \"chosen\": %d}}",
-                G2P1_MINB[0], G2P1_MINB[1], G2P1_MINB[2], t[0][0], t[0][1], t[0][2], G2P1_MINB[best[0]],
-                G2P2_MINB[0], G2P2_MINB[1], G2P2_MINB[2], t[1][0], t[1][1], t[1][2], G2P2_MINB[best[1]]);
+                adv, G2P2_MINB[0], G2P2_MINB[1], G2P2_MINB[2], t[1][0], t[1][1], t[1][2], G2P2_MINB[best[1]]);
   c->tuning = buf;
   c->graph_valid = false;
   return KMPM_OK;

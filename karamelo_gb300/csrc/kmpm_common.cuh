@@ -266,6 +266,16 @@ template <> __device__ __forceinline__ void basis<3>(float r, int nt, float ih, 
   }
 }
 
+// A particle's coordinate in cells, (x - lo) / h, and its offset from node i
+// in cells, (x - (lo + i h)) / h, each rounded once: the multiplications are
+// kept out of fused multiply-adds, so that every kernel that evaluates a
+// particle's basis (the scatters, the gathers and the fused MUSL pass) gets
+// the same weights bit for bit, whatever the compiler contracts around them.
+__device__ __forceinline__ float cells_of(float x, float lo, float ih) { return __fmul_rn(x - lo, ih); }
+__device__ __forceinline__ float node_offset_cells(float x, float lo, int i, float h, float ih) {
+  return __fmul_rn(x - __fadd_rn(lo, __fmul_rn((float)i, h)), ih);
+}
+
 // Cubic B-spline values and slopes of the four nodes c-1..c+2 of a particle at
 // fractional position f in cell c, when all four have ntype 0: the same
 // polynomials as src/basis_functions.h:40-104 evaluated without branches.
@@ -304,7 +314,7 @@ template <int BASIS> struct Axis {
   __device__ __forceinline__ void eval(float xp, float lo, float ih, float h, int n, int ng) {
     // the reference truncates (src/tlmpm.cpp:145); the clamp keeps indices of a
     // non-finite or far-away position in range (such a particle raises an error)
-    float t = fminf(fmaxf((xp - lo) * ih, -4.f), (float)(n + 4));
+    float t = fminf(fmaxf(cells_of(xp, lo, ih), -4.f), (float)(n + 4));
     int c = (int)t;
     i0 = c * Stencil<BASIS>::SC - Stencil<BASIS>::LO;
     if (BASIS == 1 && cubic_interior(i0, n, ng)) {
@@ -318,8 +328,7 @@ template <int BASIS> struct Axis {
     for (int k = 0; k < S; k++) {
       int i = i0 + k;
       if (i < 0 || i >= n) { s[k] = 0.f; ds[k] = 0.f; o[k] = 0.f; continue; }
-      float xn = lo + (float)i * h;
-      float r = (xp - xn) * ih;
+      const float r = node_offset_cells(xp, lo, i, h, ih);
       basis<BASIS>(r, node_type<BASIS>(i, ng), ih, s[k], ds[k]);
       ds[k] = s[k] != 0.f ? ds[k] : 0.f;
       o[k] = -r;

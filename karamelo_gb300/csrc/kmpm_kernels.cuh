@@ -63,6 +63,12 @@ struct P2GArgs {
   int mls;                   // ULMPM MLS: internal forces from moments, Di = mls_di
   float mls_di;
   const float *mbp;          // P2G_EXT: external particle forces, 3 rows of ps floats
+  // the fused MUSL gather + re-map (k_g2p1_remap_row): what k_g2p1 reads
+  const float4 *nodeA;       // v, v_update interleaved, stride NODE_STRIDE
+  float pic_flip;
+  float boxlo[3], boxhi[3];  // ULMPM: the domain the moved particles must stay in
+  ErrState *err;
+  int indep;                 // per-solid clocks (independent instances)
 };
 
 struct GridArgs {
@@ -152,6 +158,10 @@ struct StepKernels {
   // (LAW_EOS_LINEAR_JC; 3-D, nullptr elsewhere)
   void *g2p2_jc[2][3];
   void *g2p2_jcq[3];  // 3-D cubic TLMPM, linear EOS + Johnson-Cook, queueing plastic steps
+  // MUSL gather + re-map in one pass (k_g2p1_remap_row) [TL]: 3-D cubic and
+  // quadratic splines (nullptr elsewhere), and its dynamic shared memory
+  void *g2p1_remap[2];
+  int g2p1_remap_smem;
 };
 constexpr int G2P_NVAR = 3;
 // node staging of the gathers (k_g2p1, k_g2p2): nodes of a block's stencil

@@ -255,7 +255,7 @@ __global__ void __launch_bounds__(256, (p2g_min_blocks<DIM, MODE, THERMAL>())) k
           if (it >= cnt * DIM) continue;
           const int i0d = d == 0 ? i0[0] : (d == 1 ? i0[1] : i0[2]);
           const float lod = d == 0 ? glo0 : (d == 1 ? glo1 : glo2);
-          const float t = ((d == 0 ? px : (d == 1 ? py : pz)) - lod) * ih;
+          const float t = cells_of(d == 0 ? px : (d == 1 ? py : pz), lod, ih);
           float sv[4], dsv[4];
           const float f = t - (float)(i0d + 1);
           cubic_weights(f, ih, sv, dsv);
@@ -286,8 +286,7 @@ __global__ void __launch_bounds__(256, (p2g_min_blocks<DIM, MODE, THERMAL>())) k
         const float lod = d == 0 ? glo0 : (d == 1 ? glo1 : glo2);
         float sv = 0.f, dsv = 0.f, ov = 0.f;
         if (i >= 0 && i < nd) {
-          const float xn = lod + (float)i * h;
-          const float r = ((d == 0 ? px : (d == 1 ? py : pz)) - xn) * ih;
+          const float r = node_offset_cells(d == 0 ? px : (d == 1 ? py : pz), lod, i, h, ih);
           basis<BASIS>(r, node_type<BASIS>(i, ngd), ih, sv, dsv);
           dsv = sv != 0.f ? dsv : 0.f;  // as Axis::eval
           ov = -r;
@@ -520,7 +519,7 @@ __global__ void __launch_bounds__(256, (MODE == P2G_VEL ? 4 : 3)) k_p2g_row(P2GA
           const int ngd = d == 0 ? g.ng[0] : (d == 1 ? g.ng[1] : g.ng[2]);
           float sv[S], dsv[S];
           if (BASIS == 1 && cubic_interior(i0[d], nd, ngd)) {
-            cubic_weights((xp - lod) * ih - (float)(i0[d] + 1), ih, sv, dsv);
+            cubic_weights(cells_of(xp, lod, ih) - (float)(i0[d] + 1), ih, sv, dsv);
           } else {
 #pragma unroll
             for (int kk = 0; kk < S; kk++) {
@@ -528,7 +527,7 @@ __global__ void __launch_bounds__(256, (MODE == P2G_VEL ? 4 : 3)) k_p2g_row(P2GA
               sv[kk] = 0.f;
               dsv[kk] = 0.f;
               if (i >= 0 && i < nd) {
-                const float r = (xp - (lod + (float)i * h)) * ih;
+                const float r = node_offset_cells(xp, lod, i, h, ih);
                 basis<BASIS>(r, node_type<BASIS>(i, ngd), ih, sv[kk], dsv[kk]);
                 dsv[kk] = sv[kk] != 0.f ? dsv[kk] : 0.f;  // as Axis::eval
               }
@@ -849,13 +848,23 @@ __global__ void __launch_bounds__(256, MINB) k_g2p1(PartArgs a) {
   const int i0[3] = {ax.ax[0].i0, ax.ax[1].i0, ax.ax[2].i0};
   int lo[3], nb[3], vol;
   const bool staged = stage_box<DIM, S>(valid, i0, G2P_STAGE_NODES, lo, nb, vol);
+  // mechanical runs stage the six values of a node as a float4 (v, v_update.x)
+  // and a float2 (v_update.y, v_update.z) in two arrays: two loads of 6
+  // shared-memory wavefronts per warp and node, where two float4 take 8;
+  // thermal runs stage (v, -) and (v_update, T)
+  float2 *stage2 = reinterpret_cast<float2 *>(g2p_stage + G2P_STAGE_NODES);
   if (staged) {
     for (int e = threadIdx.x; e < vol; e += blockDim.x) {
       const int n = stage_node(g, lo, nb, e);
       float4 A = make_float4(0.f, 0.f, 0.f, 0.f), B = A;
       if (n >= 0) ld_node_pair(NA + NODE_STRIDE * n, A, B);
-      g2p_stage[2 * e] = A;
-      g2p_stage[2 * e + 1] = B;
+      if (THERMAL) {
+        g2p_stage[2 * e] = A;
+        g2p_stage[2 * e + 1] = B;
+      } else {
+        g2p_stage[e] = make_float4(A.x, A.y, A.z, B.x);
+        stage2[e] = make_float2(B.y, B.z);
+      }
     }
     __syncthreads();
   }
@@ -869,11 +878,20 @@ __global__ void __launch_bounds__(256, MINB) k_g2p1(PartArgs a) {
 #pragma unroll
       for (int j = 0; j < SY; j++) {
         const float sxy = ax.ax[0].s[i] * ax.ax[1].s[j];
-        const float4 *row = g2p_stage + 2 * (base + (i * nb[1] + j) * nb[2]);
+        const int r = base + (i * nb[1] + j) * nb[2];
 #pragma unroll
         for (int k = 0; k < SZ; k++) {
           const float w = sxy * ax.ax[2].s[k];
-          const float4 A = row[2 * k], B = row[2 * k + 1];
+          float4 A, B;
+          if (THERMAL) {
+            A = g2p_stage[2 * (r + k)];
+            B = g2p_stage[2 * (r + k) + 1];
+          } else {
+            const float4 A4 = g2p_stage[r + k];
+            const float2 B2 = stage2[r + k];
+            A = A4;
+            B = make_float4(A4.w, B2.x, B2.y, 0.f);
+          }
           vu[0] = fmaf(w, B.x, vu[0]); vu[1] = fmaf(w, B.y, vu[1]); vu[2] = fmaf(w, B.z, vu[2]);
           va[0] = fmaf(w, A.x, va[0]); va[1] = fmaf(w, A.y, va[1]); va[2] = fmaf(w, A.z, va[2]);
           if (THERMAL) Tp = fmaf(w, B.w, Tp);
@@ -938,6 +956,234 @@ __global__ void __launch_bounds__(256, MINB) k_g2p1(PartArgs a) {
           xn[2] >= a.boxlo[2] && xn[2] <= a.boxhi[2]))
       raise_error(a.err, ERR_LEFT, p, sc.ntimestep);
   }
+}
+
+// MUSL grid_to_points + advance_particles + velocities_to_grid in one pass
+// (src/musl.cpp:59-67; src/tlmpm.cpp:418-452, src/ulmpm.cpp:386-451): the
+// gather of k_g2p1 and the re-map scatter of k_p2g_row<.., P2G_VEL> for the
+// particles of one tile, whose weights both phases share.  3-D, cubic and
+// quadratic splines, FLIP/PIC transfers, mechanical runs.
+//   - the tile's node footprint of (v, v_update) is staged in shared memory
+//     once (a float4 (v, v_update.x) and a float2 (v_update.y, v_update.z)
+//     per node);
+//   - each warp walks its rows of cells as k_p2g_row does; in the stage phase
+//     a lane evaluates its particle's basis values, gathers the 64 nodes from
+//     the staged footprint in k_g2p1's order, writes the particle's new
+//     velocity and position, and stages m v_new for the re-map;
+//   - accumulate and flush as k_p2g_row<.., P2G_VEL>.
+// Every sum has the order of the two separate kernels, so the results are
+// the same bit for bit (KMPM_SPLIT_MUSL=1 selects the separate kernels).
+template <int BASIS, bool TL>
+__global__ void __launch_bounds__(256, 3) k_g2p1_remap_row(P2GArgs a) {
+  static_assert(Stencil<BASIS>::S == 4 && Stencil<BASIS>::SC == 1, "four-wide stencils");
+  using TS = TileShape<3, BASIS>;
+  constexpr int S = 4, LO = Stencil<BASIS>::LO;
+  constexpr int TX = TS::TX, TY = TS::TY, TZ = TS::TZ;
+  constexpr int WY = TS::WY, WZ = TS::WZ, NW = TS::NW, NF = TS::NF, FX = TS::FX;
+  static_assert(TS::L == 1 && TZ == 4 && FX == 4, "one x-layer of 4 x 4 cells per warp");
+  constexpr int Q = 3;                       // m v
+  constexpr int SLAB = (Q * NF + 3) & ~3;
+  constexpr int SROW = 33;                   // basis rows of one float per staged particle, padded
+  constexpr int STAGE = 32 * 4 + SROW * 3 * S;
+  constexpr int NWP = (NW + 1) & ~1;
+
+  extern __shared__ __align__(16) float smem[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  float *slab = smem + warp * SLAB;
+  float *spay = smem + TS::NWARP * SLAB + warp * STAGE;  // [32][4]
+  float *sbas = spay + 32 * 4;                           // [axis][slot][SROW]
+  float4 *fpA = reinterpret_cast<float4 *>(smem + TS::NWARP * (SLAB + STAGE));
+  float2 *fpB = reinterpret_cast<float2 *>(fpA + NWP);
+
+  const int2 td = a.tiles[blockIdx.x];
+  const GridDev g = a.grids[td.x];
+  const int tlin = td.y;
+  const int tile_global = g.tile_off + tlin;
+  if (a.tile_end[tile_global] == a.tile_start[tile_global] || run_finished(a.scalars)) return;
+  const int tc2 = tlin % g.ntile[2], tc1 = (tlin / g.ntile[2]) % g.ntile[1], tc0 = tlin / (g.ntile[1] * g.ntile[2]);
+  const float h = g.cellsize, ih = g.inv_cellsize;
+  float *P = *a.Pp;
+  const size_t ps = a.ps;
+  const StepScalars &sc = a.scalars[a.indep ? g.solid0 : 0];
+  const float dt = (float)sc.dt;
+  const float alpha = a.pic_flip;
+
+  for (int k = lane; k < Q * NF; k += 32) slab[k] = 0.f;
+  // the tile's node footprint: nodes (tc TX - LO + fx, ...), fx < WX
+  {
+    const float4 *__restrict__ NA = a.nodeA + NODE_STRIDE * g.node_off;
+    const int b0 = tc0 * TX - LO, b1 = tc1 * TY - LO, b2 = tc2 * TZ - LO;
+    for (int e = threadIdx.x; e < NW; e += blockDim.x) {
+      const int fz = e % WZ, fy = (e / WZ) % WY, fx = e / (WY * WZ);
+      const int ix = b0 + fx, iy = b1 + fy, iz = b2 + fz;
+      float4 A = make_float4(0.f, 0.f, 0.f, 0.f), B = A;
+      if (ix >= 0 && ix < g.n[0] && iy >= 0 && iy < g.n[1] && iz >= 0 && iz < g.n[2])
+        ld_node_pair(NA + NODE_STRIDE * ((ix * g.n[1] + iy) * g.n[2] + iz), A, B);
+      fpA[e] = make_float4(A.x, A.y, A.z, B.x);
+      fpB[e] = make_float2(B.y, B.z);
+    }
+  }
+  __syncthreads();
+
+  const int sa = lane >> 3, sb = (lane >> 1) & 3, sc_ = lane & 1;
+  const float *px = sbas + (0 * S + sa) * SROW, *py = sbas + (1 * S + sb) * SROW;
+  const float *pz0 = sbas + (2 * S + sc_) * SROW, *pz2 = sbas + (2 * S + sc_ + 2) * SROW;
+  const int i0x = (tc0 * TX + warp) - LO;
+
+  for (int ly = 0; ly < TY; ly++) {
+    const int cbase = tile_global * TS::NCELL + (warp * TY + ly) * TZ;
+    const int cv = lane < 8 ? (lane < 4 ? a.cell_start[cbase + lane] : a.cell_end[cbase + lane - 4]) : 0;
+    int st[4], en[4], lo4[4];
+    int rs = INT_MAX, re = INT_MIN;
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      st[k] = __shfl_sync(0xffffffffu, cv, k);
+      en[k] = __shfl_sync(0xffffffffu, cv, 4 + k);
+      const bool full = en[k] > st[k];
+      lo4[k] = full ? st[k] : INT_MAX;
+      rs = full ? min(rs, st[k]) : rs;
+      re = full ? max(re, en[k]) : re;
+    }
+    if (rs == INT_MAX) continue;
+    const int i0y = (tc1 * TY + ly) - LO;
+    float acc[6][Q];
+#pragma unroll
+    for (int m = 0; m < 6; m++)
+#pragma unroll
+      for (int qq = 0; qq < Q; qq++) acc[m][qq] = 0.f;
+
+    for (int c0 = rs; c0 < re; c0 += 32) {
+      const int cnt = min(32, re - c0);
+      // ---- stage (lane = particle): weights, gather, particle update, payload
+      if (lane < cnt) {
+        const int p = c0 + lane;
+        int lz = 0;
+#pragma unroll
+        for (int k = 1; k < 4; k++) lz = lo4[k] <= p ? k : lz;
+        const int i0[3] = {i0x, i0y, (tc2 * TZ + lz) - LO};
+        float sv[3][S], up[3];
+#pragma unroll
+        for (int d = 0; d < 3; d++) {
+          up[d] = P[(PF_X + d) * ps + p];
+          const float xp = P[(PF_X0 + d) * ps + p] + (TL ? 0.f : up[d]);
+          const float lod = d == 0 ? g.lo[0] : (d == 1 ? g.lo[1] : g.lo[2]);
+          const int nd = d == 0 ? g.n[0] : (d == 1 ? g.n[1] : g.n[2]);
+          const int ngd = d == 0 ? g.ng[0] : (d == 1 ? g.ng[1] : g.ng[2]);
+          float dsv[S];
+          if (BASIS == 1 && cubic_interior(i0[d], nd, ngd)) {
+            cubic_weights(cells_of(xp, lod, ih) - (float)(i0[d] + 1), ih, sv[d], dsv);
+          } else {
+#pragma unroll
+            for (int kk = 0; kk < S; kk++) {
+              const int i = i0[d] + kk;
+              sv[d][kk] = 0.f;
+              dsv[kk] = 0.f;
+              if (i >= 0 && i < nd) {
+                const float r = node_offset_cells(xp, lod, i, h, ih);
+                basis<BASIS>(r, node_type<BASIS>(i, ngd), ih, sv[d][kk], dsv[kk]);
+              }
+            }
+          }
+#pragma unroll
+          for (int kk = 0; kk < S; kk++) sbas[(d * S + kk) * SROW + lane] = sv[d][kk];
+        }
+        // the gather of k_g2p1 from the footprint: stencil node (i, j, k) is
+        // footprint node (warp + i, ly + j, lz + k)
+        float vu[3] = {0.f, 0.f, 0.f}, va[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+        for (int i = 0; i < S; i++) {
+#pragma unroll
+          for (int j = 0; j < S; j++) {
+            const float sxy = sv[0][i] * sv[1][j];
+            const int r = ((warp + i) * WY + (ly + j)) * WZ + lz;
+#pragma unroll
+            for (int k = 0; k < S; k++) {
+              const float w = sxy * sv[2][k];
+              const float4 A = fpA[r + k];
+              const float2 B = fpB[r + k];
+              vu[0] = fmaf(w, A.w, vu[0]); vu[1] = fmaf(w, B.x, vu[1]); vu[2] = fmaf(w, B.y, vu[2]);
+              va[0] = fmaf(w, A.x, va[0]); va[1] = fmaf(w, A.y, va[1]); va[2] = fmaf(w, A.z, va[2]);
+            }
+          }
+        }
+        const float m = P[PF_MASS * ps + p];
+        float xn[3];
+#pragma unroll
+        for (int d = 0; d < 3; d++) {
+          const float v = P[(PF_V + d) * ps + p];
+          const float vnew = (1.f - alpha) * vu[d] + alpha * (v + (vu[d] - va[d]));
+          const float un = up[d] + dt * vu[d];
+          if (TL) {
+            P[(PF_X + d) * ps + p] = un;
+          } else {
+            P[(PF_XN + d) * ps + p] = un;
+            xn[d] = P[(PF_X0 + d) * ps + p] + un;
+          }
+          P[(PF_V + d) * ps + p] = vnew;
+          spay[lane * 4 + d] = m * vnew;
+        }
+        if (!TL && !(xn[0] >= a.boxlo[0] && xn[0] <= a.boxhi[0] && xn[1] >= a.boxlo[1] && xn[1] <= a.boxhi[1] &&
+                     xn[2] >= a.boxlo[2] && xn[2] <= a.boxhi[2]))
+          raise_error(a.err, ERR_LEFT, p, sc.ntimestep);
+      }
+      __syncwarp();
+      // ---- accumulate (lane = node): cell after cell, particles in sorted order
+#pragma unroll
+      for (int lz = 0; lz < 4; lz++) {
+        const int jlo = max(st[lz] - c0, 0), jhi = min(en[lz] - c0, cnt);
+        for (int j = jlo; j < jhi; j++) {
+          const float4 t4 = reinterpret_cast<const float4 *>(spay)[j];
+          const float wxy = px[j] * py[j];
+          const float q0 = wxy * t4.x, q1 = wxy * t4.y, q2 = wxy * t4.z;
+          const float z0 = pz0[j], z2 = pz2[j];
+          acc[lz][0] = fmaf(z0, q0, acc[lz][0]);
+          acc[lz][1] = fmaf(z0, q1, acc[lz][1]);
+          acc[lz][2] = fmaf(z0, q2, acc[lz][2]);
+          acc[lz + 2][0] = fmaf(z2, q0, acc[lz + 2][0]);
+          acc[lz + 2][1] = fmaf(z2, q1, acc[lz + 2][1]);
+          acc[lz + 2][2] = fmaf(z2, q2, acc[lz + 2][2]);
+        }
+      }
+      __syncwarp();
+    }
+    // ---- flush (as k_p2g_row)
+#pragma unroll
+    for (int m = 0; m < 5; m++)
+#pragma unroll
+      for (int qq = 0; qq < Q; qq++) {
+        const float o = __shfl_xor_sync(0xffffffffu, acc[m][qq], 1);
+        if (sc_ == 0) acc[m + 1][qq] += o;
+      }
+    const int fy = ly + sb;
+#pragma unroll
+    for (int m = 0; m < 6; m++) {
+      if (sc_ == 1 && m < 5) continue;
+      const int fz = m + sc_;
+      const int fi = (sa * WY + fy) * WZ + fz;
+#pragma unroll
+      for (int qq = 0; qq < Q; qq++) slab[qq * NF + fi] += acc[m][qq];
+    }
+    __syncwarp();
+  }
+  __syncthreads();
+  // ---- sum the slabs in warp order into the tile footprint
+  float *out = a.partial + (size_t)tile_global * a.pstride_tile;
+  for (int k = threadIdx.x; k < Q * NW; k += blockDim.x) {
+    const int qq = k / NW, fi = k % NW;
+    const int fx = fi / (WY * WZ), fyz = fi % (WY * WZ);
+    float sum = 0.f;
+#pragma unroll
+    for (int w = 0; w < TS::NWARP; w++) {
+      const int x = fx - w;
+      if (x >= 0 && x < FX) sum += smem[w * SLAB + qq * NF + x * WY * WZ + fyz];
+    }
+    out[k] = sum;
+  }
+}
+// dynamic shared memory of k_g2p1_remap_row (bytes)
+template <int BASIS> constexpr int g2p1_remap_smem() {
+  using TS = TileShape<3, BASIS>;
+  return 4 * (TS::NWARP * (((3 * TS::NF + 3) & ~3) + 32 * 4 + 33 * 3 * 4) + 6 * ((TS::NW + 1) & ~1));
 }
 
 // Node sources of the velocity-gradient gather: (v, T) of stencil node
@@ -1401,8 +1647,13 @@ void fill_step_kernels(StepKernels &k) {
     k.p2g_row[0] = (void *)k_p2g_row<BASIS, P2G_TL>;
     k.p2g_row[1] = (void *)k_p2g_row<BASIS, P2G_UL>;
     k.p2g_row[2] = (void *)k_p2g_row<BASIS, P2G_VEL>;
+    k.g2p1_remap[0] = (void *)k_g2p1_remap_row<BASIS, false>;
+    k.g2p1_remap[1] = (void *)k_g2p1_remap_row<BASIS, true>;
+    k.g2p1_remap_smem = g2p1_remap_smem<BASIS>();
   } else {
     k.p2g_row[0] = k.p2g_row[1] = k.p2g_row[2] = nullptr;
+    k.g2p1_remap[0] = k.g2p1_remap[1] = nullptr;
+    k.g2p1_remap_smem = 0;
   }
   // APIC runs with the cubic and quadratic splines, and for TLMPM with the
   // linear basis (src/solid.cpp:1447-1473)

@@ -98,6 +98,7 @@ def test_gpu_matches_reference(gpu_lib, name):
         assert abs(st["dt"] / float(fx[f"{lab}__dt"]) - 1) < 1e-5
         assert abs(st["time"] / float(fx[f"{lab}__time"]) - 1) < 1e-5
         err = RC.compare(fx, lab, st)
+        print(f"\n{name} {lab}: " + ", ".join(f"{f} {err[f]:.2e}" for f in GPU_TOL[name]))
         for f, tol in GPU_TOL[name].items():
             assert err[f] < tol, f"{name} {lab} {f}: rel L2 {err[f]:.3e} >= {tol}"
             assert err[f"rss_{f}"] < tol, f"{name} {lab} rss {f}: {err['rss_' + f]:.3e} >= {tol}"
@@ -133,9 +134,11 @@ def test_gpu_two_disks_3000_steps(gpu_lib):
     assert np.max(np.abs(states["s100"]["sigma"])) < 1e-2  # Pa; the collision stresses are ~100 Pa
     for lab, fl in C1_FLOOR.items():
         err = RC.compare(fx, lab, states[lab])
+        print(f"\n{name} {lab}: " + ", ".join(f"{f} {err[f]:.2e}" for f in fl))
         for f, floor in fl.items():
             assert err[f] < C1_FACTOR * floor, f"{lab} {f}: {err[f]:.3e} >= {C1_FACTOR} x floor {floor:.1e}"
     ref = fx["E__vals"]
     assert np.array_equal(E[:, 0], fx["E__step"])
     dev = np.max(np.abs(E[:, 2:].sum(1) - ref.sum(1))) / np.max(ref.sum(1))
+    print(f"\n{name} Ek + Es over 3000 steps: {dev:.2e} of the largest total")
     assert dev < C1_FACTOR * C1_ENERGY_FLOOR, f"Ek + Es: {dev:.3e}"
