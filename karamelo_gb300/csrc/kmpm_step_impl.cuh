@@ -959,7 +959,7 @@ __global__ void __launch_bounds__(256, MINB) k_g2p1(PartArgs a) {
 }
 
 // MUSL grid_to_points + advance_particles + velocities_to_grid in one pass
-// (src/musl.cpp:59-67; src/tlmpm.cpp:418-452, src/ulmpm.cpp:386-451): the
+// (src/musl.cpp:59-67; src/tlmpm.cpp:418-452, src/ulmpm.cpp:442-496): the
 // gather of k_g2p1 and the re-map scatter of k_p2g_row<.., P2G_VEL> for the
 // particles of one tile, whose weights both phases share.  3-D, cubic and
 // quadratic splines, FLIP/PIC transfers, mechanical runs.
@@ -974,7 +974,7 @@ __global__ void __launch_bounds__(256, MINB) k_g2p1(PartArgs a) {
 // Every sum has the order of the two separate kernels, so the results are
 // the same bit for bit (KMPM_SPLIT_MUSL=1 selects the separate kernels).
 template <int BASIS, bool TL>
-__global__ void __launch_bounds__(256, 3) k_g2p1_remap_row(P2GArgs a) {
+__global__ void __launch_bounds__(256, 4) k_g2p1_remap_row(P2GArgs a) {
   static_assert(Stencil<BASIS>::S == 4 && Stencil<BASIS>::SC == 1, "four-wide stencils");
   using TS = TileShape<3, BASIS>;
   constexpr int S = 4, LO = Stencil<BASIS>::LO;
