@@ -441,7 +441,7 @@ int build(kmpm_ctx *c) {
   const int dim = c->prm.dim, basis = c->prm.basis;
   if (c->hsolids.empty()) return fail(c, KMPM_ERR_STATE, "no solid was added");
   get_step_kernels(dim, basis, c->K);
-  // the plain 3-D four-wide scatters by cell rows (KMPM_CELL_SCATTER=1: cell by cell)
+  // the plain 2-D and 3-D four-wide scatters by cell rows (KMPM_CELL_SCATTER=1: cell by cell)
   if (c->K.p2g_row[0]) {
     const char *ev = std::getenv("KMPM_CELL_SCATTER");
     if (!(ev && ev[0] == '1')) {

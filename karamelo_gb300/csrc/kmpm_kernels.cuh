@@ -141,8 +141,8 @@ struct LaunchSet {
 // kernel entry points of one (dim, basis) instantiation
 struct StepKernels {
   void *p2g_mass, *p2g_tl, *p2g_tl_th, *p2g_ul, *p2g_ul_th, *p2g_vel, *p2g_vel_th;
-  // the row scatter (k_p2g_row) of the plain TL, UL and velocity modes: 3-D
-  // cubic and quadratic splines (nullptr elsewhere)
+  // the row scatters (k_p2g_row, k_p2g_row2) of the plain TL, UL and
+  // velocity modes: 2-D and 3-D cubic and quadratic splines (nullptr elsewhere)
   void *p2g_row[3];
   void *p2g_tl_apic, *p2g_ul_apic, *p2g_vel_apic;  // cubic spline only (nullptr otherwise)
   // the force scatters with external particle forces (P2G_EXT): [thermal]

@@ -590,6 +590,218 @@ __global__ void __launch_bounds__(256, (MODE == P2G_VEL ? 4 : 3)) k_p2g_row(P2GA
   }
 }
 
+// ============================================================== 2-D P2G by cell rows
+// The scatter of the 2-D four-wide stencils (cubic and quadratic B-splines)
+// for the plain modes, on the tiles, warps and slab footprints of k_p2g (a
+// warp owns two x-columns of 16 cells).  A column is visited in rows of 4
+// cells along y (contiguous in the sorted order):
+//   - stage (lane = particle): up to 32 particles of the row, each lane its
+//     own particle's payload and per-axis basis values;
+//   - accumulate: four lane groups of 8 take the row's particles in turn
+//     (particle j of the row goes to group j mod 4, j counted from the row's
+//     first particle); lane (a, c) of a group adds into x slot a and y slots
+//     c and c + 2 of each of its particles, six register accumulators over
+//     the row's y nodes c .. c + 5, as k_p2g_row does along z;
+//   - flush once per row: a fixed butterfly adds the four groups, the c = 1
+//     lanes hand their y = 1..5 sums to the c = 0 lanes, and group 0 adds
+//     the row into the warp's slab.
+// Every sum runs in a fixed order: the result is bit-reproducible.
+template <int BASIS, int MODE>
+__global__ void __launch_bounds__(256, (MODE == P2G_VEL ? 4 : 3)) k_p2g_row2(P2GArgs a) {
+  static_assert(Stencil<BASIS>::S == 4 && Stencil<BASIS>::SC == 1, "four-wide stencils");
+  using TS = TileShape<2, BASIS>;
+  constexpr int S = 4, LO = Stencil<BASIS>::LO;
+  constexpr int TX = TS::TX, TY = TS::TY, L = TS::L;
+  constexpr int WY = TS::WY, NW = TS::NW, NF = TS::NF, FX = TS::FX;
+  static_assert(TY % 4 == 0 && TS::WZ == 1, "rows of 4 cells along y");
+  constexpr int Q = p2g_nq(MODE, false);
+  constexpr int QIN = p2g_nin(MODE, false);
+  constexpr int QINP = (QIN + 3) & ~3;
+  constexpr int SLAB = (Q * NF + 3) & ~3;
+  constexpr int SROW = 33;
+  constexpr int STAGE = 32 * QINP + SROW * 2 * S * 2;
+  constexpr int OM = MODE == P2G_UL ? 1 : 0;  // UL sums start with the mass
+  constexpr bool FORCE = MODE != P2G_VEL;
+
+  extern __shared__ __align__(16) float smem[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  float *slab = smem + warp * SLAB;
+  float *spay = smem + TS::NWARP * SLAB + warp * STAGE;           // [32][QINP]
+  float2 *sbas = reinterpret_cast<float2 *>(spay + 32 * QINP);    // [axis][slot][SROW]
+
+  const int2 td = a.tiles[blockIdx.x];
+  const GridDev g = a.grids[td.x];
+  const int tlin = td.y;
+  const int tile_global = g.tile_off + tlin;
+  if (a.tile_end[tile_global] == a.tile_start[tile_global] || run_finished(a.scalars)) return;
+  const int tc1 = tlin % g.ntile[1], tc0 = tlin / g.ntile[1];
+  const float h = g.cellsize, ih = g.inv_cellsize;
+  const float *P = *a.Pp;
+  const size_t ps = a.ps;
+  const bool use_u = a.pos_field == PF_X;
+
+  for (int k = lane; k < Q * NF; k += 32) slab[k] = 0.f;
+
+  const int grp = lane >> 3, sa = (lane >> 1) & 3, sc = lane & 1;
+  const float2 *px = sbas + (0 * S + sa) * SROW;
+  const float2 *py0 = sbas + (1 * S + sc) * SROW, *py2 = sbas + (1 * S + sc + 2) * SROW;
+
+  for (int lx = 0; lx < L; lx++) {
+    const int i0x = (tc0 * TX + warp * L + lx) - LO;
+    for (int ly0 = 0; ly0 < TY; ly0 += 4) {
+      // the row's four cells (local index lx' TY + ly) and their ranges
+      const int cbase = tile_global * TS::NCELL + (warp * L + lx) * TY + ly0;
+      const int cv = lane < 8 ? (lane < 4 ? a.cell_start[cbase + lane] : a.cell_end[cbase + lane - 4]) : 0;
+      int st[4], en[4], lo4[4];
+      int rs = INT_MAX, re = INT_MIN;
+#pragma unroll
+      for (int k = 0; k < 4; k++) {
+        st[k] = __shfl_sync(0xffffffffu, cv, k);
+        en[k] = __shfl_sync(0xffffffffu, cv, 4 + k);
+        const bool full = en[k] > st[k];
+        lo4[k] = full ? st[k] : INT_MAX;
+        rs = full ? min(rs, st[k]) : rs;
+        re = full ? max(re, en[k]) : re;
+      }
+      if (rs == INT_MAX) continue;
+      float acc[6][Q];
+#pragma unroll
+      for (int m = 0; m < 6; m++)
+#pragma unroll
+        for (int qq = 0; qq < Q; qq++) acc[m][qq] = 0.f;
+
+      for (int c0 = rs; c0 < re; c0 += 32) {
+        const int cnt = min(32, re - c0);
+        // ---- stage (lane = particle)
+        if (lane < cnt) {
+          const int p = c0 + lane;
+          int ly = 0;  // the non-empty cell holding p: the last one starting at or before it
+#pragma unroll
+          for (int k = 1; k < 4; k++) ly = lo4[k] <= p ? k : ly;
+          float pay[QIN];
+          p2g_payload<MODE, false>(a, P, p, pay);
+#pragma unroll
+          for (int v = 0; v < QINP / 4; v++)
+            reinterpret_cast<float4 *>(spay + lane * QINP)[v] =
+                make_float4(pay[4 * v], 4 * v + 1 < QIN ? pay[min(4 * v + 1, QIN - 1)] : 0.f,
+                            4 * v + 2 < QIN ? pay[min(4 * v + 2, QIN - 1)] : 0.f,
+                            4 * v + 3 < QIN ? pay[min(4 * v + 3, QIN - 1)] : 0.f);
+          const int i0[2] = {i0x, (tc1 * TY + ly0 + ly) - LO};
+#pragma unroll
+          for (int d = 0; d < 2; d++) {
+            const float xp = P[(PF_X0 + d) * ps + p] + (use_u ? P[(PF_X + d) * ps + p] : 0.f);
+            const float lod = d == 0 ? g.lo[0] : g.lo[1];
+            const int nd = d == 0 ? g.n[0] : g.n[1];
+            const int ngd = d == 0 ? g.ng[0] : g.ng[1];
+            float sv[S], dsv[S];
+            if (BASIS == 1 && cubic_interior(i0[d], nd, ngd)) {
+              cubic_weights(cells_of(xp, lod, ih) - (float)(i0[d] + 1), ih, sv, dsv);
+            } else {
+#pragma unroll
+              for (int kk = 0; kk < S; kk++) {
+                const int i = i0[d] + kk;
+                sv[kk] = 0.f;
+                dsv[kk] = 0.f;
+                if (i >= 0 && i < nd) {
+                  const float r = node_offset_cells(xp, lod, i, h, ih);
+                  basis<BASIS>(r, node_type<BASIS>(i, ngd), ih, sv[kk], dsv[kk]);
+                  dsv[kk] = sv[kk] != 0.f ? dsv[kk] : 0.f;  // as Axis::eval
+                }
+              }
+            }
+#pragma unroll
+            for (int kk = 0; kk < S; kk++) sbas[(d * S + kk) * SROW + lane] = make_float2(sv[kk], dsv[kk]);
+          }
+        }
+        __syncwarp();
+        // ---- accumulate: group grp takes particles j = grp, grp + 4, ... of
+        // each cell's share of this chunk (c0 - rs is a multiple of 32)
+#pragma unroll
+        for (int ly = 0; ly < 4; ly++) {
+          const int jlo = max(st[ly] - c0, 0), jhi = min(en[ly] - c0, cnt);
+          for (int j = jlo + ((grp - jlo - (c0 - rs)) & 3); j < jhi; j += 4) {
+            float pay[QINP];
+#pragma unroll
+            for (int v = 0; v < QINP / 4; v++) {
+              const float4 t4 = reinterpret_cast<const float4 *>(spay + j * QINP)[v];
+              pay[4 * v] = t4.x; pay[4 * v + 1] = t4.y; pay[4 * v + 2] = t4.z; pay[4 * v + 3] = t4.w;
+            }
+            const float2 bx = px[j], b0 = py0[j], b2 = py2[j];
+            // momentum (and UL mass): w = sx sy; force: -(T[r][0] dsx sy + T[r][1] sx dsy)
+            float q[3 + OM];
+#pragma unroll
+            for (int d = 0; d < 3 + OM; d++) q[d] = bx.x * pay[d];
+#pragma unroll
+            for (int d = 0; d < 3 + OM; d++) {
+              if (d == OM + 2) continue;  // v_z = 0 in 2-D: the sum stays 0
+              acc[ly][d] = fmaf(b0.x, q[d], acc[ly][d]);
+              acc[ly + 2][d] = fmaf(b2.x, q[d], acc[ly + 2][d]);
+            }
+            if (FORCE) {
+#pragma unroll
+              for (int r = 0; r < 2; r++) {
+                float T0, T1;
+                if (MODE == P2G_TL) {  // vol0 PK1, row-major
+                  T0 = pay[3 + 3 * r]; T1 = pay[4 + 3 * r];
+                } else {  // vol sigma, symmetric xx yy zz xy xz yz
+                  const float *sg = pay + 4;
+                  T0 = r == 0 ? sg[0] : sg[3];
+                  T1 = r == 0 ? sg[3] : sg[1];
+                }
+                const float tx = T0 * bx.y, ty = T1 * bx.x;
+                acc[ly][3 + OM + r] = fmaf(-b0.x, tx, fmaf(-b0.y, ty, acc[ly][3 + OM + r]));
+                acc[ly + 2][3 + OM + r] = fmaf(-b2.x, tx, fmaf(-b2.y, ty, acc[ly + 2][3 + OM + r]));
+              }
+            }
+          }
+        }
+        __syncwarp();
+      }
+      // ---- flush: add the four groups (fixed butterfly), then lanes c = 1
+      // hand their y = 1..5 sums to the c = 0 lanes (a fixed order)
+#pragma unroll
+      for (int m = 0; m < 6; m++)
+#pragma unroll
+        for (int qq = 0; qq < Q; qq++) {
+          acc[m][qq] += __shfl_xor_sync(0xffffffffu, acc[m][qq], 8);
+          acc[m][qq] += __shfl_xor_sync(0xffffffffu, acc[m][qq], 16);
+        }
+#pragma unroll
+      for (int m = 0; m < 5; m++)
+#pragma unroll
+        for (int qq = 0; qq < Q; qq++) {
+          const float o = __shfl_xor_sync(0xffffffffu, acc[m][qq], 1);
+          if (sc == 0) acc[m + 1][qq] += o;
+        }
+      if (grp == 0) {
+#pragma unroll
+        for (int m = 0; m < 6; m++) {
+          if (sc == 1 && m < 5) continue;
+          const int fy = ly0 + m + sc;
+          const int fi = (lx + sa) * WY + fy;
+#pragma unroll
+          for (int qq = 0; qq < Q; qq++) slab[qq * NF + fi] += acc[m][qq];
+        }
+      }
+      __syncwarp();
+    }
+  }
+  __syncthreads();
+  // ---- sum the slabs in warp order into the tile footprint
+  float *out = a.partial + (size_t)tile_global * a.pstride_tile;
+  for (int k = threadIdx.x; k < Q * NW; k += blockDim.x) {
+    const int qq = k / NW, fi = k % NW;
+    const int fx = fi / WY, fy = fi % WY;
+    float sum = 0.f;
+#pragma unroll
+    for (int w = 0; w < TS::NWARP; w++) {
+      const int x = fx - w * L;
+      if (x >= 0 && x < FX) sum += smem[w * SLAB + qq * NF + x * WY + fy];
+    }
+    out[k] = sum;
+  }
+}
+
 // ============================================================== grid
 // Sum of the tile partials covering one node, in a fixed tile order.
 template <int DIM, int BASIS, int Q, typename ACC>
@@ -1650,6 +1862,12 @@ void fill_step_kernels(StepKernels &k) {
     k.g2p1_remap[0] = (void *)k_g2p1_remap_row<BASIS, false>;
     k.g2p1_remap[1] = (void *)k_g2p1_remap_row<BASIS, true>;
     k.g2p1_remap_smem = g2p1_remap_smem<BASIS>();
+  } else if constexpr (DIM == 2 && (BASIS == 1 || BASIS == 3)) {
+    k.p2g_row[0] = (void *)k_p2g_row2<BASIS, P2G_TL>;
+    k.p2g_row[1] = (void *)k_p2g_row2<BASIS, P2G_UL>;
+    k.p2g_row[2] = (void *)k_p2g_row2<BASIS, P2G_VEL>;
+    k.g2p1_remap[0] = k.g2p1_remap[1] = nullptr;
+    k.g2p1_remap_smem = 0;
   } else {
     k.p2g_row[0] = k.p2g_row[1] = k.p2g_row[2] = nullptr;
     k.g2p1_remap[0] = k.g2p1_remap[1] = nullptr;
