@@ -266,6 +266,14 @@ template <> __device__ __forceinline__ void basis<3>(float r, int nt, float ih, 
   }
 }
 
+// Packed FP32 pairs (sm_100 and later): one instruction issues two IEEE
+// single-precision operations, each rounded exactly as the scalar fmaf / fmul
+// would round it, so a loop written with them gives the same bits as its
+// scalar form while taking half the issue slots.  bc2(x) is the pair (x, x).
+__device__ __forceinline__ float2 bc2(float x) { return make_float2(x, x); }
+__device__ __forceinline__ float2 ffma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 fmul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+
 // A particle's coordinate in cells, (x - lo) / h, and its offset from node i
 // in cells, (x - (lo + i h)) / h, each rounded once: the multiplications are
 // kept out of fused multiply-adds, so that every kernel that evaluates a

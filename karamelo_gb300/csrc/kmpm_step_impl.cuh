@@ -1301,23 +1301,32 @@ __global__ void __launch_bounds__(256, 4) k_g2p1_remap_row(P2GArgs a) {
         }
         // the gather of k_g2p1 from the footprint: stencil node (i, j, k) is
         // footprint node (warp + i, ly + j, lz + k)
-        float vu[3] = {0.f, 0.f, 0.f}, va[3] = {0.f, 0.f, 0.f};
+        // in packed pairs (v_x, v_y), (v_z, vu_x), (vu_y, vu_z): the footprint's
+        // node layout, each component summed as w * value in node order
+        float2 g01 = make_float2(0.f, 0.f), g2u0 = g01, u12 = g01;
+        {
+          float2 sz2[S];
 #pragma unroll
-        for (int i = 0; i < S; i++) {
+          for (int k = 0; k < S; k++) sz2[k] = bc2(sv[2][k]);
 #pragma unroll
-          for (int j = 0; j < S; j++) {
-            const float sxy = sv[0][i] * sv[1][j];
-            const int r = ((warp + i) * WY + (ly + j)) * WZ + lz;
+          for (int i = 0; i < S; i++) {
+            const float2 sx2 = bc2(sv[0][i]);
 #pragma unroll
-            for (int k = 0; k < S; k++) {
-              const float w = sxy * sv[2][k];
-              const float4 A = fpA[r + k];
-              const float2 B = fpB[r + k];
-              vu[0] = fmaf(w, A.w, vu[0]); vu[1] = fmaf(w, B.x, vu[1]); vu[2] = fmaf(w, B.y, vu[2]);
-              va[0] = fmaf(w, A.x, va[0]); va[1] = fmaf(w, A.y, va[1]); va[2] = fmaf(w, A.z, va[2]);
+            for (int j = 0; j < S; j++) {
+              const float2 sxy = fmul2(sx2, bc2(sv[1][j]));
+              const int r = ((warp + i) * WY + (ly + j)) * WZ + lz;
+#pragma unroll
+              for (int k = 0; k < S; k++) {
+                const float2 w = fmul2(sxy, sz2[k]);
+                const float4 A = fpA[r + k];
+                g01 = ffma2(w, make_float2(A.x, A.y), g01);
+                g2u0 = ffma2(w, make_float2(A.z, A.w), g2u0);
+                u12 = ffma2(w, fpB[r + k], u12);
+              }
             }
           }
         }
+        const float va[3] = {g01.x, g01.y, g2u0.x}, vu[3] = {g2u0.y, u12.x, u12.y};
         const float m = P[PF_MASS * ps + p];
         float xn[3];
 #pragma unroll
@@ -1424,11 +1433,12 @@ template <int S, bool THERMAL> struct GradFetchGlobal {
 // A = sum_k s_z V and B = sum_k ds_z V, then grad v += (ds_x s_y A,
 // s_x ds_y A, s_x s_y B) (dropped pairs add 0: see Axis::eval).  Also the
 // thermal gradient (qg -= grad T) and, in 2-D, sum w v_r.
-template <int DIM, int BASIS, bool THERMAL, typename F>
+template <int DIM, int BASIS, bool THERMAL, bool PACK, typename F>
 __device__ __forceinline__ void grad_gather(const PAxes<DIM, BASIS> &ax, const F &f, float (&G)[9], float (&qg)[3],
                                             float &vr) {
   constexpr int S = Stencil<BASIS>::S;
   constexpr int SY = DIM >= 2 ? S : 1, SZ = DIM == 3 ? S : 1;
+  // the z sums in packed pairs over the node's (v_x, v_y) and (v_z, T)
 #pragma unroll
   for (int i = 0; i < S; i++) {
     const float sx = ax.ax[0].s[i], dsx = ax.ax[0].ds[i];
@@ -1437,19 +1447,37 @@ __device__ __forceinline__ void grad_gather(const PAxes<DIM, BASIS> &ax, const F
       const float sy = ax.ax[1].s[j], dsy = ax.ax[1].ds[j];
       const int row = f.row(i, j, 0);
       float A[3] = {0.f, 0.f, 0.f}, B[3] = {0.f, 0.f, 0.f}, AT = 0.f, BT = 0.f;
+      if (PACK) {
+        float2 A01 = make_float2(0.f, 0.f), A2T = A01, B01 = A01, B2T = A01;
 #pragma unroll
-      for (int k = 0; k < SZ; k++) {
-        const float sz = ax.ax[2].s[k], dsz = ax.ax[2].ds[k];
-        const float4 V = f.at(row, k);
-        const float vn[3] = {V.x, V.y, V.z};
-#pragma unroll
-        for (int r = 0; r < DIM; r++) {
-          A[r] += sz * vn[r];
-          if (DIM == 3) B[r] += dsz * vn[r];
+        for (int k = 0; k < SZ; k++) {
+          const float4 V = f.at(row, k);
+          const float2 xy = make_float2(V.x, V.y), zt = make_float2(V.z, V.w);
+          const float2 sz = bc2(ax.ax[2].s[k]);
+          A01 = ffma2(sz, xy, A01);
+          A2T = ffma2(sz, zt, A2T);
+          if (DIM == 3) {
+            const float2 dsz = bc2(ax.ax[2].ds[k]);
+            B01 = ffma2(dsz, xy, B01);
+            B2T = ffma2(dsz, zt, B2T);
+          }
         }
-        if (THERMAL) {
-          AT += sz * V.w;
-          if (DIM == 3) BT += dsz * V.w;
+        A[0] = A01.x; A[1] = A01.y; A[2] = A2T.x; B[0] = B01.x; B[1] = B01.y; B[2] = B2T.x; AT = A2T.y; BT = B2T.y;
+      } else {
+#pragma unroll
+        for (int k = 0; k < SZ; k++) {
+          const float sz = ax.ax[2].s[k], dsz = ax.ax[2].ds[k];
+          const float4 V = f.at(row, k);
+          const float vn[3] = {V.x, V.y, V.z};
+#pragma unroll
+          for (int r = 0; r < DIM; r++) {
+            A[r] += sz * vn[r];
+            if (DIM == 3) B[r] += dsz * vn[r];
+          }
+          if (THERMAL) {
+            AT += sz * V.w;
+            if (DIM == 3) BT += dsz * V.w;
+          }
         }
       }
       const float sxy = sx * sy, gx = dsx * sy, gy = sx * dsy;
@@ -1558,7 +1586,7 @@ __global__ void __launch_bounds__(256, MINB) k_g2p2(PartArgs a) {
     if (staged) {
       GradFetchStage f{g2p_stage, ((i0[0] - lo[0]) * nb[1] + (i0[1] - lo[1])) * nb[2] + (i0[2] - lo[2]), nb[1],
                        nb[2]};
-      grad_gather<DIM, BASIS, THERMAL>(ax, f, G, qg, vr);
+      grad_gather<DIM, BASIS, THERMAL, true>(ax, f, G, qg, vr);
     } else {
       GradFetchGlobal<S, THERMAL> f;
       f.NV = NV;
@@ -1572,7 +1600,7 @@ __global__ void __launch_bounds__(256, MINB) k_g2p2(PartArgs a) {
         f.cy[k] = SY > 1 ? min(max(i0[1] + k, 0), g.n[1] - 1) : 0;
         f.cz[k] = SZ > 1 ? min(max(i0[2] + k, 0), g.n[2] - 1) : 0;
       }
-      grad_gather<DIM, BASIS, THERMAL>(ax, f, G, qg, vr);
+      grad_gather<DIM, BASIS, THERMAL, false>(ax, f, G, qg, vr);
     }
     if (DIM == 2 && a.axisym) {
       // Fdot(2,2) / L(2,2) += sum w v_r / r, r = x0_r (TL) or the x_r of the
