@@ -86,6 +86,14 @@ struct kmpm_ctx {
   MatDev *d_mats = nullptr;
   float4 *nodeA = nullptr, *nodeB = nullptr, *nodeX = nullptr;
   float *nodeT = nullptr;
+  // TLMPM MUSL momentum reuse (P2G_FONLY): the re-map's nodal momentum sums,
+  // kept for the next step's grid update, whose scatter then sums the forces
+  // only.  reuse_p: this configuration takes it (select_scatters); p_valid:
+  // nodeP holds the sums of the particles' current velocities (set by every
+  // step, cleared by anything that changes the particle state between steps)
+  float4 *nodeP = nullptr;
+  bool reuse_p = false, p_valid = false;
+  int smem_fonly = 0;
   int tdim[3] = {0, 0, 0}, NCELL = 0, ntiles_total = 0;
   int2 *d_tiles = nullptr;
   int ntiles_launch = 0;
@@ -120,6 +128,7 @@ struct kmpm_ctx {
   std::vector<int> ul_fields;
   StepKernels K{};
   cudaGraphExec_t gexec = nullptr;
+  cudaGraphExec_t gexec_r = nullptr;  // the step with the momentum reuse (reuse_p)
   bool graph_valid = false;
   int launches_per_step = 0;
   int smem[4][2] = {{0}};
@@ -348,6 +357,7 @@ GridArgs grid_args(kmpm_ctx *c, int remap) {
   a.scalars = c->d_scalars;
   a.indep = c->indep();
   a.remap = remap;
+  a.nodeP = c->reuse_p ? c->nodeP : nullptr;
   return a;
 }
 
@@ -580,6 +590,7 @@ int build(kmpm_ctx *c) {
   c->nodeB = c->nodeA + 1;
   DALLOC(c->nodeX, c->nnodes_pad);
   DALLOC(c->nodeT, c->nnodes_pad);
+  if (c->TL() && c->musl()) DALLOC(c->nodeP, c->nnodes_pad);
   {
     std::vector<float4> X(c->nnodes_pad, make_float4(0, 0, 0, 0));
     for (size_t gi = 0; gi < c->hgrids.size(); gi++) {
@@ -976,12 +987,29 @@ int select_scatters(kmpm_ctx *c) {
   c->smem_usf = p2g_smem_bytes(c->prm.dim, c->prm.basis, mode_usf, false);
   CK(cudaFuncSetAttribute(c->sc_force, cudaFuncAttributeMaxDynamicSharedMemorySize, c->smem_force));
   CK(cudaFuncSetAttribute(c->sc_usf, cudaFuncAttributeMaxDynamicSharedMemorySize, c->smem_usf));
+  // TLMPM MUSL with FLIP/PIC on the plain row scatter, mechanical, FP32: the
+  // scatter of the next step sums the forces only (P2G_FONLY).
+  // KMPM_NO_MOMENTUM_REUSE=1 keeps the full scatter every step.
+  {
+    const char *ev = std::getenv("KMPM_NO_MOMENTUM_REUSE");
+    c->reuse_p = TL && c->musl() && !th && flags == 0 && !c->apic() && c->nodeP &&
+                 c->prm.precision == KMPM_PREC_FP32 && c->K.p2g_row_fonly && c->sc_force == c->K.p2g_row[0] &&
+                 !(ev && ev[0] == '1');
+    c->p_valid = false;
+    if (c->reuse_p) {
+      c->smem_fonly = p2g_smem_bytes(c->prm.dim, c->prm.basis, P2G_TL | P2G_FONLY, false);
+      CK(cudaFuncSetAttribute(c->K.p2g_row_fonly, cudaFuncAttributeMaxDynamicSharedMemorySize, c->smem_fonly));
+    }
+  }
   return KMPM_OK;
 }
 
 // ---------------------------------------------------------------- one step
 // USL::run (src/usl.cpp:43-92) / MUSL::run (src/musl.cpp:43-93)
-int enqueue_step(kmpm_ctx *c) {
+// reuse: the step after another step of the same particle state (reuse_p):
+// the scatter sums the forces only and the grid update takes the momentum the
+// last re-map summed (P2G_FONLY)
+int enqueue_step(kmpm_ctx *c, bool reuse = false) {
   int nl = 0;
   const bool TL = c->TL(), th = c->prm.thermal != 0, musl = c->musl();
   const int prec = c->prm.precision == KMPM_PREC_FP64_ISLANDS ? 1 : 0;
@@ -1040,10 +1068,15 @@ int enqueue_step(kmpm_ctx *c) {
   p.apic_pos = TL ? -1 : PF_X;
   // (with w mbp added to the node forces when contacts exist, and the hoop
   // term in axisymmetric runs: select_scatters)
-  LAUNCH(c->sc_force, c->ntiles_launch, 256, c->smem_force, p);
-  MARK("p2g");
+  if (reuse) {
+    LAUNCH(c->K.p2g_row_fonly, c->ntiles_launch, 256, c->smem_fonly, p);
+    MARK("p2g_force");
+  } else {
+    LAUNCH(c->sc_force, c->ntiles_launch, 256, c->smem_force, p);
+    MARK("p2g");
+  }
   // update_grid_state + fixes
-  LAUNCH(c->K.grid_upd[TL][th][prec], c->nblk_g, 256, 0, g1);
+  LAUNCH(reuse ? c->K.grid_upd_fonly : c->K.grid_upd[TL][th][prec], c->nblk_g, 256, 0, g1);
   MARK("grid_update");
   if (c->usf()) {
     // USF::run (src/usf.cpp:43-86): the stress from the grid velocities of the
@@ -1138,18 +1171,36 @@ int enqueue_step(kmpm_ctx *c) {
   return KMPM_OK;
 }
 
-int ensure_graph(kmpm_ctx *c) {
-  if (c->graph_valid) return KMPM_OK;
-  if (c->gexec) { cudaGraphExecDestroy(c->gexec); c->gexec = nullptr; }
+int capture_step(kmpm_ctx *c, bool reuse, cudaGraphExec_t *out) {
+  if (*out) { cudaGraphExecDestroy(*out); *out = nullptr; }
   cudaGraph_t g;
   CK(cudaStreamBeginCapture(c->st, cudaStreamCaptureModeThreadLocal));
-  int r = enqueue_step(c);
+  int r = enqueue_step(c, reuse);
   cudaError_t e = cudaStreamEndCapture(c->st, &g);
   if (r != KMPM_OK) return r;
   if (e != cudaSuccess) return fail(c, KMPM_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
-  CK(cudaGraphInstantiate(&c->gexec, g, 0));
+  CK(cudaGraphInstantiate(out, g, 0));
   cudaGraphDestroy(g);
+  return KMPM_OK;
+}
+
+int ensure_graph(kmpm_ctx *c) {
+  if (c->graph_valid) return KMPM_OK;
+  c->p_valid = false;
+  int r = capture_step(c, false, &c->gexec);
+  if (r == KMPM_OK && c->reuse_p) r = capture_step(c, true, &c->gexec_r);
+  if (r != KMPM_OK) return r;
   c->graph_valid = true;
+  return KMPM_OK;
+}
+
+// n replays of the step graph: the momentum-reuse step wherever the last
+// re-map's sums are those of the current particle state
+int launch_steps(kmpm_ctx *c, int n) {
+  for (int i = 0; i < n; i++) {
+    CK(cudaGraphLaunch(c->reuse_p && c->p_valid ? c->gexec_r : c->gexec, c->st));
+    c->p_valid = c->reuse_p;
+  }
   return KMPM_OK;
 }
 
@@ -1365,12 +1416,13 @@ int kmpm_destroy(kmpm_ctx *c) {
   if (!c) return KMPM_OK;
   if (c->st) cudaStreamSynchronize(c->st);
   if (c->gexec) cudaGraphExecDestroy(c->gexec);
+  if (c->gexec_r) cudaGraphExecDestroy(c->gexec_r);
   for (auto *m : c->d_masks) cudaFree(m);
   for (auto e : c->prof_ev) cudaEventDestroy(e);
   dfree(c->buf[0]); dfree(c->buf[1]); dfree(c->d_pp); dfree(c->d_ranges); dfree(c->d_blk_range);
   dfree(c->d_solid_mat); dfree(c->d_grids); dfree(c->d_blk_grid); dfree(c->d_grid_blk0); dfree(c->d_mats);
   c->nodeB = nullptr;  // inside nodeA's allocation
-  dfree(c->nodeA); dfree(c->nodeX); dfree(c->nodeT); dfree(c->d_tiles);
+  dfree(c->nodeA); dfree(c->nodeX); dfree(c->nodeT); dfree(c->nodeP); dfree(c->d_tiles);
   dfree(c->d_cs); dfree(c->d_ce); dfree(c->d_ts); dfree(c->d_te); dfree(c->partial);
   dfree(c->d_fixes); dfree(c->d_fix_start); dfree(c->d_fix_count); dfree(c->d_scalars); dfree(c->d_dtcfl);
   dfree(c->d_dump);
@@ -1539,7 +1591,8 @@ int kmpm_run(kmpm_ctx *c, int nsteps) {
   }
   r = set_maxtime(c, 1e300);
   if (r != KMPM_OK) return r;
-  for (int i = 0; i < nsteps; i++) CK(cudaGraphLaunch(c->gexec, c->st));
+  r = launch_steps(c, nsteps);
+  if (r != KMPM_OK) return r;
   return check_error(c);
 }
 
@@ -1560,7 +1613,8 @@ int kmpm_run_time(kmpm_ctx *c, double maxtime, int *nsteps_done) {
   r = set_maxtime(c, maxtime);
   if (r != KMPM_OK) return r;
   while (s.time < maxtime) {
-    for (int i = 0; i < 64; i++) CK(cudaGraphLaunch(c->gexec, c->st));
+    r = launch_steps(c, 64);
+    if (r != KMPM_OK) return r;
     r = check_error(c);
     if (r != KMPM_OK) return r;
     r = read_scalars(c, s);
@@ -1589,7 +1643,8 @@ int kmpm_run_until(kmpm_ctx *c, int nsteps, double maxtime, int *nsteps_done) {
   if (r != KMPM_OK) return r;
   while (s.time < maxtime && s.ntimestep - n0 < nsteps) {
     const int k = (int)std::min<long long>(64, nsteps - (s.ntimestep - n0));
-    for (int i = 0; i < k; i++) CK(cudaGraphLaunch(c->gexec, c->st));
+    r = launch_steps(c, k);
+    if (r != KMPM_OK) return r;
     r = check_error(c);
     if (r != KMPM_OK) return r;
     r = read_scalars(c, s);
@@ -1805,6 +1860,7 @@ int kmpm_upload_particles(kmpm_ctx *c, int solid, int field, const double *in) {
     c->dump_cap = need;
   }
   CK(cudaMemcpyAsync(c->d_dump, in, sizeof(double) * need, cudaMemcpyHostToDevice, c->st));
+  c->p_valid = false;  // the next scatter sums the momentum of the new state
   const int ri = c->TL() ? c->solid_range[solid] : 0;
   launch_load(part_args(c), ri, c->ranges[ri].count, solid, c->solid_base[solid], field, c->TL() ? 1 : 0, c->T_ref,
               c->d_dump, c->st);
@@ -1901,6 +1957,7 @@ int kmpm_load_state(kmpm_ctx *c, const void *in, unsigned long long bytes) {
   std::memcpy(&h, o, sizeof(h));
   o += sizeof(h);
   if (std::memcmp(h.magic, SNAP_MAGIC, 8) != 0 || h.version != 1) return fail(c, KMPM_ERR_ARG, "not a snapshot");
+  c->p_valid = false;  // the next scatter sums the momentum of the loaded state
   std::vector<int> fl = active_fields(c);
   if (h.nfields != (int)fl.size() && !c->restored_state) {
     // a snapshot of a context that had uploaded plastic strain or damage
@@ -1992,9 +2049,10 @@ int kmpm_profile(kmpm_ctx *c, int nsteps, double *phase_ms, int max_phases, int 
   for (int s = 0; s < nsteps; s++) {
     c->profiling = true;
     c->prof_n = 0;
-    r = enqueue_step(c);
+    r = enqueue_step(c, c->reuse_p && c->p_valid);
     c->profiling = false;
     if (r != KMPM_OK) return r;
+    c->p_valid = c->reuse_p;
     CK(cudaStreamSynchronize(c->st));
     acc.resize(std::max<size_t>(acc.size(), c->prof_n), 0.0);
     for (int k = 1; k < c->prof_n; k++) {

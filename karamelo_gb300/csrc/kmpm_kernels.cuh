@@ -25,22 +25,33 @@ enum P2GMode : int {
   // T_zz / r (1) joins the payload, and -w T_zz / r the radial force sums
   // (src/solid.cpp:472-475, 513-519, 565-571)
   P2G_AXI = 16,
+  // flag on P2G_TL (TLMPM MUSL, FLIP/PIC, mechanical): the force sums only.
+  // TLMPM's weights and masses do not change, and no velocity changes
+  // between a step's re-map and the next step's scatter, so the nodal
+  // momentum of that scatter is the re-map's sum, bit for bit: the velocity
+  // pass of the grid keeps it (GridArgs::nodeP) and the next grid update
+  // reads it there
+  P2G_FONLY = 32,
 };
 __host__ __device__ constexpr int p2g_kind(int mode) { return mode & 7; }
 __host__ __device__ constexpr bool p2g_axi(int mode) { return (mode & P2G_AXI) != 0; }
 __host__ __device__ constexpr int p2g_base(int mode) { return p2g_kind(mode) >= P2G_TL_APIC ? p2g_kind(mode) - 3 : p2g_kind(mode); }
 __host__ __device__ constexpr bool p2g_apic(int mode) { return p2g_kind(mode) >= P2G_TL_APIC; }
 __host__ __device__ constexpr bool p2g_ext(int mode) { return (mode & P2G_EXT) != 0; }
-enum GridMode : int { GM_MASS = 0, GM_UPDATE = 1, GM_VEL = 2 };
+__host__ __device__ constexpr bool p2g_fonly(int mode) { return (mode & P2G_FONLY) != 0; }
+// GM_UPDATE_F: the grid update after a P2G_FONLY scatter (momentum from nodeP)
+enum GridMode : int { GM_MASS = 0, GM_UPDATE = 1, GM_VEL = 2, GM_UPDATE_F = 3 };
 
 __host__ __device__ constexpr int p2g_nq(int mode, bool th) {
-  return p2g_base(mode) == P2G_MASS  ? 1
+  return p2g_fonly(mode) ? 3
+         : p2g_base(mode) == P2G_MASS  ? 1
          : p2g_base(mode) == P2G_TL ? (th ? 9 : 6)
          : p2g_base(mode) == P2G_UL ? (th ? 10 : 7)
                                     : (th ? 4 : 3);
 }
 __host__ __device__ constexpr int p2g_nin(int mode, bool th) {
-  return (p2g_base(mode) == P2G_MASS  ? 1
+  return p2g_fonly(mode) ? 9
+         : (p2g_base(mode) == P2G_MASS  ? 1
           : p2g_base(mode) == P2G_TL ? (th ? 17 : 12)
           : p2g_base(mode) == P2G_UL ? (th ? 15 : 10)
                                      : (th ? 4 : 3)) +
@@ -84,6 +95,10 @@ struct GridArgs {
   StepScalars *scalars;
   int indep;                 // per-solid clocks (independent instances)
   int remap;                 // GM_VEL: MUSL re-map (else positions only)
+  // TLMPM MUSL momentum reuse (P2G_FONLY): GM_VEL stores the re-map's nodal
+  // momentum sums (before the velocity BCs) here and GM_UPDATE_F reads them;
+  // nullptr where the reuse is off
+  float4 *nodeP;
 };
 
 struct PartArgs {
@@ -144,6 +159,10 @@ struct StepKernels {
   // the row scatters (k_p2g_row, k_p2g_row2) of the plain TL, UL and
   // velocity modes: 2-D and 3-D cubic and quadratic splines (nullptr elsewhere)
   void *p2g_row[3];
+  // the 3-D row scatter of the force sums only (P2G_TL | P2G_FONLY) and the
+  // grid update that takes the stored momentum (GM_UPDATE_F): TLMPM, FP32,
+  // mechanical, cubic and quadratic splines (nullptr elsewhere)
+  void *p2g_row_fonly, *grid_upd_fonly;
   void *p2g_tl_apic, *p2g_ul_apic, *p2g_vel_apic;  // cubic spline only (nullptr otherwise)
   // the force scatters with external particle forces (P2G_EXT): [thermal]
   void *p2g_tl_ext[2], *p2g_ul_ext[2], *p2g_tl_apic_ext, *p2g_ul_apic_ext;
@@ -272,11 +291,34 @@ void launch_permute(float *const *src_pp, float *const *dst_pp, size_t ps, const
                     const int *fields, int nfields, cudaStream_t st);
 void launch_swap_ptrs(float **pp, cudaStream_t st);
 
+// Starts the DRAM reads of particles [p0, p1) of field rows row0 .. row0 +
+// nrows - 1 into L2, one prefetch per 128-byte line, spread over the block's
+// threads.  A hint that holds no registers: a tile kernel issues it before
+// staging its node footprint, so that the loads of its particle rows, row
+// after row, find them in L2.  Field rows start on 1 KB boundaries (the field
+// stride is a multiple of 256 particles), and every line lies inside its row.
+__device__ __forceinline__ void prefetch_rows_l2(const float *P, size_t ps, int row0, int nrows, int p0, int p1) {
+  if (p1 <= p0) return;
+  const int l0 = p0 >> 5, nl = ((p1 - 1) >> 5) - l0 + 1;  // 32 floats per line
+  const float *base = P + (size_t)row0 * ps + (size_t)l0 * 32;
+  for (int e = threadIdx.x; e < nrows * nl; e += blockDim.x) {
+    const int f = e / nl, l = e - f * nl;
+    asm volatile("prefetch.global.L2 [%0];" ::"l"(base + (size_t)f * ps + (size_t)l * 32));
+  }
+}
+
+static_assert(PF_X == PF_X0 + 3 && PF_V == PF_X + 3 && PF_MASS == PF_V + 3, "x0, u, v, mass rows are contiguous");
+
 // ---- payload staged per particle for the scatter
 template <int MODE_, bool TH>
 __device__ __forceinline__ void p2g_payload(const P2GArgs &a, const float *P, int p, float *pay) {
   constexpr int MODE = p2g_base(MODE_);
   const size_t ps = a.ps;
+  if (p2g_fonly(MODE_)) {  // vol0 PK1 only
+#pragma unroll
+    for (int k = 0; k < 9; k++) pay[k] = P[(PF_PK + k) * ps + p];
+    return;
+  }
   const float m = P[PF_MASS * ps + p];
   if (MODE == P2G_MASS) { pay[0] = m; return; }
   int o = 0;

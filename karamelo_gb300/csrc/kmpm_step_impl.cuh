@@ -390,6 +390,18 @@ __global__ void __launch_bounds__(256, (p2g_min_blocks<DIM, MODE, THERMAL>())) k
 template <int MODE, int Q>
 __device__ __forceinline__ void p2g_row_particle(float (&A0)[Q], float (&A2)[Q], const float *pay, float2 bx,
                                                  float2 by, float2 bz0, float2 bz2) {
+  if constexpr (p2g_fonly(MODE)) {
+    // the force sums only (P2G_FONLY; payload vol0 PK1, row-major), in the
+    // arithmetic of the P2G_TL force sums below, so that both give the same bits
+    const float wxy = bx.x * by.x, gxy0 = bx.y * by.x, gxy1 = bx.x * by.y;
+#pragma unroll
+    for (int r = 0; r < 3; r++) {
+      const float t = fmaf(pay[3 * r], gxy0, pay[3 * r + 1] * gxy1), t2 = pay[3 * r + 2] * wxy;
+      A0[r] = fmaf(-bz0.x, t, fmaf(-bz0.y, t2, A0[r]));
+      A2[r] = fmaf(-bz2.x, t, fmaf(-bz2.y, t2, A2[r]));
+    }
+    return;
+  }
   constexpr int OM = MODE == P2G_UL ? 1 : 0;  // UL sums start with the mass
   constexpr bool FORCE = MODE != P2G_VEL;
   const float wxy = bx.x * by.x;
@@ -404,15 +416,45 @@ __device__ __forceinline__ void p2g_row_particle(float (&A0)[Q], float (&A2)[Q],
       float T0, T1, T2;
       if (MODE == P2G_TL) {  // vol0 PK1, row-major
         T0 = pay[3 + 3 * r]; T1 = pay[4 + 3 * r]; T2 = pay[5 + 3 * r];
+        t[r] = fmaf(T0, gxy0, T1 * gxy1);  // as the force-only scatter
       } else {  // vol sigma, symmetric xx yy zz xy xz yz
         const float *sg = pay + 4;
         T0 = r == 0 ? sg[0] : (r == 1 ? sg[3] : sg[4]);
         T1 = r == 0 ? sg[3] : (r == 1 ? sg[1] : sg[5]);
         T2 = r == 0 ? sg[4] : (r == 1 ? sg[5] : sg[2]);
+        t[r] = T0 * gxy0 + T1 * gxy1;
       }
-      t[r] = T0 * gxy0 + T1 * gxy1;
       t2[r] = T2 * wxy;
     }
+  }
+  if (MODE == P2G_TL || MODE == P2G_UL) {
+    // packed pairs of neighbouring sums, each still a = fma(s, q, a) for the
+    // momentum (and UL mass) sums and a = fma(-s, t, fma(-ds, t2, a)) for the
+    // forces (fma(s, -t, .) rounds as fma(-s, t, .)):
+    //   TL (6 sums): (p_x, p_y) (p_z, f_x) (f_y, f_z);
+    //   UL (7 sums): (m, p_x) (p_y, p_z) (f_x, f_y) f_z
+    const float nt[3] = {-t[0], -t[1], -t[2]};
+    const auto slot = [&](float (&A)[Q], float2 bz) {
+      const float2 s2 = bc2(bz.x), nd2 = bc2(-bz.y);
+      if (MODE == P2G_TL) {
+        A[3] = fmaf(-bz.y, t2[0], A[3]);
+        float2 f12 = ffma2(nd2, make_float2(t2[1], t2[2]), make_float2(A[4], A[5]));
+        const float2 p01 = ffma2(s2, make_float2(q[0], q[1]), make_float2(A[0], A[1]));
+        const float2 p2f0 = ffma2(s2, make_float2(q[2], nt[0]), make_float2(A[2], A[3]));
+        f12 = ffma2(s2, make_float2(nt[1], nt[2]), f12);
+        A[0] = p01.x; A[1] = p01.y; A[2] = p2f0.x; A[3] = p2f0.y; A[4] = f12.x; A[5] = f12.y;
+      } else {
+        const float2 mp = ffma2(s2, make_float2(q[0], q[1]), make_float2(A[0], A[1]));
+        const float2 pp = ffma2(s2, make_float2(q[2], q[3]), make_float2(A[2], A[3]));
+        float2 f01 = ffma2(nd2, make_float2(t2[0], t2[1]), make_float2(A[4], A[5]));
+        f01 = ffma2(s2, make_float2(nt[0], nt[1]), f01);
+        A[6] = fmaf(-bz.x, t[2], fmaf(-bz.y, t2[2], A[6]));
+        A[0] = mp.x; A[1] = mp.y; A[2] = pp.x; A[3] = pp.y; A[4] = f01.x; A[5] = f01.y;
+      }
+    };
+    slot(A0, bz0);
+    slot(A2, bz2);
+    return;
   }
 #pragma unroll
   for (int d = 0; d < 3 + OM; d++) {
@@ -428,7 +470,7 @@ __device__ __forceinline__ void p2g_row_particle(float (&A0)[Q], float (&A2)[Q],
 }
 
 template <int BASIS, int MODE>
-__global__ void __launch_bounds__(256, (MODE == P2G_VEL ? 4 : 3)) k_p2g_row(P2GArgs a) {
+__global__ void __launch_bounds__(256, (MODE == P2G_VEL || p2g_fonly(MODE) ? 4 : 3)) k_p2g_row(P2GArgs a) {
   static_assert(Stencil<BASIS>::S == 4 && Stencil<BASIS>::SC == 1, "four-wide stencils");
   using TS = TileShape<3, BASIS>;
   constexpr int S = 4, LO = Stencil<BASIS>::LO;
@@ -460,6 +502,12 @@ __global__ void __launch_bounds__(256, (MODE == P2G_VEL ? 4 : 3)) k_p2g_row(P2GA
   const float *P = *a.Pp;
   const size_t ps = a.ps;
   const bool use_u = a.pos_field == PF_X;
+  {  // the tile's particle rows that the stage phase reads, into L2
+    const int t0 = a.tile_start[tile_global], t1 = a.tile_end[tile_global];
+    prefetch_rows_l2(P, ps, PF_X0, use_u ? 6 : 3, t0, t1);
+    if (!p2g_fonly(MODE)) prefetch_rows_l2(P, ps, PF_V, 4, t0, t1);  // v, mass
+    if (MODE != P2G_VEL) prefetch_rows_l2(P, ps, PF_PK, p2g_base(MODE) == P2G_TL ? 9 : 6, t0, t1);
+  }
 
   for (int k = lane; k < Q * NF; k += 32) slab[k] = 0.f;
 
@@ -869,21 +917,32 @@ __global__ void __launch_bounds__(256) k_grid(GridArgs a) {
     a.nodeA[NODE_STRIDE * node] = A;
     return;
   }
-  if (GMODE == GM_UPDATE) {
-    // quantities: TL [p3 f3 (+mT Qext Qint)]; UL [m p3 f3 (+...)]
-    constexpr int Q = TL ? (THERMAL ? 9 : 6) : (THERMAL ? 10 : 7);
+  if (GMODE == GM_UPDATE || GMODE == GM_UPDATE_F) {
+    // quantities: TL [p3 f3 (+mT Qext Qint)]; UL [m p3 f3 (+...)];
+    // GM_UPDATE_F (TL, mechanical): [f3], p as the last re-map summed it
+    constexpr bool FO = GMODE == GM_UPDATE_F;
+    static_assert(!FO || (TL && !THERMAL), "the momentum reuse is TLMPM and mechanical");
+    constexpr int Q = FO ? 3 : TL ? (THERMAL ? 9 : 6) : (THERMAL ? 10 : 7);
     R s[Q];
     gather_partials<DIM, BASIS, Q, R>(a, g, li, ix, s);
     const int o = TL ? 0 : 1;
     float4 A = a.nodeA[NODE_STRIDE * node];
     const R m = TL ? (R)A.w : s[0];
     R v[3], f[3], mb[3] = {0, 0, 0}, vu[3];
+    R pm[3];
+    if (FO) {
+      const float4 Pn = a.nodeP[node];
+      pm[0] = Pn.x; pm[1] = Pn.y; pm[2] = Pn.z;
+    } else {
+#pragma unroll
+      for (int d = 0; d < 3; d++) pm[d] = s[o + d];
+    }
     // Solid::compute_velocity_nodes: v = p/m only where m > 0 (src/solid.cpp:357)
     const R im = m > R(0) ? R(1) / m : R(0);
 #pragma unroll
     for (int d = 0; d < 3; d++) {
-      v[d] = s[o + d] * im;
-      f[d] = s[o + 3 + d];
+      v[d] = pm[d] * im;
+      f[d] = s[(FO ? 0 : o + 3) + d];
     }
     // body force on nodes with mass (src/fix_body_force.cpp:122-136)
     for (int k = a.fix_start[gi]; k < a.fix_start[gi] + a.fix_count[gi]; k++) {
@@ -896,7 +955,7 @@ __global__ void __launch_bounds__(256) k_grid(GridArgs a) {
 #pragma unroll
     for (int d = 0; d < 3; d++) vu[d] = m != R(0) ? v[d] + dt * (f[d] + mb[d]) * im : v[d];
     R T = 0, Tu = 0;
-    if (THERMAL) {
+    if constexpr (THERMAL && !FO) {
       T = s[o + 6] * im;
       Tu = m != R(0) ? T + dt * (s[o + 8] + s[o + 7]) * im : T;  // src/grid.cpp:1354-1361
     }
@@ -919,6 +978,8 @@ __global__ void __launch_bounds__(256) k_grid(GridArgs a) {
     constexpr int Q = THERMAL ? 4 : 3;
     R s[Q];
     gather_partials<DIM, BASIS, Q, R>(a, g, li, ix, s);
+    // the momentum sums before the BCs, for the next grid update (P2G_FONLY)
+    if (TL && !THERMAL && a.nodeP) a.nodeP[node] = make_float4((float)s[0], (float)s[1], (float)s[2], 0.f);
     const R m = A.w;
     const R im = m > R(0) ? R(1) / m : R(0);
 #pragma unroll
@@ -1219,6 +1280,8 @@ __global__ void __launch_bounds__(256, 4) k_g2p1_remap_row(P2GArgs a) {
   const StepScalars &sc = a.scalars[a.indep ? g.solid0 : 0];
   const float dt = (float)sc.dt;
   const float alpha = a.pic_flip;
+  // the tile's x0, u, v and mass rows, into L2 while the footprint is staged
+  prefetch_rows_l2(P, ps, PF_X0, PF_MASS + 1 - PF_X0, a.tile_start[tile_global], a.tile_end[tile_global]);
 
   for (int k = lane; k < Q * NF; k += 32) slab[k] = 0.f;
   // the tile's node footprint: nodes (tc TX - LO + fx, ...), fx < WX
@@ -1883,7 +1946,10 @@ void fill_step_kernels(StepKernels &k) {
   k.p2g_ul_th = (void *)k_p2g<DIM, BASIS, P2G_UL, true>;
   k.p2g_vel = (void *)k_p2g<DIM, BASIS, P2G_VEL, false>;
   k.p2g_vel_th = (void *)k_p2g<DIM, BASIS, P2G_VEL, true>;
+  k.p2g_row_fonly = k.grid_upd_fonly = nullptr;
   if constexpr (DIM == 3 && (BASIS == 1 || BASIS == 3)) {
+    k.p2g_row_fonly = (void *)k_p2g_row<BASIS, P2G_TL | P2G_FONLY>;
+    k.grid_upd_fonly = (void *)k_grid<DIM, BASIS, GM_UPDATE_F, true, false, float>;
     k.p2g_row[0] = (void *)k_p2g_row<BASIS, P2G_TL>;
     k.p2g_row[1] = (void *)k_p2g_row<BASIS, P2G_UL>;
     k.p2g_row[2] = (void *)k_p2g_row<BASIS, P2G_VEL>;

@@ -1,0 +1,62 @@
+"""TLMPM MUSL momentum reuse against the full scatter of every step.
+
+TLMPM's weights and masses never change, and no particle velocity changes
+between a step's re-map (velocities_to_grid, src/musl.cpp:59-67) and the next
+step's scatter (particles_to_grid): the nodal momentum that scatter would sum
+is the re-map's, bit for bit.  With the reuse the velocity pass of the grid
+keeps the re-map's sums and the next scatter sums the forces only (P2G_FONLY);
+KMPM_NO_MOMENTUM_REUSE=1 scatters the momentum every step.  Both must give
+the same bits, including after an upload between steps (which must make the
+next step scatter the momentum of the new state) and across kmpm_run calls."""
+import os
+
+import numpy as np
+import pytest
+
+from karamelo_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+FIELDS = ("x", "v", "sigma", "F", "eps_p")
+
+
+def _run(basis, reuse, upload):
+    if not reuse:
+        os.environ["KMPM_NO_MOMENTUM_REUSE"] = "1"
+    try:
+        sim = W.taylor_bar(None, cellsize=0.8, basis=basis)
+        sim.run(1)
+        W.taylor_bar_wall(sim)
+        sim.run(12)
+        if upload:
+            v = sim.particles(0, "v")
+            sim.backend.upload(0, "v", v * 0.97)
+        for _ in range(3):  # several run calls: the reuse carries across them
+            sim.run(6)
+        phases = sim.backend.profile(1)
+        out = {f: sim.particles(0, f) for f in FIELDS}
+        out["grid_v"] = sim.backend.grid(0, "v")
+        out["scalars"] = np.array(sim.backend.scalars(), float)
+        sim.backend.close()
+    finally:
+        os.environ.pop("KMPM_NO_MOMENTUM_REUSE", None)
+    return phases, out
+
+
+@pytest.mark.parametrize("basis", ["cubic-spline", "quadratic-spline"])
+@pytest.mark.parametrize("upload", [False, True], ids=["steps", "upload_between"])
+def test_momentum_reuse_bit_identical(gpu_lib, basis, upload):
+    ph_r, a = _run(basis, True, upload)
+    ph_f, b = _run(basis, False, upload)
+    assert "p2g_force" in ph_r and "p2g" not in ph_r
+    assert "p2g" in ph_f and "p2g_force" not in ph_f
+    for k in a:
+        assert np.array_equal(a[k], b[k]), f"{k}: max |diff| {np.max(np.abs(a[k] - b[k])):.3e}"
+
+
+def test_upload_changes_the_run(gpu_lib):
+    """The upload case above is not vacuous: the scaled velocities change the
+    state that the steps after it produce."""
+    _, a = _run("cubic-spline", True, False)
+    _, b = _run("cubic-spline", True, True)
+    assert not np.array_equal(a["x"], b["x"])
