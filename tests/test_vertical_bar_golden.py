@@ -86,3 +86,19 @@ def test_gpu_follows_reference_run_n20(gpu_lib):
     sim.backend = GpuBackend(sim.s, autotune=False)
     rel = _follow(sim, sim.backend, "n20_ppc2", 100)
     assert rel[2:].max() < 1e-3, rel.max()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("key,ppc,sub,basis", [
+    ("linear_n20_ppc1", 1, "FLIP", "linear"),
+    ("apic_n20_ppc2", 2, "APIC", "cubic-spline"),
+    ("apic_linear_n20_ppc2", 2, "APIC", "linear"),
+])
+def test_gpu_follows_reference_run_basis_and_transfer(gpu_lib, key, ppc, sub, basis):
+    """The CUDA path (FP32) on the linear-basis FLIP run and the two APIC
+    runs at N = 20, through step 50, at the bound of the cubic FLIP run."""
+    from karamelo_gb300.gpu import GpuBackend
+    sim = W.vertical_bar(None, N=20, ppc=ppc, sub=sub, basis=basis)
+    sim.backend = GpuBackend(sim.s, autotune=False)
+    rel = _follow(sim, sim.backend, key, 50)
+    assert rel[2:].max() < 1e-3, rel.max()
