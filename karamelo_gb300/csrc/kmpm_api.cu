@@ -970,7 +970,7 @@ bool sur_queued(const kmpm_ctx *c) {
 
 void *g2p2_variant(const kmpm_ctx *c, int v) {
   const bool TL = c->TL();
-  if (c->law_jc && c->K.g2p2_jc[TL][v]) return c->K.g2p2_jc[TL][v];
+  if (c->law_jc && !c->apic() && c->K.g2p2_jc[TL][v]) return c->K.g2p2_jc[TL][v];
   return c->K.g2p2_v[TL][v];
 }
 

@@ -1566,7 +1566,7 @@ __device__ __forceinline__ void grad_gather(const PAxes<DIM, BASIS> &ax, const F
 // return map's queue with what k_learn_queue needs to redo its update
 template <int DIM, int BASIS, bool TL, bool THERMAL, int PREC, int MINB = 3, int LAW = LAW_ANY, bool QUEUE = false>
 __global__ void __launch_bounds__(256, MINB) k_g2p2(PartArgs a) {
-  __shared__ float red_c[256], red_h[256];
+  __shared__ float red_c[8], red_h[8];
   extern __shared__ __align__(16) float4 g2p_stage[];  // G2P_STAGE_NODES (v, T) of the staged box
   if (run_finished(a.scalars)) return;
   RangeDev rd;
@@ -1576,6 +1576,9 @@ __global__ void __launch_bounds__(256, MINB) k_g2p2(PartArgs a) {
   float my_c = 0.f, my_h = 1.f;
   float *P = *a.Pp;
   const size_t ps = a.ps;
+  // the linear EOS + Johnson-Cook kernels serve FLIP/PIC runs only (APIC runs
+  // take the general ones): no affine moments, no per-slot offsets kept
+  const bool apic = LAW == LAW_EOS_LINEAR_JC ? false : a.apic != 0;
   const GridDev g = a.grids[rd.grid];
   float xp[3];
 #pragma unroll
@@ -1620,7 +1623,7 @@ __global__ void __launch_bounds__(256, MINB) k_g2p2(PartArgs a) {
         asm volatile("{ .reg .u64 ad; mad.lo.u64 ad, %1, %2, %0; prefetch.global.L2 [ad]; }" ::"l"(base),
                      "l"(row_bytes), "l"((unsigned long long)r));
     }
-    if ((BASIS == 0 || BASIS == 1 || BASIS == 3) && a.apic) {
+    if ((BASIS == 0 || BASIS == 1 || BASIS == 3) && apic) {
       // APIC (compute_rate_deformation_gradient_{TL,UL}_APIC,
       // src/solid.cpp:1006-1153): grad v = sum w v_node (x_node - x_p)^T Di with
       // Di = 3 / cellsize^2 (cubic) or 4 / cellsize^2 (quadratic)
@@ -1672,7 +1675,7 @@ __global__ void __launch_bounds__(256, MINB) k_g2p2(PartArgs a) {
       const float r = P[PF_X0 * ps + p] + (TL ? 0.f : P[(a.use_vu ? PF_X : PF_XN) * ps + p]);
       G[8] += vr / r;
     }
-    if ((BASIS == 0 || BASIS == 1 || BASIS == 3) && a.apic)
+    if ((BASIS == 0 || BASIS == 1 || BASIS == 3) && apic)
 #pragma unroll
       for (int k = 0; k < 9; k++) P[(PF_C + k) * ps + p] = G[k];  // C of the next transfers
     // ---- deformation gradient (src/solid.cpp:1155-1244), stored as H = F - I
@@ -1919,20 +1922,27 @@ __global__ void __launch_bounds__(256, MINB) k_g2p2(PartArgs a) {
       if (TL) my_h = fminf(1.f, min_abs_eig_real(H));
     }
   }
-  // block reduction (order-free min / max)
-  red_c[threadIdx.x] = my_c;
-  red_h[threadIdx.x] = my_h;
-  __syncthreads();
-  for (int s = 128; s > 0; s >>= 1) {
-    if (threadIdx.x < s) {
-      red_c[threadIdx.x] = fmaxf(red_c[threadIdx.x], red_c[threadIdx.x + s]);
-      red_h[threadIdx.x] = fminf(red_h[threadIdx.x], red_h[threadIdx.x + s]);
-    }
-    __syncthreads();
+  // block reduction (order-free min / max): within each warp by shuffles,
+  // then over the eight warps
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    my_c = fmaxf(my_c, __shfl_xor_sync(0xffffffffu, my_c, o));
+    my_h = fminf(my_h, __shfl_xor_sync(0xffffffffu, my_h, o));
   }
+  if ((threadIdx.x & 31) == 0) {
+    red_c[threadIdx.x >> 5] = my_c;
+    red_h[threadIdx.x >> 5] = my_h;
+  }
+  __syncthreads();
   if (threadIdx.x == 0) {
-    a.blk_c[blockIdx.x] = red_c[0];
-    a.blk_h[blockIdx.x] = red_h[0];
+    float c = red_c[0], hh = red_h[0];
+#pragma unroll
+    for (int w = 1; w < 8; w++) {
+      c = fmaxf(c, red_c[w]);
+      hh = fminf(hh, red_h[w]);
+    }
+    a.blk_c[blockIdx.x] = c;
+    a.blk_h[blockIdx.x] = hh;
   }
 }
 
