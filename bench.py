@@ -50,6 +50,8 @@ PHASE_BYTES = {
     # TLMPM MUSL after a step of the same particle state: the forces only
     # (the momentum is the last re-map's nodal sum)
     "p2g_force": (48, 12),      # x0, vol0*PK1 -> nodal f
+    # the velocity scatter where the momentum is not the last re-map's
+    "p2g_momentum": (28, 28),   # x0, m, v -> nodal p (kept, 16 B per node)
     "grid_update": (0, 52),     # m, p, f -> v, v_update (+ fixes)
     "g2p_advance": (60, 24),    # x0, u, v -> u, v ; gathers v, v_update
     "p2g_velocity": (28, 12),   # x0, m, v -> nodal p

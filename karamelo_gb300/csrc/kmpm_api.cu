@@ -86,13 +86,17 @@ struct kmpm_ctx {
   MatDev *d_mats = nullptr;
   float4 *nodeA = nullptr, *nodeB = nullptr, *nodeX = nullptr;
   float *nodeT = nullptr;
-  // TLMPM MUSL momentum reuse (P2G_FONLY): the re-map's nodal momentum sums,
-  // kept for the next step's grid update, whose scatter then sums the forces
-  // only.  reuse_p: this configuration takes it (select_scatters); p_valid:
-  // nodeP holds the sums of the particles' current velocities (set by every
-  // step, cleared by anything that changes the particle state between steps)
+  // TLMPM MUSL force-only scatter and momentum reuse (P2G_FONLY): the step's
+  // scatter sums the forces only (k_p2g_force_row) and the grid update takes
+  // the nodal momentum from nodeP: the last re-map's sums, kept by the grid
+  // velocity pass, or, where those are not the current state's, the sums of
+  // a velocity scatter run first.  fonly: this configuration takes that path
+  // (select_scatters); reuse_ok: the re-map's sums may be reused
+  // (KMPM_NO_MOMENTUM_REUSE=1: never); p_valid: nodeP holds the sums of the
+  // particles' current velocities (set by every step, cleared by anything
+  // that changes the particle state between steps)
   float4 *nodeP = nullptr;
-  bool reuse_p = false, p_valid = false;
+  bool fonly = false, reuse_ok = false, p_valid = false;
   int smem_fonly = 0;
   int tdim[3] = {0, 0, 0}, NCELL = 0, ntiles_total = 0;
   int2 *d_tiles = nullptr;
@@ -128,7 +132,7 @@ struct kmpm_ctx {
   std::vector<int> ul_fields;
   StepKernels K{};
   cudaGraphExec_t gexec = nullptr;
-  cudaGraphExec_t gexec_r = nullptr;  // the step with the momentum reuse (reuse_p)
+  cudaGraphExec_t gexec_r = nullptr;  // the step with the momentum reuse (fonly and reuse_ok)
   bool graph_valid = false;
   int launches_per_step = 0;
   int smem[4][2] = {{0}};
@@ -357,7 +361,7 @@ GridArgs grid_args(kmpm_ctx *c, int remap) {
   a.scalars = c->d_scalars;
   a.indep = c->indep();
   a.remap = remap;
-  a.nodeP = c->reuse_p ? c->nodeP : nullptr;
+  a.nodeP = c->fonly ? c->nodeP : nullptr;
   return a;
 }
 
@@ -988,16 +992,16 @@ int select_scatters(kmpm_ctx *c) {
   CK(cudaFuncSetAttribute(c->sc_force, cudaFuncAttributeMaxDynamicSharedMemorySize, c->smem_force));
   CK(cudaFuncSetAttribute(c->sc_usf, cudaFuncAttributeMaxDynamicSharedMemorySize, c->smem_usf));
   // TLMPM MUSL with FLIP/PIC on the plain row scatter, mechanical, FP32: the
-  // scatter of the next step sums the forces only (P2G_FONLY).
-  // KMPM_NO_MOMENTUM_REUSE=1 keeps the full scatter every step.
+  // force-only scatter, with the momentum of the last re-map where it is the
+  // current state's (KMPM_NO_MOMENTUM_REUSE=1: a velocity scatter every step)
   {
     const char *ev = std::getenv("KMPM_NO_MOMENTUM_REUSE");
-    c->reuse_p = TL && c->musl() && !th && flags == 0 && !c->apic() && c->nodeP &&
-                 c->prm.precision == KMPM_PREC_FP32 && c->K.p2g_row_fonly && c->sc_force == c->K.p2g_row[0] &&
-                 !(ev && ev[0] == '1');
+    c->fonly = TL && c->musl() && !th && flags == 0 && !c->apic() && c->nodeP &&
+               c->prm.precision == KMPM_PREC_FP32 && c->K.p2g_row_fonly && c->sc_force == c->K.p2g_row[0];
+    c->reuse_ok = c->fonly && !(ev && ev[0] == '1');
     c->p_valid = false;
-    if (c->reuse_p) {
-      c->smem_fonly = p2g_smem_bytes(c->prm.dim, c->prm.basis, P2G_TL | P2G_FONLY, false);
+    if (c->fonly) {
+      c->smem_fonly = c->K.p2g_row_fonly_smem;
       CK(cudaFuncSetAttribute(c->K.p2g_row_fonly, cudaFuncAttributeMaxDynamicSharedMemorySize, c->smem_fonly));
     }
   }
@@ -1006,9 +1010,8 @@ int select_scatters(kmpm_ctx *c) {
 
 // ---------------------------------------------------------------- one step
 // USL::run (src/usl.cpp:43-92) / MUSL::run (src/musl.cpp:43-93)
-// reuse: the step after another step of the same particle state (reuse_p):
-// the scatter sums the forces only and the grid update takes the momentum the
-// last re-map summed (P2G_FONLY)
+// reuse (fonly configurations): nodeP holds the last re-map's momentum, which
+// is the current state's, so no velocity scatter runs before the force scatter
 int enqueue_step(kmpm_ctx *c, bool reuse = false) {
   int nl = 0;
   const bool TL = c->TL(), th = c->prm.thermal != 0, musl = c->musl();
@@ -1068,7 +1071,15 @@ int enqueue_step(kmpm_ctx *c, bool reuse = false) {
   p.apic_pos = TL ? -1 : PF_X;
   // (with w mbp added to the node forces when contacts exist, and the hoop
   // term in axisymmetric runs: select_scatters)
-  if (reuse) {
+  if (c->fonly) {
+    if (!reuse) {
+      // compute_velocity_nodes: the sums the re-map forms (the velocity row
+      // scatter), kept in nodeP
+      LAUNCH(c->K.p2g_vel, c->ntiles_launch, 256, c->smem[3][0], p);
+      LAUNCH(c->K.grid_store_p, c->nblk_g, 256, 0, g1);
+      MARK("p2g_momentum");
+    }
+    // compute_internal_forces_nodes_TL
     LAUNCH(c->K.p2g_row_fonly, c->ntiles_launch, 256, c->smem_fonly, p);
     MARK("p2g_force");
   } else {
@@ -1076,7 +1087,7 @@ int enqueue_step(kmpm_ctx *c, bool reuse = false) {
     MARK("p2g");
   }
   // update_grid_state + fixes
-  LAUNCH(reuse ? c->K.grid_upd_fonly : c->K.grid_upd[TL][th][prec], c->nblk_g, 256, 0, g1);
+  LAUNCH(c->fonly ? c->K.grid_upd_fonly : c->K.grid_upd[TL][th][prec], c->nblk_g, 256, 0, g1);
   MARK("grid_update");
   if (c->usf()) {
     // USF::run (src/usf.cpp:43-86): the stress from the grid velocities of the
@@ -1188,7 +1199,7 @@ int ensure_graph(kmpm_ctx *c) {
   if (c->graph_valid) return KMPM_OK;
   c->p_valid = false;
   int r = capture_step(c, false, &c->gexec);
-  if (r == KMPM_OK && c->reuse_p) r = capture_step(c, true, &c->gexec_r);
+  if (r == KMPM_OK && c->reuse_ok) r = capture_step(c, true, &c->gexec_r);
   if (r != KMPM_OK) return r;
   c->graph_valid = true;
   return KMPM_OK;
@@ -1198,8 +1209,8 @@ int ensure_graph(kmpm_ctx *c) {
 // re-map's sums are those of the current particle state
 int launch_steps(kmpm_ctx *c, int n) {
   for (int i = 0; i < n; i++) {
-    CK(cudaGraphLaunch(c->reuse_p && c->p_valid ? c->gexec_r : c->gexec, c->st));
-    c->p_valid = c->reuse_p;
+    CK(cudaGraphLaunch(c->reuse_ok && c->p_valid ? c->gexec_r : c->gexec, c->st));
+    c->p_valid = c->reuse_ok;
   }
   return KMPM_OK;
 }
@@ -2049,10 +2060,10 @@ int kmpm_profile(kmpm_ctx *c, int nsteps, double *phase_ms, int max_phases, int 
   for (int s = 0; s < nsteps; s++) {
     c->profiling = true;
     c->prof_n = 0;
-    r = enqueue_step(c, c->reuse_p && c->p_valid);
+    r = enqueue_step(c, c->reuse_ok && c->p_valid);
     c->profiling = false;
     if (r != KMPM_OK) return r;
-    c->p_valid = c->reuse_p;
+    c->p_valid = c->reuse_ok;
     CK(cudaStreamSynchronize(c->st));
     acc.resize(std::max<size_t>(acc.size(), c->prof_n), 0.0);
     for (int k = 1; k < c->prof_n; k++) {

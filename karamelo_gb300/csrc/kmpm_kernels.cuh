@@ -25,12 +25,12 @@ enum P2GMode : int {
   // T_zz / r (1) joins the payload, and -w T_zz / r the radial force sums
   // (src/solid.cpp:472-475, 513-519, 565-571)
   P2G_AXI = 16,
-  // flag on P2G_TL (TLMPM MUSL, FLIP/PIC, mechanical): the force sums only.
-  // TLMPM's weights and masses do not change, and no velocity changes
-  // between a step's re-map and the next step's scatter, so the nodal
-  // momentum of that scatter is the re-map's sum, bit for bit: the velocity
-  // pass of the grid keeps it (GridArgs::nodeP) and the next grid update
-  // reads it there
+  // flag on P2G_TL (TLMPM MUSL, FLIP/PIC, mechanical): the force sums only
+  // (k_p2g_force_row).  TLMPM's weights and masses do not change, and no
+  // velocity changes between a step's re-map and the next step's scatter, so
+  // the nodal momentum of that scatter is the re-map's sum, bit for bit: the
+  // velocity pass of the grid keeps it (GridArgs::nodeP) and the next grid
+  // update reads it there
   P2G_FONLY = 32,
 };
 __host__ __device__ constexpr int p2g_kind(int mode) { return mode & 7; }
@@ -39,8 +39,9 @@ __host__ __device__ constexpr int p2g_base(int mode) { return p2g_kind(mode) >= 
 __host__ __device__ constexpr bool p2g_apic(int mode) { return p2g_kind(mode) >= P2G_TL_APIC; }
 __host__ __device__ constexpr bool p2g_ext(int mode) { return (mode & P2G_EXT) != 0; }
 __host__ __device__ constexpr bool p2g_fonly(int mode) { return (mode & P2G_FONLY) != 0; }
-// GM_UPDATE_F: the grid update after a P2G_FONLY scatter (momentum from nodeP)
-enum GridMode : int { GM_MASS = 0, GM_UPDATE = 1, GM_VEL = 2, GM_UPDATE_F = 3 };
+// GM_UPDATE_F: the grid update after a P2G_FONLY scatter (momentum from
+// nodeP); GM_STORE_P: the momentum sums of a P2G_VEL scatter into nodeP
+enum GridMode : int { GM_MASS = 0, GM_UPDATE = 1, GM_VEL = 2, GM_UPDATE_F = 3, GM_STORE_P = 4 };
 
 __host__ __device__ constexpr int p2g_nq(int mode, bool th) {
   return p2g_fonly(mode) ? 3
@@ -159,10 +160,13 @@ struct StepKernels {
   // the row scatters (k_p2g_row, k_p2g_row2) of the plain TL, UL and
   // velocity modes: 2-D and 3-D cubic and quadratic splines (nullptr elsewhere)
   void *p2g_row[3];
-  // the 3-D row scatter of the force sums only (P2G_TL | P2G_FONLY) and the
-  // grid update that takes the stored momentum (GM_UPDATE_F): TLMPM, FP32,
-  // mechanical, cubic and quadratic splines (nullptr elsewhere)
-  void *p2g_row_fonly, *grid_upd_fonly;
+  // the 3-D scatter of the force sums only (k_p2g_force_row, P2G_TL |
+  // P2G_FONLY) and its dynamic shared memory, the grid update that takes the
+  // stored momentum (GM_UPDATE_F) and the pass that stores the momentum of a
+  // velocity scatter (GM_STORE_P): TLMPM, FP32, mechanical, cubic and
+  // quadratic splines (nullptr elsewhere)
+  void *p2g_row_fonly, *grid_upd_fonly, *grid_store_p;
+  int p2g_row_fonly_smem;
   void *p2g_tl_apic, *p2g_ul_apic, *p2g_vel_apic;  // cubic spline only (nullptr otherwise)
   // the force scatters with external particle forces (P2G_EXT): [thermal]
   void *p2g_tl_ext[2], *p2g_ul_ext[2], *p2g_tl_apic_ext, *p2g_ul_apic_ext;

@@ -390,18 +390,6 @@ __global__ void __launch_bounds__(256, (p2g_min_blocks<DIM, MODE, THERMAL>())) k
 template <int MODE, int Q>
 __device__ __forceinline__ void p2g_row_particle(float (&A0)[Q], float (&A2)[Q], const float *pay, float2 bx,
                                                  float2 by, float2 bz0, float2 bz2) {
-  if constexpr (p2g_fonly(MODE)) {
-    // the force sums only (P2G_FONLY; payload vol0 PK1, row-major), in the
-    // arithmetic of the P2G_TL force sums below, so that both give the same bits
-    const float wxy = bx.x * by.x, gxy0 = bx.y * by.x, gxy1 = bx.x * by.y;
-#pragma unroll
-    for (int r = 0; r < 3; r++) {
-      const float t = fmaf(pay[3 * r], gxy0, pay[3 * r + 1] * gxy1), t2 = pay[3 * r + 2] * wxy;
-      A0[r] = fmaf(-bz0.x, t, fmaf(-bz0.y, t2, A0[r]));
-      A2[r] = fmaf(-bz2.x, t, fmaf(-bz2.y, t2, A2[r]));
-    }
-    return;
-  }
   constexpr int OM = MODE == P2G_UL ? 1 : 0;  // UL sums start with the mass
   constexpr bool FORCE = MODE != P2G_VEL;
   const float wxy = bx.x * by.x;
@@ -416,7 +404,7 @@ __device__ __forceinline__ void p2g_row_particle(float (&A0)[Q], float (&A2)[Q],
       float T0, T1, T2;
       if (MODE == P2G_TL) {  // vol0 PK1, row-major
         T0 = pay[3 + 3 * r]; T1 = pay[4 + 3 * r]; T2 = pay[5 + 3 * r];
-        t[r] = fmaf(T0, gxy0, T1 * gxy1);  // as the force-only scatter
+        t[r] = fmaf(T0, gxy0, T1 * gxy1);
       } else {  // vol sigma, symmetric xx yy zz xy xz yz
         const float *sg = pay + 4;
         T0 = r == 0 ? sg[0] : (r == 1 ? sg[3] : sg[4]);
@@ -470,7 +458,7 @@ __device__ __forceinline__ void p2g_row_particle(float (&A0)[Q], float (&A2)[Q],
 }
 
 template <int BASIS, int MODE>
-__global__ void __launch_bounds__(256, (MODE == P2G_VEL || p2g_fonly(MODE) ? 4 : 3)) k_p2g_row(P2GArgs a) {
+__global__ void __launch_bounds__(256, (MODE == P2G_VEL ? 4 : 3)) k_p2g_row(P2GArgs a) {
   static_assert(Stencil<BASIS>::S == 4 && Stencil<BASIS>::SC == 1, "four-wide stencils");
   using TS = TileShape<3, BASIS>;
   constexpr int S = 4, LO = Stencil<BASIS>::LO;
@@ -505,8 +493,8 @@ __global__ void __launch_bounds__(256, (MODE == P2G_VEL || p2g_fonly(MODE) ? 4 :
   {  // the tile's particle rows that the stage phase reads, into L2
     const int t0 = a.tile_start[tile_global], t1 = a.tile_end[tile_global];
     prefetch_rows_l2(P, ps, PF_X0, use_u ? 6 : 3, t0, t1);
-    if (!p2g_fonly(MODE)) prefetch_rows_l2(P, ps, PF_V, 4, t0, t1);  // v, mass
-    if (MODE != P2G_VEL) prefetch_rows_l2(P, ps, PF_PK, p2g_base(MODE) == P2G_TL ? 9 : 6, t0, t1);
+    prefetch_rows_l2(P, ps, PF_V, 4, t0, t1);  // v, mass
+    if (MODE != P2G_VEL) prefetch_rows_l2(P, ps, PF_PK, MODE == P2G_TL ? 9 : 6, t0, t1);
   }
 
   for (int k = lane; k < Q * NF; k += 32) slab[k] = 0.f;
@@ -619,6 +607,197 @@ __global__ void __launch_bounds__(256, (MODE == P2G_VEL || p2g_fonly(MODE) ? 4 :
       const int fi = (sa * WY + fy) * WZ + fz;
 #pragma unroll
       for (int qq = 0; qq < Q; qq++) slab[qq * NF + fi] += acc[m][qq];
+    }
+    __syncwarp();
+  }
+  __syncthreads();
+  // ---- sum the slabs in warp order into the tile footprint
+  float *out = a.partial + (size_t)tile_global * a.pstride_tile;
+  for (int k = threadIdx.x; k < Q * NW; k += blockDim.x) {
+    const int qq = k / NW, fi = k % NW;
+    const int fx = fi / (WY * WZ), fyz = fi % (WY * WZ);
+    float sum = 0.f;
+#pragma unroll
+    for (int w = 0; w < TS::NWARP; w++) {
+      const int x = fx - w;
+      if (x >= 0 && x < FX) sum += smem[w * SLAB + qq * NF + x * WY * WZ + fyz];
+    }
+    out[k] = sum;
+  }
+}
+
+// dynamic shared memory of k_p2g_force_row (bytes)
+template <int BASIS> constexpr int p2g_force_row_smem() {
+  using TS = TileShape<3, BASIS>;
+  return 4 * TS::NWARP * (((3 * TS::NF + 3) & ~3) + 32 * 12 + 34 * 2 * 4 * 2 + 2 * 32 * 4);
+}
+
+// ============================================================== force-only P2G by half-warps
+// The TLMPM force scatter of the momentum reuse (P2G_TL | P2G_FONLY): the
+// tiles, warps, rows of four cells and slab footprints of k_p2g_row, with
+// the row's particles shared between the two half-warps:
+//   - stage (lane = particle): payload vol0 PK1 (9 floats) and the per-axis
+//     values and slopes, the z axis as two float4 (s0 ds0 s1 ds1) (s2 ds2
+//     s3 ds3) per particle;
+//   - accumulate: half-warp h takes particles jlo + h, jlo + h + 2, ... of
+//     each cell, in sorted order; lane (a, b) of a half adds into x slot a,
+//     y slot b and all four z slots, seven register sums per force
+//     component over the row's z nodes.  The per-particle terms of a lane
+//     (the (a, b) products of PK1 with the x and y values and slopes) are
+//     formed once for four slots, where k_p2g_row forms them for two;
+//   - flush once per row: half 1's sums join half 0's by one shuffle, and
+//     half 0 adds the row into the warp's slab.
+// Every sum runs in a fixed order: the result is bit-reproducible.
+template <int BASIS>
+__global__ void __launch_bounds__(256, 4) k_p2g_force_row(P2GArgs a) {
+  static_assert(Stencil<BASIS>::S == 4 && Stencil<BASIS>::SC == 1, "four-wide stencils");
+  using TS = TileShape<3, BASIS>;
+  constexpr int S = 4, LO = Stencil<BASIS>::LO;
+  constexpr int TX = TS::TX, TY = TS::TY, TZ = TS::TZ;
+  constexpr int WY = TS::WY, WZ = TS::WZ, NW = TS::NW, NF = TS::NF, FX = TS::FX;
+  static_assert(TS::L == 1 && TZ == 4 && FX == 4, "one x-layer of 4 x 4 cells per warp");
+  constexpr int Q = 3;
+  constexpr int SLAB = (Q * NF + 3) & ~3;
+  constexpr int SROW = 34;  // x, y rows of float2: the two halves' reads fall in different banks
+  constexpr int STAGE = 32 * 12 + SROW * 2 * S * 2 + 2 * 32 * 4;
+  static_assert(p2g_force_row_smem<BASIS>() == 4 * TS::NWARP * (SLAB + STAGE), "shared-memory size");
+
+  extern __shared__ __align__(16) float smem[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  float *slab = smem + warp * SLAB;
+  float *spay = smem + TS::NWARP * SLAB + warp * STAGE;                 // [32][12]
+  float2 *sbxy = reinterpret_cast<float2 *>(spay + 32 * 12);           // [axis x, y][slot][SROW]
+  float4 *sbz = reinterpret_cast<float4 *>(sbxy + 2 * S * SROW);       // [pair][32]
+
+  const int2 td = a.tiles[blockIdx.x];
+  const GridDev g = a.grids[td.x];
+  const int tlin = td.y;
+  const int tile_global = g.tile_off + tlin;
+  if (a.tile_end[tile_global] == a.tile_start[tile_global] || run_finished(a.scalars)) return;
+  const int tc2 = tlin % g.ntile[2], tc1 = (tlin / g.ntile[2]) % g.ntile[1], tc0 = tlin / (g.ntile[1] * g.ntile[2]);
+  const float h = g.cellsize, ih = g.inv_cellsize;
+  const float *P = *a.Pp;
+  const size_t ps = a.ps;
+  {  // the tile's x0 and vol0 PK1 rows, into L2
+    const int t0 = a.tile_start[tile_global], t1 = a.tile_end[tile_global];
+    prefetch_rows_l2(P, ps, PF_X0, 3, t0, t1);
+    prefetch_rows_l2(P, ps, PF_PK, 9, t0, t1);
+  }
+
+  for (int k = lane; k < Q * NF; k += 32) slab[k] = 0.f;
+
+  // this lane's half and stencil slots in the accumulate phase
+  const int hw = lane >> 4, sa = (lane >> 2) & 3, sb = lane & 3;
+  const float2 *px = sbxy + (0 * S + sa) * SROW, *py = sbxy + (1 * S + sb) * SROW;
+  const int i0x = (tc0 * TX + warp) - LO;
+
+  for (int ly = 0; ly < TY; ly++) {
+    // the row's four cells and their particle ranges (as k_p2g_row)
+    const int cbase = tile_global * TS::NCELL + (warp * TY + ly) * TZ;
+    const int cv = lane < 8 ? (lane < 4 ? a.cell_start[cbase + lane] : a.cell_end[cbase + lane - 4]) : 0;
+    int st[4], en[4], lo4[4];
+    int rs = INT_MAX, re = INT_MIN;
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      st[k] = __shfl_sync(0xffffffffu, cv, k);
+      en[k] = __shfl_sync(0xffffffffu, cv, 4 + k);
+      const bool full = en[k] > st[k];
+      lo4[k] = full ? st[k] : INT_MAX;
+      rs = full ? min(rs, st[k]) : rs;
+      re = full ? max(re, en[k]) : re;
+    }
+    if (rs == INT_MAX) continue;
+    const int i0y = (tc1 * TY + ly) - LO;
+    float acc[7][Q];
+#pragma unroll
+    for (int m = 0; m < 7; m++)
+#pragma unroll
+      for (int qq = 0; qq < Q; qq++) acc[m][qq] = 0.f;
+
+    for (int c0 = rs; c0 < re; c0 += 32) {
+      const int cnt = min(32, re - c0);
+      // ---- stage (lane = particle)
+      if (lane < cnt) {
+        const int p = c0 + lane;
+        int lz = 0;
+#pragma unroll
+        for (int k = 1; k < 4; k++) lz = lo4[k] <= p ? k : lz;
+        float pay[9];
+#pragma unroll
+        for (int k = 0; k < 9; k++) pay[k] = P[(PF_PK + k) * ps + p];
+        reinterpret_cast<float4 *>(spay + lane * 12)[0] = make_float4(pay[0], pay[1], pay[2], pay[3]);
+        reinterpret_cast<float4 *>(spay + lane * 12)[1] = make_float4(pay[4], pay[5], pay[6], pay[7]);
+        spay[lane * 12 + 8] = pay[8];
+        const int i0[3] = {i0x, i0y, (tc2 * TZ + lz) - LO};
+#pragma unroll
+        for (int d = 0; d < 3; d++) {
+          const float xp = P[(PF_X0 + d) * ps + p];
+          const float lod = d == 0 ? g.lo[0] : (d == 1 ? g.lo[1] : g.lo[2]);
+          const int nd = d == 0 ? g.n[0] : (d == 1 ? g.n[1] : g.n[2]);
+          const int ngd = d == 0 ? g.ng[0] : (d == 1 ? g.ng[1] : g.ng[2]);
+          float sv[S], dsv[S];
+          if (BASIS == 1 && cubic_interior(i0[d], nd, ngd)) {
+            cubic_weights(cells_of(xp, lod, ih) - (float)(i0[d] + 1), ih, sv, dsv);
+          } else {
+#pragma unroll
+            for (int kk = 0; kk < S; kk++) {
+              const int i = i0[d] + kk;
+              sv[kk] = 0.f;
+              dsv[kk] = 0.f;
+              if (i >= 0 && i < nd) {
+                const float r = node_offset_cells(xp, lod, i, h, ih);
+                basis<BASIS>(r, node_type<BASIS>(i, ngd), ih, sv[kk], dsv[kk]);
+                dsv[kk] = sv[kk] != 0.f ? dsv[kk] : 0.f;  // as Axis::eval
+              }
+            }
+          }
+          if (d < 2) {
+#pragma unroll
+            for (int kk = 0; kk < S; kk++) sbxy[(d * S + kk) * SROW + lane] = make_float2(sv[kk], dsv[kk]);
+          } else {
+            sbz[lane] = make_float4(sv[0], dsv[0], sv[1], dsv[1]);
+            sbz[32 + lane] = make_float4(sv[2], dsv[2], sv[3], dsv[3]);
+          }
+        }
+      }
+      __syncwarp();
+      // ---- accumulate (half-warp = particle, lane = (x, y) slot pair)
+#pragma unroll
+      for (int lz = 0; lz < 4; lz++) {
+        const int jlo = max(st[lz] - c0, 0), jhi = min(en[lz] - c0, cnt);
+        for (int j = jlo + hw; j < jhi; j += 2) {
+          const float4 pa = reinterpret_cast<const float4 *>(spay + j * 12)[0];
+          const float4 pb = reinterpret_cast<const float4 *>(spay + j * 12)[1];
+          const float p8 = spay[j * 12 + 8];
+          const float T[9] = {pa.x, pa.y, pa.z, pa.w, pb.x, pb.y, pb.z, pb.w, p8};
+          const float2 bx = px[j], by = py[j];
+          const float4 z01 = sbz[j], z23 = sbz[32 + j];
+          const float zs[4] = {z01.x, z01.z, z23.x, z23.z}, zd[4] = {z01.y, z01.w, z23.y, z23.w};
+          const float wxy = bx.x * by.x, gxy0 = bx.y * by.x, gxy1 = bx.x * by.y;
+#pragma unroll
+          for (int r = 0; r < 3; r++) {
+            // f_r -= PK1(r, :) . grad w: the x and y parts t, the z part t2
+            const float t = fmaf(T[3 * r], gxy0, T[3 * r + 1] * gxy1), t2 = T[3 * r + 2] * wxy;
+#pragma unroll
+            for (int c = 0; c < 4; c++) acc[lz + c][r] = fmaf(-zs[c], t, fmaf(-zd[c], t2, acc[lz + c][r]));
+          }
+        }
+      }
+      __syncwarp();
+    }
+    // ---- flush: half 1's sums join half 0's, which adds the row into the slab
+#pragma unroll
+    for (int m = 0; m < 7; m++)
+#pragma unroll
+      for (int qq = 0; qq < Q; qq++) acc[m][qq] += __shfl_xor_sync(0xffffffffu, acc[m][qq], 16);
+    if (hw == 0) {
+      const int fy = ly + sb;
+#pragma unroll
+      for (int m = 0; m < 7; m++) {
+        const int fi = (sa * WY + fy) * WZ + m;
+#pragma unroll
+        for (int qq = 0; qq < Q; qq++) slab[qq * NF + fi] += acc[m][qq];
+      }
     }
     __syncwarp();
   }
@@ -915,6 +1094,14 @@ __global__ void __launch_bounds__(256) k_grid(GridArgs a) {
     float4 A = a.nodeA[NODE_STRIDE * node];
     A.w = (float)s[0];
     a.nodeA[NODE_STRIDE * node] = A;
+    return;
+  }
+  if (GMODE == GM_STORE_P) {
+    // the momentum of a P2G_VEL scatter of the current state into nodeP, as
+    // GM_VEL keeps the re-map's (TLMPM, mechanical)
+    R s[3];
+    gather_partials<DIM, BASIS, 3, R>(a, g, li, ix, s);
+    a.nodeP[node] = make_float4((float)s[0], (float)s[1], (float)s[2], 0.f);
     return;
   }
   if (GMODE == GM_UPDATE || GMODE == GM_UPDATE_F) {
@@ -1956,10 +2143,13 @@ void fill_step_kernels(StepKernels &k) {
   k.p2g_ul_th = (void *)k_p2g<DIM, BASIS, P2G_UL, true>;
   k.p2g_vel = (void *)k_p2g<DIM, BASIS, P2G_VEL, false>;
   k.p2g_vel_th = (void *)k_p2g<DIM, BASIS, P2G_VEL, true>;
-  k.p2g_row_fonly = k.grid_upd_fonly = nullptr;
+  k.p2g_row_fonly = k.grid_upd_fonly = k.grid_store_p = nullptr;
+  k.p2g_row_fonly_smem = 0;
   if constexpr (DIM == 3 && (BASIS == 1 || BASIS == 3)) {
-    k.p2g_row_fonly = (void *)k_p2g_row<BASIS, P2G_TL | P2G_FONLY>;
+    k.p2g_row_fonly = (void *)k_p2g_force_row<BASIS>;
+    k.p2g_row_fonly_smem = p2g_force_row_smem<BASIS>();
     k.grid_upd_fonly = (void *)k_grid<DIM, BASIS, GM_UPDATE_F, true, false, float>;
+    k.grid_store_p = (void *)k_grid<DIM, BASIS, GM_STORE_P, true, false, float>;
     k.p2g_row[0] = (void *)k_p2g_row<BASIS, P2G_TL>;
     k.p2g_row[1] = (void *)k_p2g_row<BASIS, P2G_UL>;
     k.p2g_row[2] = (void *)k_p2g_row<BASIS, P2G_VEL>;

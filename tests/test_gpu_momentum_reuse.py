@@ -1,13 +1,15 @@
-"""TLMPM MUSL momentum reuse against the full scatter of every step.
+"""TLMPM MUSL momentum reuse against a momentum scatter every step.
 
 TLMPM's weights and masses never change, and no particle velocity changes
 between a step's re-map (velocities_to_grid, src/musl.cpp:59-67) and the next
 step's scatter (particles_to_grid): the nodal momentum that scatter would sum
-is the re-map's, bit for bit.  With the reuse the velocity pass of the grid
-keeps the re-map's sums and the next scatter sums the forces only (P2G_FONLY);
-KMPM_NO_MOMENTUM_REUSE=1 scatters the momentum every step.  Both must give
-the same bits, including after an upload between steps (which must make the
-next step scatter the momentum of the new state) and across kmpm_run calls."""
+is the re-map's, bit for bit.  The step's scatter sums the forces only
+(k_p2g_force_row); with the reuse the velocity pass of the grid keeps the
+re-map's momentum for the next grid update, and KMPM_NO_MOMENTUM_REUSE=1
+runs the velocity row scatter (the re-map's sums) before it every step.
+Both must give the same bits, including after an upload between steps
+(which must make the next step scatter the momentum of the new state) and
+across kmpm_run calls."""
 import os
 
 import numpy as np
@@ -48,8 +50,10 @@ def _run(basis, reuse, upload):
 def test_momentum_reuse_bit_identical(gpu_lib, basis, upload):
     ph_r, a = _run(basis, True, upload)
     ph_f, b = _run(basis, False, upload)
-    assert "p2g_force" in ph_r and "p2g" not in ph_r
-    assert "p2g" in ph_f and "p2g_force" not in ph_f
+    # both run the force-only scatter; without the reuse a velocity scatter
+    # forms the momentum first every step
+    assert "p2g_force" in ph_r and "p2g_momentum" not in ph_r and "p2g" not in ph_r
+    assert "p2g_force" in ph_f and "p2g_momentum" in ph_f and "p2g" not in ph_f
     for k in a:
         assert np.array_equal(a[k], b[k]), f"{k}: max |diff| {np.max(np.abs(a[k] - b[k])):.3e}"
 
