@@ -817,6 +817,191 @@ __global__ void __launch_bounds__(256, 4) k_p2g_force_row(P2GArgs a) {
   }
 }
 
+// ============================================================== velocity row scatter by half-warps
+// The sums of compute_velocity_nodes (Σ w m v, the MUSL re-map) over the
+// rows of four cells of k_p2g_row, the row's particles shared between the
+// two half-warps as in k_p2g_force_row: half-warp hw takes particles
+// jlo + hw, jlo + hw + 2, ... of each cell in sorted order, and lane (a, b)
+// of a half adds into x slot a, y slot b and all four z slots, seven
+// register sums per component over the row's z nodes.  The fused MUSL pass
+// (k_g2p1_remap_row) and the velocity scatter (k_p2g_vel_row) share this
+// code, so they give the same bits.  Staged per warp: m v (float4 per
+// particle), the x and y weights in rows of VROW floats per slot (the two
+// halves' reads fall in different banks), the four z weights as one float4.
+constexpr int VROW = 36;
+constexpr int VEL_STAGE = 32 * 4 + 2 * 4 * VROW + 32 * 4;  // floats per warp
+
+__device__ __forceinline__ void vel_row_stage_basis(float *sbxy, float4 *sbz, int lane, const float (&sv)[3][4]) {
+#pragma unroll
+  for (int kk = 0; kk < 4; kk++) {
+    sbxy[kk * VROW + lane] = sv[0][kk];
+    sbxy[(4 + kk) * VROW + lane] = sv[1][kk];
+  }
+  sbz[lane] = make_float4(sv[2][0], sv[2][1], sv[2][2], sv[2][3]);
+}
+
+__device__ __forceinline__ void vel_row_accumulate(float (&acc)[7][3], const float *spay, const float *px,
+                                                   const float *py, const float4 *sbz, const int (&st)[4],
+                                                   const int (&en)[4], int c0, int cnt, int hw) {
+#pragma unroll
+  for (int lz = 0; lz < 4; lz++) {
+    const int jlo = max(st[lz] - c0, 0), jhi = min(en[lz] - c0, cnt);
+    for (int j = jlo + hw; j < jhi; j += 2) {
+      const float4 t4 = reinterpret_cast<const float4 *>(spay)[j];
+      const float wxy = px[j] * py[j];
+      const float q[3] = {wxy * t4.x, wxy * t4.y, wxy * t4.z};
+      const float4 z = sbz[j];
+      const float zs[4] = {z.x, z.y, z.z, z.w};
+#pragma unroll
+      for (int c = 0; c < 4; c++)
+#pragma unroll
+        for (int r = 0; r < 3; r++) acc[lz + c][r] = fmaf(zs[c], q[r], acc[lz + c][r]);
+    }
+  }
+}
+
+// flush of one row: half 1's sums join half 0's, which adds them into the
+// warp's slab (x slot sa, y node ly + sb, z nodes 0..6 of the row)
+template <int WY, int WZ, int NF>
+__device__ __forceinline__ void vel_row_flush(float (&acc)[7][3], float *slab, int hw, int sa, int sb, int ly) {
+#pragma unroll
+  for (int m = 0; m < 7; m++)
+#pragma unroll
+    for (int r = 0; r < 3; r++) acc[m][r] += __shfl_xor_sync(0xffffffffu, acc[m][r], 16);
+  if (hw == 0) {
+#pragma unroll
+    for (int m = 0; m < 7; m++) {
+      const int fi = (sa * WY + ly + sb) * WZ + m;
+#pragma unroll
+      for (int r = 0; r < 3; r++) slab[r * NF + fi] += acc[m][r];
+    }
+  }
+}
+
+// The velocity scatter (P2G_VEL) of the plain 3-D four-wide modes: the tiles,
+// warps, rows and slab footprints of k_p2g_row, the sums of vel_row_accumulate.
+template <int BASIS>
+__global__ void __launch_bounds__(256, 4) k_p2g_vel_row(P2GArgs a) {
+  static_assert(Stencil<BASIS>::S == 4 && Stencil<BASIS>::SC == 1, "four-wide stencils");
+  using TS = TileShape<3, BASIS>;
+  constexpr int S = 4, LO = Stencil<BASIS>::LO;
+  constexpr int TX = TS::TX, TY = TS::TY, TZ = TS::TZ;
+  constexpr int WY = TS::WY, WZ = TS::WZ, NW = TS::NW, NF = TS::NF, FX = TS::FX;
+  static_assert(TS::L == 1 && TZ == 4 && FX == 4, "one x-layer of 4 x 4 cells per warp");
+  constexpr int Q = 3;
+  constexpr int SLAB = (Q * NF + 3) & ~3;
+
+  extern __shared__ __align__(16) float smem[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  float *slab = smem + warp * SLAB;
+  float *spay = smem + TS::NWARP * SLAB + warp * VEL_STAGE;  // [32][4]
+  float *sbxy = spay + 32 * 4;                               // [axis x, y][slot][VROW]
+  float4 *sbz = reinterpret_cast<float4 *>(sbxy + 2 * 4 * VROW);
+
+  const int2 td = a.tiles[blockIdx.x];
+  const GridDev g = a.grids[td.x];
+  const int tlin = td.y;
+  const int tile_global = g.tile_off + tlin;
+  if (a.tile_end[tile_global] == a.tile_start[tile_global] || run_finished(a.scalars)) return;
+  const int tc2 = tlin % g.ntile[2], tc1 = (tlin / g.ntile[2]) % g.ntile[1], tc0 = tlin / (g.ntile[1] * g.ntile[2]);
+  const float h = g.cellsize, ih = g.inv_cellsize;
+  const float *P = *a.Pp;
+  const size_t ps = a.ps;
+  const bool use_u = a.pos_field == PF_X;
+  {  // the tile's particle rows that the stage phase reads, into L2
+    const int t0 = a.tile_start[tile_global], t1 = a.tile_end[tile_global];
+    prefetch_rows_l2(P, ps, PF_X0, use_u ? 6 : 3, t0, t1);
+    prefetch_rows_l2(P, ps, PF_V, 4, t0, t1);  // v, mass
+  }
+
+  for (int k = lane; k < Q * NF; k += 32) slab[k] = 0.f;
+
+  const int hw = lane >> 4, sa = (lane >> 2) & 3, sb = lane & 3;
+  const float *px = sbxy + sa * VROW, *py = sbxy + (4 + sb) * VROW;
+  const int i0x = (tc0 * TX + warp) - LO;
+
+  for (int ly = 0; ly < TY; ly++) {
+    const int cbase = tile_global * TS::NCELL + (warp * TY + ly) * TZ;
+    const int cv = lane < 8 ? (lane < 4 ? a.cell_start[cbase + lane] : a.cell_end[cbase + lane - 4]) : 0;
+    int st[4], en[4], lo4[4];
+    int rs = INT_MAX, re = INT_MIN;
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      st[k] = __shfl_sync(0xffffffffu, cv, k);
+      en[k] = __shfl_sync(0xffffffffu, cv, 4 + k);
+      const bool full = en[k] > st[k];
+      lo4[k] = full ? st[k] : INT_MAX;
+      rs = full ? min(rs, st[k]) : rs;
+      re = full ? max(re, en[k]) : re;
+    }
+    if (rs == INT_MAX) continue;
+    const int i0y = (tc1 * TY + ly) - LO;
+    float acc[7][Q];
+#pragma unroll
+    for (int m = 0; m < 7; m++)
+#pragma unroll
+      for (int qq = 0; qq < Q; qq++) acc[m][qq] = 0.f;
+
+    for (int c0 = rs; c0 < re; c0 += 32) {
+      const int cnt = min(32, re - c0);
+      // ---- stage (lane = particle): m v and the weights
+      if (lane < cnt) {
+        const int p = c0 + lane;
+        int lz = 0;
+#pragma unroll
+        for (int k = 1; k < 4; k++) lz = lo4[k] <= p ? k : lz;
+        float pay[3];
+        p2g_payload<P2G_VEL, false>(a, P, p, pay);
+        reinterpret_cast<float4 *>(spay)[lane] = make_float4(pay[0], pay[1], pay[2], 0.f);
+        const int i0[3] = {i0x, i0y, (tc2 * TZ + lz) - LO};
+        float sv[3][S];
+#pragma unroll
+        for (int d = 0; d < 3; d++) {
+          const float xp = P[(PF_X0 + d) * ps + p] + (use_u ? P[(PF_X + d) * ps + p] : 0.f);
+          const float lod = d == 0 ? g.lo[0] : (d == 1 ? g.lo[1] : g.lo[2]);
+          const int nd = d == 0 ? g.n[0] : (d == 1 ? g.n[1] : g.n[2]);
+          const int ngd = d == 0 ? g.ng[0] : (d == 1 ? g.ng[1] : g.ng[2]);
+          float dsv[S];
+          if (BASIS == 1 && cubic_interior(i0[d], nd, ngd)) {
+            cubic_weights(cells_of(xp, lod, ih) - (float)(i0[d] + 1), ih, sv[d], dsv);
+          } else {
+#pragma unroll
+            for (int kk = 0; kk < S; kk++) {
+              const int i = i0[d] + kk;
+              sv[d][kk] = 0.f;
+              dsv[kk] = 0.f;
+              if (i >= 0 && i < nd) {
+                const float r = node_offset_cells(xp, lod, i, h, ih);
+                basis<BASIS>(r, node_type<BASIS>(i, ngd), ih, sv[d][kk], dsv[kk]);
+              }
+            }
+          }
+        }
+        vel_row_stage_basis(sbxy, sbz, lane, sv);
+      }
+      __syncwarp();
+      vel_row_accumulate(acc, spay, px, py, sbz, st, en, c0, cnt, hw);
+      __syncwarp();
+    }
+    vel_row_flush<WY, WZ, NF>(acc, slab, hw, sa, sb, ly);
+    __syncwarp();
+  }
+  __syncthreads();
+  // ---- sum the slabs in warp order into the tile footprint
+  float *out = a.partial + (size_t)tile_global * a.pstride_tile;
+  for (int k = threadIdx.x; k < Q * NW; k += blockDim.x) {
+    const int qq = k / NW, fi = k % NW;
+    const int fx = fi / (WY * WZ), fyz = fi % (WY * WZ);
+    float sum = 0.f;
+#pragma unroll
+    for (int w = 0; w < TS::NWARP; w++) {
+      const int x = fx - w;
+      if (x >= 0 && x < FX) sum += smem[w * SLAB + qq * NF + x * WY * WZ + fyz];
+    }
+    out[k] = sum;
+  }
+}
+
 // ============================================================== 2-D P2G by cell rows
 // The scatter of the 2-D four-wide stencils (cubic and quadratic B-splines)
 // for the plain modes, on the tiles, warps and slab footprints of k_p2g (a
@@ -1443,15 +1628,15 @@ __global__ void __launch_bounds__(256, 4) k_g2p1_remap_row(P2GArgs a) {
   static_assert(TS::L == 1 && TZ == 4 && FX == 4, "one x-layer of 4 x 4 cells per warp");
   constexpr int Q = 3;                       // m v
   constexpr int SLAB = (Q * NF + 3) & ~3;
-  constexpr int SROW = 33;                   // basis rows of one float per staged particle, padded
-  constexpr int STAGE = 32 * 4 + SROW * 3 * S;
+  constexpr int STAGE = VEL_STAGE;
   constexpr int NWP = (NW + 1) & ~1;
 
   extern __shared__ __align__(16) float smem[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   float *slab = smem + warp * SLAB;
   float *spay = smem + TS::NWARP * SLAB + warp * STAGE;  // [32][4]
-  float *sbas = spay + 32 * 4;                           // [axis][slot][SROW]
+  float *sbxy = spay + 32 * 4;                           // [axis x, y][slot][VROW]
+  float4 *sbz = reinterpret_cast<float4 *>(sbxy + 2 * 4 * VROW);
   float4 *fpA = reinterpret_cast<float4 *>(smem + TS::NWARP * (SLAB + STAGE));
   float2 *fpB = reinterpret_cast<float2 *>(fpA + NWP);
 
@@ -1487,9 +1672,8 @@ __global__ void __launch_bounds__(256, 4) k_g2p1_remap_row(P2GArgs a) {
   }
   __syncthreads();
 
-  const int sa = lane >> 3, sb = (lane >> 1) & 3, sc_ = lane & 1;
-  const float *px = sbas + (0 * S + sa) * SROW, *py = sbas + (1 * S + sb) * SROW;
-  const float *pz0 = sbas + (2 * S + sc_) * SROW, *pz2 = sbas + (2 * S + sc_ + 2) * SROW;
+  const int hw = lane >> 4, sa = (lane >> 2) & 3, sb = lane & 3;
+  const float *px = sbxy + sa * VROW, *py = sbxy + (4 + sb) * VROW;
   const int i0x = (tc0 * TX + warp) - LO;
 
   for (int ly = 0; ly < TY; ly++) {
@@ -1508,9 +1692,9 @@ __global__ void __launch_bounds__(256, 4) k_g2p1_remap_row(P2GArgs a) {
     }
     if (rs == INT_MAX) continue;
     const int i0y = (tc1 * TY + ly) - LO;
-    float acc[6][Q];
+    float acc[7][Q];
 #pragma unroll
-    for (int m = 0; m < 6; m++)
+    for (int m = 0; m < 7; m++)
 #pragma unroll
       for (int qq = 0; qq < Q; qq++) acc[m][qq] = 0.f;
 
@@ -1546,9 +1730,8 @@ __global__ void __launch_bounds__(256, 4) k_g2p1_remap_row(P2GArgs a) {
               }
             }
           }
-#pragma unroll
-          for (int kk = 0; kk < S; kk++) sbas[(d * S + kk) * SROW + lane] = sv[d][kk];
         }
+        vel_row_stage_basis(sbxy, sbz, lane, sv);
         // the gather of k_g2p1 from the footprint: stencil node (i, j, k) is
         // footprint node (warp + i, ly + j, lz + k)
         // in packed pairs (v_x, v_y), (v_z, vu_x), (vu_y, vu_z): the footprint's
@@ -1598,42 +1781,11 @@ __global__ void __launch_bounds__(256, 4) k_g2p1_remap_row(P2GArgs a) {
           raise_error(a.err, ERR_LEFT, p, sc.ntimestep);
       }
       __syncwarp();
-      // ---- accumulate (lane = node): cell after cell, particles in sorted order
-#pragma unroll
-      for (int lz = 0; lz < 4; lz++) {
-        const int jlo = max(st[lz] - c0, 0), jhi = min(en[lz] - c0, cnt);
-        for (int j = jlo; j < jhi; j++) {
-          const float4 t4 = reinterpret_cast<const float4 *>(spay)[j];
-          const float wxy = px[j] * py[j];
-          const float q0 = wxy * t4.x, q1 = wxy * t4.y, q2 = wxy * t4.z;
-          const float z0 = pz0[j], z2 = pz2[j];
-          acc[lz][0] = fmaf(z0, q0, acc[lz][0]);
-          acc[lz][1] = fmaf(z0, q1, acc[lz][1]);
-          acc[lz][2] = fmaf(z0, q2, acc[lz][2]);
-          acc[lz + 2][0] = fmaf(z2, q0, acc[lz + 2][0]);
-          acc[lz + 2][1] = fmaf(z2, q1, acc[lz + 2][1]);
-          acc[lz + 2][2] = fmaf(z2, q2, acc[lz + 2][2]);
-        }
-      }
+      // ---- accumulate (half-warp = particle, lane = (x, y) slot pair)
+      vel_row_accumulate(acc, spay, px, py, sbz, st, en, c0, cnt, hw);
       __syncwarp();
     }
-    // ---- flush (as k_p2g_row)
-#pragma unroll
-    for (int m = 0; m < 5; m++)
-#pragma unroll
-      for (int qq = 0; qq < Q; qq++) {
-        const float o = __shfl_xor_sync(0xffffffffu, acc[m][qq], 1);
-        if (sc_ == 0) acc[m + 1][qq] += o;
-      }
-    const int fy = ly + sb;
-#pragma unroll
-    for (int m = 0; m < 6; m++) {
-      if (sc_ == 1 && m < 5) continue;
-      const int fz = m + sc_;
-      const int fi = (sa * WY + fy) * WZ + fz;
-#pragma unroll
-      for (int qq = 0; qq < Q; qq++) slab[qq * NF + fi] += acc[m][qq];
-    }
+    vel_row_flush<WY, WZ, NF>(acc, slab, hw, sa, sb, ly);
     __syncwarp();
   }
   __syncthreads();
@@ -1654,7 +1806,7 @@ __global__ void __launch_bounds__(256, 4) k_g2p1_remap_row(P2GArgs a) {
 // dynamic shared memory of k_g2p1_remap_row (bytes)
 template <int BASIS> constexpr int g2p1_remap_smem() {
   using TS = TileShape<3, BASIS>;
-  return 4 * (TS::NWARP * (((3 * TS::NF + 3) & ~3) + 32 * 4 + 33 * 3 * 4) + 6 * ((TS::NW + 1) & ~1));
+  return 4 * (TS::NWARP * (((3 * TS::NF + 3) & ~3) + VEL_STAGE) + 6 * ((TS::NW + 1) & ~1));
 }
 
 // Node sources of the velocity-gradient gather: (v, T) of stencil node
@@ -2152,7 +2304,7 @@ void fill_step_kernels(StepKernels &k) {
     k.grid_store_p = (void *)k_grid<DIM, BASIS, GM_STORE_P, true, false, float>;
     k.p2g_row[0] = (void *)k_p2g_row<BASIS, P2G_TL>;
     k.p2g_row[1] = (void *)k_p2g_row<BASIS, P2G_UL>;
-    k.p2g_row[2] = (void *)k_p2g_row<BASIS, P2G_VEL>;
+    k.p2g_row[2] = (void *)k_p2g_vel_row<BASIS>;
     k.g2p1_remap[0] = (void *)k_g2p1_remap_row<BASIS, false>;
     k.g2p1_remap[1] = (void *)k_g2p1_remap_row<BASIS, true>;
     k.g2p1_remap_smem = g2p1_remap_smem<BASIS>();
