@@ -765,6 +765,13 @@ int build(kmpm_ctx *c) {
         for (int t = 0; t < nt; t++)
           if (te[g.tile_off + t] > ts[g.tile_off + t]) tiles.push_back(make_int2(r.grid, t));
       }
+      // launch order: the fullest tiles first, so that the partly filled
+      // tiles at the solids' surfaces fill the last wave of blocks (each tile
+      // writes its own slice: the order changes no result).  The sort is
+      // stable, so tiles of equal count, the full ones among them, keep their
+      // grid order and their shared halo nodes stay in L2 between neighbours
+      auto count = [&](int2 t) { const int tg = c->grids[t.x].tile_off + t.y; return te[tg] - ts[tg]; };
+      std::stable_sort(tiles.begin(), tiles.end(), [&](int2 a, int2 b) { return count(a) > count(b); });
     }
     c->ntiles_launch = (int)tiles.size();
     DALLOC(c->d_tiles, tiles.size());
