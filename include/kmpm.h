@@ -37,7 +37,7 @@ extern "C" {
 #define KMPM_ERR_NAN (-12)         /* nan wave speed / dtCFL, src/solid.cpp:1387-1397, src/tlmpm.cpp:498-508 */
 #define KMPM_ERR_POLDEC (-13)      /* polar decomposition failed, src/solid.cpp:1229-1236 */
 #define KMPM_ERR_DTCFL (-14)       /* dtCFL == 0, src/tlmpm.cpp:498-502 */
-#define KMPM_ERR_TIMEOUT (-15)     /* a bounded wait inside a tensor-core kernel ran out */
+#define KMPM_ERR_TIMEOUT (-15)     /* a bounded wait inside a kernel ran out (tensor-core network, staged state rows) */
 
 /* method / scheme / basis (Update::create_method, src/update.cpp:108-196) */
 #define KMPM_TLMPM 0

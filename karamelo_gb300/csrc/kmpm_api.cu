@@ -979,6 +979,15 @@ bool sur_queued(const kmpm_ctx *c) {
   return !(ev && ev[0] == '1');
 }
 
+// dynamic shared memory of a stress kernel: the linear EOS + Johnson-Cook
+// variants also stage their particles' state rows (G2P2_JC_SMEM)
+int g2p2_smem(const kmpm_ctx *c, const void *fn) {
+  for (int t = 0; t < 2; t++)
+    for (int v = 0; v < G2P_NVAR; v++)
+      if (fn && fn == c->K.g2p2_jc[t][v]) return G2P2_JC_SMEM;
+  return G2P2_SMEM;
+}
+
 void *g2p2_variant(const kmpm_ctx *c, int v) {
   const bool TL = c->TL();
   if (c->law_jc && !c->apic() && c->K.g2p2_jc[TL][v]) return c->K.g2p2_jc[TL][v];
@@ -1102,7 +1111,8 @@ int enqueue_step(kmpm_ctx *c, bool reuse = false) {
     // forces of the new stress, the grid update and the particle update
     PartArgs ps = pa;
     ps.use_vu = 0;
-    LAUNCH((th || prec) ? c->K.g2p2[TL][th][prec] : g2p2_variant(c, c->var_g2p2), c->nblk_p, 256, G2P2_SMEM, ps);
+    void *fs = (th || prec) ? c->K.g2p2[TL][th][prec] : g2p2_variant(c, c->var_g2p2);
+    LAUNCH(fs, c->nblk_p, 256, g2p2_smem(c, fs), ps);
     MARK("g2p_stress");
     LAUNCH(c->sc_usf, c->ntiles_launch, 256, c->smem_usf, p);
     MARK("p2g_forces");
@@ -1154,7 +1164,8 @@ int enqueue_step(kmpm_ctx *c, bool reuse = false) {
   }
   // compute_rate_deformation_gradient + update_deformation_gradient + update_stress
   if (c->learn_mode == MODE_PLAIN) {
-    LAUNCH((th || prec) ? c->K.g2p2[TL][th][prec] : g2p2_variant(c, c->var_g2p2), c->nblk_p, 256, G2P2_SMEM, pa);
+    void *fs = (th || prec) ? c->K.g2p2[TL][th][prec] : g2p2_variant(c, c->var_g2p2);
+    LAUNCH(fs, c->nblk_p, 256, g2p2_smem(c, fs), pa);
   } else {
     LearnArgs la{};
     la.blob = c->d_blob;
@@ -1301,7 +1312,7 @@ int autotune(kmpm_ctx *c) {
       for (int v = 0; v < G2P_NVAR; v++) {
         void *fn = k == 0 ? c->K.g2p1_v[TL][v] : g2p2_variant(c, v);
         CK(cudaEventRecord(e0, c->st));
-        int r = launch(c, fn, dim3(c->nblk_p), dim3(256), k == 0 ? G2P1_SMEM : G2P2_SMEM, &pa);
+        int r = launch(c, fn, dim3(c->nblk_p), dim3(256), k == 0 ? G2P1_SMEM : g2p2_smem(c, fn), &pa);
         if (r != KMPM_OK) return r;
         CK(cudaEventRecord(e1, c->st));
         CK(cudaEventSynchronize(e1));

@@ -193,6 +193,10 @@ constexpr int G2P_NVAR = 3;
 constexpr int G2P_STAGE_NODES = 1024;
 constexpr int G2P1_SMEM = G2P_STAGE_NODES * 32;
 constexpr int G2P2_SMEM = G2P_STAGE_NODES * 16;
+// the linear EOS + Johnson-Cook stress kernels also stage their particles'
+// state rows v .. damage (PF_V .. PF_DMG), 256 floats each
+constexpr int G2P2_STATE_ROWS = 23;
+constexpr int G2P2_JC_SMEM = G2P2_SMEM + G2P2_STATE_ROWS * 256 * 4;
 constexpr int G2P1_MINB[G2P_NVAR] = {4, 3, 6};
 constexpr int G2P2_MINB[G2P_NVAR] = {3, 2, 4};
 

@@ -11,6 +11,7 @@
 //              (src/solid.cpp:798-936, 1155-1438)
 //   k_dt_*     adjust_dt / update_time (src/tlmpm.cpp:489-514, src/update.cpp:201-206)
 #pragma once
+#include "kmpm_async.cuh"
 #include "kmpm_kernels.cuh"
 
 namespace kmpm {
@@ -1906,7 +1907,10 @@ __device__ __forceinline__ void grad_gather(const PAxes<DIM, BASIS> &ax, const F
 template <int DIM, int BASIS, bool TL, bool THERMAL, int PREC, int MINB = 3, int LAW = LAW_ANY, bool QUEUE = false>
 __global__ void __launch_bounds__(256, MINB) k_g2p2(PartArgs a) {
   __shared__ float red_c[8], red_h[8];
-  extern __shared__ __align__(16) float4 g2p_stage[];  // G2P_STAGE_NODES (v, T) of the staged box
+  __shared__ __align__(8) unsigned long long state_bar;
+  // G2P_STAGE_NODES (v, T) of the staged box; then, for the linear EOS +
+  // Johnson-Cook kernels, the state rows (G2P2_STATE_ROWS x 256 floats)
+  extern __shared__ __align__(16) float4 g2p_stage[];
   if (run_finished(a.scalars)) return;
   RangeDev rd;
   const int p0 = range_particle(a, rd);
@@ -1915,6 +1919,38 @@ __global__ void __launch_bounds__(256, MINB) k_g2p2(PartArgs a) {
   float my_c = 0.f, my_h = 1.f;
   float *P = *a.Pp;
   const size_t ps = a.ps;
+  // Linear EOS + Johnson-Cook (FP32): the block's 256-slot slices of the
+  // state rows v .. damage (PF_V .. PF_DMG: 23 rows, contiguous in the field
+  // order, each slice 1 KB at a 1 KB boundary, as the field stride and the
+  // blocks are multiples of 256 slots) come into shared memory by bulk copies
+  // (cp.async.bulk) on one mbarrier.  One thread issues them before the node
+  // staging and the gather, which then hide their latency; each thread waits
+  // (bounded) before its first state read.  A wait that runs out raises
+  // ERR_TIMEOUT (the step fails) and waits once more, bounded, so that the
+  // block does not end with copies in flight.
+  constexpr bool TMA_STATE = LAW == LAW_EOS_LINEAR_JC && PREC == 0 && !QUEUE;
+  static_assert(PF_DMG + 1 - PF_V == G2P2_STATE_ROWS, "state rows");
+  float *sstate = reinterpret_cast<float *>(g2p_stage + G2P_STAGE_NODES);  // [row - PF_V][256]
+  const uint32_t sbar = smem_u32(&state_bar);
+  bool waited = false;  // this thread saw the copies complete
+  if (TMA_STATE) {
+    if (threadIdx.x == 0) {
+      mbar_init(sbar, 1);
+      mbar_fence_init();
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      const int blk0 = rd.start + (blockIdx.x - rd.blk0) * 256;
+      mbar_expect_tx(sbar, G2P2_STATE_ROWS * 1024);
+      for (int r = 0; r < G2P2_STATE_ROWS; r++)
+        bulk_g2s(smem_u32(sstate + r * 256), P + (size_t)(PF_V + r) * ps + blk0, 1024, sbar);
+    }
+  }
+  // a state value of this thread's particle: from the staged rows or global memory
+  const auto st_ld = [&](int row) -> float {
+    if (TMA_STATE && row >= PF_V && row <= PF_DMG) return sstate[(row - PF_V) * 256 + threadIdx.x];
+    return P[(size_t)row * ps + p];
+  };
   // the linear EOS + Johnson-Cook kernels serve FLIP/PIC runs only (APIC runs
   // take the general ones): no affine moments, no per-slot offsets kept
   const bool apic = LAW == LAW_EOS_LINEAR_JC ? false : a.apic != 0;
@@ -1950,7 +1986,7 @@ __global__ void __launch_bounds__(256, MINB) k_g2p2(PartArgs a) {
     // the state rows the EOS + strength update reads after the node gather
     // (material type 2): start their DRAM reads now, into L2, so that they
     // overlap the gather (a hint: no registers held)
-    if (LAW == LAW_EOS_LINEAR_JC || (PREC == 0 && m.type == 2)) {
+    if (!TMA_STATE && (LAW == LAW_EOS_LINEAR_JC || (PREC == 0 && m.type == 2))) {
       const int rows[] = {PF_H, PF_H + 1, PF_H + 2, PF_H + 3, PF_H + 4, PF_H + 5, PF_H + 6, PF_H + 7, PF_H + 8,
                           PF_SIG, PF_SIG + 1, PF_SIG + 2, PF_SIG + 3, PF_SIG + 4, PF_SIG + 5,
                           PF_EPSP, PF_EPSDOT, PF_DMG, PF_VOL0, PF_V, PF_V + 1, PF_V + 2};
@@ -2017,10 +2053,17 @@ __global__ void __launch_bounds__(256, MINB) k_g2p2(PartArgs a) {
     if ((BASIS == 0 || BASIS == 1 || BASIS == 3) && apic)
 #pragma unroll
       for (int k = 0; k < 9; k++) P[(PF_C + k) * ps + p] = G[k];  // C of the next transfers
+    if (TMA_STATE) {
+      waited = mbar_wait(sbar, 0);
+      if (!waited) {
+        raise_error(a.err, ERR_TIMEOUT, p, sc.ntimestep);
+        waited = mbar_wait(sbar, 0);
+      }
+    }
     // ---- deformation gradient (src/solid.cpp:1155-1244), stored as H = F - I
     float H[9];
 #pragma unroll
-    for (int k = 0; k < 9; k++) H[k] = P[(PF_H + k) * ps + p];
+    for (int k = 0; k < 9; k++) H[k] = st_ld(PF_H + k);
     if (TL) {
 #pragma unroll
       for (int k = 0; k < 9; k++) H[k] += dt * G[k];  // F += dt Fdot
@@ -2053,9 +2096,9 @@ __global__ void __launch_bounds__(256, MINB) k_g2p2(PartArgs a) {
       J = 1.f + Jm1;
       cof3(F, cofF);
     }
-    float dmg = P[PF_DMG * ps + p];
+    float dmg = st_ld(PF_DMG);
     if (J <= 0.f && dmg < 1.f) raise_error(a.err, ERR_J, p, sc.ntimestep);
-    const float vol0 = P[PF_VOL0 * ps + p];
+    const float vol0 = st_ld(PF_VOL0);
     const float rho = m.f_rho0 / J;
     float R[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
     Sym<float> D;
@@ -2090,7 +2133,7 @@ __global__ void __launch_bounds__(256, MINB) k_g2p2(PartArgs a) {
     // ---- stress (src/solid.cpp:1246-1374)
     Sym<float> sig;
 #pragma unroll
-    for (int k = 0; k < 6; k++) sig.a[k] = P[(PF_SIG + k) * ps + p];
+    for (int k = 0; k < 6; k++) sig.a[k] = st_ld(PF_SIG + k);
     float PK1[9];
     bool have_pk1 = false;
     if (LAW == LAW_ANY && m.type == 0) {  // LINEAR
@@ -2132,7 +2175,7 @@ __global__ void __launch_bounds__(256, MINB) k_g2p2(PartArgs a) {
     } else {  // EOS + strength (+ damage + temperature)
       const bool hasT = LAW == LAW_ANY && m.f_cp != 0.f;
       float T = hasT ? a.T_ref + P[PF_T * ps + p] : 0.f;  // PF_T holds T - T_ref
-      float epsp = P[PF_EPSP * ps + p], epsdot = P[PF_EPSDOT * ps + p];
+      float epsp = st_ld(PF_EPSP), epsdot = st_ld(PF_EPSDOT);
       float dinit = m.damage >= 0 ? P[PF_DMGI * ps + p] : 0.f;
       float pH, dep;
       Sym<float> sdev;
@@ -2254,7 +2297,7 @@ __global__ void __launch_bounds__(256, MINB) k_g2p2(PartArgs a) {
     }
     // ---- wave speed and h ratio (src/solid.cpp:1376-1437)
     if (dmg < 1.f) {
-      const float vx = P[PF_V * ps + p], vy = P[(PF_V + 1) * ps + p], vz = P[(PF_V + 2) * ps + p];
+      const float vx = st_ld(PF_V), vy = st_ld(PF_V + 1), vz = st_ld(PF_V + 2);
       const float c = sqrtf(m.f_c2 / rho) + fmaxf(fmaxf(fabsf(vx), fabsf(vy)), fabsf(vz));
       if (isnan(c)) raise_error(a.err, ERR_NAN, p, sc.ntimestep);
       my_c = c;
@@ -2282,6 +2325,13 @@ __global__ void __launch_bounds__(256, MINB) k_g2p2(PartArgs a) {
     }
     a.blk_c[blockIdx.x] = c;
     a.blk_h[blockIdx.x] = hh;
+    // every thread with a particle has passed its wait (the barrier above);
+    // unless thread 0 saw the copies complete (a block of an empty range has
+    // no particle), it waits for them (bounded) before the block ends
+    if (TMA_STATE) {
+      if (!waited) mbar_wait(sbar, 0);
+      mbar_inval(sbar);
+    }
   }
 }
 
