@@ -1017,7 +1017,8 @@ int select_scatters(kmpm_ctx *c) {
     c->reuse_ok = c->fonly && !(ev && ev[0] == '1');
     c->p_valid = false;
     if (c->fonly) {
-      c->smem_fonly = c->K.p2g_row_fonly_smem;
+      c->smem_fonly = c->K.p2g_row_fonly_smem > 0 ? c->K.p2g_row_fonly_smem
+                                                  : p2g_smem_bytes(c->prm.dim, c->prm.basis, P2G_TL | P2G_FONLY, false);
       CK(cudaFuncSetAttribute(c->K.p2g_row_fonly, cudaFuncAttributeMaxDynamicSharedMemorySize, c->smem_fonly));
     }
   }

@@ -160,11 +160,12 @@ struct StepKernels {
   // the row scatters (k_p2g_row, k_p2g_row2) of the plain TL, UL and
   // velocity modes: 2-D and 3-D cubic and quadratic splines (nullptr elsewhere)
   void *p2g_row[3];
-  // the 3-D scatter of the force sums only (k_p2g_force_row, P2G_TL |
-  // P2G_FONLY) and its dynamic shared memory, the grid update that takes the
-  // stored momentum (GM_UPDATE_F) and the pass that stores the momentum of a
-  // velocity scatter (GM_STORE_P): TLMPM, FP32, mechanical, cubic and
-  // quadratic splines (nullptr elsewhere)
+  // the scatter of the force sums only (P2G_TL | P2G_FONLY: k_p2g_force_row
+  // in 3-D, k_p2g_row2 in 2-D) and its dynamic shared memory (0: that of
+  // p2g_smem_bytes), the grid update that takes the stored momentum
+  // (GM_UPDATE_F) and the pass that stores the momentum of a velocity
+  // scatter (GM_STORE_P): TLMPM, FP32, mechanical, cubic and quadratic
+  // splines (nullptr elsewhere)
   void *p2g_row_fonly, *grid_upd_fonly, *grid_store_p;
   int p2g_row_fonly_smem;
   void *p2g_tl_apic, *p2g_ul_apic, *p2g_vel_apic;  // cubic spline only (nullptr otherwise)

@@ -1020,7 +1020,7 @@ __global__ void __launch_bounds__(256, 4) k_p2g_vel_row(P2GArgs a) {
 //     the row into the warp's slab.
 // Every sum runs in a fixed order: the result is bit-reproducible.
 template <int BASIS, int MODE>
-__global__ void __launch_bounds__(256, (MODE == P2G_VEL ? 4 : 3)) k_p2g_row2(P2GArgs a) {
+__global__ void __launch_bounds__(256, (MODE == P2G_VEL || p2g_fonly(MODE) ? 4 : 3)) k_p2g_row2(P2GArgs a) {
   static_assert(Stencil<BASIS>::S == 4 && Stencil<BASIS>::SC == 1, "four-wide stencils");
   using TS = TileShape<2, BASIS>;
   constexpr int S = 4, LO = Stencil<BASIS>::LO;
@@ -1035,6 +1035,10 @@ __global__ void __launch_bounds__(256, (MODE == P2G_VEL ? 4 : 3)) k_p2g_row2(P2G
   constexpr int STAGE = 32 * QINP + SROW * 2 * S * 2;
   constexpr int OM = MODE == P2G_UL ? 1 : 0;  // UL sums start with the mass
   constexpr bool FORCE = MODE != P2G_VEL;
+  // P2G_TL | P2G_FONLY (TLMPM MUSL momentum reuse): the force sums only, at
+  // quantities 0..2, in the arithmetic and order of the P2G_TL force sums;
+  // payload vol0 PK1
+  constexpr bool FO = p2g_fonly(MODE);
 
   extern __shared__ __align__(16) float smem[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -1141,20 +1145,25 @@ __global__ void __launch_bounds__(256, (MODE == P2G_VEL ? 4 : 3)) k_p2g_row2(P2G
             }
             const float2 bx = px[j], b0 = py0[j], b2 = py2[j];
             // momentum (and UL mass): w = sx sy; force: -(T[r][0] dsx sy + T[r][1] sx dsy)
-            float q[3 + OM];
+            if (!FO) {
+              float q[3 + OM];
 #pragma unroll
-            for (int d = 0; d < 3 + OM; d++) q[d] = bx.x * pay[d];
+              for (int d = 0; d < 3 + OM; d++) q[d] = bx.x * pay[d];
 #pragma unroll
-            for (int d = 0; d < 3 + OM; d++) {
-              if (d == OM + 2) continue;  // v_z = 0 in 2-D: the sum stays 0
-              acc[ly][d] = fmaf(b0.x, q[d], acc[ly][d]);
-              acc[ly + 2][d] = fmaf(b2.x, q[d], acc[ly + 2][d]);
+              for (int d = 0; d < 3 + OM; d++) {
+                if (d == OM + 2) continue;  // v_z = 0 in 2-D: the sum stays 0
+                acc[ly][d] = fmaf(b0.x, q[d], acc[ly][d]);
+                acc[ly + 2][d] = fmaf(b2.x, q[d], acc[ly + 2][d]);
+              }
             }
             if (FORCE) {
+              constexpr int F0 = FO ? 0 : 3 + OM;  // the force sums' first quantity
 #pragma unroll
               for (int r = 0; r < 2; r++) {
                 float T0, T1;
-                if (MODE == P2G_TL) {  // vol0 PK1, row-major
+                if (FO) {  // vol0 PK1, row-major, alone in the payload
+                  T0 = pay[3 * r]; T1 = pay[1 + 3 * r];
+                } else if (MODE == P2G_TL) {  // vol0 PK1, row-major
                   T0 = pay[3 + 3 * r]; T1 = pay[4 + 3 * r];
                 } else {  // vol sigma, symmetric xx yy zz xy xz yz
                   const float *sg = pay + 4;
@@ -1162,8 +1171,8 @@ __global__ void __launch_bounds__(256, (MODE == P2G_VEL ? 4 : 3)) k_p2g_row2(P2G
                   T1 = r == 0 ? sg[3] : sg[1];
                 }
                 const float tx = T0 * bx.y, ty = T1 * bx.x;
-                acc[ly][3 + OM + r] = fmaf(-b0.x, tx, fmaf(-b0.y, ty, acc[ly][3 + OM + r]));
-                acc[ly + 2][3 + OM + r] = fmaf(-b2.x, tx, fmaf(-b2.y, ty, acc[ly + 2][3 + OM + r]));
+                acc[ly][F0 + r] = fmaf(-b0.x, tx, fmaf(-b0.y, ty, acc[ly][F0 + r]));
+                acc[ly + 2][F0 + r] = fmaf(-b2.x, tx, fmaf(-b2.y, ty, acc[ly + 2][F0 + r]));
               }
             }
           }
@@ -2359,6 +2368,10 @@ void fill_step_kernels(StepKernels &k) {
     k.g2p1_remap[1] = (void *)k_g2p1_remap_row<BASIS, true>;
     k.g2p1_remap_smem = g2p1_remap_smem<BASIS>();
   } else if constexpr (DIM == 2 && (BASIS == 1 || BASIS == 3)) {
+    k.p2g_row_fonly = (void *)k_p2g_row2<BASIS, P2G_TL | P2G_FONLY>;
+    k.p2g_row_fonly_smem = 0;  // p2g_smem_bytes of the mode
+    k.grid_upd_fonly = (void *)k_grid<DIM, BASIS, GM_UPDATE_F, true, false, float>;
+    k.grid_store_p = (void *)k_grid<DIM, BASIS, GM_STORE_P, true, false, float>;
     k.p2g_row[0] = (void *)k_p2g_row2<BASIS, P2G_TL>;
     k.p2g_row[1] = (void *)k_p2g_row2<BASIS, P2G_UL>;
     k.p2g_row[2] = (void *)k_p2g_row2<BASIS, P2G_VEL>;

@@ -9,7 +9,8 @@ re-map's momentum for the next grid update, and KMPM_NO_MOMENTUM_REUSE=1
 runs the velocity row scatter (the re-map's sums) before it every step.
 Both must give the same bits, including after an upload between steps
 (which must make the next step scatter the momentum of the new state) and
-across kmpm_run calls."""
+across kmpm_run calls: on the 3-D Taylor bar (cubic and quadratic splines)
+and on a 2-D tensile bar with Johnson-Cook damage (the 2-D row scatter)."""
 import os
 
 import numpy as np
@@ -22,13 +23,29 @@ pytestmark = pytest.mark.gpu
 FIELDS = ("x", "v", "sigma", "F", "eps_p")
 
 
-def _run(basis, reuse, upload):
+def _taylor(basis):
+    sim = W.taylor_bar(None, cellsize=0.8, basis=basis)
+    sim.run(1)
+    W.taylor_bar_wall(sim)
+    return sim
+
+
+def _tensile(basis):
+    sim = W.tensile_bar_2d(None, basis=basis, vend=5.0)
+    sim.run(1)
+    return sim
+
+
+CASES = {"taylor_cubic": (_taylor, "cubic-spline"), "taylor_quadratic": (_taylor, "quadratic-spline"),
+         "tensile_2d_cubic": (_tensile, "cubic-spline")}
+
+
+def _run(case, reuse, upload):
+    make, basis = CASES[case]
     if not reuse:
         os.environ["KMPM_NO_MOMENTUM_REUSE"] = "1"
     try:
-        sim = W.taylor_bar(None, cellsize=0.8, basis=basis)
-        sim.run(1)
-        W.taylor_bar_wall(sim)
+        sim = make(basis)
         sim.run(12)
         if upload:
             v = sim.particles(0, "v")
@@ -45,11 +62,11 @@ def _run(basis, reuse, upload):
     return phases, out
 
 
-@pytest.mark.parametrize("basis", ["cubic-spline", "quadratic-spline"])
+@pytest.mark.parametrize("case", list(CASES))
 @pytest.mark.parametrize("upload", [False, True], ids=["steps", "upload_between"])
-def test_momentum_reuse_bit_identical(gpu_lib, basis, upload):
-    ph_r, a = _run(basis, True, upload)
-    ph_f, b = _run(basis, False, upload)
+def test_momentum_reuse_bit_identical(gpu_lib, case, upload):
+    ph_r, a = _run(case, True, upload)
+    ph_f, b = _run(case, False, upload)
     # both run the force-only scatter; without the reuse a velocity scatter
     # forms the momentum first every step
     assert "p2g_force" in ph_r and "p2g_momentum" not in ph_r and "p2g" not in ph_r
@@ -61,6 +78,6 @@ def test_momentum_reuse_bit_identical(gpu_lib, basis, upload):
 def test_upload_changes_the_run(gpu_lib):
     """The upload case above is not vacuous: the scaled velocities change the
     state that the steps after it produce."""
-    _, a = _run("cubic-spline", True, False)
-    _, b = _run("cubic-spline", True, True)
+    _, a = _run("taylor_cubic", True, False)
+    _, b = _run("taylor_cubic", True, True)
     assert not np.array_equal(a["x"], b["x"])
