@@ -1942,18 +1942,16 @@ __global__ void __launch_bounds__(256, MINB) k_g2p2(PartArgs a) {
   float *sstate = reinterpret_cast<float *>(g2p_stage + G2P_STAGE_NODES);  // [row - PF_V][256]
   const uint32_t sbar = smem_u32(&state_bar);
   bool waited = false;  // this thread saw the copies complete
-  if (TMA_STATE) {
-    if (threadIdx.x == 0) {
-      mbar_init(sbar, 1);
-      mbar_fence_init();
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      const int blk0 = rd.start + (blockIdx.x - rd.blk0) * 256;
-      mbar_expect_tx(sbar, G2P2_STATE_ROWS * 1024);
-      for (int r = 0; r < G2P2_STATE_ROWS; r++)
-        bulk_g2s(smem_u32(sstate + r * 256), P + (size_t)(PF_V + r) * ps + blk0, 1024, sbar);
-    }
+  // (thread 0 initialises the mbarrier and issues the copies in program
+  // order; the other threads first touch it after the barrier of the node
+  // staging, stage_box, which orders them after the initialisation)
+  if (TMA_STATE && threadIdx.x == 0) {
+    mbar_init(sbar, 1);
+    mbar_fence_init();
+    const int blk0 = rd.start + (blockIdx.x - rd.blk0) * 256;
+    mbar_expect_tx(sbar, G2P2_STATE_ROWS * 1024);
+    for (int r = 0; r < G2P2_STATE_ROWS; r++)
+      bulk_g2s(smem_u32(sstate + r * 256), P + (size_t)(PF_V + r) * ps + blk0, 1024, sbar);
   }
   // a state value of this thread's particle: from the staged rows or global memory
   const auto st_ld = [&](int row) -> float {
