@@ -427,7 +427,7 @@ __device__ inline bool polar_rotation(const float *F, float *R) {
   for (int it = 0; it < 12; it++) {
     cof3(X, C);
     float dx = det3(X);
-    float g = fabsf(dx - 1.f) > 1e-3f ? cbrtf(1.f / fabsf(dx)) : 1.f;  // scaling (Higham 1986, sec. 3)
+    float g = fabsf(dx - 1.f) > 1e-3f ? rcbrtf(fabsf(dx)) : 1.f;  // scaling |det X|^(-1/3) (Higham 1986, sec. 3)
     float gi = 1.f / (g * dx);         // X^-T / g = C / (g det X)
     float diff = 0.f;
 #pragma unroll
@@ -452,21 +452,23 @@ __device__ inline float min_abs_eig_real(const float *H) {
   float a2 = H[0] + H[4] + H[8];
   float a1 = H[0] * H[4] - H[1] * H[3] + H[0] * H[8] - H[2] * H[6] + H[4] * H[8] - H[5] * H[7];
   float a0 = det3(H);
-  // mu^3 - a2 mu^2 + a1 mu - a0 = 0 ; mu = t + a2/3
-  float p = a1 - a2 * a2 / 3.f;
-  float q = -2.f * a2 * a2 * a2 / 27.f + a2 * a1 / 3.f - a0;
-  float sh = a2 / 3.f;
-  float disc = q * q / 4.f + p * p * p / 27.f;
+  // mu^3 - a2 mu^2 + a1 mu - a0 = 0 ; mu = t + a2/3 (thirds and 27ths as
+  // products with the rounded reciprocals)
+  constexpr float third = 1.f / 3.f, r27 = 1.f / 27.f;
+  float p = a1 - a2 * a2 * third;
+  float q = -2.f * a2 * a2 * a2 * r27 + a2 * a1 * third - a0;
+  float sh = a2 * third;
+  float disc = q * q * 0.25f + p * p * p * r27;
   float m;
   if (disc <= 0.f) {
-    float r = sqrtf(fmaxf(-p / 3.f, 0.f));
+    float r = sqrtf(fmaxf(-p * third, 0.f));
     float arg = r > 0.f ? (-q / 2.f) / (r * r * r) : 0.f;
     arg = fminf(1.f, fmaxf(-1.f, arg));
     float phi = acosf(arg);
     // cos(phi/3 + 2 pi k/3) for k = 0, 1, 2 from one sine and cosine:
     // cos(a + 2pi/3) = -c/2 - (sqrt 3/2) s, cos(a + 4pi/3) = -c/2 + (sqrt 3/2) s
     float sn, cs;
-    sincosf(phi / 3.f, &sn, &cs);
+    sincosf(phi * third, &sn, &cs);
     const float h3 = 0.866025403784439f * sn;
     float e0 = 1.f + sh + 2.f * r * cs;
     float e1 = 1.f + sh + 2.f * r * (-0.5f * cs - h3);

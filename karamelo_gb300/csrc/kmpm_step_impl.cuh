@@ -2117,8 +2117,9 @@ __global__ void __launch_bounds__(256, MINB) k_g2p2(PartArgs a) {
         if (!polar_rotation(F, R)) {
           if (dmg < 1.f) raise_error(a.err, ERR_POLDEC, p, sc.ntimestep);
         }
-        // L = Fdot F^-1 = Fdot cof(F)^T / J ; D = R^T sym(L) R
-        float L[9], RtL[9], Dm[9];
+        // L = Fdot F^-1 = Fdot cof(F)^T / J ; D = R^T sym(L) R, symmetric:
+        // its upper triangle (xx yy zz xy xz yz) from (R^T sym(L)) R
+        float L[9], RtL[9];
         matmulT3(G, cofF, L);
         const float iJ = 1.f / J;
 #pragma unroll
@@ -2129,9 +2130,10 @@ __global__ void __launch_bounds__(256, MINB) k_g2p2(PartArgs a) {
 #pragma unroll
           for (int c = 0; c < 3; c++) Ls[3 * r + c] = 0.5f * (L[3 * r + c] + L[3 * c + r]);
         matTmul3(R, Ls, RtL);
-        matmul3(RtL, R, Dm);
-        D.a[0] = Dm[0]; D.a[1] = Dm[4]; D.a[2] = Dm[8];
-        D.a[3] = 0.5f * (Dm[1] + Dm[3]); D.a[4] = 0.5f * (Dm[2] + Dm[6]); D.a[5] = 0.5f * (Dm[5] + Dm[7]);
+        const int di[6] = {0, 1, 2, 0, 0, 1}, dj[6] = {0, 1, 2, 1, 2, 2};
+#pragma unroll
+        for (int k = 0; k < 6; k++)
+          D.a[k] = RtL[3 * di[k]] * R[dj[k]] + RtL[3 * di[k] + 1] * R[3 + dj[k]] + RtL[3 * di[k] + 2] * R[6 + dj[k]];
       } else {
         D.a[0] = G[0]; D.a[1] = G[4]; D.a[2] = G[8];
         D.a[3] = 0.5f * (G[1] + G[3]); D.a[4] = 0.5f * (G[2] + G[6]); D.a[5] = 0.5f * (G[5] + G[7]);
@@ -2246,9 +2248,10 @@ __global__ void __launch_bounds__(256, MINB) k_g2p2(PartArgs a) {
         }
       }
       epsp += dep;
-      const float tav = 1000.f * g.cellsize / m.f_signal_velocity;
-      epsdot -= epsdot * dt / tav;
-      epsdot += dep / tav;
+      // relaxation of the plastic strain rate over tav = 1000 cellsize / c (one division)
+      const float itav = m.f_signal_velocity / (1000.f * g.cellsize);
+      epsdot -= epsdot * dt * itav;
+      epsdot += dep * itav;
       epsdot = fmaxf(0.f, epsdot);
       if (LAW == LAW_ANY && m.damage >= 0) {
         float Tdm = a.thermal ? a.T_ref + P[PF_T * ps + p] : 0.f;
@@ -2283,11 +2286,18 @@ __global__ void __launch_bounds__(256, MINB) k_g2p2(PartArgs a) {
     // ---- nodal-force operand for the next scatter
     if (TL) {
       if (!have_pk1) {
-        // vol0 J (R sigma R^T) F^-T = vol0 (R sigma R^T) cof(F)
+        // vol0 J (R sigma R^T) F^-T = vol0 (R sigma R^T) cof(F); R sigma R^T
+        // is symmetric: its upper triangle, mirrored
         float Sm[9] = {sig.a[0], sig.a[3], sig.a[4], sig.a[3], sig.a[1], sig.a[5], sig.a[4], sig.a[5], sig.a[2]};
         float RS[9], RSR[9];
         matmul3(R, Sm, RS);
-        matmulT3(RS, R, RSR);
+#pragma unroll
+        for (int i = 0; i < 3; i++)
+#pragma unroll
+          for (int j = i; j < 3; j++) {
+            RSR[3 * i + j] = RS[3 * i] * R[3 * j] + RS[3 * i + 1] * R[3 * j + 1] + RS[3 * i + 2] * R[3 * j + 2];
+            RSR[3 * j + i] = RSR[3 * i + j];
+          }
         matmul3(RSR, cofF, PK1);
       }
 #pragma unroll
