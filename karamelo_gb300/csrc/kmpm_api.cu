@@ -268,6 +268,11 @@ MatDev to_dev(const kmpm_material &m) {
   for (int i = 0; i < 12; i++) { d.f_eos_p[i] = (float)d.eos_p[i]; d.f_str_p[i] = (float)d.str_p[i]; }
   for (int i = 0; i < 8; i++) d.f_dam_p[i] = (float)d.dam_p[i];
   for (int i = 0; i < 6; i++) d.f_temp_p[i] = (float)d.temp_p[i];
+  // FP32 path: (K + 4G/3) / rho0, so that the wave speed is sqrt(f_c2_rho0 J)
+  // with no division per particle; Johnson-Cook: 1 / epsdot0 in the free
+  // parameter slot 9 (the FP64 path keeps the reference's quotients)
+  d.f_c2_rho0 = (float)((d.K + 1.333333333333333333333333333333333333333 * d.G) / d.rho0);
+  if (d.type == KMPM_MAT_EOS_STRENGTH && d.strength == 2 && d.str_p[4] != 0.0) d.f_str_p[9] = (float)(1.0 / d.str_p[4]);
   return d;
 }
 

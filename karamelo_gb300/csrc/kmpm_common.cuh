@@ -85,6 +85,7 @@ struct MatDev {
   // FP32 copies for the FP32 path (no per-particle double conversions)
   float f_rho0, f_K, f_G, f_lambda, f_signal_velocity, f_cp, f_invcp, f_kappa, f_c2;  // f_c2 = K + 4G/3
   float f_eos_p[12], f_str_p[12], f_dam_p[8], f_temp_p[6];
+  float f_c2_rho0;  // f_c2 / rho0: the squared wave speed is f_c2_rho0 J
 };
 template <typename R> struct MatP;
 template <> struct MatP<float> {
@@ -548,10 +549,14 @@ __device__ inline R eos_pressure(const MatDev &m, R J, R Jm1, R rho, R damage, R
 template <typename R>
 __device__ __forceinline__ R jc_flow_stress(const R *p, R epsp, R epsdot, R T) {
   R A = p[1], B = p[2], n = p[3], epsdot0 = p[4], C = p[5], mm = p[6], Tr = p[7], Tm = p[8];
-  R ratio = epsdot / epsdot0;
+  constexpr bool F32 = sizeof(R) == 4;
+  // FP32: epsdot / epsdot0 as a product with 1 / epsdot0 (slot 9), and the
+  // two powers of positive bases as exp2(y log2 x): relative error about
+  // |y log2 x| ulp, 1e-6 at epsp = 1e-10 and 3e-7 for epsp above 0.1
+  R ratio = F32 ? epsdot * p[9] : epsdot / epsdot0;
   ratio = ratio > R(1) ? ratio : R(1);
-  R ys = epsp < R(1.0e-10) ? A : A + B * pow(epsp, n);
-  if (C != R(0)) ys *= pow(R(1) + ratio, C);
+  R ys = epsp < R(1.0e-10) ? A : A + B * (F32 ? R(exp2f(float(n) * log2f(float(epsp)))) : pow(epsp, n));
+  if (C != R(0)) ys *= F32 ? R(exp2f(float(C) * log2f(float(R(1) + ratio)))) : pow(R(1) + ratio, C);
   if (T < Tm) {
     if (mm != R(0) && T >= Tr) ys *= R(1) - pow((T - Tr) / (Tm - Tr), mm);
   } else {

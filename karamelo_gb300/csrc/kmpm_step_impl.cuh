@@ -2315,7 +2315,7 @@ __global__ void __launch_bounds__(256, MINB) k_g2p2(PartArgs a) {
     // ---- wave speed and h ratio (src/solid.cpp:1376-1437)
     if (dmg < 1.f) {
       const float vx = st_ld(PF_V), vy = st_ld(PF_V + 1), vz = st_ld(PF_V + 2);
-      const float c = sqrtf(m.f_c2 / rho) + fmaxf(fmaxf(fabsf(vx), fabsf(vy)), fabsf(vz));
+      const float c = sqrtf(m.f_c2_rho0 * J) + fmaxf(fmaxf(fabsf(vx), fabsf(vy)), fabsf(vz));  // c2 / rho = c2 J / rho0
       if (isnan(c)) raise_error(a.err, ERR_NAN, p, sc.ntimestep);
       my_c = c;
       if (TL) my_h = fminf(1.f, min_abs_eig_real(H));
