@@ -427,15 +427,17 @@ __device__ inline bool polar_rotation(const float *F, float *R) {
   // small, where it no longer accelerates the iteration
   for (int it = 0; it < 12; it++) {
     cof3(X, C);
-    float dx = det3(X);
-    float g = fabsf(dx - 1.f) > 1e-3f ? rcbrtf(fabsf(dx)) : 1.f;  // scaling |det X|^(-1/3) (Higham 1986, sec. 3)
-    float gi = 1.f / (g * dx);         // X^-T / g = C / (g det X)
+    const float dx = X[0] * C[0] + X[1] * C[1] + X[2] * C[2];  // det X along the first row
+    const float g = fabsf(dx - 1.f) > 1e-3f ? rcbrtf(fabsf(dx)) : 1.f;  // scaling |det X|^(-1/3) (Higham 1986, sec. 3)
+    // X <- (g X + X^-T / g) / 2 with X^-T / g = C / (g det X); the halving,
+    // exact, is folded into both factors
+    const float gh = 0.5f * g, gih = 0.5f / (g * dx);
     float diff = 0.f;
 #pragma unroll
     for (int k = 0; k < 9; k++) {
-      float xn = 0.5f * (g * X[k] + gi * C[k]);
-      float e = xn - X[k];
-      diff += e * e;
+      const float xn = fmaf(gih, C[k], gh * X[k]);
+      const float e = xn - X[k];
+      diff = fmaf(e, e, diff);
       X[k] = xn;
     }
     if (diff < 1e-13f) break;
