@@ -111,6 +111,12 @@ struct kmpm_ctx {
   StepScalars *d_scalars = nullptr;
   int nscalars = 1;
   double *d_dtcfl = nullptr;
+  // TLMPM h ratio of the time step: per-range bounds, the flagged ranges
+  // (HRange, k_h_exact) and the exact pass's grid
+  HRange *d_hr = nullptr;
+  int *d_hflags = nullptr, *d_nhflag = nullptr;
+  int exact_blocks = 0;
+  bool exact_h = false;  // KMPM_EXACT_H=1: the cubic for every particle (no bounds)
   ErrState *d_err = nullptr;
   // host view of the error word: page-locked, mapped, written by a one-thread
   // kernel at the end of every run, so that reading it needs no copy engine
@@ -303,6 +309,7 @@ PartArgs part_args(kmpm_ctx *c) {
   a.thermal = c->prm.thermal;
   a.track_strain = c->prm.track_strain;
   a.apic = c->apic() ? 1 : 0;
+  a.hr = c->exact_h ? nullptr : c->d_hr;
   a.asflip = (!c->TL() && c->prm.transfer == KMPM_TRANSFER_ASFLIP) ? 1 : 0;
   a.axisym = c->prm.axisymmetric;
   a.dim = c->prm.dim;
@@ -380,6 +387,12 @@ DtArgs dt_args(kmpm_ctx *c) {
   a.scalars = c->d_scalars;
   a.err = c->d_err;
   a.nranges = (int)c->ranges.size();
+  a.hr = c->exact_h ? nullptr : c->d_hr;
+  a.hflags = c->d_hflags;
+  a.nhflag = c->d_nhflag;
+  a.Pp = c->d_pp;
+  a.ps = c->ps;
+  a.exact_blocks = c->exact_blocks;
   a.indep = c->indep();
   a.dt_constant = c->prm.dt_constant;
   a.dt_factor = c->prm.dt_factor;
@@ -644,6 +657,18 @@ int build(kmpm_ctx *c) {
     CK(cudaStreamSynchronize(c->st));
   }
   DALLOC(c->d_dtcfl, c->ranges.size());
+  if (const char *ev = std::getenv("KMPM_EXACT_H"); ev && ev[0] == '1') c->exact_h = true;
+  // one clock only: independent instances (each its own minimum over a
+  // uniformly loaded solid) leave few particles to skip
+  if (c->TL() && !c->indep()) {  // bounds 0: the first step takes the exact pass
+    DALLOC(c->d_hr, c->ranges.size());
+    DALLOC(c->d_hflags, c->ranges.size());
+    DALLOC(c->d_nhflag, 1);
+    int dev = 0, nsm = 0;
+    CK(cudaGetDevice(&dev));
+    CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    c->exact_blocks = 4 * nsm;
+  }
   DALLOC(c->d_err, 1);
   CK(cudaHostAlloc((void **)&c->h_err, sizeof(ErrState), cudaHostAllocMapped));
   CK(cudaHostGetDevicePointer((void **)&c->h_err_dev, c->h_err, 0));
@@ -1133,7 +1158,7 @@ int enqueue_step(kmpm_ctx *c, bool reuse = false) {
     }
     DtArgs da = dt_args(c);
     launch_dt(da, c->st);
-    nl += 2;
+    nl += c->d_hr && !c->exact_h ? 3 : 2;
     MARK("dt");
     CK(cudaGetLastError());
     c->launches_per_step = nl;
@@ -1199,7 +1224,7 @@ int enqueue_step(kmpm_ctx *c, bool reuse = false) {
   // update_time + adjust_dt
   DtArgs da = dt_args(c);
   launch_dt(da, c->st);
-  nl += 2;
+  nl += c->d_hr && !c->exact_h ? 3 : 2;
   MARK("dt");
   CK(cudaGetLastError());
   c->launches_per_step = nl;
@@ -1460,6 +1485,7 @@ int kmpm_destroy(kmpm_ctx *c) {
   dfree(c->nodeA); dfree(c->nodeX); dfree(c->nodeT); dfree(c->nodeP); dfree(c->d_tiles);
   dfree(c->d_cs); dfree(c->d_ce); dfree(c->d_ts); dfree(c->d_te); dfree(c->partial);
   dfree(c->d_fixes); dfree(c->d_fix_start); dfree(c->d_fix_count); dfree(c->d_scalars); dfree(c->d_dtcfl);
+  dfree(c->d_hr); dfree(c->d_hflags); dfree(c->d_nhflag);
   dfree(c->d_dump);
   free_contacts(c);
   for (auto &S : c->hsolids) dfree(S.d_in);

@@ -447,6 +447,16 @@ __device__ inline bool polar_rotation(const float *F, float *R) {
   return true;
 }
 
+// A lower bound of min |Re lambda(F)|, F = I + H.  For an eigenpair F x =
+// lambda x of the real F, Re lambda = x* S x / x* x with S = sym(F), so every
+// real part lies in the spectrum of S, which Gershgorin's discs bound from
+// below: min_i (S_ii - sum_{j != i} |S_ij|).  A bound <= 0 says nothing.
+__device__ __forceinline__ float re_eig_lower_bound(const float *H) {
+  const float s01 = 0.5f * fabsf(H[1] + H[3]), s02 = 0.5f * fabsf(H[2] + H[6]), s12 = 0.5f * fabsf(H[5] + H[7]);
+  const float l0 = 1.f + H[0] - s01 - s02, l1 = 1.f + H[4] - s01 - s12, l2 = 1.f + H[8] - s02 - s12;
+  return fminf(l0, fminf(l1, l2));
+}
+
 // Real parts of the eigenvalues of F = I + H (the reference calls
 // Eigen::EigenSolver, src/solid.cpp:1401-1409): the characteristic cubic of H
 // solved in closed form (trigonometric form for three real roots, Cardano

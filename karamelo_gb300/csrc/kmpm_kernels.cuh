@@ -102,6 +102,8 @@ struct GridArgs {
   float4 *nodeP;
 };
 
+struct HRange;  // the h-ratio bound of one range (below)
+
 struct PartArgs {
   float *const *Pp;
   size_t ps;
@@ -121,6 +123,7 @@ struct PartArgs {
   int indep, use_vu, thermal, track_strain, dim;
   int tile_t[3];
   int apic;                  // APIC transfers: k_g2p2 forms grad v from moments and stores PF_C
+  const HRange *hr;          // TLMPM, one clock: the h-ratio bound of each range (nullptr: solve every particle)
   int asflip;                // ULMPM ASFLIP: positions move with the blended velocity
   int axisym;                // 2-D axisymmetric: Fdot(2,2) / L(2,2) += v_r w / r
   // queue of the plastic particle-steps for the learned return map (the
@@ -138,6 +141,20 @@ enum { LQ_P = 0, LQ_MAT = 1, LQ_NI = 2 };
 enum { LQ_DT = 0, LQ_TAV = 1, LQ_D = 2, LQ_SIG = 8, LQ_EPSP = 14, LQ_EPSDOT = 15, LQ_PH = 16, LQ_TRE = 17,
        LQ_R = 18, LQ_COF = 27, LQ_NF = 36 };
 
+// The h ratio of the time step (TLMPM), per range: the smallest
+// min(1, |Re lambda(F)|) over its particles (src/solid.cpp:1399-1409).  The
+// stress kernel solves the characteristic cubic only for particles whose
+// cheap lower bound (re_eig_lower_bound) lies below `bound`; the others
+// report `bound`.  If the range's reduced minimum reaches `bound`, one of
+// them may hold the true minimum, and k_h_exact recomputes the range from
+// every particle: the result is the exact minimum whatever the bound.
+struct HRange {
+  float bound;  // this step's threshold: min(1, 1.001 x the last exact minimum); 0 at setup
+  float hmin;   // the range's minimum of this step (exact once the step's dt is formed)
+  float cmax;   // the range's largest wave speed of this step
+  int need;     // 1: the reduced minimum reached the bound (k_h_exact recomputes it)
+};
+
 struct DtArgs {
   const RangeDev *ranges;
   const GridDev *grids;
@@ -148,6 +165,13 @@ struct DtArgs {
   int nranges, indep, dt_constant;
   double dt_factor;
   int max_nblk;              // largest range, in 256-particle blocks (picks the reduction width)
+  // TLMPM h ratio (nullptr for ULMPM and independent instances): per-range bounds, the list of the
+  // ranges k_h_exact recomputes and its length, the particle state it reads
+  HRange *hr;
+  int *hflags, *nhflag;
+  float *const *Pp;
+  size_t ps;
+  int exact_blocks;          // grid of k_h_exact
 };
 
 struct LaunchSet {

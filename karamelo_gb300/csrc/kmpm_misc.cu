@@ -289,17 +289,74 @@ __global__ void __launch_bounds__(BS) k_dt_range(DtArgs a) {
     __syncthreads();
   }
   if (threadIdx.x == 0) {
-    const GridDev g = a.grids[rd.grid];
-    const double dtcfl = (double)g.cellsize * (double)rh[0] / (double)rc[0];
-    a.solid_dtcfl[blockIdx.x] = dtcfl;
-    if (rh[0] == 0.f || dtcfl == 0.0 || isnan(dtcfl))
-      raise_error_m(a.err, ERR_DTCFL, -1, a.scalars[a.indep ? blockIdx.x : 0].ntimestep);
+    // TLMPM: a minimum at or above the range's bound may come from a particle
+    // that reported the bound; k_h_exact then recomputes it (HRange)
+    bool need = false;
+    if (a.hr) {
+      HRange &q = a.hr[blockIdx.x];
+      need = !(rh[0] < q.bound);
+      q.need = need;
+      q.cmax = rc[0];
+      q.hmin = need ? 1.f : rh[0];
+      if (need) a.hflags[atomicAdd(a.nhflag, 1)] = blockIdx.x;
+    }
+    if (!need) {
+      const GridDev g = a.grids[rd.grid];
+      const double dtcfl = (double)g.cellsize * (double)rh[0] / (double)rc[0];
+      a.solid_dtcfl[blockIdx.x] = dtcfl;
+      if (rh[0] == 0.f || dtcfl == 0.0 || isnan(dtcfl))
+        raise_error_m(a.err, ERR_DTCFL, -1, a.scalars[a.indep ? blockIdx.x : 0].ntimestep);
+    }
+  }
+}
+
+// The exact h ratio of the ranges k_dt_range flagged: min(1, |Re lambda(F)|)
+// over every particle with damage below 1, as the stress kernel evaluates it,
+// by a grid-stride loop and an order-free minimum (non-negative floats order
+// as their bits).  With no range flagged every block returns at once.
+__global__ void __launch_bounds__(256) k_h_exact(DtArgs a) {
+  if (run_finished(a.scalars)) return;
+  const int nf = *a.nhflag;
+  if (nf == 0) return;
+  const float *P = *a.Pp;
+  const size_t ps = a.ps;
+  for (int f = 0; f < nf; f++) {
+    const int r = a.hflags[f];
+    const RangeDev rd = a.ranges[r];
+    float m = 1.f;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < rd.count; i += gridDim.x * blockDim.x) {
+      const int p = rd.start + i;
+      if (!(P[PF_DMG * ps + p] < 1.f)) continue;
+      float H[9];
+#pragma unroll
+      for (int k = 0; k < 9; k++) H[k] = P[(PF_H + k) * ps + p];
+      m = fminf(m, fminf(1.f, min_abs_eig_real(H)));
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) m = fminf(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) atomicMin(reinterpret_cast<int *>(&a.hr[r].hmin), __float_as_int(m));
   }
 }
 
 // update_time, then adjust_dt; in independent mode every range keeps its own clock
 __global__ void k_dt_final(DtArgs a) {
   if (run_finished(a.scalars)) return;
+  if (a.hr) {
+    // the ranges k_h_exact recomputed; every range's bound for the next step
+    for (int r = threadIdx.x; r < a.nranges; r += blockDim.x) {
+      HRange &q = a.hr[r];
+      if (q.need) {
+        const double dtcfl = (double)a.grids[a.ranges[r].grid].cellsize * (double)q.hmin / (double)q.cmax;
+        a.solid_dtcfl[r] = dtcfl;
+        if (q.hmin == 0.f || dtcfl == 0.0 || isnan(dtcfl))
+          raise_error_m(a.err, ERR_DTCFL, -1, a.scalars[a.indep ? r : 0].ntimestep);
+        q.need = 0;
+      }
+      q.bound = fminf(1.f, 1.001f * q.hmin);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) *a.nhflag = 0;
+  }
   if (a.indep) {
     for (int r = threadIdx.x; r < a.nranges; r += blockDim.x) {
       StepScalars &s = a.scalars[r];
@@ -329,6 +386,7 @@ void launch_dt(const DtArgs &a, cudaStream_t st) {
   // wide CTAs for few large ranges, narrow ones for many small ranges
   if (a.max_nblk > 4096) k_dt_range<1024><<<a.nranges, 1024, 0, st>>>(a);
   else k_dt_range<256><<<a.nranges, 256, 0, st>>>(a);
+  if (a.hr) k_h_exact<<<a.exact_blocks, 256, 0, st>>>(a);
   k_dt_final<<<1, 256, 0, st>>>(a);
 }
 

@@ -2318,7 +2318,12 @@ __global__ void __launch_bounds__(256, MINB) k_g2p2(PartArgs a) {
       const float c = sqrtf(m.f_c2_rho0 * J) + fmaxf(fmaxf(fabsf(vx), fabsf(vy)), fabsf(vz));  // c2 / rho = c2 J / rho0
       if (isnan(c)) raise_error(a.err, ERR_NAN, p, sc.ntimestep);
       my_c = c;
-      if (TL) my_h = fminf(1.f, min_abs_eig_real(H));
+      if (TL) {
+        // the cubic only where this particle may hold its range's minimum
+        // (HRange): elsewhere the range's bound, which k_h_exact checks
+        const float hb = a.hr ? a.hr[a.blk_range[blockIdx.x]].bound : 2.f;
+        my_h = (hb > 1.f || re_eig_lower_bound(H) < hb) ? fminf(1.f, min_abs_eig_real(H)) : hb;
+      }
     }
   }
   // block reduction (order-free min / max): within each warp by shuffles,
