@@ -1019,8 +1019,25 @@ __global__ void __launch_bounds__(256, 4) k_p2g_vel_row(P2GArgs a) {
 //     lanes hand their y = 1..5 sums to the c = 0 lanes, and group 0 adds
 //     the row into the warp's slab.
 // Every sum runs in a fixed order: the result is bit-reproducible.
-template <int BASIS, int MODE>
+__device__ __forceinline__ void raise_error(ErrState *e, int code, int p, long long step);  // (G2P below)
+
+// dynamic shared memory of k_p2g_row2<.., P2G_VEL, REMAP> (bytes): the
+// velocity scatter's, then the tile's node footprint (24 bytes per node)
+template <int BASIS> constexpr int p2g_row2_remap_smem() {
+  using TS = TileShape<2, BASIS>;
+  constexpr int QINP = (p2g_nin(P2G_VEL, false) + 3) & ~3;
+  return 4 * (TS::NWARP * (((3 * TS::NF + 3) & ~3) + 32 * QINP + 33 * 2 * 4 * 2) + 6 * ((TS::NW + 1) & ~1));
+}
+
+// REMAP (MODE P2G_VEL; 1 TLMPM, 2 ULMPM): the MUSL gather, particle update
+// and re-map in one pass, as k_g2p1_remap_row does in 3-D.  The block stages
+// its tile's node footprint of (v, v_update), and each particle's stage also
+// gathers its 16 nodes there in k_g2p1's order, moves the particle and
+// stages m v_new: the scatter that follows is this kernel's own, so the sums
+// are those of k_g2p1 then the plain velocity scatter, bit for bit.
+template <int BASIS, int MODE, int REMAP = 0>
 __global__ void __launch_bounds__(256, (MODE == P2G_VEL || p2g_fonly(MODE) ? 4 : 3)) k_p2g_row2(P2GArgs a) {
+  static_assert(REMAP == 0 || MODE == P2G_VEL, "the re-map pass is a velocity scatter");
   static_assert(Stencil<BASIS>::S == 4 && Stencil<BASIS>::SC == 1, "four-wide stencils");
   using TS = TileShape<2, BASIS>;
   constexpr int S = 4, LO = Stencil<BASIS>::LO;
@@ -1053,9 +1070,33 @@ __global__ void __launch_bounds__(256, (MODE == P2G_VEL || p2g_fonly(MODE) ? 4 :
   if (a.tile_end[tile_global] == a.tile_start[tile_global] || run_finished(a.scalars)) return;
   const int tc1 = tlin % g.ntile[1], tc0 = tlin / g.ntile[1];
   const float h = g.cellsize, ih = g.inv_cellsize;
-  const float *P = *a.Pp;
+  float *P = *a.Pp;
   const size_t ps = a.ps;
   const bool use_u = a.pos_field == PF_X;
+  constexpr int NWP = (NW + 1) & ~1;
+  float4 *fpA = reinterpret_cast<float4 *>(smem + TS::NWARP * (SLAB + STAGE));  // (v, v_update.x)
+  float2 *fpB = reinterpret_cast<float2 *>(fpA + NWP);                          // (v_update.y, v_update.z)
+  float dt = 0.f, alpha = 0.f;
+  long long nstep = 0;
+  if (REMAP) {
+    const StepScalars &sc0 = a.scalars[a.indep ? g.solid0 : 0];
+    dt = (float)sc0.dt;
+    nstep = sc0.ntimestep;
+    alpha = a.pic_flip;
+    prefetch_rows_l2(P, ps, PF_X0, PF_MASS + 1 - PF_X0, a.tile_start[tile_global], a.tile_end[tile_global]);
+    // the tile's node footprint: nodes (tc TX - LO + fx, tc TY - LO + fy)
+    const float4 *__restrict__ NA = a.nodeA + NODE_STRIDE * g.node_off;
+    const int b0 = tc0 * TX - LO, b1 = tc1 * TY - LO;
+    for (int e = threadIdx.x; e < NW; e += blockDim.x) {
+      const int fy = e % WY, fx = e / WY;
+      const int ix = b0 + fx, iy = b1 + fy;
+      float4 A = make_float4(0.f, 0.f, 0.f, 0.f), B = A;
+      if (ix >= 0 && ix < g.n[0] && iy >= 0 && iy < g.n[1]) ld_node_pair(NA + NODE_STRIDE * (ix * g.n[1] + iy), A, B);
+      fpA[e] = make_float4(A.x, A.y, A.z, B.x);
+      fpB[e] = make_float2(B.y, B.z);
+    }
+    __syncthreads();
+  }
 
   for (int k = lane; k < Q * NF; k += 32) slab[k] = 0.f;
 
@@ -1096,14 +1137,9 @@ __global__ void __launch_bounds__(256, (MODE == P2G_VEL || p2g_fonly(MODE) ? 4 :
 #pragma unroll
           for (int k = 1; k < 4; k++) ly = lo4[k] <= p ? k : ly;
           float pay[QIN];
-          p2g_payload<MODE, false>(a, P, p, pay);
-#pragma unroll
-          for (int v = 0; v < QINP / 4; v++)
-            reinterpret_cast<float4 *>(spay + lane * QINP)[v] =
-                make_float4(pay[4 * v], 4 * v + 1 < QIN ? pay[min(4 * v + 1, QIN - 1)] : 0.f,
-                            4 * v + 2 < QIN ? pay[min(4 * v + 2, QIN - 1)] : 0.f,
-                            4 * v + 3 < QIN ? pay[min(4 * v + 3, QIN - 1)] : 0.f);
+          if (!REMAP) p2g_payload<MODE, false>(a, P, p, pay);
           const int i0[2] = {i0x, (tc1 * TY + ly0 + ly) - LO};
+          float svs[2][S];
 #pragma unroll
           for (int d = 0; d < 2; d++) {
             const float xp = P[(PF_X0 + d) * ps + p] + (use_u ? P[(PF_X + d) * ps + p] : 0.f);
@@ -1127,8 +1163,55 @@ __global__ void __launch_bounds__(256, (MODE == P2G_VEL || p2g_fonly(MODE) ? 4 :
               }
             }
 #pragma unroll
-            for (int kk = 0; kk < S; kk++) sbas[(d * S + kk) * SROW + lane] = make_float2(sv[kk], dsv[kk]);
+            for (int kk = 0; kk < S; kk++) {
+              sbas[(d * S + kk) * SROW + lane] = make_float2(sv[kk], dsv[kk]);
+              svs[d][kk] = sv[kk];
+            }
           }
+          if (REMAP) {
+            // k_g2p1's gather from the footprint: stencil node (i, j) is
+            // footprint node (warp L + lx + i, ly0 + ly + j); w = s_x s_y (the
+            // unit z weight of the 2-D gather leaves it exact)
+            float vu[3] = {0.f, 0.f, 0.f}, va[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+            for (int i = 0; i < S; i++) {
+#pragma unroll
+              for (int j = 0; j < S; j++) {
+                const float w = svs[0][i] * svs[1][j];
+                const int fi = (warp * L + lx + i) * WY + (ly0 + ly + j);
+                const float4 A = fpA[fi];
+                const float2 B = fpB[fi];
+                vu[0] = fmaf(w, A.w, vu[0]); vu[1] = fmaf(w, B.x, vu[1]); vu[2] = fmaf(w, B.y, vu[2]);
+                va[0] = fmaf(w, A.x, va[0]); va[1] = fmaf(w, A.y, va[1]); va[2] = fmaf(w, A.z, va[2]);
+              }
+            }
+            const float m = P[PF_MASS * ps + p];
+            float xn[3];
+#pragma unroll
+            for (int d = 0; d < 3; d++) {
+              const float up = P[(PF_X + d) * ps + p];
+              const float v = P[(PF_V + d) * ps + p];
+              const float vnew = (1.f - alpha) * vu[d] + alpha * (v + (vu[d] - va[d]));
+              const float un = up + dt * vu[d];
+              if (REMAP == 1) {
+                P[(PF_X + d) * ps + p] = un;
+              } else {
+                P[(PF_XN + d) * ps + p] = un;
+                xn[d] = P[(PF_X0 + d) * ps + p] + un;
+              }
+              P[(PF_V + d) * ps + p] = vnew;
+              pay[d] = m * vnew;
+            }
+            if (REMAP == 2 && !(xn[0] >= a.boxlo[0] && xn[0] <= a.boxhi[0] && xn[1] >= a.boxlo[1] &&
+                                xn[1] <= a.boxhi[1] && xn[2] >= a.boxlo[2] && xn[2] <= a.boxhi[2]))
+              raise_error(a.err, ERR_LEFT, p, nstep);
+          }
+#pragma unroll
+          for (int v = 0; v < QINP / 4; v++)
+            reinterpret_cast<float4 *>(spay + lane * QINP)[v] =
+                make_float4(pay[4 * v], 4 * v + 1 < QIN ? pay[min(4 * v + 1, QIN - 1)] : 0.f,
+                            4 * v + 2 < QIN ? pay[min(4 * v + 2, QIN - 1)] : 0.f,
+                            4 * v + 3 < QIN ? pay[min(4 * v + 3, QIN - 1)] : 0.f);
         }
         __syncwarp();
         // ---- accumulate: group grp takes particles j = grp, grp + 4, ... of
@@ -2381,6 +2464,9 @@ void fill_step_kernels(StepKernels &k) {
     k.g2p1_remap[1] = (void *)k_g2p1_remap_row<BASIS, true>;
     k.g2p1_remap_smem = g2p1_remap_smem<BASIS>();
   } else if constexpr (DIM == 2 && (BASIS == 1 || BASIS == 3)) {
+    k.g2p1_remap[0] = (void *)k_p2g_row2<BASIS, P2G_VEL, 2>;
+    k.g2p1_remap[1] = (void *)k_p2g_row2<BASIS, P2G_VEL, 1>;
+    k.g2p1_remap_smem = p2g_row2_remap_smem<BASIS>();
     k.p2g_row_fonly = (void *)k_p2g_row2<BASIS, P2G_TL | P2G_FONLY>;
     k.p2g_row_fonly_smem = 0;  // p2g_smem_bytes of the mode
     k.grid_upd_fonly = (void *)k_grid<DIM, BASIS, GM_UPDATE_F, true, false, float>;
@@ -2388,8 +2474,6 @@ void fill_step_kernels(StepKernels &k) {
     k.p2g_row[0] = (void *)k_p2g_row2<BASIS, P2G_TL>;
     k.p2g_row[1] = (void *)k_p2g_row2<BASIS, P2G_UL>;
     k.p2g_row[2] = (void *)k_p2g_row2<BASIS, P2G_VEL>;
-    k.g2p1_remap[0] = k.g2p1_remap[1] = nullptr;
-    k.g2p1_remap_smem = 0;
   } else {
     k.p2g_row[0] = k.p2g_row[1] = k.p2g_row[2] = nullptr;
     k.g2p1_remap[0] = k.g2p1_remap[1] = nullptr;

@@ -3,8 +3,10 @@ separate kernels it replaces (k_g2p1, then k_p2g_row<.., P2G_VEL>;
 KMPM_SPLIT_MUSL=1 selects them).  The fused kernel forms every sum in the
 order of the separate kernels, so the particle and grid fields agree bit for
 bit: over the Taylor bar (TLMPM, weights from x0) and the dam break (ULMPM,
-re-binned every step, positions moved into the second buffer), with the cubic
-and the quadratic spline."""
+re-binned every step, positions moved into the second buffer), and in 2-D
+(k_p2g_row2's re-map mode against k_g2p1 and the 2-D velocity scatter) over a
+tensile bar (TLMPM) and a spinning disk (ULMPM), with the cubic and the
+quadratic spline."""
 import os
 
 import numpy as np
@@ -31,6 +33,18 @@ def _dam(basis):
     return sim
 
 
+def _tensile_2d(basis):
+    sim = W.tensile_bar_2d(None, basis=basis, vend=5.0)
+    sim.run(40)
+    return sim
+
+
+def _disk_ulmpm_2d(basis):
+    sim = W.spinning_disk(None, sub="FLIP", basis=basis, omega=3.0)
+    sim.run(40)
+    return sim
+
+
 def _run(make, basis, split):
     if split:
         os.environ["KMPM_SPLIT_MUSL"] = "1"
@@ -46,7 +60,8 @@ def _run(make, basis, split):
     return phases, out
 
 
-@pytest.mark.parametrize("make", [_taylor, _dam], ids=["taylor_tlmpm", "dam_ulmpm"])
+@pytest.mark.parametrize("make", [_taylor, _dam, _tensile_2d, _disk_ulmpm_2d],
+                         ids=["taylor_tlmpm", "dam_ulmpm", "tensile_tlmpm_2d", "disk_ulmpm_2d"])
 @pytest.mark.parametrize("basis", ["cubic-spline", "quadratic-spline"])
 def test_fused_remap_matches_separate_kernels(gpu_lib, make, basis):
     ph_f, fused = _run(make, basis, split=False)
