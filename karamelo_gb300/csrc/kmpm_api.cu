@@ -171,7 +171,8 @@ struct kmpm_ctx {
   int *d_lq_i = nullptr, *d_lq_count = nullptr;
   long long lq_cap = 0;
   int nsm = 0;
-  bool law_jc = false;  // every material is linear EOS + Johnson-Cook: the specialised stress kernels
+  int law = 0;           // the law set every material shares (LAW_*): the specialised stress kernels
+  bool law_jc = false;  // every material is linear EOS + Johnson-Cook
   // plastic strain or damage was uploaded (a restart): those rows may be
   // non-zero whatever the laws, and are permuted with the others
   bool restored_state = false;
@@ -490,12 +491,22 @@ int build(kmpm_ctx *c) {
     c->fuse_remap = c->K.g2p1_remap[0] && c->musl() && !c->prm.thermal && !c->apic() && !(es && es[0] == '1') &&
                     !(ec && ec[0] == '1');
   }
-  // the specialised stress kernels: every material linear EOS + Johnson-Cook,
-  // no damage, no temperature law
-  c->law_jc = !c->prm.thermal && !c->mats.empty();
-  for (const auto &m : c->mats)
-    c->law_jc = c->law_jc && m.type == KMPM_MAT_EOS_STRENGTH && m.eos == 0 && m.strength == 2 && m.damage < 0 &&
-                m.temp < 0 && m.cp == 0.0;
+  // the specialised stress kernels: every material of one law set (linear
+  // EOS + Johnson-Cook; shock EOS + Johnson-Cook + Johnson-Cook damage; fluid
+  // EOS + fluid strength), no temperature law
+  {
+    const auto kind = [](const MatDev &m) {
+      if (m.type != KMPM_MAT_EOS_STRENGTH || m.temp >= 0 || m.cp != 0.0) return (int)LAW_ANY;
+      if (m.eos == 0 && m.strength == 2 && m.damage < 0) return (int)LAW_EOS_LINEAR_JC;
+      if (m.eos == 1 && m.strength == 2 && m.damage >= 0) return (int)LAW_EOS_SHOCK_JC_DMG;
+      if (m.eos == 2 && m.strength == 4 && m.damage < 0) return (int)LAW_FLUID;
+      return (int)LAW_ANY;
+    };
+    c->law = (c->prm.thermal || c->mats.empty()) ? (int)LAW_ANY : kind(c->mats[0]);
+    for (const auto &m : c->mats)
+      if (kind(m) != c->law) c->law = LAW_ANY;
+    c->law_jc = c->law == LAW_EOS_LINEAR_JC;
+  }
   tile_dims(dim, basis, c->tdim);
   c->NCELL = c->tdim[0] * c->tdim[1] * c->tdim[2];
   // ---- grids
@@ -1020,7 +1031,11 @@ int g2p2_smem(const kmpm_ctx *c, const void *fn) {
 
 void *g2p2_variant(const kmpm_ctx *c, int v) {
   const bool TL = c->TL();
-  if (c->law_jc && !c->apic() && c->K.g2p2_jc[TL][v]) return c->K.g2p2_jc[TL][v];
+  if (!c->apic()) {
+    if (c->law == LAW_EOS_LINEAR_JC && c->K.g2p2_jc[TL][v]) return c->K.g2p2_jc[TL][v];
+    if (c->law == LAW_EOS_SHOCK_JC_DMG && c->K.g2p2_jcd[TL][v]) return c->K.g2p2_jcd[TL][v];
+    if (c->law == LAW_FLUID && c->K.g2p2_fl[TL][v]) return c->K.g2p2_fl[TL][v];
+  }
   return c->K.g2p2_v[TL][v];
 }
 
@@ -1384,10 +1399,10 @@ int autotune(kmpm_ctx *c) {
 // a later context of the same problem takes the choice without its trial
 // launches.
 struct TuneKey {
-  int tl, dim, basis, law_jc, transfer, log2n;
+  int tl, dim, basis, law, transfer, log2n;
   bool operator<(const TuneKey &o) const {
-    return std::tie(tl, dim, basis, law_jc, transfer, log2n) <
-           std::tie(o.tl, o.dim, o.basis, o.law_jc, o.transfer, o.log2n);
+    return std::tie(tl, dim, basis, law, transfer, log2n) <
+           std::tie(o.tl, o.dim, o.basis, o.law, o.transfer, o.log2n);
   }
 };
 std::mutex g_tune_mutex;
@@ -1398,7 +1413,7 @@ TuneKey tune_key(const kmpm_ctx *c) {
   for (const auto &r : c->ranges) n += r.count;
   int l = 0;
   while ((1LL << (l + 1)) <= std::max(n, 1LL)) l++;
-  return TuneKey{c->TL() ? 1 : 0, c->prm.dim, c->prm.basis, c->law_jc ? 1 : 0, c->prm.transfer, l};
+  return TuneKey{c->TL() ? 1 : 0, c->prm.dim, c->prm.basis, c->law, c->prm.transfer, l};
 }
 
 int maybe_tune(kmpm_ctx *c) {

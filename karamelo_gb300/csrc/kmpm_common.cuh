@@ -524,14 +524,22 @@ struct ConstitutiveIn {
 // the material at run time; LAW_EOS_LINEAR_JC fixes linear EOS +
 // Johnson-Cook strength without damage or temperature (the copper bar), so
 // that the other laws' code leaves the kernel.
-enum : int { LAW_ANY = 0, LAW_EOS_LINEAR_JC = 1 };
+// Stress kernels compiled for one set of laws (the others' code left out):
+// LAW_ANY reads the laws from the material; the rest fix them at compile
+// time, for runs whose every material is of that kind (no temperature law)
+enum : int { LAW_ANY = 0, LAW_EOS_LINEAR_JC = 1, LAW_EOS_SHOCK_JC_DMG = 2, LAW_FLUID = 3 };
+// the EOS, strength and damage law of a set (-1: read from the material;
+// damage 1: Johnson-Cook damage, 0: none)
+__host__ __device__ constexpr int law_eos(int law) { return law == 1 ? 0 : law == 2 ? 1 : law == 3 ? 2 : -1; }
+__host__ __device__ constexpr int law_strength(int law) { return law == 1 || law == 2 ? 2 : law == 3 ? 4 : -1; }
+__host__ __device__ constexpr int law_damage(int law) { return law == 2 ? 1 : law == 0 ? -1 : 0; }
 
 // EOS::compute_pressure (src/eos_linear.cpp:71-74, src/eos_shock.cpp:99-133,
 // src/eos_fluid.cpp:68-73); T is the particle temperature or 0.
 template <typename R, int LAW = LAW_ANY>
 __device__ inline R eos_pressure(const MatDev &m, R J, R Jm1, R rho, R damage, R trD, R cellsize, R T) {
   const auto *ep = MatP<R>::eos(m);
-  const int eos = LAW == LAW_EOS_LINEAR_JC ? 0 : m.eos;
+  const int eos = law_eos(LAW) >= 0 ? law_eos(LAW) : m.eos;
   if (eos == 0) return -R(ep[1]) * Jm1 * (R(1) - damage);
   // rho/rho0 = 1/J; the compressions below are written in J - 1 so that FP32
   // keeps them accurate when J is close to 1 (no 1/J - 1 cancellation)
@@ -583,7 +591,7 @@ __device__ inline Sym<R> strength_update(const MatDev &m, R dt, const Sym<R> &si
   Sym<R> out;
   dep = R(0);
   const auto *p = MatP<R>::str(m);
-  const int strength = LAW == LAW_EOS_LINEAR_JC ? 2 : m.strength;
+  const int strength = law_strength(LAW) >= 0 ? law_strength(LAW) : m.strength;
   if (strength == 0) {  // linear: dev(sigma) + dt 2G(1-D) dev(D)
     Sym<R> s = sig, d = D;
     s.dev(); d.dev();

@@ -206,6 +206,9 @@ struct StepKernels {
   // (LAW_EOS_LINEAR_JC; 3-D, nullptr elsewhere)
   void *g2p2_jc[2][3];
   void *g2p2_jcq[3];  // 3-D cubic TLMPM, linear EOS + Johnson-Cook, queueing plastic steps
+  // compiled for shock EOS + Johnson-Cook + Johnson-Cook damage (2-D cubic
+  // TLMPM) and for fluid EOS + fluid strength (3-D cubic ULMPM) [TL][variant]
+  void *g2p2_jcd[2][3], *g2p2_fl[2][3];
   // MUSL gather + re-map in one pass (k_g2p1_remap_row) [TL]: 3-D cubic and
   // quadratic splines (nullptr elsewhere), and its dynamic shared memory
   void *g2p1_remap[2];

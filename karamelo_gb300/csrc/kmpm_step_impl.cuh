@@ -2041,9 +2041,9 @@ __global__ void __launch_bounds__(256, MINB) k_g2p2(PartArgs a) {
     if (TMA_STATE && row >= PF_V && row <= PF_DMG) return sstate[(row - PF_V) * 256 + threadIdx.x];
     return P[(size_t)row * ps + p];
   };
-  // the linear EOS + Johnson-Cook kernels serve FLIP/PIC runs only (APIC runs
-  // take the general ones): no affine moments, no per-slot offsets kept
-  const bool apic = LAW == LAW_EOS_LINEAR_JC ? false : a.apic != 0;
+  // the kernels compiled for one set of laws serve FLIP/PIC runs only (APIC
+  // runs take the general ones): no affine moments, no per-slot offsets kept
+  const bool apic = LAW != LAW_ANY ? false : a.apic != 0;
   const GridDev g = a.grids[rd.grid];
   float xp[3];
 #pragma unroll
@@ -2076,7 +2076,7 @@ __global__ void __launch_bounds__(256, MINB) k_g2p2(PartArgs a) {
     // the state rows the EOS + strength update reads after the node gather
     // (material type 2): start their DRAM reads now, into L2, so that they
     // overlap the gather (a hint: no registers held)
-    if (!TMA_STATE && (LAW == LAW_EOS_LINEAR_JC || (PREC == 0 && m.type == 2))) {
+    if (!TMA_STATE && (LAW != LAW_ANY || (PREC == 0 && m.type == 2))) {
       const int rows[] = {PF_H, PF_H + 1, PF_H + 2, PF_H + 3, PF_H + 4, PF_H + 5, PF_H + 6, PF_H + 7, PF_H + 8,
                           PF_SIG, PF_SIG + 1, PF_SIG + 2, PF_SIG + 3, PF_SIG + 4, PF_SIG + 5,
                           PF_EPSP, PF_EPSDOT, PF_DMG, PF_VOL0, PF_V, PF_V + 1, PF_V + 2};
@@ -2268,7 +2268,9 @@ __global__ void __launch_bounds__(256, MINB) k_g2p2(PartArgs a) {
       const bool hasT = LAW == LAW_ANY && m.f_cp != 0.f;
       float T = hasT ? a.T_ref + P[PF_T * ps + p] : 0.f;  // PF_T holds T - T_ref
       float epsp = st_ld(PF_EPSP), epsdot = st_ld(PF_EPSDOT);
-      float dinit = m.damage >= 0 ? P[PF_DMGI * ps + p] : 0.f;
+      // Johnson-Cook damage: on for its law set, else as the material says
+      const bool dmg_law = law_damage(LAW) == 1 || (LAW == LAW_ANY && m.damage >= 0);
+      float dinit = dmg_law ? P[PF_DMGI * ps + p] : 0.f;
       float pH, dep;
       Sym<float> sdev;
       if (PREC == 1) {
@@ -2336,7 +2338,7 @@ __global__ void __launch_bounds__(256, MINB) k_g2p2(PartArgs a) {
       epsdot -= epsdot * dt * itav;
       epsdot += dep * itav;
       epsdot = fmaxf(0.f, epsdot);
-      if (LAW == LAW_ANY && m.damage >= 0) {
+      if (dmg_law) {
         float Tdm = a.thermal ? a.T_ref + P[PF_T * ps + p] : 0.f;
         damage_update<float>(m, dinit, dmg, pH, sdev, epsdot, dep, Tdm);
         P[PF_DMGI * ps + p] = dinit;
@@ -2572,6 +2574,18 @@ void fill_step_kernels(StepKernels &k) {
 #undef KMPM_JC_SET
   }
   for (int v = 0; v < G2P_NVAR; v++) k.g2p2_jcq[v] = nullptr;
+  for (int t = 0; t < 2; t++)
+    for (int v = 0; v < G2P_NVAR; v++) k.g2p2_jcd[t][v] = k.g2p2_fl[t][v] = nullptr;
+  if constexpr (DIM == 2 && BASIS == 1) {  // batches of damage bars
+    k.g2p2_jcd[1][0] = (void *)k_g2p2<DIM, BASIS, true, false, 0, G2P2_MINB[0], LAW_EOS_SHOCK_JC_DMG>;
+    k.g2p2_jcd[1][1] = (void *)k_g2p2<DIM, BASIS, true, false, 0, G2P2_MINB[1], LAW_EOS_SHOCK_JC_DMG>;
+    k.g2p2_jcd[1][2] = (void *)k_g2p2<DIM, BASIS, true, false, 0, G2P2_MINB[2], LAW_EOS_SHOCK_JC_DMG>;
+  }
+  if constexpr (DIM == 3 && BASIS == 1) {  // fluids (ULMPM)
+    k.g2p2_fl[0][0] = (void *)k_g2p2<DIM, BASIS, false, false, 0, G2P2_MINB[0], LAW_FLUID>;
+    k.g2p2_fl[0][1] = (void *)k_g2p2<DIM, BASIS, false, false, 0, G2P2_MINB[1], LAW_FLUID>;
+    k.g2p2_fl[0][2] = (void *)k_g2p2<DIM, BASIS, false, false, 0, G2P2_MINB[2], LAW_FLUID>;
+  }
   if constexpr (DIM == 3 && BASIS == 1) {  // the learned return map's path
     k.g2p2_jcq[0] = (void *)k_g2p2<DIM, BASIS, true, false, 0, G2P2_MINB[0], LAW_EOS_LINEAR_JC, true>;
     k.g2p2_jcq[1] = (void *)k_g2p2<DIM, BASIS, true, false, 0, G2P2_MINB[1], LAW_EOS_LINEAR_JC, true>;
