@@ -210,6 +210,20 @@ int kmpm_contact_force(struct kmpm_ctx *ctx, int contact, double out[3]);
  * src/musl.cpp:34-95), each step fully on the GPU. */
 int kmpm_run(struct kmpm_ctx *ctx, int nsteps);
 
+/* kmpm_run without the wait (no counterpart in the reference, whose steps
+ * run on the calling thread): the nsteps steps are queued on the context's
+ * stream and the call returns, so that the caller can queue downloads and
+ * further runs while the GPU steps.  A step's error (J <= 0, a particle
+ * outside the domain, ...) does not stop the steps queued after it, as
+ * within one kmpm_run; the next kmpm_sync or kmpm_run reports the first one,
+ * with its step.  Calls that read the device state (kmpm_scalars, the
+ * downloads) run in order after the queued steps. */
+int kmpm_run_async(struct kmpm_ctx *ctx, int nsteps);
+
+/* Wait for every step queued on the context's stream and report the first
+ * error any of them raised (KMPM_OK if none). */
+int kmpm_sync(struct kmpm_ctx *ctx);
+
 /* RunTime::command (src/run_time.cpp:30-60): steps until time >= maxtime. */
 int kmpm_run_time(struct kmpm_ctx *ctx, double maxtime, int *nsteps_done);
 

@@ -1672,6 +1672,30 @@ int kmpm_run(kmpm_ctx *c, int nsteps) {
   return check_error(c);
 }
 
+// kmpm_run without the final wait: the steps' graph launches are queued and
+// the error word is read by the next kmpm_sync / kmpm_run
+int kmpm_run_async(kmpm_ctx *c, int nsteps) {
+  if (!c || nsteps < 0) return KMPM_ERR_ARG;
+  int r = prepare(c);
+  if (r != KMPM_OK) return r;
+  if (nsteps > 0) {
+    r = maybe_tune(c);
+    if (r != KMPM_OK) return r;
+  }
+  r = set_maxtime(c, 1e300);
+  if (r != KMPM_OK) return r;
+  r = launch_steps(c, nsteps);
+  if (r != KMPM_OK) return r;
+  CK(cudaGetLastError());
+  return KMPM_OK;
+}
+
+int kmpm_sync(kmpm_ctx *c) {
+  if (!c) return KMPM_ERR_ARG;
+  if (!c->built) return KMPM_OK;
+  return check_error(c);
+}
+
 int kmpm_run_time(kmpm_ctx *c, double maxtime, int *nsteps_done) {
   if (!c) return KMPM_ERR_ARG;
   if (c->indep()) return fail(c, KMPM_ERR_ARG, "run_time needs one clock: not available for independent solids");
@@ -1848,18 +1872,20 @@ int kmpm_download_particles_async(kmpm_ctx *c, int solid, int field, double *out
   const auto &S = c->hsolids[solid];
   const size_t need = (size_t)S.n * w;
   if (!c->cst) CK(cudaStreamCreateWithFlags(&c->cst, cudaStreamNonBlocking));
-  // a free buffer: one whose copy has ended, else a new one
+  // the smallest free buffer that holds the field (one whose copy has
+  // ended), else a new one: a buffer is never freed and reallocated here,
+  // as cudaFree would wait for every step the caller has queued
   kmpm_ctx::AsyncBuf *b = nullptr;
-  for (auto &x : c->abufs)
-    if (!x.busy || cudaEventQuery(x.copied) == cudaSuccess) { x.busy = false; b = &x; break; }
+  for (auto &x : c->abufs) {
+    if (x.busy && cudaEventQuery(x.copied) != cudaSuccess) continue;
+    x.busy = false;
+    if (x.cap >= need && (!b || x.cap < b->cap)) b = &x;
+  }
   if (!b) {
     c->abufs.emplace_back();
     b = &c->abufs.back();
     CK(cudaEventCreateWithFlags(&b->gathered, cudaEventDisableTiming));
     CK(cudaEventCreateWithFlags(&b->copied, cudaEventDisableTiming));
-  }
-  if (need > b->cap) {
-    dfree(b->buf);
     DALLOC(b->buf, need);
     b->cap = need;
   }

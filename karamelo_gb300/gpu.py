@@ -31,7 +31,7 @@ RESTART_FIELDS_UL = ("x", "v", "sigma_raw", "strain_el", "F", "eps_p", "epsdot_p
 GRID_FIELDS = {"mass": (0, 1), "v": (1, 3), "v_update": (2, 3), "x": (3, 3), "T": (6, 1)}
 
 EXPORTED = ["kmpm_create", "kmpm_destroy", "kmpm_last_error", "kmpm_add_material", "kmpm_add_grid",
-            "kmpm_add_solid", "kmpm_add_fix", "kmpm_run", "kmpm_run_time", "kmpm_run_until", "kmpm_scalars",
+            "kmpm_add_solid", "kmpm_add_fix", "kmpm_run", "kmpm_run_async", "kmpm_sync", "kmpm_run_time", "kmpm_run_until", "kmpm_scalars",
             "kmpm_download_particles", "kmpm_upload_particles", "kmpm_download_grid", "kmpm_energy",
             "kmpm_stream", "kmpm_launches_per_step", "kmpm_profile", "kmpm_profile_phase",
             "kmpm_p2g_mass_noalloc", "kmpm_solid_scalars",
@@ -88,6 +88,8 @@ def load(path: str = LIB_PATH):
     L.kmpm_add_solid.argtypes = [p, i, i, i, dp, dp, dp, dp, dp, d]
     L.kmpm_add_fix.argtypes = [p, i, i, ctypes.POINTER(ctypes.c_ubyte), ip, dp]
     L.kmpm_run.argtypes = [p, i]
+    L.kmpm_run_async.argtypes = [p, i]
+    L.kmpm_sync.argtypes = [p]
     L.kmpm_run_time.argtypes = [p, d, ip]
     L.kmpm_run_until.argtypes = [p, i, d, ip]
     L.kmpm_scalars.argtypes = [p, dp, dp, ctypes.POINTER(ctypes.c_longlong)]
@@ -226,6 +228,14 @@ class GpuBackend:
 
     def run(self, n: int):
         self._ck(self.L.kmpm_run(self.h, int(n)))
+
+    def run_async(self, n: int):
+        """Queue n steps and return (kmpm_run_async); :meth:`sync` waits for
+        them and raises the first error they met."""
+        self._ck(self.L.kmpm_run_async(self.h, int(n)))
+
+    def sync(self):
+        self._ck(self.L.kmpm_sync(self.h))
 
     def run_time(self, t: float) -> int:
         done = ctypes.c_int(0)
