@@ -114,6 +114,7 @@ struct kmpm_ctx {
   // TLMPM h ratio of the time step: per-range bounds, the flagged ranges
   // (HRange, k_h_exact) and the exact pass's grid
   HRange *d_hr = nullptr;
+  int4 *d_gbox = nullptr;  // TLMPM: the stress kernel's node box of every block
   int *d_hflags = nullptr, *d_nhflag = nullptr;
   int exact_blocks = 0;
   bool exact_h = false;  // KMPM_EXACT_H=1: the cubic for every particle (no bounds)
@@ -314,6 +315,7 @@ PartArgs part_args(kmpm_ctx *c) {
   a.asflip = (!c->TL() && c->prm.transfer == KMPM_TRANSFER_ASFLIP) ? 1 : 0;
   a.axisym = c->prm.axisymmetric;
   a.dim = c->prm.dim;
+  a.gbox = c->TL() ? c->d_gbox : nullptr;
   for (int d = 0; d < 3; d++) a.tile_t[d] = c->tdim[d];
   a.lq_f = c->d_lq_f;
   a.lq_i = c->d_lq_i;
@@ -863,6 +865,15 @@ int build(kmpm_ctx *c) {
     LAUNCH(c->K.p2g_mass, c->ntiles_launch, 256, c->smem[0][0], p);
     GridArgs ga = grid_args(c, 0);
     LAUNCH(c->K.grid_mass[c->prm.precision == KMPM_PREC_FP64_ISLANDS ? 1 : 0], c->nblk_g, 256, 0, ga);
+    // the stress kernel's node box of every block, fixed by x0 from here on
+    if (const char *ev = std::getenv("KMPM_BOX_PER_LAUNCH"); !(ev && ev[0] == '1')) {
+      DALLOC(c->d_gbox, 2 * (size_t)c->nblk_p);
+      PartArgs pb = part_args(c);
+      pb.gbox = nullptr;
+      int4 *box = c->d_gbox;
+      void *args[] = {&pb, &box};
+      CK(cudaLaunchKernel(c->K.gather_box, dim3(c->nblk_p), dim3(256), args, 0, c->st));
+    }
     CK(cudaStreamSynchronize(c->st));
   } else {
     // ULMPM: every tile of the box grid is launched; empty ones return at once
@@ -1500,7 +1511,7 @@ int kmpm_destroy(kmpm_ctx *c) {
   dfree(c->nodeA); dfree(c->nodeX); dfree(c->nodeT); dfree(c->nodeP); dfree(c->d_tiles);
   dfree(c->d_cs); dfree(c->d_ce); dfree(c->d_ts); dfree(c->d_te); dfree(c->partial);
   dfree(c->d_fixes); dfree(c->d_fix_start); dfree(c->d_fix_count); dfree(c->d_scalars); dfree(c->d_dtcfl);
-  dfree(c->d_hr); dfree(c->d_hflags); dfree(c->d_nhflag);
+  dfree(c->d_hr); dfree(c->d_hflags); dfree(c->d_nhflag); dfree(c->d_gbox);
   dfree(c->d_dump);
   free_contacts(c);
   for (auto &S : c->hsolids) dfree(S.d_in);

@@ -126,6 +126,10 @@ struct PartArgs {
   const HRange *hr;          // TLMPM, one clock: the h-ratio bound of each range (nullptr: solve every particle)
   int asflip;                // ULMPM ASFLIP: positions move with the blended velocity
   int axisym;                // 2-D axisymmetric: Fdot(2,2) / L(2,2) += v_r w / r
+  // TLMPM: each 256-particle block's staged node box of the stress kernel's
+  // gather, fixed by x0 (k_gather_box at setup): int4 (lo, vol or -1 when
+  // not staged), int4 (nb, 0) per block; null: the kernel computes it
+  const int4 *gbox;
   // queue of the plastic particle-steps for the learned return map (the
   // stress kernel's QUEUE variant writes it, k_learn_queue reads it):
   // LQ_NF float rows and LQ_NI int rows of lq_cap entries each
@@ -209,6 +213,7 @@ struct StepKernels {
   // compiled for shock EOS + Johnson-Cook + Johnson-Cook damage (2-D cubic
   // TLMPM) and for fluid EOS + fluid strength (3-D cubic ULMPM) [TL][variant]
   void *g2p2_jcd[2][3], *g2p2_fl[2][3];
+  void *gather_box;  // TLMPM: the stress kernel's node box of every block (k_gather_box)
   // MUSL gather + re-map in one pass (k_g2p1_remap_row) [TL]: 3-D cubic and
   // quadratic splines (nullptr elsewhere), and its dynamic shared memory
   void *g2p1_remap[2];

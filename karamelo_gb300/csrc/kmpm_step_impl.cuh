@@ -1992,6 +1992,32 @@ __device__ __forceinline__ void grad_gather(const PAxes<DIM, BASIS> &ax, const F
   }
 }
 
+// TLMPM: the node box that k_g2p2 stages for each 256-particle block, from
+// the block's x0 (static, so computed once at setup): the box of stage_box
+// over the same particles, stored as int4 (lo, vol or -1 if the block gathers
+// from global memory) and int4 (nb, 0).
+template <int DIM, int BASIS>
+__global__ void __launch_bounds__(256) k_gather_box(PartArgs a, int4 *box) {
+  RangeDev rd;
+  const int p0 = range_particle(a, rd);
+  const bool valid = p0 >= 0;
+  const int p = valid ? p0 : rd.start;
+  const float *P = *a.Pp;
+  const GridDev g = a.grids[rd.grid];
+  float xp[3];
+#pragma unroll
+  for (int d = 0; d < 3; d++) xp[d] = P[(PF_X0 + d) * a.ps + p];
+  PAxes<DIM, BASIS> ax;
+  ax.eval(g, xp);
+  const int i0[3] = {ax.ax[0].i0, ax.ax[1].i0, ax.ax[2].i0};
+  int lo[3] = {0, 0, 0}, nb[3] = {1, 1, 1}, vol = 0;
+  const bool staged = stage_box<DIM, Stencil<BASIS>::S>(valid, i0, G2P_STAGE_NODES, lo, nb, vol);
+  if (threadIdx.x == 0) {
+    box[2 * blockIdx.x] = make_int4(lo[0], lo[1], lo[2], staged ? vol : -1);
+    box[2 * blockIdx.x + 1] = make_int4(nb[0], nb[1], nb[2], 0);
+  }
+}
+
 // rate of deformation + deformation gradient + stress + wave speed
 // (src/solid.cpp:798-936, 1155-1438)
 // QUEUE: also append every plastic step (undamaged particle) to the learned
@@ -2045,18 +2071,10 @@ __global__ void __launch_bounds__(256, MINB) k_g2p2(PartArgs a) {
   // runs take the general ones): no affine moments, no per-slot offsets kept
   const bool apic = LAW != LAW_ANY ? false : a.apic != 0;
   const GridDev g = a.grids[rd.grid];
-  float xp[3];
-#pragma unroll
-  for (int d = 0; d < 3; d++) xp[d] = P[(PF_X0 + d) * ps + p] + (TL ? 0.f : P[(PF_X + d) * ps + p]);
-  PAxes<DIM, BASIS> ax;
-  ax.eval(g, xp);
   constexpr int S = Stencil<BASIS>::S;
   constexpr int SY = DIM >= 2 ? S : 1, SZ = DIM == 3 ? S : 1;
-  const int i0[3] = {ax.ax[0].i0, ax.ax[1].i0, ax.ax[2].i0};
-  int lo[3], nb[3], vol;
-  const bool staged = stage_box<DIM, S>(valid, i0, G2P_STAGE_NODES, lo, nb, vol);
   const float4 *__restrict__ NV = (a.use_vu ? a.nodeB : a.nodeA) + NODE_STRIDE * g.node_off;
-  if (staged) {
+  const auto stage_nodes = [&](const int (&lo)[3], const int (&nb)[3], int vol) {
     for (int e = threadIdx.x; e < vol; e += blockDim.x) {
       const int n = stage_node(g, lo, nb, e);
       float4 V = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -2066,8 +2084,36 @@ __global__ void __launch_bounds__(256, MINB) k_g2p2(PartArgs a) {
       }
       g2p_stage[e] = V;
     }
-    __syncthreads();
+  };
+  float xp[3];
+  PAxes<DIM, BASIS> ax;
+  int lo[3], nb[3], vol;
+  bool staged;
+  if (TL && a.gbox) {
+    // the block's box from setup: the node loads start at once, and the
+    // particle's x0 loads and basis overlap them
+    const int4 b0 = a.gbox[2 * blockIdx.x], b1 = a.gbox[2 * blockIdx.x + 1];
+    lo[0] = b0.x; lo[1] = b0.y; lo[2] = b0.z;
+    nb[0] = b1.x; nb[1] = b1.y; nb[2] = b1.z;
+    vol = b0.w;
+    staged = vol >= 0;
+    if (staged) stage_nodes(lo, nb, vol);
+#pragma unroll
+    for (int d = 0; d < 3; d++) xp[d] = P[(PF_X0 + d) * ps + p];
+    ax.eval(g, xp);
+    __syncthreads();  // block-uniform; also orders every thread after the mbarrier's initialisation
+  } else {
+#pragma unroll
+    for (int d = 0; d < 3; d++) xp[d] = P[(PF_X0 + d) * ps + p] + (TL ? 0.f : P[(PF_X + d) * ps + p]);
+    ax.eval(g, xp);
+    const int i0[3] = {ax.ax[0].i0, ax.ax[1].i0, ax.ax[2].i0};
+    staged = stage_box<DIM, S>(valid, i0, G2P_STAGE_NODES, lo, nb, vol);
+    if (staged) {
+      stage_nodes(lo, nb, vol);
+      __syncthreads();
+    }
   }
+  const int i0[3] = {ax.ax[0].i0, ax.ax[1].i0, ax.ax[2].i0};
   if (valid) {
     const int mi = rd.mat >= 0 ? rd.mat : a.solid_mat[__float_as_int(P[PF_SID * ps + p])];
     const MatDev &m = a.mats[mi];
@@ -2452,6 +2498,7 @@ void fill_step_kernels(StepKernels &k) {
   k.p2g_ul_th = (void *)k_p2g<DIM, BASIS, P2G_UL, true>;
   k.p2g_vel = (void *)k_p2g<DIM, BASIS, P2G_VEL, false>;
   k.p2g_vel_th = (void *)k_p2g<DIM, BASIS, P2G_VEL, true>;
+  k.gather_box = (void *)k_gather_box<DIM, BASIS>;
   k.p2g_row_fonly = k.grid_upd_fonly = k.grid_store_p = nullptr;
   k.p2g_row_fonly_smem = 0;
   if constexpr (DIM == 3 && (BASIS == 1 || BASIS == 3)) {
