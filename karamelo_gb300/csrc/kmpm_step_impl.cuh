@@ -691,17 +691,20 @@ __global__ void __launch_bounds__(256, 4) k_p2g_force_row(P2GArgs a) {
   const int hw = lane >> 4, sa = (lane >> 2) & 3, sb = lane & 3;
   const float2 *px = sbxy + (0 * S + sa) * SROW, *py = sbxy + (1 * S + sb) * SROW;
   const int i0x = (tc0 * TX + warp) - LO;
+  // the particle ranges of the warp's TY x 4 cells, in one load: lane k < 16
+  // holds the start of cell k, lane 16 + k its end
+  static_assert(TY * TZ == 16, "16 cells per warp");
+  const int cw = tile_global * TS::NCELL + warp * TY * TZ;
+  const int cvw = lane < 16 ? a.cell_start[cw + lane] : a.cell_end[cw + lane - 16];
 
   for (int ly = 0; ly < TY; ly++) {
     // the row's four cells and their particle ranges (as k_p2g_row)
-    const int cbase = tile_global * TS::NCELL + (warp * TY + ly) * TZ;
-    const int cv = lane < 8 ? (lane < 4 ? a.cell_start[cbase + lane] : a.cell_end[cbase + lane - 4]) : 0;
     int st[4], en[4], lo4[4];
     int rs = INT_MAX, re = INT_MIN;
 #pragma unroll
     for (int k = 0; k < 4; k++) {
-      st[k] = __shfl_sync(0xffffffffu, cv, k);
-      en[k] = __shfl_sync(0xffffffffu, cv, 4 + k);
+      st[k] = __shfl_sync(0xffffffffu, cvw, ly * TZ + k);
+      en[k] = __shfl_sync(0xffffffffu, cvw, 16 + ly * TZ + k);
       const bool full = en[k] > st[k];
       lo4[k] = full ? st[k] : INT_MAX;
       rs = full ? min(rs, st[k]) : rs;
@@ -723,16 +726,19 @@ __global__ void __launch_bounds__(256, 4) k_p2g_force_row(P2GArgs a) {
         int lz = 0;
 #pragma unroll
         for (int k = 1; k < 4; k++) lz = lo4[k] <= p ? k : lz;
-        float pay[9];
+        // every load of the particle before the first shared-memory store
+        float pay[9], x0p[3];
 #pragma unroll
         for (int k = 0; k < 9; k++) pay[k] = P[(PF_PK + k) * ps + p];
+#pragma unroll
+        for (int d = 0; d < 3; d++) x0p[d] = P[(PF_X0 + d) * ps + p];
         reinterpret_cast<float4 *>(spay + lane * 12)[0] = make_float4(pay[0], pay[1], pay[2], pay[3]);
         reinterpret_cast<float4 *>(spay + lane * 12)[1] = make_float4(pay[4], pay[5], pay[6], pay[7]);
         spay[lane * 12 + 8] = pay[8];
         const int i0[3] = {i0x, i0y, (tc2 * TZ + lz) - LO};
 #pragma unroll
         for (int d = 0; d < 3; d++) {
-          const float xp = P[(PF_X0 + d) * ps + p];
+          const float xp = x0p[d];
           const float lod = d == 0 ? g.lo[0] : (d == 1 ? g.lo[1] : g.lo[2]);
           const int nd = d == 0 ? g.n[0] : (d == 1 ? g.n[1] : g.n[2]);
           const int ngd = d == 0 ? g.ng[0] : (d == 1 ? g.ng[1] : g.ng[2]);
@@ -1768,16 +1774,18 @@ __global__ void __launch_bounds__(256, 4) k_g2p1_remap_row(P2GArgs a) {
   const int hw = lane >> 4, sa = (lane >> 2) & 3, sb = lane & 3;
   const float *px = sbxy + sa * VROW, *py = sbxy + (4 + sb) * VROW;
   const int i0x = (tc0 * TX + warp) - LO;
+  // the particle ranges of the warp's TY x 4 cells, in one load (as k_p2g_force_row)
+  static_assert(TY * TZ == 16, "16 cells per warp");
+  const int cw = tile_global * TS::NCELL + warp * TY * TZ;
+  const int cvw = lane < 16 ? a.cell_start[cw + lane] : a.cell_end[cw + lane - 16];
 
   for (int ly = 0; ly < TY; ly++) {
-    const int cbase = tile_global * TS::NCELL + (warp * TY + ly) * TZ;
-    const int cv = lane < 8 ? (lane < 4 ? a.cell_start[cbase + lane] : a.cell_end[cbase + lane - 4]) : 0;
     int st[4], en[4], lo4[4];
     int rs = INT_MAX, re = INT_MIN;
 #pragma unroll
     for (int k = 0; k < 4; k++) {
-      st[k] = __shfl_sync(0xffffffffu, cv, k);
-      en[k] = __shfl_sync(0xffffffffu, cv, 4 + k);
+      st[k] = __shfl_sync(0xffffffffu, cvw, ly * TZ + k);
+      en[k] = __shfl_sync(0xffffffffu, cvw, 16 + ly * TZ + k);
       const bool full = en[k] > st[k];
       lo4[k] = full ? st[k] : INT_MAX;
       rs = full ? min(rs, st[k]) : rs;
