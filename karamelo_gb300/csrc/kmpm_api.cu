@@ -866,7 +866,7 @@ int build(kmpm_ctx *c) {
     GridArgs ga = grid_args(c, 0);
     LAUNCH(c->K.grid_mass[c->prm.precision == KMPM_PREC_FP64_ISLANDS ? 1 : 0], c->nblk_g, 256, 0, ga);
     // the stress kernel's node box of every block, fixed by x0 from here on
-    if (const char *ev = std::getenv("KMPM_BOX_PER_LAUNCH"); !(ev && ev[0] == '1')) {
+    if (const char *ev = std::getenv("KMPM_BOX_PER_LAUNCH"); dim == 3 && !(ev && ev[0] == '1')) {
       DALLOC(c->d_gbox, 2 * (size_t)c->nblk_p);
       PartArgs pb = part_args(c);
       pb.gbox = nullptr;

@@ -126,7 +126,7 @@ struct PartArgs {
   const HRange *hr;          // TLMPM, one clock: the h-ratio bound of each range (nullptr: solve every particle)
   int asflip;                // ULMPM ASFLIP: positions move with the blended velocity
   int axisym;                // 2-D axisymmetric: Fdot(2,2) / L(2,2) += v_r w / r
-  // TLMPM: each 256-particle block's staged node box of the stress kernel's
+  // 3-D TLMPM: each 256-particle block's staged node box of the stress kernel's
   // gather, fixed by x0 (k_gather_box at setup): int4 (lo, vol or -1 when
   // not staged), int4 (nb, 0) per block; null: the kernel computes it
   const int4 *gbox;

@@ -505,19 +505,23 @@ __global__ void __launch_bounds__(256, (MODE == P2G_VEL ? 4 : 3)) k_p2g_row(P2GA
   const float2 *px = sbas + (0 * S + sa) * SROW, *py = sbas + (1 * S + sb) * SROW;
   const float2 *pz0 = sbas + (2 * S + sc) * SROW, *pz2 = sbas + (2 * S + sc + 2) * SROW;
   const int i0x = (tc0 * TX + warp) - LO;
+  // the particle ranges of the warp's TY x 4 cells (local index
+  // (lx TY + ly) TZ + lz), in one load: lane k < 16 holds the start of cell
+  // k, lane 16 + k its end
+  static_assert(TY * TZ == 16, "16 cells per warp");
+  const int cw = tile_global * TS::NCELL + warp * TY * TZ;
+  const int cvw = lane < 16 ? a.cell_start[cw + lane] : a.cell_end[cw + lane - 16];
 
   for (int ly = 0; ly < TY; ly++) {
-    // the row's four cells (local index (lx TY + ly) TZ + lz) and their
-    // particle ranges [st, en); the non-empty ones are contiguous in the
-    // sorted order (an empty cell's range is st == en, of any value)
-    const int cbase = tile_global * TS::NCELL + (warp * TY + ly) * TZ;
-    const int cv = lane < 8 ? (lane < 4 ? a.cell_start[cbase + lane] : a.cell_end[cbase + lane - 4]) : 0;
+    // the row's four cells and their particle ranges [st, en); the non-empty
+    // ones are contiguous in the sorted order (an empty cell's range is
+    // st == en, of any value)
     int st[4], en[4], lo4[4];
     int rs = INT_MAX, re = INT_MIN;
 #pragma unroll
     for (int k = 0; k < 4; k++) {
-      st[k] = __shfl_sync(0xffffffffu, cv, k);
-      en[k] = __shfl_sync(0xffffffffu, cv, 4 + k);
+      st[k] = __shfl_sync(0xffffffffu, cvw, ly * TZ + k);
+      en[k] = __shfl_sync(0xffffffffu, cvw, 16 + ly * TZ + k);
       const bool full = en[k] > st[k];
       lo4[k] = full ? st[k] : INT_MAX;
       rs = full ? min(rs, st[k]) : rs;
@@ -926,16 +930,18 @@ __global__ void __launch_bounds__(256, 4) k_p2g_vel_row(P2GArgs a) {
   const int hw = lane >> 4, sa = (lane >> 2) & 3, sb = lane & 3;
   const float *px = sbxy + sa * VROW, *py = sbxy + (4 + sb) * VROW;
   const int i0x = (tc0 * TX + warp) - LO;
+  // the particle ranges of the warp's TY x 4 cells, in one load (as k_p2g_force_row)
+  static_assert(TY * TZ == 16, "16 cells per warp");
+  const int cw = tile_global * TS::NCELL + warp * TY * TZ;
+  const int cvw = lane < 16 ? a.cell_start[cw + lane] : a.cell_end[cw + lane - 16];
 
   for (int ly = 0; ly < TY; ly++) {
-    const int cbase = tile_global * TS::NCELL + (warp * TY + ly) * TZ;
-    const int cv = lane < 8 ? (lane < 4 ? a.cell_start[cbase + lane] : a.cell_end[cbase + lane - 4]) : 0;
     int st[4], en[4], lo4[4];
     int rs = INT_MAX, re = INT_MIN;
 #pragma unroll
     for (int k = 0; k < 4; k++) {
-      st[k] = __shfl_sync(0xffffffffu, cv, k);
-      en[k] = __shfl_sync(0xffffffffu, cv, 4 + k);
+      st[k] = __shfl_sync(0xffffffffu, cvw, ly * TZ + k);
+      en[k] = __shfl_sync(0xffffffffu, cvw, 16 + ly * TZ + k);
       const bool full = en[k] > st[k];
       lo4[k] = full ? st[k] : INT_MAX;
       rs = full ? min(rs, st[k]) : rs;
@@ -1110,18 +1116,22 @@ __global__ void __launch_bounds__(256, (MODE == P2G_VEL || p2g_fonly(MODE) ? 4 :
   const float2 *px = sbas + (0 * S + sa) * SROW;
   const float2 *py0 = sbas + (1 * S + sc) * SROW, *py2 = sbas + (1 * S + sc + 2) * SROW;
 
+  // the particle ranges of the warp's L x TY cells (local index lx' TY + ly),
+  // in one load: lane k holds the start and the end of cell k
+  static_assert(L * TY == 32, "32 cells per warp");
+  const int cw = tile_global * TS::NCELL + warp * L * TY;
+  const int cvs = a.cell_start[cw + lane], cve = a.cell_end[cw + lane];
+
   for (int lx = 0; lx < L; lx++) {
     const int i0x = (tc0 * TX + warp * L + lx) - LO;
     for (int ly0 = 0; ly0 < TY; ly0 += 4) {
-      // the row's four cells (local index lx' TY + ly) and their ranges
-      const int cbase = tile_global * TS::NCELL + (warp * L + lx) * TY + ly0;
-      const int cv = lane < 8 ? (lane < 4 ? a.cell_start[cbase + lane] : a.cell_end[cbase + lane - 4]) : 0;
+      // the row's four cells and their ranges
       int st[4], en[4], lo4[4];
       int rs = INT_MAX, re = INT_MIN;
 #pragma unroll
       for (int k = 0; k < 4; k++) {
-        st[k] = __shfl_sync(0xffffffffu, cv, k);
-        en[k] = __shfl_sync(0xffffffffu, cv, 4 + k);
+        st[k] = __shfl_sync(0xffffffffu, cvs, lx * TY + ly0 + k);
+        en[k] = __shfl_sync(0xffffffffu, cve, lx * TY + ly0 + k);
         const bool full = en[k] > st[k];
         lo4[k] = full ? st[k] : INT_MAX;
         rs = full ? min(rs, st[k]) : rs;
@@ -1753,6 +1763,11 @@ __global__ void __launch_bounds__(256, 4) k_g2p1_remap_row(P2GArgs a) {
   const float alpha = a.pic_flip;
   // the tile's x0, u, v and mass rows, into L2 while the footprint is staged
   prefetch_rows_l2(P, ps, PF_X0, PF_MASS + 1 - PF_X0, a.tile_start[tile_global], a.tile_end[tile_global]);
+  // the particle ranges of the warp's TY x 4 cells, in one load (as
+  // k_p2g_force_row), issued before the footprint's loads and barrier
+  static_assert(TY * TZ == 16, "16 cells per warp");
+  const int cw = tile_global * TS::NCELL + warp * TY * TZ;
+  const int cvw = lane < 16 ? a.cell_start[cw + lane] : a.cell_end[cw + lane - 16];
 
   for (int k = lane; k < Q * NF; k += 32) slab[k] = 0.f;
   // the tile's node footprint: nodes (tc TX - LO + fx, ...), fx < WX
@@ -1774,10 +1789,6 @@ __global__ void __launch_bounds__(256, 4) k_g2p1_remap_row(P2GArgs a) {
   const int hw = lane >> 4, sa = (lane >> 2) & 3, sb = lane & 3;
   const float *px = sbxy + sa * VROW, *py = sbxy + (4 + sb) * VROW;
   const int i0x = (tc0 * TX + warp) - LO;
-  // the particle ranges of the warp's TY x 4 cells, in one load (as k_p2g_force_row)
-  static_assert(TY * TZ == 16, "16 cells per warp");
-  const int cw = tile_global * TS::NCELL + warp * TY * TZ;
-  const int cvw = lane < 16 ? a.cell_start[cw + lane] : a.cell_end[cw + lane - 16];
 
   for (int ly = 0; ly < TY; ly++) {
     int st[4], en[4], lo4[4];
@@ -2000,7 +2011,7 @@ __device__ __forceinline__ void grad_gather(const PAxes<DIM, BASIS> &ax, const F
   }
 }
 
-// TLMPM: the node box that k_g2p2 stages for each 256-particle block, from
+// 3-D TLMPM: the node box that k_g2p2 stages for each 256-particle block, from
 // the block's x0 (static, so computed once at setup): the box of stage_box
 // over the same particles, stored as int4 (lo, vol or -1 if the block gathers
 // from global memory) and int4 (nb, 0).
@@ -2097,9 +2108,10 @@ __global__ void __launch_bounds__(256, MINB) k_g2p2(PartArgs a) {
   PAxes<DIM, BASIS> ax;
   int lo[3], nb[3], vol;
   bool staged;
-  if (TL && a.gbox) {
+  if (TL && DIM == 3 && a.gbox) {
     // the block's box from setup: the node loads start at once, and the
-    // particle's x0 loads and basis overlap them
+    // particle's x0 loads and basis overlap them (3-D: in 2-D the box's own
+    // load costs more than the shorter chain it saves)
     const int4 b0 = a.gbox[2 * blockIdx.x], b1 = a.gbox[2 * blockIdx.x + 1];
     lo[0] = b0.x; lo[1] = b0.y; lo[2] = b0.z;
     nb[0] = b1.x; nb[1] = b1.y; nb[2] = b1.z;

@@ -1,16 +1,16 @@
-"""TLMPM: the stress kernel's node box per 256-particle block, computed once
-at setup from x0 (k_gather_box), against the box each launch computes from
-the same particles (KMPM_BOX_PER_LAUNCH=1): the staged gathers read the same
-nodes in the same order, so every field agrees bit for bit.  3-D Taylor bar
-(cubic and quadratic splines), a 2-D tensile bar and a batch of bars
-(independent instances, one block range per bar)."""
+"""3-D TLMPM: the stress kernel's node box per 256-particle block, computed
+once at setup from x0 (k_gather_box), against the box each launch computes
+from the same particles (KMPM_BOX_PER_LAUNCH=1): the staged gathers read the
+same nodes in the same order, so every field agrees bit for bit.  The Taylor
+bar (cubic and quadratic splines) and two spheres in Hertz contact (two
+solids, each its own block range and grid).  2-D runs compute the box in
+every launch either way."""
 import os
 
 import numpy as np
 import pytest
 
 from karamelo_gb300 import workloads as W
-from karamelo_gb300.batch import Batch, tensile_sweep
 
 pytestmark = pytest.mark.gpu
 
@@ -25,17 +25,10 @@ def _taylor(basis):
     return [{f: sim.particles(0, f) for f in FIELDS}], sim.backend
 
 
-def _tensile_2d(basis):
-    sim = W.tensile_bar_2d(None, basis=basis, vend=5.0)
-    sim.run(40)
-    return [{f: sim.particles(0, f) for f in FIELDS}], sim.backend
-
-
-def _batch(basis):
-    sims, _ = tensile_sweep(4, seed=3, nmin=400, nmax=3000, vmin=20.0, vmax=60.0)
-    b = Batch(sims)
-    b.run(200)
-    return [{f: b.particles(i, f) for f in FIELDS} for i in range(4)], b.backend
+def _spheres(basis):
+    sim = W.hertz_spheres(None, basis=basis)
+    sim.run(60)
+    return [{f: sim.particles(i, f) for f in FIELDS} for i in range(2)], sim.backend
 
 
 def _run(make, basis, box):
@@ -50,8 +43,8 @@ def _run(make, basis, box):
 
 
 @pytest.mark.parametrize("make,basis", [(_taylor, "cubic-spline"), (_taylor, "quadratic-spline"),
-                                        (_tensile_2d, "cubic-spline"), (_batch, None)],
-                         ids=["taylor_cubic", "taylor_quadratic", "tensile_2d", "batch"])
+                                        (_spheres, "cubic-spline")],
+                         ids=["taylor_cubic", "taylor_quadratic", "hertz_spheres"])
 def test_setup_box_matches_per_launch_box(gpu_lib, make, basis):
     a = _run(make, basis, box=True)
     b = _run(make, basis, box=False)
