@@ -112,8 +112,8 @@ class ClockSampler:
             for k, nm in enumerate(names):
                 if len(r) > 5 + k and r[5 + k].lower() in ("active", "0x1", "1"):
                     reasons.add(nm)
-        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
-                "reasons": sorted(reasons), "samples": len(self.rows)}
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_min_mhz": min(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": sorted(reasons), "samples": len(self.rows)}
 
 
 def dist_env():
@@ -250,6 +250,9 @@ def bench_ours(args):
     # (cudaFree) would synchronise the device in the middle of the steps
     gc.collect()
     gc.disable()
+    clocks_e2e = ClockSampler(local)  # started before the timed region
+    clocks_e2e.start()
+    time.sleep(0.3)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     sim2.backend = GpuBackend(sim2.s, precision=args.precision, track_strain=False)
@@ -278,6 +281,7 @@ def bench_ours(args):
     be2.sync_downloads()
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - t0
+    clk_e2e = clocks_e2e.stop()
     gc.enable()
     e2e_parts = {"create": t_create - t0, "first_step_and_wall": t_first - t_create, "run_calls": t_runs,
                  "download_waits": t_waits, "download_queueing": t_queue, "final_sync": e2e_s - (t_loop - t0)}
@@ -313,7 +317,7 @@ def bench_ours(args):
                         "components of the rotated stress, FP64, into two alternating sets of page-locked "
                         "buffers, first touched before the timed region) every 10 steps + kmpm_sync, which "
                         "reports any step's error; launch shapes as tuned by the first context of the process",
-                "seconds": {k: round(v, 4) for k, v in e2e_parts.items()}},
+                "seconds": {k: round(v, 4) for k, v in e2e_parts.items()}, "clocks": clk_e2e},
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,
                      "alg_bytes_per_launch": alg},
