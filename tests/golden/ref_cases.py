@@ -72,40 +72,40 @@ def _every(n, plan):
 
 # name -> (builder(factory, method) -> MPM, CPU method keyword, plan, description)
 CASES = {
-    # BASELINE C1: 2-D ULMPM, USL, linear basis, two linear-elastic disks; the
-    # energy trace of every step through 3000 steps and the particle state on the way
+    # 2-D ULMPM, USL, linear basis, two linear-elastic disks: the energy trace
+    # of every step through 3000 steps and the particle state on the way
     "disks_ulmpm_usl_linear": (
         lambda f, m: W.two_disks(f, method=m), "ulmpm",
         [_every(100, [("run", 1), ("vars", "E")]), ("state", "s100"),
          _every(900, [("run", 1), ("vars", "E")]), ("state", "s1000"),
          _every(2000, [("run", 1), ("vars", "E")]), ("state", "s3000")],
-        "C1: two colliding disks, 416 particles, 3000 steps"),
-    # BASELINE C2 physics at cellsize 0.8 mm: TLMPM MUSL cubic, Johnson-Cook + linear EOS
+        "two colliding disks, 416 particles, 3000 steps"),
+    # the Taylor bar's physics at cellsize 0.8 mm: TLMPM MUSL cubic, Johnson-Cook + linear EOS
     "taylor_tlmpm_musl_cubic_jc_0.8": (
         lambda f, m: W.taylor_bar(f, cellsize=0.8, method=m), "tlmpm",
         [("run", 1), ("call", _wall), ("run", 10), ("state", "w10"), ("run", 90), ("state", "w100")],
-        "C2 physics at 0.8 mm (16,848 particles): step 1, wall, 100 steps"),
-    # BASELINE C2 itself: cellsize 0.2 mm, 1,045,872 particles
+        "Taylor bar at 0.8 mm (16,848 particles): step 1, wall, 100 steps"),
+    # the Taylor bar at cellsize 0.2 mm, 1,045,872 particles
     "taylor_tlmpm_musl_cubic_jc_0.2": (
         lambda f, m: W.taylor_bar(f, cellsize=0.2, method=m), "tlmpm",
         [("run", 1), ("call", _wall), ("run", 10), ("state", "w10")],
-        "C2 at 0.2 mm (1,045,872 particles): step 1, wall, 10 steps"),
-    # BASELINE C3 physics at 50 mm: ULMPM MUSL cubic, Tait EOS + viscosity, gravity, slip walls
+        "Taylor bar at 0.2 mm (1,045,872 particles): step 1, wall, 10 steps"),
+    # the dam break's physics at 50 mm: ULMPM MUSL cubic, Tait EOS + viscosity, gravity, slip walls
     "dam_ulmpm_musl_cubic_50mm": (
         lambda f, m: W.dam_break(f, cellsize=0.05, method=m), "ulmpm",
         [("run", 50), ("state", "s50"), ("run", 150), ("state", "s200")],
-        "C3 physics at 50 mm (8,192 particles): 200 steps"),
-    # BASELINE C3 at 10 mm: 1,024,000 particles
+        "dam break at 50 mm (8,192 particles): 200 steps"),
+    # the dam break at 10 mm: 1,024,000 particles
     "dam_ulmpm_musl_cubic_10mm": (
         lambda f, m: W.dam_break(f, cellsize=0.01, method=m), "ulmpm",
         [("run", 10), ("state", "s10")],
-        "C3 at 10 mm (1,024,000 particles): 10 steps"),
-    # BASELINE C5 physics: 2-D TLMPM MUSL cubic tensile bar, shock EOS +
-    # Johnson-Cook strength + damage, ends pulled at 50 m/s
+        "dam break at 10 mm (1,024,000 particles): 10 steps"),
+    # the physics of the batch of bars: 2-D TLMPM MUSL cubic tensile bar, shock
+    # EOS + Johnson-Cook strength + damage, ends pulled at 50 m/s
     "tensile_tlmpm_jc_damage": (
         lambda f, m: W.tensile_bar_2d(f, cellsize=0.8, vend=50.0, ramp=False, method=m), "tlmpm",
         [("run", 1500), ("state", "s1500"), ("run", 1500), ("state", "s3000")],
-        "C5 physics: one 2-D tensile bar with Johnson-Cook damage, 3000 steps"),
+        "one 2-D tensile bar with Johnson-Cook damage, 3000 steps"),
     # Johnson-Cook with plastic-work heating (thermo-mechanical TLMPM)
     "block_tlmpm_jc_thermal": (
         lambda f, m: W.block_bar(f, m, "johnson_cook", thermal=True), "tlmpm",

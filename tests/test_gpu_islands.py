@@ -11,7 +11,7 @@ produces:
   - det and inverse of F: F and J = det F;
   - the return: the stress σ and the plastic strain ε_p;
 and the positions.  Both modes are held to the parity test's bounds; the
-measured errors are printed (pytest -s) and quoted in the design doc."""
+measured errors are printed (pytest -s)."""
 import numpy as np
 import pytest
 

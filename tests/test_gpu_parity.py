@@ -101,7 +101,7 @@ def test_two_disks_cubic_collision(gpu_lib, oracle_mod):
 
 
 def test_two_disks_linear_usl(gpu_lib, oracle_mod):
-    """The C1 configuration (2-D ULMPM USL linear).  Its rigid free flight has
+    """The two-disk configuration (2-D ULMPM USL linear).  Its rigid free flight has
     exactly zero stress in FP64; FP32 rounding of p/m leaves ~1e-5 Pa of stress
     noise, which near-empty nodes amplify once particles land exactly on nodes
     (step ~125).  Parity is therefore checked before that event."""

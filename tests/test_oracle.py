@@ -139,7 +139,7 @@ def test_linear_eos_and_fluid_eos(oracle_mod):
 
 
 def test_oracle_two_disks_energy_exchange(oracle_mod):
-    """C1 (two colliding elastic disks): kinetic energy turns into strain energy and back."""
+    """Two colliding elastic disks: kinetic energy turns into strain energy and back."""
     from karamelo_gb300 import workloads as W
     sim = W.two_disks(oracle_mod.OracleBackend, method="ulmpm")
     e0 = None

@@ -48,10 +48,10 @@ def test_fixtures_present_and_consistent():
             assert np.all(np.diff(pt) > 0) and len(pt) <= int(fx[f"{lab}__n"])
             for f in RC.FIELDS:
                 assert np.all(np.isfinite(fx[f"{lab}__{f}"]))
-    # C1's published sizes: 416 particles (208 per disk), 3000 steps logged
+    # the two disks' published sizes: 416 particles (208 per disk), 3000 steps logged
     fx = _fixture("disks_ulmpm_usl_linear")
     assert int(fx["s3000__n"]) == 416 and len(fx["E__step"]) == 3000
-    # C2 at 0.2 mm: 1,045,872 particles; C3 at 10 mm: 1,024,000
+    # the Taylor bar at 0.2 mm: 1,045,872 particles; the dam break at 10 mm: 1,024,000
     assert int(_fixture("taylor_tlmpm_musl_cubic_jc_0.2")["w10__n"]) == 1045872
     assert int(_fixture("dam_ulmpm_musl_cubic_10mm")["s10__n"]) == 1024000
 
@@ -104,7 +104,7 @@ def test_gpu_matches_reference(gpu_lib, name):
             assert err[f"rss_{f}"] < tol, f"{name} {lab} rss {f}: {err['rss_' + f]:.3e} >= {tol}"
 
 
-# C1 (2-D ULMPM, USL, linear basis, 3000 steps).  The disks fly rigidly until
+# The two disks (2-D ULMPM, USL, linear basis, 3000 steps).  The disks fly rigidly until
 # their particles reach the nodes (step ~125); there the near-empty nodes of
 # the linear basis amplify rounding, and FP32 and FP64 runs part.  The
 # oracle's own sensitivity floor, measured by running it from the initial
