@@ -237,7 +237,7 @@ def bench_ours(args):
             t.zero_()
     # the caller's particle arrays in page-locked host memory too: the upload
     # inside the timed region then runs at the link's rate, not at the rate of
-    # the driver's staging copy of pageable memory (9-150 GB/s from box to box)
+    # the driver's staging copy of pageable memory (9-150 GB/s from machine to machine)
     keep = []
     for sol in sim2.s.solids:
         for f in ("x0", "v", "mass", "vol0"):
