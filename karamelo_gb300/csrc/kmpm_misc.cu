@@ -261,34 +261,48 @@ __device__ __forceinline__ void raise_error_m(ErrState *e, int code, int p, long
 // per range: dtCFL = cellsize * min_h_ratio / max_p_wave_speed (src/solid.cpp:1430)
 template <int BS>
 __global__ void __launch_bounds__(BS) k_dt_range(DtArgs a) {
-  __shared__ float rc[BS], rh[BS];
+  static_assert(BS % 32 == 0 && BS <= 1024, "whole warps");
+  __shared__ float rc[BS / 32], rh[BS / 32];
   if (run_finished(a.scalars)) return;
   const RangeDev rd = a.ranges[blockIdx.x];
   float c = 0.f, h = 1.f;
-  // four independent loads in flight per thread (max / min are order-free)
+  // eight independent loads of each kind in flight per thread (max / min are
+  // order-free), then the block's maximum and minimum by warp shuffles
   const int end = rd.blk0 + rd.nblk;
   int b = rd.blk0 + threadIdx.x;
-  for (; b + 3 * BS < end; b += 4 * BS) {
-    const float c0 = a.blk_c[b], c1 = a.blk_c[b + BS], c2 = a.blk_c[b + 2 * BS], c3 = a.blk_c[b + 3 * BS];
-    const float h0 = a.blk_h[b], h1 = a.blk_h[b + BS], h2 = a.blk_h[b + 2 * BS], h3 = a.blk_h[b + 3 * BS];
-    c = fmaxf(c, fmaxf(fmaxf(c0, c1), fmaxf(c2, c3)));
-    h = fminf(h, fminf(fminf(h0, h1), fminf(h2, h3)));
+  for (; b + 7 * BS < end; b += 8 * BS) {
+    float cv[8], hv[8];
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+      cv[k] = a.blk_c[b + k * BS];
+      hv[k] = a.blk_h[b + k * BS];
+    }
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+      c = fmaxf(c, cv[k]);
+      h = fminf(h, hv[k]);
+    }
   }
   for (; b < end; b += BS) {
     c = fmaxf(c, a.blk_c[b]);
     h = fminf(h, a.blk_h[b]);
   }
-  rc[threadIdx.x] = c;
-  rh[threadIdx.x] = h;
-  __syncthreads();
-  for (int s = BS / 2; s > 0; s >>= 1) {
-    if (threadIdx.x < s) {
-      rc[threadIdx.x] = fmaxf(rc[threadIdx.x], rc[threadIdx.x + s]);
-      rh[threadIdx.x] = fminf(rh[threadIdx.x], rh[threadIdx.x + s]);
-    }
-    __syncthreads();
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    c = fmaxf(c, __shfl_xor_sync(0xffffffffu, c, o));
+    h = fminf(h, __shfl_xor_sync(0xffffffffu, h, o));
   }
+  if ((threadIdx.x & 31) == 0) {
+    rc[threadIdx.x >> 5] = c;
+    rh[threadIdx.x >> 5] = h;
+  }
+  __syncthreads();
   if (threadIdx.x == 0) {
+#pragma unroll
+    for (int w = 1; w < BS / 32; w++) {
+      rc[0] = fmaxf(rc[0], rc[w]);
+      rh[0] = fminf(rh[0], rh[w]);
+    }
     // TLMPM: a minimum at or above the range's bound may come from a particle
     // that reported the bound; k_h_exact then recomputes it (HRange)
     bool need = false;

@@ -2109,17 +2109,17 @@ __global__ void __launch_bounds__(256, MINB) k_g2p2(PartArgs a) {
   int lo[3], nb[3], vol;
   bool staged;
   if (TL && DIM == 3 && a.gbox) {
-    // the block's box from setup: the node loads start at once, and the
-    // particle's x0 loads and basis overlap them (3-D: in 2-D the box's own
-    // load costs more than the shorter chain it saves)
+    // the block's box from setup: the particle's x0 loads and the block's
+    // node loads start at once, and the basis overlaps them (3-D: in 2-D the
+    // box's own load costs more than the shorter chain it saves)
     const int4 b0 = a.gbox[2 * blockIdx.x], b1 = a.gbox[2 * blockIdx.x + 1];
     lo[0] = b0.x; lo[1] = b0.y; lo[2] = b0.z;
     nb[0] = b1.x; nb[1] = b1.y; nb[2] = b1.z;
     vol = b0.w;
     staged = vol >= 0;
-    if (staged) stage_nodes(lo, nb, vol);
 #pragma unroll
     for (int d = 0; d < 3; d++) xp[d] = P[(PF_X0 + d) * ps + p];
+    if (staged) stage_nodes(lo, nb, vol);
     ax.eval(g, xp);
     __syncthreads();  // block-uniform; also orders every thread after the mbarrier's initialisation
   } else {
